@@ -1,0 +1,1729 @@
+// Host runtime and C ABI of freud_gb300 (declared in include/freud_gb300.h).
+//
+// Mirrors the reference's object model (NeighborQuery / NeighborList / RDF /
+// Steinhardt, freud/locality, freud/density, freud/order) over device-resident
+// buffers. Argument validation and error classes follow the reference's C++
+// (NeighborQuery.h:86-111, 195-228, 315-329, 496-509; LinkCell.cc:222-260;
+// RDF.cc:25-42; NeighborList.cc:51-82, 286-307). All device work is issued on one
+// stream; every entry point synchronises before returning.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/freud_gb300.h"
+#include "fg_kernels.cuh"
+#include "fg_nlist.cuh"
+#include "fg_steinhardt.cuh"
+
+namespace fg {
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error
+{
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+static thread_local std::string g_last_error;
+
+#define FG_CUDA(call)                                                                                            \
+    do                                                                                                           \
+    {                                                                                                            \
+        cudaError_t e_ = (call);                                                                                 \
+        if (e_ != cudaSuccess)                                                                                   \
+        {                                                                                                        \
+            throw Error(e_ == cudaErrorMemoryAllocation ? FG_ERR_MEMORY : FG_ERR_CUDA,                           \
+                        std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " #call);                    \
+        }                                                                                                        \
+    } while (0)
+
+static void value_error(const std::string& m)
+{
+    throw Error(FG_ERR_VALUE, m);
+}
+static void runtime_error(const std::string& m)
+{
+    throw Error(FG_ERR_RUNTIME, m);
+}
+
+// ---------------------------------------------------------------------------
+// Stream and device memory
+// ---------------------------------------------------------------------------
+static cudaStream_t g_user_stream = nullptr;
+static bool g_user_stream_set = false;
+
+static cudaStream_t stream()
+{
+    if (g_user_stream_set)
+    {
+        return g_user_stream;
+    }
+    static thread_local cudaStream_t own = nullptr;
+    static thread_local int own_dev = -1;
+    int dev = 0;
+    FG_CUDA(cudaGetDevice(&dev));
+    if (own == nullptr || own_dev != dev)
+    {
+        FG_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+        own_dev = dev;
+        // keep freed blocks in the stream-ordered pool for reuse across frames
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+        {
+            uint64_t thr = std::numeric_limits<uint64_t>::max();
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
+    return own;
+}
+
+// Stream-ordered device buffer.
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes)
+    {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    DevBuf& operator=(DevBuf&& o) noexcept
+    {
+        if (this != &o)
+        {
+            release();
+            p = o.p;
+            bytes = o.bytes;
+            o.p = nullptr;
+            o.bytes = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p != nullptr)
+        {
+            cudaFreeAsync(p, stream());
+            p = nullptr;
+            bytes = 0;
+        }
+    }
+    void alloc(size_t n)
+    {
+        if (n <= bytes && p != nullptr)
+        {
+            return;
+        }
+        release();
+        const size_t want = n == 0 ? 16 : n;
+        FG_CUDA(cudaMallocAsync(&p, want, stream()));
+        bytes = want;
+    }
+    template<typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+static void sync()
+{
+    FG_CUDA(cudaStreamSynchronize(stream()));
+    FG_CUDA(cudaGetLastError());
+}
+
+// Device error word shared by the kernels of one call.
+static int* dev_err()
+{
+    static thread_local DevBuf* buf = nullptr;
+    if (buf == nullptr)
+    {
+        buf = new DevBuf();
+        buf->alloc(sizeof(int));
+    }
+    return buf->as<int>();
+}
+
+static void reset_dev_err()
+{
+    FG_CUDA(cudaMemsetAsync(dev_err(), 0, sizeof(int), stream()));
+}
+
+static void check_dev_err(const char* what)
+{
+    int h = 0;
+    FG_CUDA(cudaMemcpyAsync(&h, dev_err(), sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    sync();
+    if (h == DEV_CAPACITY)
+    {
+        runtime_error(std::string(what) + ": a per-query capacity limit was exceeded");
+    }
+    if (h != DEV_OK)
+    {
+        runtime_error(std::string(what) + ": device error code " + std::to_string(h));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Box (host float32 arithmetic in the reference order; built with -ffp-contract=off)
+// ---------------------------------------------------------------------------
+struct HostBox
+{
+    float L[3];
+    float xy, xz, yz;
+    bool is2d;
+    bool periodic[3];
+};
+
+static HostBox to_host_box(const fg_box* b)
+{
+    HostBox h;
+    h.is2d = b->is2D != 0;
+    h.L[0] = b->Lx;
+    h.L[1] = b->Ly;
+    h.L[2] = h.is2d ? 0.0f : b->Lz;
+    h.xy = b->xy;
+    h.xz = b->xz;
+    h.yz = b->yz;
+    h.periodic[0] = b->periodic_x != 0;
+    h.periodic[1] = b->periodic_y != 0;
+    h.periodic[2] = b->periodic_z != 0;
+    return h;
+}
+
+static fg_box to_c_box(const HostBox& h)
+{
+    fg_box b;
+    b.Lx = h.L[0];
+    b.Ly = h.L[1];
+    b.Lz = h.L[2];
+    b.xy = h.xy;
+    b.xz = h.xz;
+    b.yz = h.yz;
+    b.is2D = h.is2d ? 1 : 0;
+    b.periodic_x = h.periodic[0];
+    b.periodic_y = h.periodic[1];
+    b.periodic_z = h.periodic[2];
+    return b;
+}
+
+// Box::getNearestPlaneDistance, Box.h:489-497
+static void nearest_plane(const HostBox& b, float d[3])
+{
+    const float t = fsub(fmul(b.xy, b.yz), b.xz);
+    d[0] = fdiv(b.L[0], std::sqrt(fadd(fadd(1.0f, fmul(b.xy, b.xy)), fmul(t, t))));
+    d[1] = fdiv(b.L[1], std::sqrt(fadd(1.0f, fmul(b.yz, b.yz))));
+    d[2] = b.L[2];
+}
+
+static float box_volume(const HostBox& b)
+{
+    return b.is2d ? fmul(b.L[0], b.L[1]) : fmul(fmul(b.L[0], b.L[1]), b.L[2]);
+}
+
+// DevBox with the reference's image vectors (NeighborQuery.h:531-560):
+// image(i, j, k) = (float(i) * a1 + float(j) * a2) + float(k) * a3.
+static DevBox make_devbox(const HostBox& h)
+{
+    DevBox d;
+    for (int a = 0; a < 3; ++a)
+    {
+        d.L[a] = h.L[a];
+        d.lo[a] = -(fdiv(h.L[a], 2.0f));
+    }
+    d.xy = h.xy;
+    d.xz = h.xz;
+    d.yz = h.yz;
+    d.is2d = h.is2d ? 1 : 0;
+    const float a1[3] = {h.L[0], 0.0f, 0.0f};
+    const float a2[3] = {fmul(h.L[1], h.xy), h.L[1], 0.0f};
+    float a3[3] = {0.0f, 0.0f, 0.0f};
+    if (!h.is2d)
+    {
+        a3[0] = fmul(h.L[2], h.xz);
+        a3[1] = fmul(h.L[2], h.yz);
+        a3[2] = h.L[2];
+    }
+    for (int i = -1; i <= 1; ++i)
+    {
+        for (int j = -1; j <= 1; ++j)
+        {
+            for (int k = -1; k <= 1; ++k)
+            {
+                const int code = (i + 1) * 9 + (j + 1) * 3 + (k + 1);
+                for (int c = 0; c < 3; ++c)
+                {
+                    d.img[code][c] = fadd(fadd(fmul(static_cast<float>(i), a1[c]), fmul(static_cast<float>(j), a2[c])),
+                                          fmul(static_cast<float>(k), a3[c]));
+                }
+            }
+        }
+    }
+    return d;
+}
+
+} // namespace fg
+
+using namespace fg;
+
+// ---------------------------------------------------------------------------
+// Opaque handles
+// ---------------------------------------------------------------------------
+struct GridEntry
+{
+    int dim[3];
+    int ncell;
+    DevBuf start, cpos, cidx;
+};
+
+struct fg_nq
+{
+    HostBox box;
+    DevBox dbox;
+    int kind;
+    float cell_width;
+    uint32_t n;
+    const float* dpts;
+    DevBuf own;
+    std::vector<std::unique_ptr<GridEntry>> grids;
+};
+
+struct fg_nlist
+{
+    uint64_t nb = 0;
+    uint32_t nq = 0, np = 0;
+    DevBuf ij, dist, vec, weights; // weights empty => all 1
+    bool unit_weights = true;
+    DevBuf seg, cnt;
+    bool seg_valid = false;
+};
+
+struct fg_rdf
+{
+    uint32_t bins;
+    float r_max, r_min;
+    int finite_size = 0;
+    DevBuf hist;
+    HostBox box {};
+    uint32_t frames = 0, n_points = 0, n_query = 0;
+};
+
+struct fg_steinhardt
+{
+    std::vector<uint32_t> ls;
+    bool average, wl, weighted, wl_normalize;
+    uint32_t n = 0;
+    StLs st {};
+    size_t stride = 0; // sum of (2l + 1)
+    DevBuf qlm, qlm_ave, ql, ql_ave, wlv, sys;
+    std::vector<DevBuf> w3j;
+    std::vector<float> order;
+    bool computed = false;
+};
+
+namespace {
+
+// Runs f, mapping exceptions to status codes.
+template<typename F> fg_status guard(F&& f)
+{
+    try
+    {
+        f();
+        return FG_OK;
+    }
+    catch (const Error& e)
+    {
+        g_last_error = e.what();
+        return e.code;
+    }
+    catch (const std::bad_alloc&)
+    {
+        g_last_error = "host allocation failed";
+        return FG_ERR_MEMORY;
+    }
+    catch (const std::exception& e)
+    {
+        g_last_error = e.what();
+        return FG_ERR_RUNTIME;
+    }
+}
+
+void require(const void* p, const char* what)
+{
+    if (p == nullptr)
+    {
+        value_error(std::string(what) + " must not be NULL");
+    }
+}
+
+// Grid dims for a minimum cell width (nearest-plane distances / width, at least 1;
+// 2D boxes are one cell deep). The grid is coarsened to at most ~2 cells per point.
+void grid_dims(const HostBox& b, float width, uint32_t n, int dim[3])
+{
+    float pd[3];
+    nearest_plane(b, pd);
+    for (int a = 0; a < 3; ++a)
+    {
+        double d = std::floor(static_cast<double>(pd[a]) / static_cast<double>(width));
+        if (!(d >= 1.0))
+            d = 1.0;
+        if (d > 2048.0)
+            d = 2048.0;
+        dim[a] = static_cast<int>(d);
+    }
+    if (b.is2d)
+        dim[2] = 1;
+    const double limit = 2.0 * n + 64.0;
+    while (static_cast<double>(dim[0]) * dim[1] * dim[2] > limit)
+    {
+        for (int a = 0; a < (b.is2d ? 2 : 3); ++a)
+            dim[a] = dim[a] > 1 ? (dim[a] * 3) / 4 : 1;
+    }
+}
+
+// Builds (or reuses) the cell-sorted view of a point set for the given dims.
+void build_grid(const DevBox& db, const float* dpts, uint32_t n, const int dim[3], GridEntry& g)
+{
+    cudaStream_t s = stream();
+    g.dim[0] = dim[0];
+    g.dim[1] = dim[1];
+    g.dim[2] = dim[2];
+    g.ncell = dim[0] * dim[1] * dim[2];
+    DevBuf cell_of, rank, counts, scratch;
+    cell_of.alloc(sizeof(uint32_t) * n);
+    rank.alloc(sizeof(uint32_t) * n);
+    counts.alloc(sizeof(uint32_t) * (g.ncell + 1));
+    g.start.alloc(sizeof(uint32_t) * (g.ncell + 1));
+    g.cpos.alloc(sizeof(float4) * n);
+    g.cidx.alloc(sizeof(uint32_t) * n);
+    scratch.alloc(scan_scratch_bytes(g.ncell + 1));
+    FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (g.ncell + 1), s));
+    launch_assign(db, dpts, n, dim, cell_of.as<uint32_t>(), rank.as<uint32_t>(), counts.as<uint32_t>(), s);
+    scan_u32_to_u32(counts.as<uint32_t>(), g.start.as<uint32_t>(), g.ncell + 1, scratch.p, s);
+    launch_scatter(db, dpts, n, cell_of.as<uint32_t>(), rank.as<uint32_t>(), g.start.as<uint32_t>(), g.cpos.as<float4>(),
+                   g.cidx.as<uint32_t>(), s);
+    FG_CUDA(cudaGetLastError());
+}
+
+GridEntry& nq_grid(fg_nq* nq, const int dim[3])
+{
+    for (auto& g : nq->grids)
+    {
+        if (g->dim[0] == dim[0] && g->dim[1] == dim[1] && g->dim[2] == dim[2])
+            return *g;
+    }
+    if (nq->grids.size() >= 4)
+        nq->grids.erase(nq->grids.begin());
+    nq->grids.push_back(std::make_unique<GridEntry>());
+    build_grid(nq->dbox, nq->dpts, nq->n, dim, *nq->grids.back());
+    return *nq->grids.back();
+}
+
+DevGrid view(const GridEntry& g)
+{
+    DevGrid d;
+    d.dim[0] = g.dim[0];
+    d.dim[1] = g.dim[1];
+    d.dim[2] = g.dim[2];
+    d.ncell = g.ncell;
+    d.start = g.start.as<uint32_t>();
+    d.cpos = g.cpos.as<float4>();
+    d.cidx = g.cidx.as<uint32_t>();
+    return d;
+}
+
+// QueryArgs validation and mode inference (NeighborQuery.h:195-228, 278-292).
+void validate_args(fg_query_args& a)
+{
+    if (a.mode == FG_MODE_NONE)
+    {
+        if (a.num_neighbors != 0xffffffffu)
+            a.mode = FG_MODE_NEAREST;
+        else if (a.r_max != -1.0f)
+            a.mode = FG_MODE_BALL;
+    }
+    if (a.mode == FG_MODE_BALL)
+    {
+        if (a.r_max == -1.0f)
+            runtime_error("You must set r_max in the query arguments when performing ball queries.");
+        if (a.num_neighbors != 0xffffffffu)
+            runtime_error("You cannot set num_neighbors in the query arguments when performing ball queries.");
+    }
+    else if (a.mode == FG_MODE_NEAREST)
+    {
+        if (a.num_neighbors == 0xffffffffu)
+            runtime_error("You must set num_neighbors in the query arguments when performing number of neighbor "
+                          "queries.");
+        if (a.r_max == -1.0f)
+            a.r_max = std::numeric_limits<float>::infinity();
+    }
+    else
+    {
+        runtime_error("Unknown mode");
+    }
+    // per-point iterator checks (NeighborQuery.h:315-329)
+    if (a.r_max <= 0.0f)
+        value_error("NeighborQuery requires r_max to be positive.");
+    if (a.r_max <= a.r_min)
+        value_error("NeighborQuery requires that r_max must be greater than r_min.");
+}
+
+void check_periodic(const HostBox& b)
+{
+    if (!(b.periodic[0] && b.periodic[1] && b.periodic[2]))
+        throw Error(FG_ERR_VALUE, "Pair queries in a non-periodic box are not implemented.");
+}
+
+// The sorted query set: the object's own cell-sorted points, or the query points
+// sorted into a grid with the same dims.
+struct QuerySet
+{
+    const float4* qpos;
+    const uint32_t* qidx;
+    GridEntry own;
+};
+
+void make_query_set(fg_nq* nq, const GridEntry& g, const float* dq, uint32_t nqp, QuerySet& qs)
+{
+    if (dq == nullptr)
+    {
+        qs.qpos = g.cpos.as<float4>();
+        qs.qidx = g.cidx.as<uint32_t>();
+        return;
+    }
+    build_grid(nq->dbox, dq, nqp, g.dim, qs.own);
+    qs.qpos = qs.own.cpos.as<float4>();
+    qs.qidx = qs.own.cidx.as<uint32_t>();
+}
+
+// Ball query -> NeighborList in reference order (count, scan, emit).
+void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a, int by_distance, fg_nlist& out)
+{
+    cudaStream_t s = stream();
+    const int arith = nq->kind == FG_NQ_LINKCELL ? ARITH_WRAP : ARITH_AABB;
+    if (arith == ARITH_AABB)
+    {
+        // updateImageVectors(r_max, true), NeighborQuery.h:504-509
+        float pd[3];
+        nearest_plane(nq->box, pd);
+        if (pd[0] <= a.r_max * 2.0 || pd[1] <= a.r_max * 2.0 || (!nq->box.is2d && pd[2] <= a.r_max * 2.0))
+            runtime_error("The AABBQuery r_max is too large for this box.");
+    }
+    int dim[3];
+    grid_dims(nq->box, a.r_max * (1.0f + 1e-5f), nq->n, dim);
+    GridEntry& g = nq_grid(nq, dim);
+    QuerySet qs;
+    make_query_set(nq, g, dq, nqp, qs);
+    BallParams p;
+    p.r_max_sq = fmul(a.r_max, a.r_max);
+    p.r_min_sq = fmul(a.r_min, a.r_min);
+    p.exclude_ii = a.exclude_ii;
+    p.arith = arith;
+    p.nq = nqp;
+    DevBuf counts, offsets, scratch, heavy, heavy_n;
+    counts.alloc(sizeof(uint32_t) * (nqp + 1));
+    offsets.alloc(sizeof(uint64_t) * (nqp + 1));
+    scratch.alloc(scan_scratch_bytes(nqp + 1));
+    FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (nqp + 1), s));
+    reset_dev_err();
+    launch_ball_count(nq->dbox, view(g), qs.qpos, qs.qidx, p, counts.as<uint32_t>(), s);
+    scan_u32_to_u64(counts.as<uint32_t>(), offsets.as<uint64_t>(), nqp + 1, scratch.p, s);
+    uint64_t total = 0;
+    FG_CUDA(cudaMemcpyAsync(&total, offsets.as<uint64_t>() + nqp, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    sync();
+    if (total > 0xffffffffull)
+        runtime_error("The query produced more than 2^32 - 1 bonds, beyond what a NeighborList can index.");
+    out.nb = total;
+    out.nq = nqp;
+    out.np = nq->n;
+    out.ij.alloc(sizeof(uint2) * total);
+    out.dist.alloc(sizeof(float) * total);
+    out.vec.alloc(sizeof(float) * 3 * total);
+    out.unit_weights = true;
+    out.seg_valid = false;
+    heavy.alloc(sizeof(uint32_t) * (nqp + 1));
+    heavy_n.alloc(sizeof(uint32_t));
+    FG_CUDA(cudaMemsetAsync(heavy_n.p, 0, sizeof(uint32_t), s));
+    launch_ball_emit(nq->dbox, view(g), qs.qpos, qs.qidx, p, counts.as<uint32_t>(), offsets.as<uint64_t>(), by_distance,
+                     out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(), heavy.as<uint32_t>(),
+                     heavy_n.as<uint32_t>(), dev_err(), s);
+    uint32_t nh = 0;
+    FG_CUDA(cudaMemcpyAsync(&nh, heavy_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    sync();
+    launch_ball_emit_heavy(nq->dbox, view(g), qs.qpos, qs.qidx, p, counts.as<uint32_t>(), offsets.as<uint64_t>(),
+                           by_distance, heavy.as<uint32_t>(), nh, out.ij.as<uint2>(), out.dist.as<float>(),
+                           out.vec.as<float>(), dev_err(), s);
+    FG_CUDA(cudaGetLastError());
+    check_dev_err("ball query");
+    // keep the counts as the list's segment counts
+    out.cnt = std::move(counts);
+    out.seg.alloc(sizeof(uint32_t) * nqp);
+    // segments = offsets (first bond of each query; 0 for empty queries after the reference's rule)
+    launch_segments(out.ij.as<uint2>(), out.nb, nqp, out.seg.as<uint32_t>(), out.cnt.as<uint32_t>(), s);
+    out.seg_valid = true;
+}
+
+// kNN query -> NeighborList (AABBQuery.cc:152-281 / LinkCell.cc:575-679).
+void knn_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a, int by_distance, fg_nlist& out)
+{
+    cudaStream_t s = stream();
+    const int arith = nq->kind == FG_NQ_LINKCELL ? ARITH_WRAP : ARITH_AABB;
+    if (arith == ARITH_AABB)
+    {
+        // validateNearestNeighborArgs (NeighborQuery.h:235-270)
+        if (a.scale != -1.0f && a.scale <= 1.0f)
+            runtime_error("The scale query argument must be greater than 1.");
+    }
+    const uint32_t k = a.num_neighbors;
+    // cell width ~1.5x the expected k-th neighbour distance (or r_max when smaller)
+    const double vol = box_volume(nq->box);
+    const double per = vol / std::max<uint32_t>(nq->n, 1) * std::max<uint32_t>(k, 1);
+    double rk = nq->box.is2d ? std::sqrt(per / M_PI) : std::cbrt(3.0 * per / (4.0 * M_PI));
+    double width = 1.5 * rk;
+    if (std::isfinite(a.r_max) && a.r_max * (1.0 + 1e-5) < width)
+    {
+        width = a.r_max * (1.0 + 1e-5);
+    }
+    int dim[3];
+    grid_dims(nq->box, static_cast<float>(width), nq->n, dim);
+    GridEntry& g = nq_grid(nq, dim);
+    QuerySet qs;
+    make_query_set(nq, g, dq, nqp, qs);
+    float pd[3];
+    nearest_plane(nq->box, pd);
+    float covered = std::numeric_limits<float>::infinity();
+    for (int ax = 0; ax < (nq->box.is2d ? 2 : 3); ++ax)
+    {
+        if (dim[ax] >= 3)
+            covered = std::min(covered, static_cast<float>(static_cast<double>(pd[ax]) / dim[ax] * (1.0 - 1e-5)));
+    }
+    KnnParams p;
+    p.r_max_sq = fmul(a.r_max, a.r_max);
+    p.r_min = a.r_min;
+    p.r_min_sq = fmul(a.r_min, a.r_min);
+    p.exclude_ii = a.exclude_ii;
+    p.arith = arith;
+    p.k = k;
+    p.nq = nqp;
+    p.covered = covered;
+    DevBuf tj, td, tv, counts, offsets, scratch, fail, fail_n;
+    const size_t rows = static_cast<size_t>(nqp) * std::max<uint32_t>(k, 1);
+    tj.alloc(sizeof(uint32_t) * rows);
+    td.alloc(sizeof(float) * rows);
+    tv.alloc(sizeof(float) * 3 * rows);
+    counts.alloc(sizeof(uint32_t) * (nqp + 1));
+    offsets.alloc(sizeof(uint64_t) * (nqp + 1));
+    scratch.alloc(scan_scratch_bytes(nqp + 1));
+    fail.alloc(sizeof(uint32_t) * (nqp + 1));
+    fail_n.alloc(sizeof(uint32_t));
+    FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (nqp + 1), s));
+    FG_CUDA(cudaMemsetAsync(fail_n.p, 0, sizeof(uint32_t), s));
+    reset_dev_err();
+    uint32_t nfail = 0;
+    if (k == 0)
+    {
+        // nothing to find
+    }
+    else if (k <= 32)
+    {
+        launch_knn_warp(nq->dbox, view(g), qs.qpos, qs.qidx, p, tj.as<uint32_t>(), td.as<float>(), tv.as<float>(),
+                        counts.as<uint32_t>(), fail.as<uint32_t>(), fail_n.as<uint32_t>(), s);
+        FG_CUDA(cudaMemcpyAsync(&nfail, fail_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        sync();
+    }
+    else
+    {
+        std::vector<uint32_t> all(nqp);
+        for (uint32_t t = 0; t < nqp; ++t)
+            all[t] = t;
+        FG_CUDA(cudaMemcpyAsync(fail.p, all.data(), sizeof(uint32_t) * nqp, cudaMemcpyHostToDevice, s));
+        nfail = nqp;
+    }
+    if (nfail > 0)
+    {
+        launch_knn_block(nq->dbox, g.cpos.as<float4>(), g.cidx.as<uint32_t>(), nq->n, qs.qpos, qs.qidx, p,
+                         fail.as<uint32_t>(), nfail, tj.as<uint32_t>(), td.as<float>(), tv.as<float>(),
+                         counts.as<uint32_t>(), dev_err(), s);
+    }
+    FG_CUDA(cudaGetLastError());
+    scan_u32_to_u64(counts.as<uint32_t>(), offsets.as<uint64_t>(), nqp + 1, scratch.p, s);
+    uint64_t total = 0;
+    FG_CUDA(cudaMemcpyAsync(&total, offsets.as<uint64_t>() + nqp, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    check_dev_err("nearest-neighbour query");
+    out.nb = total;
+    out.nq = nqp;
+    out.np = nq->n;
+    out.ij.alloc(sizeof(uint2) * total);
+    out.dist.alloc(sizeof(float) * total);
+    out.vec.alloc(sizeof(float) * 3 * total);
+    out.unit_weights = true;
+    launch_knn_compact(tj.as<uint32_t>(), td.as<float>(), tv.as<float>(), std::max<uint32_t>(k, 1), nqp,
+                       counts.as<uint32_t>(), offsets.as<uint64_t>(), by_distance, out.ij.as<uint2>(),
+                       out.dist.as<float>(), out.vec.as<float>(), s);
+    out.cnt = std::move(counts);
+    out.seg.alloc(sizeof(uint32_t) * nqp);
+    launch_segments(out.ij.as<uint2>(), out.nb, nqp, out.seg.as<uint32_t>(), out.cnt.as<uint32_t>(), s);
+    out.seg_valid = true;
+    FG_CUDA(cudaGetLastError());
+    sync();
+}
+
+void run_query(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args* args, int by_distance, fg_nlist& out)
+{
+    fg_query_args a = *args;
+    if (nq->kind != FG_NQ_RAWPOINTS)
+        check_periodic(nq->box);
+    validate_args(a);
+    if (a.mode == FG_MODE_BALL)
+        ball_nlist(nq, dq, nqp, a, by_distance, out);
+    else
+        knn_nlist(nq, dq, nqp, a, by_distance, out);
+}
+
+void ensure_segments(const fg_nlist* cnl)
+{
+    auto* nl = const_cast<fg_nlist*>(cnl);
+    if (nl->seg_valid)
+        return;
+    nl->seg.alloc(sizeof(uint32_t) * std::max<uint32_t>(nl->nq, 1));
+    nl->cnt.alloc(sizeof(uint32_t) * (std::max<uint32_t>(nl->nq, 1) + 1));
+    launch_segments(nl->ij.as<uint2>(), nl->nb, nl->nq, nl->seg.as<uint32_t>(), nl->cnt.as<uint32_t>(), stream());
+    FG_CUDA(cudaGetLastError());
+    nl->seg_valid = true;
+}
+
+// Copies host points to a device buffer (N x 3 float32).
+void upload_points(const float* host, uint32_t n, DevBuf& buf)
+{
+    buf.alloc(sizeof(float) * 3 * static_cast<size_t>(n));
+    if (n > 0)
+        FG_CUDA(cudaMemcpyAsync(buf.p, host, sizeof(float) * 3 * static_cast<size_t>(n), cudaMemcpyHostToDevice,
+                                stream()));
+}
+
+void nq_init(fg_nq* nq, const fg_box* box, uint32_t n, int kind, float cell_width, const float* host_pts_for_check)
+{
+    if (kind < FG_NQ_RAWPOINTS || kind > FG_NQ_LINKCELL)
+        value_error("unknown neighbour-query kind");
+    if (n == 0)
+        value_error("Cannot create a NeighborQuery with 0 particles.");
+    nq->box = to_host_box(box);
+    nq->dbox = make_devbox(nq->box);
+    nq->kind = kind;
+    nq->n = n;
+    if (nq->box.is2d && host_pts_for_check != nullptr)
+    {
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            if (std::abs(host_pts_for_check[3 * static_cast<size_t>(i) + 2]) > 1e-6)
+                value_error("A point with z != 0 was provided in a 2D box.");
+        }
+    }
+    nq->cell_width = cell_width;
+    if (kind == FG_NQ_LINKCELL)
+    {
+        // LinkCell.cc:222-260
+        if (cell_width == 0.0f)
+        {
+            const uint32_t desired = std::max<uint32_t>(n / 10u, 1u);
+            nq->cell_width = std::cbrt(fdiv(box_volume(nq->box), static_cast<float>(desired)));
+        }
+        float pd[3];
+        nearest_plane(nq->box, pd);
+        const double w2 = nq->cell_width * 2.0;
+        if (w2 > pd[0] || w2 > pd[1] || (!nq->box.is2d && w2 > pd[2]))
+            runtime_error("Cannot generate a cell list where cell_width is larger than half the box.");
+    }
+}
+
+// Wigner 3j symbol (l l l; m1 m2 m3) by the Racah formula (long double factorials).
+double wigner3j(int l, int m1, int m2, int m3)
+{
+    if (m1 + m2 + m3 != 0)
+        return 0.0;
+    auto lf = [](int x) { return std::lgamma(static_cast<long double>(x) + 1.0L); };
+    const long double tri = 0.5L * (lf(l) + lf(l) + lf(l) - lf(3 * l + 1));
+    const long double pre = 0.5L * (lf(l + m1) + lf(l - m1) + lf(l + m2) + lf(l - m2) + lf(l + m3) + lf(l - m3));
+    const int kmin = std::max(0, std::max(-m1, m2));
+    const int kmax = std::min(l, std::min(l - m1, l + m2));
+    long double sum = 0.0L;
+    for (int kk = kmin; kk <= kmax; ++kk)
+    {
+        const long double lt = lf(kk) + lf(l - kk) + lf(l - m1 - kk) + lf(l + m2 - kk) + lf(m1 + kk) + lf(kk - m2);
+        const long double term = std::exp(tri + pre - lt);
+        sum += (kk % 2) ? -term : term;
+    }
+    const int ph = -m3;
+    return static_cast<double>(((ph % 2) != 0 ? -1.0L : 1.0L) * sum);
+}
+
+// Coefficients in the reference's iteration order (Wigner3j.cc:40-54).
+std::vector<double> wigner3j_table(int l)
+{
+    std::vector<double> v;
+    for (int m1 = -l; m1 <= l; ++m1)
+    {
+        for (int m2 = std::max(-l - m1, -l); m2 <= std::min(l - m1, l); ++m2)
+            v.push_back(wigner3j(l, m1, m2, -m1 - m2));
+    }
+    return v;
+}
+
+double reduce_w3j_host(const double* q, int l, const std::vector<double>& w)
+{
+    auto idx = [l](int m) { return m < 0 ? l - m : m; };
+    double res = 0.0;
+    size_t c = 0;
+    for (int m1 = -l; m1 <= l; ++m1)
+    {
+        for (int m2 = std::max(-l - m1, -l); m2 <= std::min(l - m1, l); ++m2, ++c)
+        {
+            const int m3 = -m1 - m2;
+            const double* a = q + 2 * idx(m1);
+            const double* b = q + 2 * idx(m2);
+            const double* cc = q + 2 * idx(m3);
+            const double abr = a[0] * b[0] - a[1] * b[1];
+            const double abi = a[0] * b[1] + a[1] * b[0];
+            res += w[c] * (abr * cc[0] - abi * cc[1]);
+        }
+    }
+    return res;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* fg_last_error(void)
+{
+    return g_last_error.c_str();
+}
+
+int fg_version(void)
+{
+    return 1;
+}
+
+fg_status fg_set_stream(void* cuda_stream)
+{
+    return guard([&] {
+        g_user_stream = static_cast<cudaStream_t>(cuda_stream);
+        g_user_stream_set = cuda_stream != nullptr;
+    });
+}
+
+// ---- NeighborQuery ----------------------------------------------------------------
+fg_status fg_nq_create(const fg_box* box, const float* points, uint32_t n, int kind, float cell_width, fg_nq** out)
+{
+    return guard([&] {
+        require(box, "box");
+        require(out, "out");
+        if (n > 0)
+            require(points, "points");
+        auto nq = std::make_unique<fg_nq>();
+        nq_init(nq.get(), box, n, kind, cell_width, points);
+        upload_points(points, n, nq->own);
+        nq->dpts = nq->own.as<float>();
+        sync();
+        *out = nq.release();
+    });
+}
+
+fg_status fg_nq_create_device(const fg_box* box, const float* device_points, uint32_t n, int kind, float cell_width,
+                              fg_nq** out)
+{
+    return guard([&] {
+        require(box, "box");
+        require(out, "out");
+        if (n > 0)
+            require(device_points, "device_points");
+        auto nq = std::make_unique<fg_nq>();
+        nq_init(nq.get(), box, n, kind, cell_width, nullptr);
+        nq->dpts = device_points;
+        *out = nq.release();
+    });
+}
+
+fg_status fg_nq_destroy(fg_nq* nq)
+{
+    return guard([&] {
+        delete nq;
+        sync();
+    });
+}
+
+fg_status fg_nq_cell_width(const fg_nq* nq, float* out)
+{
+    return guard([&] {
+        require(nq, "nq");
+        *out = nq->cell_width;
+    });
+}
+
+fg_status fg_nq_num_points(const fg_nq* nq, uint32_t* out)
+{
+    return guard([&] {
+        require(nq, "nq");
+        *out = nq->n;
+    });
+}
+
+fg_status fg_nq_query(fg_nq* nq, const float* query_points, uint32_t n_query, const fg_query_args* args,
+                      int sort_by_distance, fg_nlist** out)
+{
+    return guard([&] {
+        require(nq, "nq");
+        require(args, "args");
+        require(out, "out");
+        DevBuf dq;
+        const float* qp = nullptr;
+        uint32_t nqp = nq->n;
+        if (query_points != nullptr)
+        {
+            upload_points(query_points, n_query, dq);
+            qp = dq.as<float>();
+            nqp = n_query;
+        }
+        auto nl = std::make_unique<fg_nlist>();
+        run_query(nq, qp, nqp, args, sort_by_distance, *nl);
+        sync();
+        *out = nl.release();
+    });
+}
+
+fg_status fg_nq_query_device(fg_nq* nq, const float* device_query_points, uint32_t n_query, const fg_query_args* args,
+                             int sort_by_distance, fg_nlist** out)
+{
+    return guard([&] {
+        require(nq, "nq");
+        require(args, "args");
+        require(out, "out");
+        auto nl = std::make_unique<fg_nlist>();
+        run_query(nq, device_query_points, device_query_points ? n_query : nq->n, args, sort_by_distance, *nl);
+        sync();
+        *out = nl.release();
+    });
+}
+
+// ---- NeighborList -------------------------------------------------------------------
+fg_status fg_nlist_from_arrays(uint64_t num_bonds, const uint32_t* qi, uint32_t num_query_points, const uint32_t* pi,
+                               uint32_t num_points, const float* vectors, const float* weights, fg_nlist** out)
+{
+    return guard([&] {
+        require(out, "out");
+        if (num_bonds > 0)
+        {
+            require(qi, "query_point_indices");
+            require(pi, "point_indices");
+            require(vectors, "vectors");
+        }
+        // NeighborList.cc:62-80
+        uint32_t last = 0;
+        for (uint64_t b = 0; b < num_bonds; ++b)
+        {
+            if (qi[b] < last)
+                value_error("NeighborList query_point_index must be sorted.");
+            if (qi[b] >= num_query_points)
+                value_error("NeighborList query_point_index values must be less than num_query_points.");
+            if (pi[b] >= num_points)
+                value_error("NeighborList point_index values must be less than num_points.");
+            last = qi[b];
+        }
+        cudaStream_t s = stream();
+        auto nl = std::make_unique<fg_nlist>();
+        nl->nb = num_bonds;
+        nl->nq = num_query_points;
+        nl->np = num_points;
+        DevBuf dqi, dpi;
+        dqi.alloc(sizeof(uint32_t) * num_bonds);
+        dpi.alloc(sizeof(uint32_t) * num_bonds);
+        nl->ij.alloc(sizeof(uint2) * num_bonds);
+        nl->dist.alloc(sizeof(float) * num_bonds);
+        nl->vec.alloc(sizeof(float) * 3 * num_bonds);
+        if (num_bonds > 0)
+        {
+            FG_CUDA(cudaMemcpyAsync(dqi.p, qi, sizeof(uint32_t) * num_bonds, cudaMemcpyHostToDevice, s));
+            FG_CUDA(cudaMemcpyAsync(dpi.p, pi, sizeof(uint32_t) * num_bonds, cudaMemcpyHostToDevice, s));
+            FG_CUDA(cudaMemcpyAsync(nl->vec.p, vectors, sizeof(float) * 3 * num_bonds, cudaMemcpyHostToDevice, s));
+        }
+        launch_from_arrays(dqi.as<uint32_t>(), dpi.as<uint32_t>(), nl->vec.as<float>(), num_bonds, nl->ij.as<uint2>(),
+                           nl->dist.as<float>(), s);
+        nl->unit_weights = true;
+        if (weights != nullptr)
+        {
+            bool all_one = true;
+            for (uint64_t b = 0; b < num_bonds; ++b)
+            {
+                if (weights[b] != 1.0f)
+                {
+                    all_one = false;
+                    break;
+                }
+            }
+            if (!all_one)
+            {
+                nl->unit_weights = false;
+                nl->weights.alloc(sizeof(float) * num_bonds);
+                FG_CUDA(cudaMemcpyAsync(nl->weights.p, weights, sizeof(float) * num_bonds, cudaMemcpyHostToDevice, s));
+            }
+        }
+        FG_CUDA(cudaGetLastError());
+        sync();
+        *out = nl.release();
+    });
+}
+
+fg_status fg_nlist_all_pairs(const fg_box* box, const float* points, uint32_t num_points, const float* query_points,
+                             uint32_t num_query_points, int exclude_ii, fg_nlist** out)
+{
+    return guard([&] {
+        require(box, "box");
+        require(out, "out");
+        const HostBox hb = to_host_box(box);
+        const DevBox db = make_devbox(hb);
+        const uint64_t nii = exclude_ii ? std::min(num_points, num_query_points) : 0u;
+        const uint64_t nb = static_cast<uint64_t>(num_points) * num_query_points - nii;
+        DevBuf dp, dq;
+        upload_points(points, num_points, dp);
+        upload_points(query_points, num_query_points, dq);
+        auto nl = std::make_unique<fg_nlist>();
+        nl->nb = nb;
+        nl->nq = num_query_points;
+        nl->np = num_points;
+        nl->ij.alloc(sizeof(uint2) * nb);
+        nl->dist.alloc(sizeof(float) * nb);
+        nl->vec.alloc(sizeof(float) * 3 * nb);
+        launch_all_pairs(db, dp.as<float>(), num_points, dq.as<float>(), num_query_points, exclude_ii, nb,
+                         nl->ij.as<uint2>(), nl->dist.as<float>(), nl->vec.as<float>(), stream());
+        FG_CUDA(cudaGetLastError());
+        sync();
+        *out = nl.release();
+    });
+}
+
+fg_status fg_nlist_destroy(fg_nlist* nl)
+{
+    return guard([&] {
+        delete nl;
+        sync();
+    });
+}
+
+fg_status fg_nlist_copy(const fg_nlist* src, fg_nlist** out)
+{
+    return guard([&] {
+        require(src, "src");
+        require(out, "out");
+        cudaStream_t s = stream();
+        auto nl = std::make_unique<fg_nlist>();
+        nl->nb = src->nb;
+        nl->nq = src->nq;
+        nl->np = src->np;
+        nl->unit_weights = src->unit_weights;
+        nl->ij.alloc(sizeof(uint2) * src->nb);
+        nl->dist.alloc(sizeof(float) * src->nb);
+        nl->vec.alloc(sizeof(float) * 3 * src->nb);
+        if (src->nb > 0)
+        {
+            FG_CUDA(cudaMemcpyAsync(nl->ij.p, src->ij.p, sizeof(uint2) * src->nb, cudaMemcpyDeviceToDevice, s));
+            FG_CUDA(cudaMemcpyAsync(nl->dist.p, src->dist.p, sizeof(float) * src->nb, cudaMemcpyDeviceToDevice, s));
+            FG_CUDA(cudaMemcpyAsync(nl->vec.p, src->vec.p, sizeof(float) * 3 * src->nb, cudaMemcpyDeviceToDevice, s));
+            if (!src->unit_weights)
+            {
+                nl->weights.alloc(sizeof(float) * src->nb);
+                FG_CUDA(cudaMemcpyAsync(nl->weights.p, src->weights.p, sizeof(float) * src->nb,
+                                        cudaMemcpyDeviceToDevice, s));
+            }
+        }
+        sync();
+        *out = nl.release();
+    });
+}
+
+fg_status fg_nlist_num_bonds(const fg_nlist* nl, uint64_t* out)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        *out = nl->nb;
+    });
+}
+
+fg_status fg_nlist_num_query_points(const fg_nlist* nl, uint32_t* out)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        *out = nl->nq;
+    });
+}
+
+fg_status fg_nlist_num_points(const fg_nlist* nl, uint32_t* out)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        *out = nl->np;
+    });
+}
+
+fg_status fg_nlist_get(const fg_nlist* nl, uint32_t* neighbors, float* distances, float* weights, float* vectors)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        cudaStream_t s = stream();
+        if (nl->nb == 0)
+            return;
+        if (neighbors != nullptr)
+            FG_CUDA(cudaMemcpyAsync(neighbors, nl->ij.p, sizeof(uint2) * nl->nb, cudaMemcpyDeviceToHost, s));
+        if (distances != nullptr)
+            FG_CUDA(cudaMemcpyAsync(distances, nl->dist.p, sizeof(float) * nl->nb, cudaMemcpyDeviceToHost, s));
+        if (vectors != nullptr)
+            FG_CUDA(cudaMemcpyAsync(vectors, nl->vec.p, sizeof(float) * 3 * nl->nb, cudaMemcpyDeviceToHost, s));
+        if (weights != nullptr)
+        {
+            if (nl->unit_weights)
+            {
+                for (uint64_t b = 0; b < nl->nb; ++b)
+                    weights[b] = 1.0f;
+            }
+            else
+            {
+                FG_CUDA(cudaMemcpyAsync(weights, nl->weights.p, sizeof(float) * nl->nb, cudaMemcpyDeviceToHost, s));
+            }
+        }
+        sync();
+    });
+}
+
+fg_status fg_nlist_device_arrays(const fg_nlist* nl, const uint32_t** neighbors, const float** distances,
+                                 const float** vectors)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        if (neighbors)
+            *neighbors = nl->ij.as<uint32_t>();
+        if (distances)
+            *distances = nl->dist.as<float>();
+        if (vectors)
+            *vectors = nl->vec.as<float>();
+    });
+}
+
+fg_status fg_nlist_segments(const fg_nlist* nl, uint32_t* segments, uint32_t* counts)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        ensure_segments(nl);
+        cudaStream_t s = stream();
+        if (nl->nq > 0)
+        {
+            if (segments)
+                FG_CUDA(cudaMemcpyAsync(segments, nl->seg.p, sizeof(uint32_t) * nl->nq, cudaMemcpyDeviceToHost, s));
+            if (counts)
+                FG_CUDA(cudaMemcpyAsync(counts, nl->cnt.p, sizeof(uint32_t) * nl->nq, cudaMemcpyDeviceToHost, s));
+        }
+        sync();
+    });
+}
+
+fg_status fg_nlist_find_first_index(const fg_nlist* nl, uint32_t i, uint32_t* out)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        if (nl->nb == 0)
+        {
+            *out = 0;
+            return;
+        }
+        DevBuf r;
+        r.alloc(sizeof(uint64_t));
+        launch_first_index(nl->ij.as<uint2>(), nl->nb, i, r.as<uint64_t>(), stream());
+        uint64_t h = 0;
+        FG_CUDA(cudaMemcpyAsync(&h, r.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream()));
+        sync();
+        *out = static_cast<uint32_t>(h);
+    });
+}
+
+static void nlist_apply_keep(fg_nlist* nl, DevBuf& keep)
+{
+    cudaStream_t s = stream();
+    DevBuf pos, scratch;
+    pos.alloc(sizeof(uint64_t) * (nl->nb + 1));
+    scratch.alloc(scan_scratch_bytes(nl->nb + 1));
+    FG_CUDA(cudaMemsetAsync(keep.as<uint32_t>() + nl->nb, 0, sizeof(uint32_t), s));
+    scan_u32_to_u64(keep.as<uint32_t>(), pos.as<uint64_t>(), nl->nb + 1, scratch.p, s);
+    uint64_t total = 0;
+    FG_CUDA(cudaMemcpyAsync(&total, pos.as<uint64_t>() + nl->nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    sync();
+    fg_nlist tmp;
+    tmp.ij.alloc(sizeof(uint2) * total);
+    tmp.dist.alloc(sizeof(float) * total);
+    tmp.vec.alloc(sizeof(float) * 3 * total);
+    if (!nl->unit_weights)
+        tmp.weights.alloc(sizeof(float) * total);
+    launch_compact(keep.as<uint32_t>(), pos.as<uint64_t>(), nl->nb, nl->ij.as<uint2>(), nl->dist.as<float>(),
+                   nl->unit_weights ? nullptr : nl->weights.as<float>(), nl->vec.as<float>(), tmp.ij.as<uint2>(),
+                   tmp.dist.as<float>(), nl->unit_weights ? nullptr : tmp.weights.as<float>(), tmp.vec.as<float>(), s);
+    FG_CUDA(cudaGetLastError());
+    nl->ij = std::move(tmp.ij);
+    nl->dist = std::move(tmp.dist);
+    nl->vec = std::move(tmp.vec);
+    if (!nl->unit_weights)
+        nl->weights = std::move(tmp.weights);
+    nl->nb = total;
+    nl->seg_valid = false;
+    sync();
+}
+
+fg_status fg_nlist_filter(fg_nlist* nl, const uint8_t* keep_mask)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        if (nl->nb == 0)
+            return;
+        require(keep_mask, "keep");
+        DevBuf u8, keep;
+        u8.alloc(nl->nb);
+        keep.alloc(sizeof(uint32_t) * (nl->nb + 1));
+        FG_CUDA(cudaMemcpyAsync(u8.p, keep_mask, nl->nb, cudaMemcpyHostToDevice, stream()));
+        launch_keep_u8(u8.as<uint8_t>(), nl->nb, keep.as<uint32_t>(), stream());
+        nlist_apply_keep(nl, keep);
+    });
+}
+
+fg_status fg_nlist_filter_r(fg_nlist* nl, float r_max, float r_min)
+{
+    return guard([&] {
+        require(nl, "nlist");
+        if (r_max <= 0.0f)
+            value_error("NeighborList.filter_r requires r_max to be positive.");
+        if (r_min < 0.0f)
+            value_error("NeighborList.filter_r requires r_min to be non-negative.");
+        if (r_max <= r_min)
+            value_error("NeighborList.filter_r requires that r_max must be greater than r_min.");
+        if (nl->nb == 0)
+            return;
+        DevBuf keep;
+        keep.alloc(sizeof(uint32_t) * (nl->nb + 1));
+        launch_keep_r(nl->dist.as<float>(), nl->nb, r_max, r_min, keep.as<uint32_t>(), stream());
+        nlist_apply_keep(nl, keep);
+    });
+}
+
+fg_status fg_nlist_sort(fg_nlist* nl, int by_distance)
+{
+    // NeighborList::sort (NeighborList.cc:371-399): a post-processing utility, done on
+    // the host copy of the bonds.
+    return guard([&] {
+        require(nl, "nlist");
+        const uint64_t nb = nl->nb;
+        if (nb == 0)
+            return;
+        std::vector<uint32_t> ij(2 * nb);
+        std::vector<float> d(nb), w(nb), v(3 * nb);
+        FG_CUDA(cudaMemcpyAsync(ij.data(), nl->ij.p, sizeof(uint2) * nb, cudaMemcpyDeviceToHost, stream()));
+        FG_CUDA(cudaMemcpyAsync(d.data(), nl->dist.p, sizeof(float) * nb, cudaMemcpyDeviceToHost, stream()));
+        FG_CUDA(cudaMemcpyAsync(v.data(), nl->vec.p, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost, stream()));
+        if (!nl->unit_weights)
+            FG_CUDA(cudaMemcpyAsync(w.data(), nl->weights.p, sizeof(float) * nb, cudaMemcpyDeviceToHost, stream()));
+        else
+            std::fill(w.begin(), w.end(), 1.0f);
+        sync();
+        std::vector<uint64_t> idx(nb);
+        for (uint64_t b = 0; b < nb; ++b)
+            idx[b] = b;
+        auto less_tuple = [&](uint64_t a, uint64_t b) {
+            if (ij[2 * a] != ij[2 * b])
+                return ij[2 * a] < ij[2 * b];
+            if (ij[2 * a + 1] != ij[2 * b + 1])
+                return ij[2 * a + 1] < ij[2 * b + 1];
+            if (w[a] != w[b])
+                return w[a] < w[b];
+            return d[a] < d[b];
+        };
+        auto less_dist = [&](uint64_t a, uint64_t b) {
+            if (ij[2 * a] != ij[2 * b])
+                return ij[2 * a] < ij[2 * b];
+            if (d[a] != d[b])
+                return d[a] < d[b];
+            if (ij[2 * a + 1] != ij[2 * b + 1])
+                return ij[2 * a + 1] < ij[2 * b + 1];
+            return w[a] < w[b];
+        };
+        if (by_distance)
+            std::stable_sort(idx.begin(), idx.end(), less_dist);
+        else
+            std::stable_sort(idx.begin(), idx.end(), less_tuple);
+        std::vector<uint32_t> ij2(2 * nb);
+        std::vector<float> d2(nb), w2(nb), v2(3 * nb);
+        for (uint64_t b = 0; b < nb; ++b)
+        {
+            const uint64_t s = idx[b];
+            ij2[2 * b] = ij[2 * s];
+            ij2[2 * b + 1] = ij[2 * s + 1];
+            d2[b] = d[s];
+            w2[b] = w[s];
+            v2[3 * b] = v[3 * s];
+            v2[3 * b + 1] = v[3 * s + 1];
+            v2[3 * b + 2] = v[3 * s + 2];
+        }
+        FG_CUDA(cudaMemcpyAsync(nl->ij.p, ij2.data(), sizeof(uint2) * nb, cudaMemcpyHostToDevice, stream()));
+        FG_CUDA(cudaMemcpyAsync(nl->dist.p, d2.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, stream()));
+        FG_CUDA(cudaMemcpyAsync(nl->vec.p, v2.data(), sizeof(float) * 3 * nb, cudaMemcpyHostToDevice, stream()));
+        if (!nl->unit_weights)
+            FG_CUDA(cudaMemcpyAsync(nl->weights.p, w2.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, stream()));
+        nl->seg_valid = false;
+        sync();
+    });
+}
+
+// ---- RDF ------------------------------------------------------------------------------
+fg_status fg_rdf_create(uint32_t bins, float r_max, float r_min, fg_rdf** out)
+{
+    return guard([&] {
+        require(out, "out");
+        // RDF.cc:27-42
+        if (bins == 0)
+            value_error("RDF requires a nonzero number of bins.");
+        if (r_max <= 0.0f)
+            value_error("RDF requires r_max to be positive.");
+        if (r_min < 0.0f)
+            value_error("RDF requires r_min to be non-negative.");
+        if (r_max <= r_min)
+            value_error("RDF requires that r_max must be greater than r_min.");
+        auto r = std::make_unique<fg_rdf>();
+        r->bins = bins;
+        r->r_max = r_max;
+        r->r_min = r_min;
+        r->hist.alloc(sizeof(unsigned long long) * bins);
+        FG_CUDA(cudaMemsetAsync(r->hist.p, 0, sizeof(unsigned long long) * bins, stream()));
+        sync();
+        *out = r.release();
+    });
+}
+
+fg_status fg_rdf_destroy(fg_rdf* rdf)
+{
+    return guard([&] {
+        delete rdf;
+        sync();
+    });
+}
+
+fg_status fg_rdf_set_mode(fg_rdf* rdf, int finite_size)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        rdf->finite_size = finite_size != 0;
+    });
+}
+
+fg_status fg_rdf_reset(fg_rdf* rdf)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        FG_CUDA(cudaMemsetAsync(rdf->hist.p, 0, sizeof(unsigned long long) * rdf->bins, stream()));
+        rdf->frames = 0;
+        sync();
+    });
+}
+
+static HistParams hist_params(const fg_rdf* r)
+{
+    HistParams h;
+    h.h_min = r->r_min;
+    h.h_max = r->r_max;
+    // Histogram.h:130-131
+    const float bw = fdiv(fsub(r->r_max, r->r_min), static_cast<float>(r->bins));
+    h.h_inv = fdiv(1.0f, bw);
+    h.bins = r->bins;
+    return h;
+}
+
+static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp, const fg_nlist* nlist,
+                           const fg_query_args* args)
+{
+    cudaStream_t s = stream();
+    const HistParams h = hist_params(rdf);
+    if (nlist != nullptr)
+    {
+        launch_hist_distances(nlist->dist.as<float>(), nlist->nb, h, rdf->hist.as<unsigned long long>(), s);
+    }
+    else
+    {
+        require(args, "args");
+        fg_query_args a = *args;
+        if (nq->kind != FG_NQ_RAWPOINTS)
+            check_periodic(nq->box);
+        validate_args(a);
+        if (a.mode == FG_MODE_BALL)
+        {
+            const int arith = nq->kind == FG_NQ_LINKCELL ? ARITH_WRAP : ARITH_AABB;
+            if (arith == ARITH_AABB)
+            {
+                float pd[3];
+                nearest_plane(nq->box, pd);
+                if (pd[0] <= a.r_max * 2.0 || pd[1] <= a.r_max * 2.0 || (!nq->box.is2d && pd[2] <= a.r_max * 2.0))
+                    runtime_error("The AABBQuery r_max is too large for this box.");
+            }
+            int dim[3];
+            grid_dims(nq->box, a.r_max * (1.0f + 1e-5f), nq->n, dim);
+            GridEntry& g = nq_grid(nq, dim);
+            QuerySet qs;
+            make_query_set(nq, g, dq, nqp, qs);
+            BallParams p;
+            p.r_max_sq = fmul(a.r_max, a.r_max);
+            p.r_min_sq = fmul(a.r_min, a.r_min);
+            p.exclude_ii = a.exclude_ii;
+            p.arith = arith;
+            p.nq = nqp;
+            launch_ball_hist(nq->dbox, view(g), qs.qpos, qs.qidx, p, h, rdf->hist.as<unsigned long long>(), s);
+            FG_CUDA(cudaGetLastError());
+            sync();
+        }
+        else
+        {
+            fg_nlist tmp;
+            knn_nlist(nq, dq, nqp, a, 0, tmp);
+            launch_hist_distances(tmp.dist.as<float>(), tmp.nb, h, rdf->hist.as<unsigned long long>(), s);
+            FG_CUDA(cudaGetLastError());
+            sync();
+        }
+    }
+    FG_CUDA(cudaGetLastError());
+    // BondHistogramCompute::accumulateGeneral (BondHistogramCompute.h:115-126)
+    rdf->box = nq->box;
+    rdf->frames += 1;
+    rdf->n_points = nq->n;
+    rdf->n_query = nqp;
+    sync();
+}
+
+fg_status fg_rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* query_points, uint32_t n_query, const fg_nlist* nlist,
+                            const fg_query_args* args)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        require(nq, "nq");
+        DevBuf dq;
+        const float* qp = nullptr;
+        uint32_t nqp = nq->n;
+        if (query_points != nullptr)
+        {
+            upload_points(query_points, n_query, dq);
+            qp = dq.as<float>();
+            nqp = n_query;
+        }
+        rdf_accumulate(rdf, nq, qp, nqp, nlist, args);
+    });
+}
+
+fg_status fg_rdf_accumulate_device(fg_rdf* rdf, fg_nq* nq, const float* device_query_points, uint32_t n_query,
+                                   const fg_nlist* nlist, const fg_query_args* args)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        require(nq, "nq");
+        rdf_accumulate(rdf, nq, device_query_points, device_query_points ? n_query : nq->n, nlist, args);
+    });
+}
+
+static void rdf_edges(const fg_rdf* r, std::vector<float>& edges)
+{
+    // Histogram.h:126-138: edges[i] = min + float(i) * bin_width
+    const float bw = fdiv(fsub(r->r_max, r->r_min), static_cast<float>(r->bins));
+    edges.resize(r->bins + 1);
+    for (uint32_t i = 0; i <= r->bins; ++i)
+        edges[i] = fadd(r->r_min, fmul(static_cast<float>(i), bw));
+}
+
+fg_status fg_rdf_get(fg_rdf* rdf, uint32_t* bin_counts, float* rdf_out, float* n_r)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        std::vector<unsigned long long> h(rdf->bins);
+        FG_CUDA(cudaMemcpyAsync(h.data(), rdf->hist.p, sizeof(unsigned long long) * rdf->bins, cudaMemcpyDeviceToHost,
+                                stream()));
+        sync();
+        std::vector<uint32_t> c(rdf->bins);
+        for (uint32_t i = 0; i < rdf->bins; ++i)
+            c[i] = static_cast<uint32_t>(h[i]); // the reference's unsigned int bins
+        if (bin_counts)
+            std::memcpy(bin_counts, c.data(), sizeof(uint32_t) * rdf->bins);
+        if (rdf_out == nullptr && n_r == nullptr)
+            return;
+        // RDF::reduce in float32 (RDF.cc:52-63, 73-99)
+        std::vector<float> e;
+        rdf_edges(rdf, e);
+        const float volume_prefactor = static_cast<float>((4.0f / 3.0f) * M_PI);
+        const float nqp = static_cast<float>(rdf->n_query);
+        float number_density = fdiv(nqp, box_volume(rdf->box));
+        if (rdf->finite_size)
+            number_density = fmul(number_density, fdiv(static_cast<float>(rdf->n_query - 1), static_cast<float>(rdf->n_query)));
+        const float np = static_cast<float>(rdf->n_points);
+        const float nf = static_cast<float>(rdf->frames);
+        const float prefactor = fdiv(1.0f, fmul(fmul(np, number_density), nf));
+        for (uint32_t i = 0; i < rdf->bins; ++i)
+        {
+            const float r = e[i];
+            const float nr = e[i + 1];
+            float vol;
+            if (rdf->box.is2d)
+                vol = static_cast<float>(M_PI * static_cast<double>(fsub(fmul(nr, nr), fmul(r, r))));
+            else
+                vol = fmul(volume_prefactor, fsub(fmul(fmul(nr, nr), nr), fmul(fmul(r, r), r)));
+            if (rdf_out)
+                rdf_out[i] = fdiv(fmul(static_cast<float>(c[i]), prefactor), vol);
+        }
+        if (n_r)
+        {
+            const float pf2 = fdiv(1.0f, fmul(nqp, static_cast<float>(rdf->frames)));
+            n_r[0] = fmul(static_cast<float>(c[0]), pf2);
+            for (uint32_t i = 1; i < rdf->bins; ++i)
+                n_r[i] = fadd(n_r[i - 1], fmul(static_cast<float>(c[i]), pf2));
+        }
+    });
+}
+
+fg_status fg_rdf_get_u64(fg_rdf* rdf, uint64_t* bin_counts, double* rdf_out, double* n_r)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        std::vector<unsigned long long> h(rdf->bins);
+        FG_CUDA(cudaMemcpyAsync(h.data(), rdf->hist.p, sizeof(unsigned long long) * rdf->bins, cudaMemcpyDeviceToHost,
+                                stream()));
+        sync();
+        if (bin_counts)
+            for (uint32_t i = 0; i < rdf->bins; ++i)
+                bin_counts[i] = h[i];
+        // FP64 normalisation: shell volumes x density x frame count in double
+        const double w = (static_cast<double>(rdf->r_max) - rdf->r_min) / rdf->bins;
+        const double V = rdf->box.is2d ? static_cast<double>(rdf->box.L[0]) * rdf->box.L[1]
+                                       : static_cast<double>(rdf->box.L[0]) * rdf->box.L[1] * rdf->box.L[2];
+        double rho = rdf->n_query / V;
+        if (rdf->finite_size)
+            rho *= (rdf->n_query - 1.0) / rdf->n_query;
+        const double pre = 1.0 / (static_cast<double>(rdf->n_points) * rho * rdf->frames);
+        double acc = 0.0;
+        for (uint32_t i = 0; i < rdf->bins; ++i)
+        {
+            const double r0 = rdf->r_min + i * w;
+            const double r1 = rdf->r_min + (i + 1) * w;
+            const double vol = rdf->box.is2d ? M_PI * (r1 * r1 - r0 * r0) : 4.0 / 3.0 * M_PI * (r1 * r1 * r1 - r0 * r0 * r0);
+            if (rdf_out)
+                rdf_out[i] = static_cast<double>(h[i]) * pre / vol;
+            acc += static_cast<double>(h[i]) / (static_cast<double>(rdf->n_query) * rdf->frames);
+            if (n_r)
+                n_r[i] = acc;
+        }
+    });
+}
+
+fg_status fg_rdf_bin_edges(const fg_rdf* rdf, float* edges, float* centers)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        std::vector<float> e;
+        rdf_edges(rdf, e);
+        if (edges)
+            std::memcpy(edges, e.data(), sizeof(float) * (rdf->bins + 1));
+        if (centers)
+            for (uint32_t i = 0; i < rdf->bins; ++i)
+                centers[i] = fdiv(fadd(e[i], e[i + 1]), 2.0f);
+    });
+}
+
+fg_status fg_rdf_state(const fg_rdf* rdf, fg_box* box, uint32_t* n_frames, uint32_t* n_points, uint32_t* n_query)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        if (box)
+            *box = to_c_box(rdf->box);
+        if (n_frames)
+            *n_frames = rdf->frames;
+        if (n_points)
+            *n_points = rdf->n_points;
+        if (n_query)
+            *n_query = rdf->n_query;
+    });
+}
+
+// ---- Steinhardt ----------------------------------------------------------------------
+fg_status fg_steinhardt_create(const uint32_t* ls, uint32_t n_l, int average, int wl, int weighted, int wl_normalize,
+                               fg_steinhardt** out)
+{
+    return guard([&] {
+        require(out, "out");
+        if (n_l == 0)
+            value_error("At least one l must be specified.");
+        require(ls, "ls");
+        if (n_l > static_cast<uint32_t>(ST_MAX_NL))
+            value_error("at most " + std::to_string(ST_MAX_NL) + " values of l are supported per Steinhardt object");
+        auto st = std::make_unique<fg_steinhardt>();
+        st->ls.assign(ls, ls + n_l);
+        st->average = average != 0;
+        st->wl = wl != 0;
+        st->weighted = weighted != 0;
+        st->wl_normalize = wl_normalize != 0;
+        st->st.nl = static_cast<int>(n_l);
+        st->st.max_l = 0;
+        for (uint32_t k = 0; k < n_l; ++k)
+        {
+            if (ls[k] > static_cast<uint32_t>(ST_MAX_L))
+                value_error("l above " + std::to_string(ST_MAX_L) + " is not supported");
+            st->st.l[k] = static_cast<int>(ls[k]);
+            st->st.max_l = std::max(st->st.max_l, static_cast<int>(ls[k]));
+            st->st.norm[k] = static_cast<float>(4.0 * M_PI / (2 * ls[k] + 1));
+            st->stride += 2 * ls[k] + 1;
+        }
+        st_upload_tables(stream());
+        for (uint32_t k = 0; k < n_l; ++k)
+        {
+            DevBuf b;
+            if (st->wl)
+            {
+                const std::vector<double> w = wigner3j_table(static_cast<int>(ls[k]));
+                std::vector<float> f(w.begin(), w.end());
+                b.alloc(sizeof(float) * f.size());
+                FG_CUDA(cudaMemcpyAsync(b.p, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice, stream()));
+            }
+            st->w3j.push_back(std::move(b));
+        }
+        sync();
+        *out = st.release();
+    });
+}
+
+fg_status fg_steinhardt_destroy(fg_steinhardt* st)
+{
+    return guard([&] {
+        delete st;
+        sync();
+    });
+}
+
+fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nlist, const fg_query_args* args)
+{
+    return guard([&] {
+        require(st, "steinhardt");
+        require(nq, "nq");
+        cudaStream_t s = stream();
+        fg_nlist own;
+        const fg_nlist* nl = nlist;
+        if (nl == nullptr)
+        {
+            require(args, "args");
+            run_query(nq, nullptr, nq->n, args, 0, own);
+            nl = &own;
+        }
+        ensure_segments(nl);
+        const uint32_t n = nq->n;
+        st->n = n;
+        // per-l offsets in one buffer
+        size_t off = 0;
+        for (int k = 0; k < st->st.nl; ++k)
+        {
+            st->st.qlm_offset[k] = off;
+            off += static_cast<size_t>(n) * (2 * st->st.l[k] + 1);
+        }
+        st->qlm.alloc(sizeof(float2) * std::max<size_t>(off, 1));
+        st->ql.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(n) * st->st.nl, 1));
+        const bool use_w = st->weighted && !nl->unit_weights;
+        launch_qlm(nq->dbox, nq->dpts, n, nl->ij.as<uint2>(), nl->dist.as<float>(),
+                   use_w ? nl->weights.as<float>() : nullptr, nl->seg.as<uint32_t>(), nl->cnt.as<uint32_t>(), st->st,
+                   use_w ? 1 : 0, st->qlm.as<float2>(), st->ql.as<float>(), s);
+        const float2* src = st->qlm.as<float2>();
+        const float* qn = st->ql.as<float>();
+        if (st->average)
+        {
+            st->qlm_ave.alloc(sizeof(float2) * std::max<size_t>(off, 1));
+            st->ql_ave.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(n) * st->st.nl, 1));
+            launch_ave(n, nl->ij.as<uint2>(), nl->seg.as<uint32_t>(), nl->cnt.as<uint32_t>(), st->st, st->qlm.as<float2>(),
+                       st->qlm_ave.as<float2>(), st->ql_ave.as<float>(), s);
+            src = st->qlm_ave.as<float2>();
+            qn = st->ql_ave.as<float>();
+        }
+        st->sys.alloc(sizeof(double) * 2 * st->stride);
+        FG_CUDA(cudaMemsetAsync(st->sys.p, 0, sizeof(double) * 2 * st->stride, s));
+        launch_sys(n, st->st, src, st->sys.as<double>(), s);
+        if (st->wl)
+        {
+            st->wlv.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(n) * st->st.nl, 1));
+            for (int k = 0; k < st->st.nl; ++k)
+                launch_wl(n, st->st, k, src, st->w3j[k].as<float>(), qn, st->wl_normalize ? 1 : 0, st->wlv.as<float>(), s);
+        }
+        FG_CUDA(cudaGetLastError());
+        std::vector<double> sys(2 * st->stride);
+        FG_CUDA(cudaMemcpyAsync(sys.data(), st->sys.p, sizeof(double) * 2 * st->stride, cudaMemcpyDeviceToHost, s));
+        sync();
+        // Steinhardt::normalizeSystem (Steinhardt.cc:291-327), in double
+        st->order.assign(st->st.nl, 0.0f);
+        size_t col = 0;
+        for (int k = 0; k < st->st.nl; ++k)
+        {
+            const int l = st->st.l[k];
+            const double nf = 4.0 * M_PI / (2 * l + 1);
+            double acc = 0.0;
+            for (int m = 0; m < 2 * l + 1; ++m)
+                acc += sys[2 * (col + m)] * sys[2 * (col + m)] + sys[2 * (col + m) + 1] * sys[2 * (col + m) + 1];
+            const double qsys = std::sqrt(acc * nf);
+            if (st->wl)
+            {
+                double v = reduce_w3j_host(&sys[2 * col], l, wigner3j_table(l));
+                if (st->wl_normalize)
+                {
+                    const double w = std::sqrt(nf) / qsys;
+                    v *= w * w * w;
+                }
+                st->order[k] = static_cast<float>(v);
+            }
+            else
+            {
+                st->order[k] = static_cast<float>(qsys);
+            }
+            col += 2 * l + 1;
+        }
+        st->computed = true;
+    });
+}
+
+fg_status fg_steinhardt_num_particles(const fg_steinhardt* st, uint32_t* out)
+{
+    return guard([&] {
+        require(st, "steinhardt");
+        *out = st->n;
+    });
+}
+
+fg_status fg_steinhardt_get(const fg_steinhardt* st, float* ql, float* particle_order, float* qlm, float* order)
+{
+    return guard([&] {
+        require(st, "steinhardt");
+        if (!st->computed)
+            runtime_error("Steinhardt has not been computed");
+        cudaStream_t s = stream();
+        const size_t nl = static_cast<size_t>(st->n) * st->st.nl;
+        const DevBuf& qlb = st->average ? st->ql_ave : st->ql;
+        if (ql && nl)
+            FG_CUDA(cudaMemcpyAsync(ql, qlb.p, sizeof(float) * nl, cudaMemcpyDeviceToHost, s));
+        if (particle_order && nl)
+        {
+            const DevBuf& pb = st->wl ? st->wlv : qlb;
+            FG_CUDA(cudaMemcpyAsync(particle_order, pb.p, sizeof(float) * nl, cudaMemcpyDeviceToHost, s));
+        }
+        if (qlm && st->n)
+            FG_CUDA(cudaMemcpyAsync(qlm, st->qlm.p, sizeof(float2) * st->stride * st->n, cudaMemcpyDeviceToHost, s));
+        if (order)
+            std::memcpy(order, st->order.data(), sizeof(float) * st->order.size());
+        sync();
+    });
+}
+
+} // extern "C"

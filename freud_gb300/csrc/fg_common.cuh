@@ -1,0 +1,132 @@
+// Shared device/host definitions for the freud_gb300 CUDA library.
+//
+// Exact float32 box arithmetic: every operation that decides a neighbour set,
+// a bond vector, a distance or an RDF bin uses the explicitly rounded intrinsics
+// (__fadd_rn, __fsub_rn, __fmul_rn, __fdiv_rn, __fsqrt_rn) so nvcc cannot contract
+// them into FMAs. The order of operations follows freud/box/Box.h:212-329 and
+// freud/util/VectorMath.h:270-273, which makes the results bit-identical to the
+// reference's x86-64 build.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fg {
+
+constexpr int WARP = 32;
+
+// Device view of a periodic box (freud::box::Box with all three periodic flags set).
+struct DevBox
+{
+    float L[3];   // Lx, Ly, Lz (Lz = 0 in 2D)
+    float lo[3];  // -L/2
+    float xy, xz, yz;
+    int is2d;
+    float img[27][3]; // reference image vectors, index (kx+1)*9 + (ky+1)*3 + (kz+1)
+};
+
+__host__ __device__ inline float fadd(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    volatile float r = a + b;
+    return r;
+#endif
+}
+__host__ __device__ inline float fsub(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    volatile float r = a - b;
+    return r;
+#endif
+}
+__host__ __device__ inline float fmul(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    volatile float r = a * b;
+    return r;
+#endif
+}
+__host__ __device__ inline float fdiv(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fdiv_rn(a, b);
+#else
+    volatile float r = a / b;
+    return r;
+#endif
+}
+
+// (x*x + y*y) + z*z, VectorMath.h:270-273
+__device__ __forceinline__ float dot3(float x, float y, float z)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+}
+
+// fmodf(a, 1.0f) is exactly a - truncf(a): the fractional part of a float is
+// representable, so the subtraction is exact (also for |a| >= 2^23 and +-0).
+__device__ __forceinline__ float fmod1(float a)
+{
+    return __fsub_rn(a, truncf(a));
+}
+
+// util::modulusPositive(a, 1.0f) = fmod(fmod(a, 1) + 1, 1), utils.h:29-32
+__device__ __forceinline__ float mod_pos1(float a)
+{
+    return fmod1(__fadd_rn(fmod1(a), 1.0f));
+}
+
+// Box::makeFractional, Box.h:243-255
+__device__ __forceinline__ void make_fractional(const DevBox& b, float vx, float vy, float vz, float& fx,
+                                                float& fy, float& fz)
+{
+    float dx = __fsub_rn(vx, b.lo[0]);
+    float dy = __fsub_rn(vy, b.lo[1]);
+    float dz = __fsub_rn(vz, b.lo[2]);
+    const float t2 = __fsub_rn(b.xz, __fmul_rn(b.yz, b.xy));
+    dx = __fsub_rn(dx, __fadd_rn(__fmul_rn(t2, vz), __fmul_rn(b.xy, vy)));
+    dy = __fsub_rn(dy, __fmul_rn(b.yz, vz));
+    fx = __fdiv_rn(dx, b.L[0]);
+    fy = __fdiv_rn(dy, b.L[1]);
+    fz = b.is2d ? 0.0f : __fdiv_rn(dz, b.L[2]);
+}
+
+// Box::makeAbsolute, Box.h:212-222
+__device__ __forceinline__ void make_absolute(const DevBox& b, float fx, float fy, float fz, float& x, float& y,
+                                              float& z)
+{
+    x = __fadd_rn(b.lo[0], __fmul_rn(fx, b.L[0]));
+    y = __fadd_rn(b.lo[1], __fmul_rn(fy, b.L[1]));
+    z = __fadd_rn(b.lo[2], __fmul_rn(fz, b.L[2]));
+    x = __fadd_rn(x, __fadd_rn(__fmul_rn(b.xy, y), __fmul_rn(b.xz, z)));
+    y = __fadd_rn(y, __fmul_rn(b.yz, z));
+    if (b.is2d)
+    {
+        z = 0.0f;
+    }
+}
+
+// Box::wrap for a fully periodic box, Box.h:307-329
+__device__ __forceinline__ void box_wrap(const DevBox& b, float vx, float vy, float vz, float& x, float& y,
+                                         float& z)
+{
+    float fx, fy, fz;
+    make_fractional(b, vx, vy, vz, fx, fy, fz);
+    make_absolute(b, mod_pos1(fx), mod_pos1(fy), mod_pos1(fz), x, y, z);
+}
+
+// Error word written by kernels whose waits or capacities are bounded.
+enum DeviceError : int
+{
+    DEV_OK = 0,
+    DEV_CAPACITY = 1,  // a per-query staging buffer overflowed
+    DEV_TIMEOUT = 2,   // a bounded spin gave up
+    DEV_RANGE = 3,     // an index fell outside its buffer (debug checks)
+};
+
+} // namespace fg

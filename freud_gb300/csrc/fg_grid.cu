@@ -1,0 +1,315 @@
+// Cell-list build (counting sort of points into cells) and exclusive scans.
+//
+// Replaces the serial head/next linked list of freud/locality/LinkCell.cc:316-336
+// and the serial AABB tree build of freud/locality/AABBQuery.cc:53-69 with a
+// data-parallel counting sort: cell index from the exact makeFractional
+// arithmetic, per-cell counts by atomics, exclusive scan, scatter into a
+// cell-sorted float4 array (x, y, z, packed integer box image) so candidate
+// loads in the query kernels are 16-byte and coalesced.
+#include "fg_kernels.cuh"
+#include "fg_prof.cuh"
+
+namespace fg {
+
+__device__ __forceinline__ int pack_image(int nx, int ny, int nz)
+{
+    return (nx & 0xff) | ((ny & 0xff) << 8) | ((nz & 0xff) << 16);
+}
+
+__device__ __forceinline__ int clamp_img(float n)
+{
+    return n < -100.0f ? -100 : (n > 100.0f ? 100 : static_cast<int>(n));
+}
+
+// Wrapped cell coordinate and integer image of a point (fractional coordinate
+// f = n + u with n = floor(f), u in [0, 1)).
+__device__ __forceinline__ void point_cell(const DevBox& b, const int dim[3], float x, float y, float z,
+                                           int& cx, int& cy, int& cz, int& img)
+{
+    float fx, fy, fz;
+    make_fractional(b, x, y, z, fx, fy, fz);
+    const float nx = floorf(fx);
+    const float ny = floorf(fy);
+    const float nz = floorf(fz);
+    const float ux = __fsub_rn(fx, nx);
+    const float uy = __fsub_rn(fy, ny);
+    const float uz = __fsub_rn(fz, nz);
+    cx = min(static_cast<int>(ux * static_cast<float>(dim[0])), dim[0] - 1);
+    cy = min(static_cast<int>(uy * static_cast<float>(dim[1])), dim[1] - 1);
+    cz = b.is2d ? 0 : min(static_cast<int>(uz * static_cast<float>(dim[2])), dim[2] - 1);
+    cx = max(cx, 0);
+    cy = max(cy, 0);
+    cz = max(cz, 0);
+    img = pack_image(clamp_img(nx), clamp_img(ny), b.is2d ? 0 : clamp_img(nz));
+}
+
+__global__ void k_assign(DevBox b, const float* __restrict__ pts, uint32_t n, int dx, int dy, int dz,
+                         uint32_t* __restrict__ cell_of, uint32_t* __restrict__ rank,
+                         uint32_t* __restrict__ cell_count)
+{
+    const int dim[3] = {dx, dy, dz};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        int cx, cy, cz, img;
+        point_cell(b, dim, pts[3 * (size_t) i], pts[3 * (size_t) i + 1], pts[3 * (size_t) i + 2], cx, cy, cz,
+                   img);
+        const uint32_t cell = static_cast<uint32_t>(cx + dx * (cy + dy * cz));
+        cell_of[i] = cell;
+        rank[i] = atomicAdd(&cell_count[cell], 1u);
+    }
+}
+
+__global__ void k_scatter(DevBox b, const float* __restrict__ pts, uint32_t n, int dx, int dy, int dz,
+                          const uint32_t* __restrict__ cell_of, const uint32_t* __restrict__ rank,
+                          const uint32_t* __restrict__ start, float4* __restrict__ cpos,
+                          uint32_t* __restrict__ cidx)
+{
+    const int dim[3] = {dx, dy, dz};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const float x = pts[3 * (size_t) i];
+        const float y = pts[3 * (size_t) i + 1];
+        const float z = pts[3 * (size_t) i + 2];
+        int cx, cy, cz, img;
+        point_cell(b, dim, x, y, z, cx, cy, cz, img);
+        const uint32_t pos = start[cell_of[i]] + rank[i];
+        cpos[pos] = make_float4(x, y, b.is2d ? 0.0f : z, __int_as_float(img));
+        cidx[pos] = i;
+    }
+}
+
+static int grid_for(size_t n, int threads)
+{
+    size_t blocks = (n + threads - 1) / threads;
+    if (blocks > 152 * 32)
+    {
+        blocks = 152 * 32;
+    }
+    return blocks < 1 ? 1 : static_cast<int>(blocks);
+}
+
+void launch_assign(const DevBox& box, const float* pts, uint32_t n, const int dim[3], uint32_t* cell_of,
+                   uint32_t* rank, uint32_t* cell_count, cudaStream_t s)
+{
+    if (n == 0)
+    {
+        return;
+    }
+    {
+        ProfScope prof_("k_assign", s);
+        k_assign<<<grid_for(n, 256), 256, 0, s>>>(box, pts, n, dim[0], dim[1], dim[2], cell_of, rank, cell_count);
+    }
+}
+
+void launch_scatter(const DevBox& box, const float* pts, uint32_t n, const uint32_t* cell_of,
+                    const uint32_t* rank, const uint32_t* start, float4* cpos, uint32_t* cidx, cudaStream_t s)
+{
+    // dims are only used to recompute the packed image; any dims give the same image
+    if (n == 0)
+    {
+        return;
+    }
+    {
+        ProfScope prof_("k_scatter", s);
+        k_scatter<<<grid_for(n, 256), 256, 0, s>>>(box, pts, n, 1, 1, 1, cell_of, rank, start, cpos, cidx);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan: per-tile sums -> recursive scan of tile sums -> tile scan.
+// ---------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+template<typename TI, typename TO> __global__ void k_tile_sums(const TI* __restrict__ in, size_t n, TO* sums)
+{
+    __shared__ TO warp_sums[SCAN_THREADS / 32];
+    const size_t base = static_cast<size_t>(blockIdx.x) * SCAN_TILE;
+    TO acc = 0;
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+    {
+        const size_t idx = base + static_cast<size_t>(k) * SCAN_THREADS + threadIdx.x;
+        if (idx < n)
+        {
+            acc += static_cast<TO>(in[idx]);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        acc += __shfl_down_sync(0xffffffffu, acc, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        warp_sums[threadIdx.x >> 5] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        TO t = 0;
+        for (int w = 0; w < SCAN_THREADS / 32; ++w)
+        {
+            t += warp_sums[w];
+        }
+        sums[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of one tile with an added base offset (offsets[blockIdx.x] or 0).
+template<typename TI, typename TO>
+__global__ void k_tile_scan(const TI* __restrict__ in, TO* __restrict__ out, size_t n, const TO* offsets)
+{
+    __shared__ TO warp_tot[SCAN_THREADS / 32];
+    const size_t base = static_cast<size_t>(blockIdx.x) * SCAN_TILE + static_cast<size_t>(threadIdx.x) * SCAN_ITEMS;
+    TO v[SCAN_ITEMS];
+    TO local = 0;
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+    {
+        const size_t idx = base + k;
+        v[k] = idx < n ? static_cast<TO>(in[idx]) : 0;
+        local += v[k];
+    }
+    // inclusive warp scan of per-thread totals
+    TO incl = local;
+    const int lane = threadIdx.x & 31;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        TO t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+        {
+            incl += t;
+        }
+    }
+    if (lane == 31)
+    {
+        warp_tot[threadIdx.x >> 5] = incl;
+    }
+    __syncthreads();
+    TO warp_off = 0;
+    for (int w = 0; w < static_cast<int>(threadIdx.x >> 5); ++w)
+    {
+        warp_off += warp_tot[w];
+    }
+    TO run = (offsets != nullptr ? offsets[blockIdx.x] : 0) + warp_off + incl - local;
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+    {
+        const size_t idx = base + k;
+        if (idx < n)
+        {
+            out[idx] = run;
+        }
+        run += v[k];
+    }
+}
+
+size_t scan_scratch_bytes(size_t n)
+{
+    size_t total = 0;
+    size_t m = n;
+    while (m > 1)
+    {
+        m = (m + SCAN_TILE - 1) / SCAN_TILE;
+        total += (m + 1) * sizeof(uint64_t) * 2;
+    }
+    return total + 256;
+}
+
+template<typename TI, typename TO> static void scan_impl(const TI* in, TO* out, size_t n, char* scratch, cudaStream_t s)
+{
+    if (n == 0)
+    {
+        return;
+    }
+    const size_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (tiles == 1)
+    {
+        {
+            ProfScope prof_("k_tile_scan<TI, TO>", s);
+            k_tile_scan<TI, TO><<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+        }
+        return;
+    }
+    TO* sums = reinterpret_cast<TO*>(scratch);
+    TO* sums_scan = sums + tiles + 1;
+    char* next = reinterpret_cast<char*>(sums_scan + tiles + 1);
+    {
+        ProfScope prof_("k_tile_sums<TI, TO>", s);
+        k_tile_sums<TI, TO><<<static_cast<unsigned>(tiles), SCAN_THREADS, 0, s>>>(in, n, sums);
+    }
+    scan_impl<TO, TO>(sums, sums_scan, tiles, next, s);
+    {
+        ProfScope prof_("k_tile_scan<TI, TO>", s);
+        k_tile_scan<TI, TO><<<static_cast<unsigned>(tiles), SCAN_THREADS, 0, s>>>(in, out, n, sums_scan);
+    }
+}
+
+void scan_u32_to_u32(const uint32_t* in, uint32_t* out, size_t n, void* scratch, cudaStream_t s)
+{
+    scan_impl<uint32_t, uint32_t>(in, out, n, static_cast<char*>(scratch), s);
+}
+
+void scan_u32_to_u64(const uint32_t* in, uint64_t* out, size_t n, void* scratch, cudaStream_t s)
+{
+    scan_impl<uint32_t, uint64_t>(in, out, n, static_cast<char*>(scratch), s);
+}
+
+// ---------------------------------------------------------------------------
+// NeighborList helpers
+// ---------------------------------------------------------------------------
+__global__ void k_fill_f32(float* a, float v, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+    {
+        a[i] = v;
+    }
+}
+
+void launch_fill_f32(float* a, float v, uint64_t n, cudaStream_t s)
+{
+    if (n == 0)
+    {
+        return;
+    }
+    {
+        ProfScope prof_("k_fill_f32", s);
+        k_fill_f32<<<grid_for(n, 256), 256, 0, s>>>(a, v, n);
+    }
+}
+
+// segments[i] = first bond of query i, counts[i] = its bond count
+// (NeighborList::updateSegmentCounts, NeighborList.cc:199-232; queries with no
+// bonds keep segment 0 and count 0 as the reference leaves them).
+__global__ void k_segments(const uint2* __restrict__ ij, uint64_t nb, uint32_t* segments, uint32_t* counts)
+{
+    for (uint64_t b = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; b < nb; b += (uint64_t) gridDim.x * blockDim.x)
+    {
+        const uint32_t i = ij[b].x;
+        if (b == 0 || ij[b - 1].x != i)
+        {
+            segments[i] = static_cast<uint32_t>(b);
+            uint64_t e = b + 1;
+            while (e < nb && ij[e].x == i)
+            {
+                ++e;
+            }
+            counts[i] = static_cast<uint32_t>(e - b);
+        }
+    }
+}
+
+void launch_segments(const uint2* ij, uint64_t nb, uint32_t nq, uint32_t* segments, uint32_t* counts,
+                     cudaStream_t s)
+{
+    cudaMemsetAsync(segments, 0, sizeof(uint32_t) * nq, s);
+    cudaMemsetAsync(counts, 0, sizeof(uint32_t) * nq, s);
+    if (nb == 0)
+    {
+        return;
+    }
+    {
+        ProfScope prof_("k_segments", s);
+        k_segments<<<grid_for(nb, 256), 256, 0, s>>>(ij, nb, segments, counts);
+    }
+}
+
+} // namespace fg

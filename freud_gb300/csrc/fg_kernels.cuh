@@ -1,0 +1,120 @@
+// Host-side launch interface of the freud_gb300 kernels (implemented in the .cu files).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fg_common.cuh"
+
+namespace fg {
+
+enum Arith : int
+{
+    ARITH_AABB = 0, // r = p_j - (q + image)   AABBQuery.cc:93,125 (also RawPoints, the default)
+    ARITH_WRAP = 1, // r = box.wrap(p_j - q)   LinkCell.cc:522
+};
+
+// Cell-sorted view of a point set: points reordered by cell, with cell offsets.
+struct DevGrid
+{
+    int dim[3];
+    int ncell;
+    const uint32_t* start; // ncell + 1 exclusive offsets
+    const float4* cpos;    // positions sorted by cell; w = packed integer box image
+    const uint32_t* cidx;  // original point index of each sorted slot
+};
+
+// Per-query staging capacity of the warp-per-query emit kernel; queries with more
+// bonds are written by the block-per-query kernel.
+constexpr int EMIT_CAP = 256;
+constexpr int HEAVY_CAP = 8192;
+
+// ---- grid build ---------------------------------------------------------------
+// Computes dims for a cell width and fills cell_of/rank and counts (atomics).
+void launch_assign(const DevBox& box, const float* pts, uint32_t n, const int dim[3], uint32_t* cell_of,
+                   uint32_t* rank, uint32_t* cell_count, cudaStream_t s);
+void launch_scatter(const DevBox& box, const float* pts, uint32_t n, const uint32_t* cell_of,
+                    const uint32_t* rank, const uint32_t* start, float4* cpos, uint32_t* cidx, cudaStream_t s);
+
+// Exclusive scans. scratch must hold scan_scratch_bytes(n) bytes.
+size_t scan_scratch_bytes(size_t n);
+void scan_u32_to_u32(const uint32_t* in, uint32_t* out, size_t n, void* scratch, cudaStream_t s);
+void scan_u32_to_u64(const uint32_t* in, uint64_t* out, size_t n, void* scratch, cudaStream_t s);
+
+// ---- ball queries -------------------------------------------------------------
+struct BallParams
+{
+    float r_max_sq;
+    float r_min_sq;
+    int exclude_ii;
+    int arith;
+    uint32_t nq;
+};
+
+// counts[i] = number of bonds of query i (original query index).
+void launch_ball_count(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
+                       const BallParams& p, uint32_t* counts, cudaStream_t s);
+
+// Writes bonds in reference order at offsets[i]. Queries with more than EMIT_CAP
+// bonds are appended to heavy_list (heavy_count) and written by launch_ball_emit_heavy.
+void launch_ball_emit(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
+                      const BallParams& p, const uint32_t* counts, const uint64_t* offsets, int by_distance,
+                      uint2* ij, float* dist, float* vec, uint32_t* heavy_list, uint32_t* heavy_count,
+                      int* err, cudaStream_t s);
+void launch_ball_emit_heavy(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
+                            const BallParams& p, const uint32_t* counts, const uint64_t* offsets,
+                            int by_distance, const uint32_t* heavy_list, uint32_t n_heavy, uint2* ij,
+                            float* dist, float* vec, int* err, cudaStream_t s);
+
+// Fused ball query + RDF histogram into uint64 counts (bins <= HIST_SMEM_BINS use
+// block-private shared-memory histograms).
+struct HistParams
+{
+    float h_min, h_max, h_inv;
+    uint32_t bins;
+};
+void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
+                      const BallParams& p, const HistParams& h, unsigned long long* hist, cudaStream_t s);
+
+// Histogram of a distance array (RDF over a NeighborList).
+void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,
+                           cudaStream_t s);
+
+// ---- k nearest neighbours ------------------------------------------------------
+struct KnnParams
+{
+    float r_max_sq;
+    float r_min;     // AABB arithmetic filters on distance >= r_min
+    float r_min_sq;  // wrap arithmetic filters on r_sq >= r_min^2
+    int exclude_ii;
+    int arith;
+    uint32_t k;
+    uint32_t nq;
+    float covered;   // radius fully covered by the 27-cell stencil
+};
+// k <= 32: warp-per-query bitonic top-k over the 27-cell stencil. Results go to
+// row i of (j, d, vec) temp arrays [nq * k]; counts[i] = number found. Queries
+// whose k-th neighbour is not provably inside the stencil go to fail_list.
+void launch_knn_warp(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
+                     const KnnParams& p, uint32_t* tj, float* td, float* tv, uint32_t* counts,
+                     uint32_t* fail_list, uint32_t* fail_count, cudaStream_t s);
+// Block-per-query brute force over every point (minimum over the 27 images in AABB
+// arithmetic), used for k > 32 and for queries the warp kernel could not prove.
+// list holds positions in the sorted query array. Needs the number of accepted
+// points per query <= knn_block_capacity() (else err = DEV_CAPACITY).
+void launch_knn_block(const DevBox& box, const float4* cpos, const uint32_t* cidx, uint32_t n, const float4* qpos,
+                      const uint32_t* qidx, const KnnParams& p, const uint32_t* list, uint32_t nlist, uint32_t* tj,
+                      float* td, float* tv, uint32_t* counts, int* err, cudaStream_t s);
+size_t knn_block_capacity();
+// Compacts temp rows into a NeighborList (sorted by j, or by distance then j).
+void launch_knn_compact(const uint32_t* tj, const float* td, const float* tv, uint32_t k, uint32_t nq,
+                        const uint32_t* counts, const uint64_t* offsets, int by_distance, uint2* ij,
+                        float* dist, float* vec, cudaStream_t s);
+
+// ---- NeighborList helpers -------------------------------------------------------
+void launch_fill_f32(float* a, float v, uint64_t n, cudaStream_t s);
+void launch_segments(const uint2* ij, uint64_t nb, uint32_t nq, uint32_t* segments, uint32_t* counts,
+                     cudaStream_t s);
+
+} // namespace fg

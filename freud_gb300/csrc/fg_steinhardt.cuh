@@ -1,0 +1,36 @@
+// Launch interface of the Steinhardt kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fg_common.cuh"
+
+namespace fg {
+
+constexpr int ST_MAX_L = 31;   // largest spherical-harmonic degree supported
+constexpr int ST_MAX_NL = 10;  // largest number of l values per Steinhardt object
+
+// The requested degrees (in the caller's order) and where each one's qlm array
+// starts inside one contiguous float2 buffer.
+struct StLs
+{
+    int nl;
+    int max_l;
+    int l[ST_MAX_NL];
+    size_t qlm_offset[ST_MAX_NL]; // in float2 units
+    float norm[ST_MAX_NL];        // float(4 pi / (2l + 1))
+};
+
+void st_upload_tables(cudaStream_t s);
+void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
+                const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
+                float2* qlm, float* ql, cudaStream_t s);
+void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
+                const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s);
+void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float* w3j_dev, const float* qnorm,
+               int normalize, float* wl, cudaStream_t s);
+void launch_sys(uint32_t n, const StLs& ls, const float2* src, double* sys, cudaStream_t s);
+
+} // namespace fg

@@ -1,0 +1,133 @@
+"""Radial distribution function, API-compatible with freud.density.RDF
+(freud/density.py:535-696). Pair finding and binning run on the GPU; bin counts
+are exact uint64 on the device and reported as the reference's uint32, and
+rdf / n_r use the reference's float32 normalisation (RDF.cc:73-99)."""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .box import Box
+from .locality import NeighborList, _SpatialHistogram1D
+from .util import _Compute
+
+
+class RDF(_SpatialHistogram1D):
+    """Computes g(r) and the cumulative N(r).
+
+    Args:
+        bins (unsigned int): number of bins.
+        r_max (float): largest distance binned.
+        r_min (float, optional): smallest distance binned (default 0).
+        normalization_mode (str, optional): ``'exact'`` or ``'finite_size'``.
+    """
+
+    def __init__(self, bins, r_max, r_min=0, normalization_mode="exact"):
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib.fg_rdf_create(int(bins), float(r_max), float(r_min), ctypes.byref(h)))
+        self._handle = _lib.Handle(h, _lib.lib.fg_rdf_destroy)
+        self._bins = int(bins)
+        self.mode = normalization_mode
+        self.r_max = r_max
+        self._r_min = r_min
+
+    @property
+    def _h(self):
+        return self._handle.value
+
+    @property
+    def mode(self):
+        return self._mode
+
+    @mode.setter
+    def mode(self, value):
+        if value not in ("exact", "finite_size"):
+            raise ValueError("An invalid normalization mode was provided.")
+        self._mode = value
+        _lib.check(_lib.lib.fg_rdf_set_mode(self._h, int(value == "finite_size")))
+
+    def _reset(self):
+        _lib.check(_lib.lib.fg_rdf_reset(self._h))
+
+    def compute(self, system, query_points=None, neighbors=None, reset=True):
+        """Accumulate the pair distances of one frame (reset=False keeps adding frames)."""
+        if reset:
+            self._reset()
+        nq, nlist, qargs, l_query_points, num_query_points = self._preprocess_arguments(
+            system, query_points, neighbors)
+        qp = np.ascontiguousarray(l_query_points, dtype=np.float32)
+        qp_arg = None if nq._same_points(qp) else qp
+        _lib.check(_lib.lib.fg_rdf_accumulate(
+            self._h, nq._h, _lib.ptr(qp_arg), len(qp), None if nlist is None else nlist._h,
+            ctypes.byref(qargs._c())))
+        return self
+
+    def _get(self):
+        c = np.zeros(self._bins, np.uint32)
+        g = np.zeros(self._bins, np.float32)
+        nr = np.zeros(self._bins, np.float32)
+        _lib.check(_lib.lib.fg_rdf_get(self._h, _lib.ptr(c), _lib.ptr(g), _lib.ptr(nr)))
+        return c, g, nr
+
+    @_Compute._computed_property
+    def rdf(self):
+        return self._get()[1]
+
+    @_Compute._computed_property
+    def n_r(self):
+        return self._get()[2]
+
+    @_Compute._computed_property
+    def bin_counts(self):
+        return self._get()[0]
+
+    @_Compute._computed_property
+    def bin_counts_u64(self):
+        """Full-width uint64 bin counts (the reference stores uint32)."""
+        c = np.zeros(self._bins, np.uint64)
+        _lib.check(_lib.lib.fg_rdf_get_u64(self._h, _lib.ptr(c), None, None))
+        return c
+
+    @_Compute._computed_property
+    def rdf_fp64(self):
+        """g(r) normalised in FP64 from the uint64 counts."""
+        g = np.zeros(self._bins, np.float64)
+        _lib.check(_lib.lib.fg_rdf_get_u64(self._h, None, _lib.ptr(g), None))
+        return g
+
+    @_Compute._computed_property
+    def n_r_fp64(self):
+        nr = np.zeros(self._bins, np.float64)
+        _lib.check(_lib.lib.fg_rdf_get_u64(self._h, None, None, _lib.ptr(nr)))
+        return nr
+
+    @_Compute._computed_property
+    def box(self):
+        b = _lib.fg_box()
+        _lib.check(_lib.lib.fg_rdf_state(self._h, ctypes.byref(b), None, None, None))
+        return Box(b.Lx, b.Ly, b.Lz, b.xy, b.xz, b.yz, bool(b.is2D))
+
+    @property
+    def bin_edges(self):
+        e = np.zeros(self._bins + 1, np.float32)
+        _lib.check(_lib.lib.fg_rdf_bin_edges(self._h, _lib.ptr(e), None))
+        return e.astype(np.float64)
+
+    @property
+    def bin_centers(self):
+        c = np.zeros(self._bins, np.float32)
+        _lib.check(_lib.lib.fg_rdf_bin_edges(self._h, None, _lib.ptr(c)))
+        return c.astype(np.float64)
+
+    @property
+    def bounds(self):
+        return (float(np.float32(self._r_min)), float(np.float32(self.r_max)))
+
+    @property
+    def nbins(self):
+        return self._bins
+
+    def __repr__(self):
+        return "freud.density.{}(bins={}, r_max={}, r_min={})".format(
+            type(self).__name__, self._bins, self.bounds[1], self.bounds[0])

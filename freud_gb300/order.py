@@ -1,0 +1,115 @@
+"""Steinhardt order parameters, API-compatible with freud.order.Steinhardt
+(freud/order.py:375-643). Ylm, qlm, averaging and Wl run on the GPU."""
+
+import collections.abc
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .locality import _PairCompute
+from .util import _Compute
+
+
+class Steinhardt(_PairCompute):
+    """Rotationally invariant Steinhardt q_l / w_l for each particle.
+
+    Args:
+        l (unsigned int or sequence of unsigned int): spherical-harmonic degrees.
+        average (bool): average qlm over the first neighbour shell (Lechner-Dellago).
+        wl (bool): compute the third-order invariant w_l.
+        weighted (bool): weight neighbours by the NeighborList weights.
+        wl_normalize (bool): normalise w_l.
+    """
+
+    def __init__(self, l, average=False, wl=False, weighted=False, wl_normalize=False):
+        if not isinstance(l, collections.abc.Sequence):
+            l = [l]
+        if len(l) == 0:
+            raise ValueError("At least one l must be specified.")
+        self._ls = [int(x) for x in l]
+        ls = np.asarray(self._ls, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib.fg_steinhardt_create(_lib.ptr(ls), len(ls), int(average), int(wl), int(weighted),
+                                                 int(wl_normalize), ctypes.byref(h)))
+        self._handle = _lib.Handle(h, _lib.lib.fg_steinhardt_destroy)
+        self._average, self._wl, self._weighted, self._wl_normalize = (bool(average), bool(wl), bool(weighted),
+                                                                       bool(wl_normalize))
+        self._cache = None
+
+    @property
+    def _h(self):
+        return self._handle.value
+
+    @property
+    def average(self):
+        return self._average
+
+    @property
+    def wl(self):
+        return self._wl
+
+    @property
+    def weighted(self):
+        return self._weighted
+
+    @property
+    def wl_normalize(self):
+        return self._wl_normalize
+
+    @property
+    def l(self):
+        return self._ls[0] if len(self._ls) == 1 else list(self._ls)
+
+    def compute(self, system, neighbors=None):
+        nq, nlist, qargs, _qp, _nqp = self._preprocess_arguments(system, neighbors=neighbors)
+        _lib.check(_lib.lib.fg_steinhardt_compute(self._h, nq._h, None if nlist is None else nlist._h,
+                                                  ctypes.byref(qargs._c())))
+        self._cache = None
+        return self
+
+    def _outputs(self):
+        if self._cache is None:
+            n = ctypes.c_uint32()
+            _lib.check(_lib.lib.fg_steinhardt_num_particles(self._h, ctypes.byref(n)))
+            n = n.value
+            nl = len(self._ls)
+            stride = sum(2 * l + 1 for l in self._ls)
+            ql = np.zeros((n, nl), np.float32)
+            po = np.zeros((n, nl), np.float32)
+            qlm = np.zeros(n * stride * 2, np.float32)
+            order = np.zeros(nl, np.float32)
+            _lib.check(_lib.lib.fg_steinhardt_get(self._h, _lib.ptr(ql), _lib.ptr(po), _lib.ptr(qlm),
+                                                  _lib.ptr(order)))
+            qc = qlm.view(np.complex64)
+            per_l, off = [], 0
+            for l in self._ls:
+                m = 2 * l + 1
+                per_l.append(qc[off:off + n * m].reshape(n, m))
+                off += n * m
+            self._cache = {"ql": ql, "po": po, "qlm": per_l, "order": order}
+        return self._cache
+
+    @_Compute._computed_property
+    def order(self):
+        order = self._outputs()["order"]
+        return order[0] if len(order) == 1 else order
+
+    @_Compute._computed_property
+    def particle_order(self):
+        p = self._outputs()["po"]
+        return np.ravel(p) if p.shape[1] == 1 else p
+
+    @_Compute._computed_property
+    def ql(self):
+        q = self._outputs()["ql"]
+        return np.ravel(q) if q.shape[1] == 1 else q
+
+    @_Compute._computed_property
+    def particle_harmonics(self):
+        qlm = self._outputs()["qlm"]
+        return qlm if len(qlm) > 1 else qlm[0]
+
+    def __repr__(self):
+        return ("freud.order.{}(l={}, average={}, wl={}, weighted={}, wl_normalize={})".format(
+            type(self).__name__, self.l, self.average, self.wl, self.weighted, self.wl_normalize))

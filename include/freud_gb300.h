@@ -1,0 +1,190 @@
+/*
+ * freud_gb300.h -- C ABI of the GB300-native neighbour-query -> pair-reduction
+ * path (LinkCell / AABBQuery queries, NeighborList, RDF, Steinhardt).
+ *
+ * Every entry point returns an fg_status; on failure fg_last_error() gives a
+ * thread-local message. Status classes mirror how the reference's C++ exceptions
+ * reach Python (freud/locality/export-*.cc via nanobind):
+ *   FG_ERR_VALUE   <- std::invalid_argument / std::domain_error  (ValueError)
+ *   FG_ERR_RUNTIME <- std::runtime_error                         (RuntimeError)
+ *   FG_ERR_INDEX   <- std::out_of_range                          (IndexError)
+ *   FG_ERR_CUDA / FG_ERR_MEMORY for device failures               (RuntimeError)
+ *
+ * Host pointers are plain C arrays (float32 points are packed x,y,z triples, as
+ * the reference's vec3<float>). Objects are opaque handles with explicit destroy.
+ * Calls are synchronous: when a call returns, its results are complete.
+ */
+#ifndef FREUD_GB300_H
+#define FREUD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int fg_status;
+#define FG_OK 0
+#define FG_ERR_VALUE 1
+#define FG_ERR_RUNTIME 2
+#define FG_ERR_INDEX 3
+#define FG_ERR_CUDA 4
+#define FG_ERR_MEMORY 5
+
+/* Periodic box, freud::box::Box(Lx, Ly, Lz, xy, xz, yz, is2D)
+ * (reference freud/box/Box.h:77-86; Python freud/box.py:58-76). */
+typedef struct fg_box
+{
+    float Lx, Ly, Lz, xy, xz, yz;
+    int is2D;
+    int periodic_x, periodic_y, periodic_z;
+} fg_box;
+
+/* Query modes, freud::locality::QueryType (freud/locality/NeighborQuery.h:34-39). */
+#define FG_MODE_NONE 0
+#define FG_MODE_BALL 1
+#define FG_MODE_NEAREST 2
+
+/* freud::locality::QueryArgs (freud/locality/NeighborQuery.h:60-73), same defaults:
+ * num_neighbors 0xffffffff, r_max -1, r_min 0, r_guess -1, scale -1, exclude_ii 0. */
+typedef struct fg_query_args
+{
+    int mode;
+    uint32_t num_neighbors;
+    float r_max;
+    float r_min;
+    float r_guess;
+    float scale;
+    int exclude_ii;
+} fg_query_args;
+
+/* Neighbour-query kinds. RAWPOINTS is the reference's default behind every
+ * (box, points) tuple (freud/locality/RawPoints.h:30-77) and uses AABB arithmetic. */
+#define FG_NQ_RAWPOINTS 0
+#define FG_NQ_AABB 1
+#define FG_NQ_LINKCELL 2
+
+typedef struct fg_nq fg_nq;
+typedef struct fg_nlist fg_nlist;
+typedef struct fg_rdf fg_rdf;
+typedef struct fg_steinhardt fg_steinhardt;
+
+/* Library */
+const char* fg_last_error(void);
+int fg_version(void);
+/* Stream the library launches on (a cudaStream_t); NULL restores the library's own. */
+fg_status fg_set_stream(void* cuda_stream);
+
+/* Kernel launch accounting and per-kernel device timing (no counterpart in the
+ * reference, which has no device code). fg_launch_count: kernels launched by
+ * this library since load. fg_profile_enable(1) resets the per-kernel table and
+ * brackets every launch with CUDA events on its stream; fg_profile_report writes
+ * one line "name launches total_ms" per kernel. */
+fg_status fg_launch_count(uint64_t* out);
+fg_status fg_profile_enable(int enable);
+fg_status fg_profile_report(char* buf, size_t len);
+
+/* ---- NeighborQuery -------------------------------------------------------
+ * Replaces freud::locality::AABBQuery(box, points, n) (freud/locality/AABBQuery.cc:18-24),
+ * LinkCell(box, points, n, cell_width) (freud/locality/LinkCell.cc:222-260) and
+ * RawPoints(box, points, n) (freud/locality/RawPoints.h:36-38); Python bindings
+ * freud/locality/export-NeighborQuery.cc:35-65. Points are copied to the device. */
+fg_status fg_nq_create(const fg_box* box, const float* points, uint32_t n, int kind, float cell_width, fg_nq** out);
+/* Same with points already resident on the current device (not copied, must outlive the handle). */
+fg_status fg_nq_create_device(const fg_box* box, const float* device_points, uint32_t n, int kind, float cell_width,
+                              fg_nq** out);
+fg_status fg_nq_destroy(fg_nq* nq);
+/* LinkCell::getCellWidth (freud/locality/LinkCell.h:189-192). */
+fg_status fg_nq_cell_width(const fg_nq* nq, float* out);
+fg_status fg_nq_num_points(const fg_nq* nq, uint32_t* out);
+
+/* NeighborQuery::query(...) -> NeighborQueryIterator::toNeighborList(sort_by_distance)
+ * (freud/locality/NeighborQuery.h:130-142, 434-481; export-NeighborQuery.cc:26-33,130-135).
+ * query_points == NULL queries the object's own points. Bonds come out in the
+ * reference order: (i, j, weight, distance), or (i, distance, j, weight). */
+fg_status fg_nq_query(fg_nq* nq, const float* query_points, uint32_t n_query, const fg_query_args* args,
+                      int sort_by_distance, fg_nlist** out);
+/* Same with query points already on the device. */
+fg_status fg_nq_query_device(fg_nq* nq, const float* device_query_points, uint32_t n_query,
+                             const fg_query_args* args, int sort_by_distance, fg_nlist** out);
+
+/* ---- NeighborList ----------------------------------------------------------
+ * freud::locality::NeighborList (freud/locality/NeighborList.h:29-158, .cc:24-430;
+ * bindings freud/locality/export-NeighborList.cc:24-86). */
+/* NeighborList(num_bonds, query_point_index, num_query_points, point_index, num_points,
+ * vectors, weights) (NeighborList.cc:51-82): validates sorted query indices; distances
+ * are sqrt(dot(v, v)). weights may be NULL (all 1). */
+fg_status fg_nlist_from_arrays(uint64_t num_bonds, const uint32_t* query_point_indices, uint32_t num_query_points,
+                               const uint32_t* point_indices, uint32_t num_points, const float* vectors,
+                               const float* weights, fg_nlist** out);
+/* NeighborList(points, query_points, box, exclude_ii) all pairs (NeighborList.cc:84-128). */
+fg_status fg_nlist_all_pairs(const fg_box* box, const float* points, uint32_t num_points, const float* query_points,
+                             uint32_t num_query_points, int exclude_ii, fg_nlist** out);
+fg_status fg_nlist_destroy(fg_nlist* nl);
+/* NeighborList::copy (NeighborList.cc:354-366). */
+fg_status fg_nlist_copy(const fg_nlist* src, fg_nlist** out);
+fg_status fg_nlist_num_bonds(const fg_nlist* nl, uint64_t* out);
+fg_status fg_nlist_num_query_points(const fg_nlist* nl, uint32_t* out);
+fg_status fg_nlist_num_points(const fg_nlist* nl, uint32_t* out);
+/* getNeighbors (B,2) / getDistances / getWeights / getVectors (B,3) copied to host;
+ * any output may be NULL. */
+fg_status fg_nlist_get(const fg_nlist* nl, uint32_t* neighbors, float* distances, float* weights, float* vectors);
+/* Device pointers of the bond arrays (valid until the list is destroyed or modified). */
+fg_status fg_nlist_device_arrays(const fg_nlist* nl, const uint32_t** neighbors, const float** distances,
+                                 const float** vectors);
+/* getSegments / getCounts (NeighborList.cc:199-232). */
+fg_status fg_nlist_segments(const fg_nlist* nl, uint32_t* segments, uint32_t* counts);
+/* find_first_index (NeighborList.cc:309-316). */
+fg_status fg_nlist_find_first_index(const fg_nlist* nl, uint32_t i, uint32_t* out);
+/* filter(bool*) (NeighborList.cc:234-284); keep is one byte per bond. */
+fg_status fg_nlist_filter(fg_nlist* nl, const uint8_t* keep);
+/* filter_r (NeighborList.cc:286-307). */
+fg_status fg_nlist_filter_r(fg_nlist* nl, float r_max, float r_min);
+/* sort(by_distance) (NeighborList.cc:371-399). */
+fg_status fg_nlist_sort(fg_nlist* nl, int by_distance);
+
+/* ---- RDF ---------------------------------------------------------------------
+ * freud::density::RDF (freud/density/RDF.cc:25-110; bindings export-RDF.cc:22-47,
+ * BondHistogramCompute export-BondHistogramCompute.cc:67-76). */
+fg_status fg_rdf_create(uint32_t bins, float r_max, float r_min, fg_rdf** out);
+fg_status fg_rdf_destroy(fg_rdf* rdf);
+/* RDF::mode: 0 = exact, 1 = finite_size (RDF.h:20-24). */
+fg_status fg_rdf_set_mode(fg_rdf* rdf, int finite_size);
+/* BondHistogramCompute::reset (BondHistogramCompute.h:39-49). */
+fg_status fg_rdf_reset(fg_rdf* rdf);
+/* RDF::accumulate (RDF.cc:101-110): nlist == NULL queries nq with args. */
+fg_status fg_rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* query_points, uint32_t n_query,
+                            const fg_nlist* nlist, const fg_query_args* args);
+/* Same with query points already on the device. */
+fg_status fg_rdf_accumulate_device(fg_rdf* rdf, fg_nq* nq, const float* device_query_points, uint32_t n_query,
+                                   const fg_nlist* nlist, const fg_query_args* args);
+/* getBinCounts (uint32, reference dtype), getRDF, getNr (RDF.cc:73-99, float32 arithmetic
+ * identical to the reference). Any output may be NULL. */
+fg_status fg_rdf_get(fg_rdf* rdf, uint32_t* bin_counts, float* rdf_out, float* n_r);
+/* Full-width uint64 counts and an FP64 normalisation of the same quantities. */
+fg_status fg_rdf_get_u64(fg_rdf* rdf, uint64_t* bin_counts, double* rdf_out, double* n_r);
+/* getBinEdges / getBinCenters (Histogram.h:72-80, 126-138). */
+fg_status fg_rdf_bin_edges(const fg_rdf* rdf, float* edges, float* centers);
+/* getBox of the last accumulated frame; frame counter. */
+fg_status fg_rdf_state(const fg_rdf* rdf, fg_box* box, uint32_t* n_frames, uint32_t* n_points, uint32_t* n_query);
+
+/* ---- Steinhardt ----------------------------------------------------------------
+ * freud::order::Steinhardt (freud/order/Steinhardt.h:59-223, Steinhardt.cc:85-359;
+ * bindings export-Steinhardt.cc:19-34). */
+fg_status fg_steinhardt_create(const uint32_t* ls, uint32_t n_l, int average, int wl, int weighted,
+                               int wl_normalize, fg_steinhardt** out);
+fg_status fg_steinhardt_destroy(fg_steinhardt* st);
+/* Steinhardt::compute(nlist, points, qargs): nlist == NULL queries nq with args. */
+fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nlist, const fg_query_args* args);
+fg_status fg_steinhardt_num_particles(const fg_steinhardt* st, uint32_t* out);
+/* getQl (N, n_l), getParticleOrder (N, n_l), getQlm (per l an (N, 2l+1) complex64
+ * array, concatenated in l order, as interleaved re/im floats), getOrder (n_l).
+ * Any output may be NULL. */
+fg_status fg_steinhardt_get(const fg_steinhardt* st, float* ql, float* particle_order, float* qlm, float* order);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FREUD_GB300_H */

@@ -1,0 +1,228 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden
+vectors and the oracle. Neighbour sets, distances, vectors and RDF counts are
+compared bit for bit; Steinhardt within the tolerances written in each test."""
+
+import numpy as np
+import pytest
+from conftest import golden_names, load_golden
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+KIND_CLASS = {0: "_RawPoints", 1: "AABBQuery", 2: "LinkCell"}
+ARITH = {0: O.ARITH_AABB, 1: O.ARITH_AABB, 2: O.ARITH_WRAP}
+
+
+def box_of(freud, b):
+    return freud.box.Box(float(b[0]), float(b[1]), float(b[2]), float(b[3]), float(b[4]), float(b[5]), bool(b[6]))
+
+
+def make_nq(freud, kind, box, pts, cell_width=0.0):
+    if kind == 2:
+        return freud.locality.LinkCell(box, pts, cell_width)
+    if kind == 1:
+        return freud.locality.AABBQuery(box, pts)
+    return freud.locality._RawPoints(box, pts)
+
+
+def assert_nlist_equal(nl, ij, d, v):
+    assert len(nl) == len(ij)
+    np.testing.assert_array_equal(nl[:], ij)
+    np.testing.assert_array_equal(nl.distances, d)
+    np.testing.assert_array_equal(nl.vectors, v)
+
+
+@pytest.mark.parametrize("name", golden_names("ball_"))
+def test_ball_golden(freud, name):
+    g = load_golden(name)
+    box = box_of(freud, g["box"])
+    nq = make_nq(freud, int(g["kind"]), box, g["points"], float(g.get("cell_width", 0.0)))
+    qp = g.get("query_points")
+    args = dict(mode="ball", r_max=float(g["r_max"]), r_min=float(g.get("r_min", 0.0)), exclude_ii=qp is None)
+    nl = nq.query(g["points"] if qp is None else qp, args).toNeighborList(sort_by_distance=name.endswith("_bydist"))
+    assert_nlist_equal(nl, g["ij"], g["d"], g["v"])
+
+
+@pytest.mark.parametrize("name", golden_names("knn_"))
+def test_knn_golden(freud, name):
+    g = load_golden(name)
+    box = box_of(freud, g["box"])
+    nq = make_nq(freud, int(g["kind"]), box, g["points"], 1.6)
+    args = dict(num_neighbors=int(g["k"]), exclude_ii=name != "knn_aabb_rmax")
+    if "r_max" in g:
+        args["r_max"] = float(g["r_max"])
+    nl = nq.query(g["points"], args).toNeighborList()
+    assert_nlist_equal(nl, g["ij"], g["d"], g["v"])
+
+
+def test_rdf_plain_golden(freud):
+    g = load_golden("rdf_plain")
+    rdf = freud.density.RDF(int(g["bins"]), float(g["r_max"]))
+    rdf.compute((box_of(freud, g["box"]), g["points"]))
+    np.testing.assert_array_equal(rdf.bin_counts, g["counts"])
+    np.testing.assert_array_equal(rdf.rdf, g["rdf"])
+    np.testing.assert_array_equal(rdf.n_r, g["n_r"])
+
+
+def test_rdf_frames_golden(freud):
+    g = load_golden("rdf_frames")
+    rdf = freud.density.RDF(int(g["bins"]), float(g["r_max"]), float(g["r_min"]))
+    for f in range(int(g["nframes"])):
+        rdf.compute((box_of(freud, g["box%d" % f]), g["points%d" % f]), reset=(f == 0))
+    np.testing.assert_array_equal(rdf.bin_counts, g["counts"])
+    np.testing.assert_array_equal(rdf.rdf, g["rdf"])
+    np.testing.assert_array_equal(rdf.n_r, g["n_r"])
+
+
+def test_rdf_finite_size_golden(freud):
+    g = load_golden("rdf_finite_size")
+    rdf = freud.density.RDF(int(g["bins"]), float(g["r_max"]), normalization_mode="finite_size")
+    rdf.compute((box_of(freud, g["box"]), g["points"]), neighbors={"r_max": float(g["r_max"]), "exclude_ii": False})
+    np.testing.assert_array_equal(rdf.bin_counts, g["counts"])
+    np.testing.assert_array_equal(rdf.rdf, g["rdf"])
+    np.testing.assert_array_equal(rdf.n_r, g["n_r"])
+
+
+@pytest.mark.parametrize("name", golden_names("st_"))
+def test_steinhardt_golden(freud, name):
+    g = load_golden(name)
+    ls = [int(x) for x in g["ls"]]
+    av, wl, wn = bool(g.get("average", 0)), bool(g.get("wl", 0)), bool(g.get("wl_normalize", 0))
+    st = freud.order.Steinhardt(ls if len(ls) > 1 else ls[0], average=av, wl=wl, wl_normalize=wn)
+    neighbors = {"r_max": float(g["r_max"])} if "r_max" in g else {"num_neighbors": 12}
+    st.compute((box_of(freud, g["box"]), g["points"]), neighbors=neighbors)
+    ql = np.atleast_2d(np.asarray(st.ql).T).T.reshape(g["ql"].shape)
+    # Ql: 1e-5 relative to the reference (whose Ylm comes from the fsph stand-in)
+    np.testing.assert_allclose(ql, g["ql"], rtol=1e-5, atol=1e-6)
+    po = np.asarray(st.particle_order).reshape(g["particle_order"].shape)
+    scale = np.max(np.abs(g["particle_order"]), axis=0)
+    # Wl: the reference itself is float32 with cancellation; compare on the |w| scale
+    assert np.all(np.abs(po - g["particle_order"]) <= 5e-4 * scale + 1e-6)
+    np.testing.assert_allclose(np.atleast_1d(st.order), g["order"], rtol=5e-5, atol=1e-6)
+    qlm = st.particle_harmonics
+    qlm = np.concatenate([q.reshape(-1) for q in qlm]) if isinstance(qlm, list) else qlm.reshape(-1)
+    np.testing.assert_allclose(qlm, g["qlm"], atol=5e-6)
+
+
+# ---- larger seeded systems against the oracle ---------------------------------------
+
+def random_box_points(freud, L, n, seed, tilt=(0, 0, 0), is2d=False):
+    box = freud.box.Box(L, L, 0 if is2d else L, tilt[0], 0 if is2d else tilt[1], 0 if is2d else tilt[2], is2d)
+    rs = np.random.RandomState(seed)
+    f = rs.random_sample((n, 3))
+    if is2d:
+        f[:, 2] = 0
+    return box, box.make_absolute(f)
+
+
+@pytest.mark.parametrize("kind", [0, 2])
+@pytest.mark.parametrize("tilt", [(0, 0, 0), (0.2, 0.1, 0.0), (-0.4, 0.3, 0.2)])
+def test_ball_vs_oracle_medium(freud, kind, tilt):
+    box, pts = random_box_points(freud, 24.0, 20000, 7, tilt)
+    nq = make_nq(freud, kind, box, pts, 3.0)
+    nl = nq.query(pts, dict(r_max=3.0, exclude_ii=True)).toNeighborList()
+    ij, d, v = O.query(box, pts, r_max=3.0, exclude_ii=True, arith=ARITH[kind])
+    assert_nlist_equal(nl, ij, d, v)
+
+
+@pytest.mark.parametrize("kind", [1, 2])
+def test_knn_vs_oracle_medium(freud, kind):
+    box, pts = random_box_points(freud, 20.0, 8000, 9, (0.1, 0.0, 0.05))
+    nq = make_nq(freud, kind, box, pts, 2.0)
+    for k in (1, 6, 12, 32):
+        nl = nq.query(pts, dict(num_neighbors=k, exclude_ii=True)).toNeighborList()
+        ij, d, v = O.query(box, pts, num_neighbors=k, exclude_ii=True, arith=ARITH[kind])
+        assert_nlist_equal(nl, ij, d, v)
+
+
+def test_knn_large_k_small_system(freud):
+    box, pts = random_box_points(freud, 10.0, 500, 3)
+    nq = freud.locality.AABBQuery(box, pts)
+    nl = nq.query(pts, dict(num_neighbors=50, exclude_ii=True)).toNeighborList()
+    ij, d, v = O.query(box, pts, num_neighbors=50, exclude_ii=True)
+    assert_nlist_equal(nl, ij, d, v)
+
+
+def test_rdf_fused_vs_oracle_medium(freud):
+    box, pts = random_box_points(freud, 21.544, 10000, 5)
+    rdf = freud.density.RDF(200, 4.0)
+    rdf.compute((box, pts))
+    c = O.rdf_counts_query(box, pts, 200, 4.0)
+    np.testing.assert_array_equal(rdf.bin_counts_u64, c)
+
+
+def test_rdf_from_nlist_equals_fused(freud):
+    box, pts = random_box_points(freud, 18.0, 6000, 6, (0.2, 0.0, 0.0))
+    lc = freud.locality.LinkCell(box, pts, 3.0)
+    nl = lc.query(pts, dict(r_max=3.0, exclude_ii=True)).toNeighborList()
+    a = freud.density.RDF(300, 3.0).compute((box, pts), neighbors=nl)
+    b = freud.density.RDF(300, 3.0).compute(lc, neighbors=dict(r_max=3.0))
+    np.testing.assert_array_equal(a.bin_counts, b.bin_counts)
+    c = O.hist(nl.distances, 300, 3.0)
+    np.testing.assert_array_equal(a.bin_counts_u64, c)
+
+
+def test_heavy_queries(freud):
+    # dense system: every query has more bonds than the warp staging capacity
+    box, pts = random_box_points(freud, 6.0, 4000, 8)
+    for kind in (0, 2):
+        nq = make_nq(freud, kind, box, pts, 2.9)
+        nl = nq.query(pts, dict(r_max=2.9, exclude_ii=True)).toNeighborList()
+        ij, d, v = O.query(box, pts, r_max=2.9, exclude_ii=True, arith=ARITH[kind])
+        assert nl.neighbor_counts.max() > 256
+        assert_nlist_equal(nl, ij, d, v)
+
+
+def test_points_outside_box(freud):
+    box, pts = random_box_points(freud, 10.0, 800, 4)
+    shifted = pts.copy()
+    shifted[::3] += np.float32(10.0)  # one box length: same wrapped system
+    shifted[1::7] -= np.float32(10.0)
+    for kind in (0, 2):
+        nq = make_nq(freud, kind, box, shifted, 2.0)
+        nl = nq.query(shifted, dict(r_max=2.0, exclude_ii=True)).toNeighborList()
+        ij, d, v = O.query(box, shifted, r_max=2.0, exclude_ii=True, arith=ARITH[kind])
+        assert_nlist_equal(nl, ij, d, v)
+
+
+def test_small_box_few_cells(freud):
+    # LinkCell radius close to half the box: one or two cells per dimension
+    box, pts = random_box_points(freud, 5.0, 200, 12, (0.1, 0, 0))
+    lc = freud.locality.LinkCell(box, pts, 2.4)
+    nl = lc.query(pts, dict(r_max=2.45, exclude_ii=True)).toNeighborList()
+    ij, d, v = O.query(box, pts, r_max=2.45, exclude_ii=True, arith=O.ARITH_WRAP)
+    assert_nlist_equal(nl, ij, d, v)
+
+
+def test_empty_result(freud):
+    box, pts = random_box_points(freud, 10.0, 100, 1)
+    nq = freud.locality.AABBQuery(box, pts)
+    nl = nq.query(pts, dict(r_max=1e-4, exclude_ii=True)).toNeighborList()
+    assert len(nl) == 0
+    assert nl[:].shape == (0, 2)
+    np.testing.assert_array_equal(nl.neighbor_counts, np.zeros(100, np.uint32))
+
+
+def test_steinhardt_vs_fp64_oracle(freud):
+    """Ql within 1e-5 relative of the FP64 oracle; Wl within 1e-5 of the FP64 value
+    on the scale |w_l| + 1e-3 * max|w_l| (the per-particle sum cancels)."""
+    from golden.make_golden import fcc
+
+    box, pts = fcc(6, 1.5874, 0.05, 77)
+    fbox = box_of(freud, np.asarray(box, np.float32))
+    ls = [4, 6, 8, 10, 12]
+    st = freud.order.Steinhardt(ls, average=True, wl=True, wl_normalize=True)
+    st.compute((fbox, pts), neighbors={"num_neighbors": 12})
+    ij, d, v = O.query(box, pts, num_neighbors=12, exclude_ii=True)
+    o = O.steinhardt(ls, box, pts, ij, d, average=True, wl=True, wl_normalize=True)
+    np.testing.assert_allclose(st.ql, o["ql_ave"], rtol=1e-5)
+    w = o["wl"]
+    scale = np.abs(w) + 1e-3 * np.max(np.abs(w), axis=0)
+    err = np.max(np.abs(st.particle_order - w) / scale)
+    print("max Wl error on the |w| + 1e-3 max|w| scale:", err)
+    assert err < 1e-4
+    st2 = freud.order.Steinhardt(ls)
+    st2.compute((fbox, pts), neighbors={"num_neighbors": 12})
+    np.testing.assert_allclose(st2.ql, o["ql"], rtol=1e-5)
+    np.testing.assert_allclose(np.atleast_1d(st2.order), o["order"], rtol=1e-5)
