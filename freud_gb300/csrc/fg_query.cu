@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(QWARPS * 32)
     {
         for (int t = threadIdx.x; t < HIST_COPIES * static_cast<int>(h.bins); t += blockDim.x)
         {
-            s_hist[t] = 0;
+            s_hist[(t / h.bins) * HIST_SMEM_BINS + t % h.bins] = 0;
         }
     }
     __syncthreads();
@@ -529,7 +529,7 @@ __global__ void k_hist_distances(const float* __restrict__ dist, uint64_t nb, Hi
     {
         for (int t = threadIdx.x; t < HIST_COPIES * static_cast<int>(h.bins); t += blockDim.x)
         {
-            s_hist[t] = 0;
+            s_hist[(t / h.bins) * HIST_SMEM_BINS + t % h.bins] = 0;
         }
     }
     __syncthreads();
