@@ -488,6 +488,7 @@ struct QuerySet
 {
     const float4* qpos;
     const uint32_t* qidx;
+    DevGrid qg;
     GridEntry own;
 };
 
@@ -497,11 +498,36 @@ void make_query_set(fg_nq* nq, const GridEntry& g, const float* dq, uint32_t nqp
     {
         qs.qpos = g.cpos.as<float4>();
         qs.qidx = g.cidx.as<uint32_t>();
+        qs.qg = view(g);
         return;
     }
     build_grid(nq->dbox, dq, nqp, g.dim, qs.own);
     qs.qpos = qs.own.cpos.as<float4>();
     qs.qidx = qs.own.cidx.as<uint32_t>();
+    qs.qg = view(qs.own);
+}
+
+// Squared prefilter radius for the block-per-cell kernels (0 disables): wrap
+// arithmetic only, >= 3 cells on every periodic axis, and r_max + delta below half
+// the smallest nearest-plane distance, so the cell-derived image is the minimum image.
+float prefilter_r2(const fg_nq* nq, int arith, const int dim[3], float r_max)
+{
+    if (arith != ARITH_WRAP)
+        return 0.0f;
+    if (dim[0] < 3 || dim[1] < 3 || (!nq->box.is2d && dim[2] < 3))
+        return 0.0f;
+    float pd[3];
+    nearest_plane(nq->box, pd);
+    double minp = std::min(pd[0], pd[1]);
+    if (!nq->box.is2d)
+        minp = std::min(minp, static_cast<double>(pd[2]));
+    const double lmax = std::max(std::max(nq->box.L[0], nq->box.L[1]), nq->box.L[2]) *
+        (1.0 + std::abs(nq->box.xy) + std::abs(nq->box.xz) + std::abs(nq->box.yz));
+    const double delta = 2e-5 * (lmax + r_max) + 1e-6;
+    if (!(r_max + delta < 0.5 * minp))
+        return 0.0f;
+    const double r = r_max + delta;
+    return static_cast<float>(r * r * (1.0 + 1e-6));
 }
 
 // Ball query -> NeighborList in reference order (count, scan, emit).
@@ -528,13 +554,27 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     p.exclude_ii = a.exclude_ii;
     p.arith = arith;
     p.nq = nqp;
-    DevBuf counts, offsets, scratch, heavy, heavy_n;
+    const float pre_r2 = prefilter_r2(nq, arith, dim, a.r_max);
+    DevBuf counts, offsets, scratch, heavy, heavy_n, over, over_n;
     counts.alloc(sizeof(uint32_t) * (nqp + 1));
     offsets.alloc(sizeof(uint64_t) * (nqp + 1));
     scratch.alloc(scan_scratch_bytes(nqp + 1));
+    over.alloc(sizeof(uint32_t) * (nqp + 1));
+    over_n.alloc(sizeof(uint32_t));
     FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (nqp + 1), s));
+    FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
     reset_dev_err();
-    launch_ball_count(nq->dbox, view(g), qs.qpos, qs.qidx, p, counts.as<uint32_t>(), s);
+    launch_cell(0, nq->dbox, view(g), qs.qg, p, pre_r2, counts.as<uint32_t>(), nullptr, nullptr, nullptr, nullptr,
+                over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s);
+    uint32_t n_over = 0;
+    FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    sync();
+    if (n_over > 0)
+    {
+        BallParams po = p;
+        po.nq = n_over;
+        launch_ball_count(nq->dbox, view(g), qs.qpos, qs.qidx, po, counts.as<uint32_t>(), s, over.as<uint32_t>());
+    }
     scan_u32_to_u64(counts.as<uint32_t>(), offsets.as<uint64_t>(), nqp + 1, scratch.p, s);
     uint64_t total = 0;
     FG_CUDA(cudaMemcpyAsync(&total, offsets.as<uint64_t>() + nqp, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
@@ -552,23 +592,40 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     heavy.alloc(sizeof(uint32_t) * (nqp + 1));
     heavy_n.alloc(sizeof(uint32_t));
     FG_CUDA(cudaMemsetAsync(heavy_n.p, 0, sizeof(uint32_t), s));
-    launch_ball_emit(nq->dbox, view(g), qs.qpos, qs.qidx, p, counts.as<uint32_t>(), offsets.as<uint64_t>(), by_distance,
-                     out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(), heavy.as<uint32_t>(),
-                     heavy_n.as<uint32_t>(), dev_err(), s);
-    uint32_t nh = 0;
-    FG_CUDA(cudaMemcpyAsync(&nh, heavy_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    sync();
-    launch_ball_emit_heavy(nq->dbox, view(g), qs.qpos, qs.qidx, p, counts.as<uint32_t>(), offsets.as<uint64_t>(),
-                           by_distance, heavy.as<uint32_t>(), nh, out.ij.as<uint2>(), out.dist.as<float>(),
-                           out.vec.as<float>(), dev_err(), s);
+    const uint32_t* list = nullptr;
+    uint32_t nlist = nqp;
+    if (!by_distance)
+    {
+        FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
+        launch_cell(1, nq->dbox, view(g), qs.qg, p, pre_r2, counts.as<uint32_t>(), offsets.as<uint64_t>(),
+                    out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(), over.as<uint32_t>(),
+                    over_n.as<uint32_t>(), HistParams {}, nullptr, s);
+        FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        sync();
+        list = over.as<uint32_t>();
+        nlist = n_over;
+    }
+    if (nlist > 0)
+    {
+        BallParams po = p;
+        po.nq = nlist;
+        launch_ball_emit(nq->dbox, view(g), qs.qpos, qs.qidx, po, counts.as<uint32_t>(), offsets.as<uint64_t>(),
+                         by_distance, out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(),
+                         heavy.as<uint32_t>(), heavy_n.as<uint32_t>(), dev_err(), s, list);
+        uint32_t nh = 0;
+        FG_CUDA(cudaMemcpyAsync(&nh, heavy_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        sync();
+        launch_ball_emit_heavy(nq->dbox, view(g), qs.qpos, qs.qidx, p, counts.as<uint32_t>(), offsets.as<uint64_t>(),
+                               by_distance, heavy.as<uint32_t>(), nh, out.ij.as<uint2>(), out.dist.as<float>(),
+                               out.vec.as<float>(), dev_err(), s);
+    }
     FG_CUDA(cudaGetLastError());
-    check_dev_err("ball query");
-    // keep the counts as the list's segment counts
+    // segments / counts of the list straight from the query counts and offsets
+    out.seg.alloc(sizeof(uint32_t) * std::max<uint32_t>(nqp, 1));
+    launch_segments_from_offsets(counts.as<uint32_t>(), offsets.as<uint64_t>(), nqp, out.seg.as<uint32_t>(), s);
     out.cnt = std::move(counts);
-    out.seg.alloc(sizeof(uint32_t) * nqp);
-    // segments = offsets (first bond of each query; 0 for empty queries after the reference's rule)
-    launch_segments(out.ij.as<uint2>(), out.nb, nqp, out.seg.as<uint32_t>(), out.cnt.as<uint32_t>(), s);
     out.seg_valid = true;
+    check_dev_err("ball query");
 }
 
 // kNN query -> NeighborList (AABBQuery.cc:152-281 / LinkCell.cc:575-679).
@@ -668,9 +725,9 @@ void knn_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a,
     launch_knn_compact(tj.as<uint32_t>(), td.as<float>(), tv.as<float>(), std::max<uint32_t>(k, 1), nqp,
                        counts.as<uint32_t>(), offsets.as<uint64_t>(), by_distance, out.ij.as<uint2>(),
                        out.dist.as<float>(), out.vec.as<float>(), s);
+    out.seg.alloc(sizeof(uint32_t) * std::max<uint32_t>(nqp, 1));
+    launch_segments_from_offsets(counts.as<uint32_t>(), offsets.as<uint64_t>(), nqp, out.seg.as<uint32_t>(), s);
     out.cnt = std::move(counts);
-    out.seg.alloc(sizeof(uint32_t) * nqp);
-    launch_segments(out.ij.as<uint2>(), out.nb, nqp, out.seg.as<uint32_t>(), out.cnt.as<uint32_t>(), s);
     out.seg_valid = true;
     FG_CUDA(cudaGetLastError());
     sync();
@@ -1384,7 +1441,23 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
             p.exclude_ii = a.exclude_ii;
             p.arith = arith;
             p.nq = nqp;
-            launch_ball_hist(nq->dbox, view(g), qs.qpos, qs.qidx, p, h, rdf->hist.as<unsigned long long>(), s);
+            DevBuf over, over_n;
+            over.alloc(sizeof(uint32_t) * (nqp + 1));
+            over_n.alloc(sizeof(uint32_t));
+            FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
+            launch_cell(2, nq->dbox, view(g), qs.qg, p, prefilter_r2(nq, p.arith, dim, a.r_max), nullptr, nullptr,
+                        nullptr, nullptr, nullptr, over.as<uint32_t>(), over_n.as<uint32_t>(), h,
+                        rdf->hist.as<unsigned long long>(), s);
+            uint32_t n_over = 0;
+            FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            sync();
+            if (n_over > 0)
+            {
+                BallParams po = p;
+                po.nq = n_over;
+                launch_ball_hist(nq->dbox, view(g), qs.qpos, qs.qidx, po, h, rdf->hist.as<unsigned long long>(), s,
+                                 over.as<uint32_t>());
+            }
             FG_CUDA(cudaGetLastError());
             sync();
         }

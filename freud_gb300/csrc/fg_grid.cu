@@ -312,4 +312,26 @@ void launch_segments(const uint2* ij, uint64_t nb, uint32_t nq, uint32_t* segmen
     }
 }
 
+__global__ void k_seg_from_offsets(const uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets,
+                                   uint32_t nq, uint32_t* __restrict__ segments)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x)
+    {
+        segments[i] = counts[i] != 0 ? static_cast<uint32_t>(offsets[i]) : 0u;
+    }
+}
+
+void launch_segments_from_offsets(const uint32_t* counts, const uint64_t* offsets, uint32_t nq, uint32_t* segments,
+                                  cudaStream_t s)
+{
+    if (nq == 0)
+    {
+        return;
+    }
+    {
+        ProfScope prof_("k_seg_from_offsets", s);
+        k_seg_from_offsets<<<grid_for(nq, 256), 256, 0, s>>>(counts, offsets, nq, segments);
+    }
+}
+
 } // namespace fg

@@ -53,15 +53,16 @@ struct BallParams
 };
 
 // counts[i] = number of bonds of query i (original query index).
+// list (optional): process only these positions of the sorted query array; p.nq is then the list length.
 void launch_ball_count(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
-                       const BallParams& p, uint32_t* counts, cudaStream_t s);
+                       const BallParams& p, uint32_t* counts, cudaStream_t s, const uint32_t* list = nullptr);
 
 // Writes bonds in reference order at offsets[i]. Queries with more than EMIT_CAP
 // bonds are appended to heavy_list (heavy_count) and written by launch_ball_emit_heavy.
 void launch_ball_emit(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
                       const BallParams& p, const uint32_t* counts, const uint64_t* offsets, int by_distance,
                       uint2* ij, float* dist, float* vec, uint32_t* heavy_list, uint32_t* heavy_count,
-                      int* err, cudaStream_t s);
+                      int* err, cudaStream_t s, const uint32_t* list = nullptr);
 void launch_ball_emit_heavy(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
                             const BallParams& p, const uint32_t* counts, const uint64_t* offsets,
                             int by_distance, const uint32_t* heavy_list, uint32_t n_heavy, uint2* ij,
@@ -75,7 +76,17 @@ struct HistParams
     uint32_t bins;
 };
 void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
-                      const BallParams& p, const HistParams& h, unsigned long long* hist, cudaStream_t s);
+                      const BallParams& p, const HistParams& h, unsigned long long* hist, cudaStream_t s,
+                      const uint32_t* list = nullptr);
+
+// Block-per-cell ball kernels (mode 0 count, 1 emit in (i, j) order, 2 fused histogram).
+// qg is the cell-sorted query grid (same dims as g). Queries of cells that exceed the
+// shared-memory capacity are appended to overflow for the warp-per-query kernels.
+// pre_r2 > 0 enables the wrap-arithmetic prefilter with that squared radius.
+size_t cell_smem_bytes();
+void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_r2,
+                 uint32_t* counts, const uint64_t* offsets, uint2* ij, float* dist, float* vec, uint32_t* overflow,
+                 uint32_t* overflow_n, const HistParams& h, unsigned long long* hist, cudaStream_t s);
 
 // Histogram of a distance array (RDF over a NeighborList).
 void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,
@@ -116,5 +127,8 @@ void launch_knn_compact(const uint32_t* tj, const float* td, const float* tv, ui
 void launch_fill_f32(float* a, float v, uint64_t n, cudaStream_t s);
 void launch_segments(const uint2* ij, uint64_t nb, uint32_t nq, uint32_t* segments, uint32_t* counts,
                      cudaStream_t s);
+// segments[i] = counts[i] ? offsets[i] : 0 (NeighborList.cc:199-232 for a list built in query order)
+void launch_segments_from_offsets(const uint32_t* counts, const uint64_t* offsets, uint32_t nq, uint32_t* segments,
+                                  cudaStream_t s);
 
 } // namespace fg

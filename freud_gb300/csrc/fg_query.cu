@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(QWARPS * 32)
     k_ball(DevBox b, DevGrid g, const float4* __restrict__ qpos, const uint32_t* __restrict__ qidx, BallParams p,
            uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets, int by_distance, uint2* __restrict__ ij,
            float* __restrict__ dist, float* __restrict__ vec, uint32_t* heavy_list, uint32_t* heavy_count, int* err,
-           HistParams h, unsigned long long* __restrict__ hist)
+           HistParams h, unsigned long long* __restrict__ hist, const uint32_t* __restrict__ list)
 {
     __shared__ float s_img[27][3];
     __shared__ WarpStage s_stage[MODE == MODE_EMIT ? QWARPS : 1];
@@ -256,8 +256,9 @@ __global__ void __launch_bounds__(QWARPS * 32)
     const int warp = threadIdx.x >> 5;
     unsigned int* my_hist = s_hist + (warp % HIST_COPIES) * HIST_SMEM_BINS;
 
-    for (uint32_t t = blockIdx.x * QWARPS + warp; t < p.nq; t += gridDim.x * QWARPS)
+    for (uint32_t tl = blockIdx.x * QWARPS + warp; tl < p.nq; tl += gridDim.x * QWARPS)
     {
+        const uint32_t t = list != nullptr ? list[tl] : tl;
         const float4 q = qpos[t];
         const uint32_t qi = qidx[t];
         if (MODE == MODE_EMIT)
@@ -588,7 +589,7 @@ int query_blocks(uint32_t nq)
 } // namespace
 
 void launch_ball_count(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
-                       const BallParams& p, uint32_t* counts, cudaStream_t s)
+                       const BallParams& p, uint32_t* counts, cudaStream_t s, const uint32_t* list)
 {
     if (p.nq == 0)
     {
@@ -598,14 +599,14 @@ void launch_ball_count(const DevBox& box, const DevGrid& g, const float4* qpos, 
         ProfScope prof_("k_ball<MODE_COUNT>", s);
         k_ball<MODE_COUNT><<<query_blocks(p.nq), QWARPS * 32, 0, s>>>(box, g, qpos, qidx, p, counts, nullptr, 0, nullptr,
                                                                        nullptr, nullptr, nullptr, nullptr, nullptr,
-                                                                       HistParams {}, nullptr);
+                                                                       HistParams {}, nullptr, list);
     }
 }
 
 void launch_ball_emit(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
                       const BallParams& p, const uint32_t* counts, const uint64_t* offsets, int by_distance,
                       uint2* ij, float* dist, float* vec, uint32_t* heavy_list, uint32_t* heavy_count, int* err,
-                      cudaStream_t s)
+                      cudaStream_t s, const uint32_t* list)
 {
     if (p.nq == 0)
     {
@@ -615,7 +616,7 @@ void launch_ball_emit(const DevBox& box, const DevGrid& g, const float4* qpos, c
         ProfScope prof_("k_ball<MODE_EMIT>", s);
         k_ball<MODE_EMIT><<<query_blocks(p.nq), QWARPS * 32, 0, s>>>(box, g, qpos, qidx, p, const_cast<uint32_t*>(counts),
                                                                       offsets, by_distance, ij, dist, vec, heavy_list,
-                                                                      heavy_count, err, HistParams {}, nullptr);
+                                                                      heavy_count, err, HistParams {}, nullptr, list);
     }
 }
 
@@ -643,7 +644,8 @@ void launch_ball_emit_heavy(const DevBox& box, const DevGrid& g, const float4* q
 }
 
 void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
-                      const BallParams& p, const HistParams& h, unsigned long long* hist, cudaStream_t s)
+                      const BallParams& p, const HistParams& h, unsigned long long* hist, cudaStream_t s,
+                      const uint32_t* list)
 {
     if (p.nq == 0)
     {
@@ -653,7 +655,7 @@ void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, c
         ProfScope prof_("k_ball<MODE_HIST>", s);
         k_ball<MODE_HIST><<<query_blocks(p.nq), QWARPS * 32, 0, s>>>(box, g, qpos, qidx, p, nullptr, nullptr, 0, nullptr,
                                                                       nullptr, nullptr, nullptr, nullptr, nullptr, h,
-                                                                      hist);
+                                                                      hist, list);
     }
 }
 

@@ -931,10 +931,12 @@ static int lm_index(int l, int m)
     return m < 0 ? l - m : m; /* Wigner3j.cc:17-20 */
 }
 
-/* Wigner3j.cc:22-57 in double */
-static double reduce_w3j(const double* q /* 2*(2l+1) */, int l)
+/* Wigner3j.cc:22-57 in double; *mag (optional) receives the sum of |terms|, the
+ * scale against which the cancellation in the sum is judged. */
+static double reduce_w3j_mag(const double* q /* 2*(2l+1) */, int l, double* mag)
 {
     double res = 0.0;
+    double m_abs = 0.0;
     for (int m1 = -l; m1 <= l; ++m1)
     {
         const int lo = (-l - m1) > -l ? (-l - m1) : -l;
@@ -948,10 +950,19 @@ static double reduce_w3j(const double* q /* 2*(2l+1) */, int l)
             const double* c = q + 2 * lm_index(l, m3);
             const double abr = a[0] * b[0] - a[1] * b[1];
             const double abi = a[0] * b[1] + a[1] * b[0];
-            res += w * (abr * c[0] - abi * c[1]);
+            const double term = w * (abr * c[0] - abi * c[1]);
+            res += term;
+            m_abs += fabs(term);
         }
     }
+    if (mag)
+        *mag = m_abs;
     return res;
+}
+
+static double reduce_w3j(const double* q, int l)
+{
+    return reduce_w3j_mag(q, l, NULL);
 }
 
 /* Steinhardt over a NeighborList sorted by query index (Steinhardt.cc:120-359).
@@ -965,7 +976,7 @@ static double reduce_w3j(const double* q /* 2*(2l+1) */, int l)
 int ofg_steinhardt(const uint32_t* ls, uint32_t nl, int average, int wl, int weighted, int wl_normalize,
                    const float* box7, const float* pts, uint32_t n, uint64_t nbonds, const uint32_t* ij,
                    const float* bond_dist, const float* bond_w, double* ql, double* ql_ave, double* wl_out,
-                   double* qlm, double* order)
+                   double* qlm, double* order, double* wl_mag)
 {
     obox box;
     box_init(&box, box7);
@@ -1091,13 +1102,17 @@ int ofg_steinhardt(const uint32_t* ls, uint32_t nl, int average, int wl, int wei
             for (uint32_t k = 0; k < nl; ++k)
             {
                 const int l = (int) ls[k];
-                double v = reduce_w3j(&src[2 * ((size_t) i * stride + off)], l);
+                double mag = 0.0;
+                double v = reduce_w3j_mag(&src[2 * ((size_t) i * stride + off)], l, &mag);
                 if (wl_normalize)
                 {
                     const double nf = sqrt(4.0 * M_PI / (2 * l + 1)) / nsrc[(size_t) i * nl + k];
                     v *= nf * nf * nf;
+                    mag *= nf * nf * nf;
                 }
                 wl_out[(size_t) i * nl + k] = v;
+                if (wl_mag)
+                    wl_mag[(size_t) i * nl + k] = mag;
                 off += 2 * l + 1;
             }
         }

@@ -52,7 +52,7 @@ def _load():
     lib.ofg_wigner3j.restype = ctypes.c_double
     lib.ofg_wigner3j.argtypes = [i32, i32, i32, i32]
     lib.ofg_steinhardt.restype = i32
-    lib.ofg_steinhardt.argtypes = [P, u32, i32, i32, i32, i32, P, P, u32, u64, P, P, P, P, P, P, P, P]
+    lib.ofg_steinhardt.argtypes = [P, u32, i32, i32, i32, i32, P, P, u32, u64, P, P, P, P, P, P, P, P, P]
     lib.ofg_box_wrap.argtypes = [P, P, u64, P]
     lib.ofg_box_fractional.argtypes = [P, P, u64, P]
     _lib = lib
@@ -159,7 +159,8 @@ def wigner3j(l, m1, m2, m3):
 def steinhardt(ls, box, points, ij, distances, weights=None, average=False, wl=False, weighted=False,
                wl_normalize=False):
     """FP64 Steinhardt over a NeighborList sorted by query index. Returns a dict with
-    ql, ql_ave, wl (N, nl) float64, qlm list of (N, 2l+1) complex128, order (nl,)."""
+    ql, ql_ave, wl (N, nl) float64, wl_mag (N, nl) = sum of |Wigner-3j terms| (the
+    scale of the cancellation in w_l), qlm list of (N, 2l+1) complex128, order (nl,)."""
     lib = _load()
     ls = np.asarray(np.atleast_1d(ls), np.uint32)
     b = box7(box)
@@ -175,14 +176,15 @@ def steinhardt(ls, box, points, ij, distances, weights=None, average=False, wl=F
     wlo = np.zeros((n, nl))
     qlm = np.zeros((n, stride, 2))
     order = np.zeros(nl)
+    wmag = np.zeros((n, nl))
     lib.ofg_steinhardt(_p(ls), nl, int(average), int(wl), int(weighted), int(wl_normalize), _p(b), _p(pts), n,
-                       len(d), _p(ij), _p(d), _p(w), _p(ql), _p(qla), _p(wlo), _p(qlm), _p(order))
+                       len(d), _p(ij), _p(d), _p(w), _p(ql), _p(qla), _p(wlo), _p(qlm), _p(order), _p(wmag))
     qc = qlm[..., 0] + 1j * qlm[..., 1]
     out, off = [], 0
     for l in ls:
         out.append(qc[:, off:off + 2 * l + 1])
         off += 2 * l + 1
-    return {"ql": ql, "ql_ave": qla, "wl": wlo, "qlm": out, "order": order}
+    return {"ql": ql, "ql_ave": qla, "wl": wlo, "wl_mag": wmag, "qlm": out, "order": order}
 
 
 def box_wrap(box, vecs):

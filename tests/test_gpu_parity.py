@@ -205,8 +205,10 @@ def test_empty_result(freud):
 
 
 def test_steinhardt_vs_fp64_oracle(freud):
-    """Ql within 1e-5 relative of the FP64 oracle; Wl within 1e-5 of the FP64 value
-    on the scale |w_l| + 1e-3 * max|w_l| (the per-particle sum cancels)."""
+    """Ql within 1e-5 relative of the FP64 oracle. Wl: |dw| <= 1e-5 |w| + 2e-6 M, where
+    M is the sum of the magnitudes of the Wigner-3j terms (the float32 qlm feeding
+    the sum carry ~1e-7 relative error, which the cancellation in the sum amplifies
+    by M / |w|); where M / |w| is small this is a 1e-5 relative bound."""
     from golden.make_golden import fcc
 
     box, pts = fcc(6, 1.5874, 0.05, 77)
@@ -217,12 +219,13 @@ def test_steinhardt_vs_fp64_oracle(freud):
     ij, d, v = O.query(box, pts, num_neighbors=12, exclude_ii=True)
     o = O.steinhardt(ls, box, pts, ij, d, average=True, wl=True, wl_normalize=True)
     np.testing.assert_allclose(st.ql, o["ql_ave"], rtol=1e-5)
-    w = o["wl"]
-    scale = np.abs(w) + 1e-3 * np.max(np.abs(w), axis=0)
-    err = np.max(np.abs(st.particle_order - w) / scale, axis=0)
-    print("max Wl error per l on the |w| + 1e-3 max|w| scale:", err)
-    assert np.all(err < 5e-4)
+    w, mag = o["wl"], o["wl_mag"]
+    err = np.abs(st.particle_order - w)
+    print("max |dw| / |w| per l:", np.max(err / np.abs(w), axis=0))
+    print("max |dw| / M per l:", np.max(err / mag, axis=0))
+    assert np.all(err <= 1e-5 * np.abs(w) + 2e-6 * mag)
     st2 = freud.order.Steinhardt(ls)
     st2.compute((fbox, pts), neighbors={"num_neighbors": 12})
-    np.testing.assert_allclose(st2.ql, o["ql"], rtol=1e-5)
-    np.testing.assert_allclose(np.atleast_1d(st2.order), o["order"], rtol=1e-5)
+    o2 = O.steinhardt(ls, box, pts, ij, d)
+    np.testing.assert_allclose(st2.ql, o2["ql"], rtol=1e-5)
+    np.testing.assert_allclose(np.atleast_1d(st2.order), o2["order"], rtol=1e-5)
