@@ -507,15 +507,23 @@ void make_query_set(fg_nq* nq, const GridEntry& g, const float* dq, uint32_t nqp
     qs.qg = view(qs.own);
 }
 
-// Squared prefilter radius for the block-per-cell kernels (0 disables): wrap
-// arithmetic only, >= 3 cells on every periodic axis, and r_max + delta below half
-// the smallest nearest-plane distance, so the cell-derived image is the minimum image.
-float prefilter_r2(const fg_nq* nq, int arith, const int dim[3], float r_max)
+// Prefilter radii for the block-per-cell kernels (0 disables): wrap arithmetic only,
+// >= 3 cells on every periodic axis, and r_max + delta below half the smallest
+// nearest-plane distance, so the cell-derived image is the minimum image. delta
+// bounds the difference between the cell-shifted float distance and the exact one.
+struct Prefilter
 {
+    float out2 = 0.0f; // reject beyond
+    float in2 = 0.0f;  // accept inside without the exact test (count pass, r_min == 0)
+};
+
+Prefilter prefilter(const fg_nq* nq, int arith, const int dim[3], float r_max, float r_min)
+{
+    Prefilter pf;
     if (arith != ARITH_WRAP)
-        return 0.0f;
+        return pf;
     if (dim[0] < 3 || dim[1] < 3 || (!nq->box.is2d && dim[2] < 3))
-        return 0.0f;
+        return pf;
     float pd[3];
     nearest_plane(nq->box, pd);
     double minp = std::min(pd[0], pd[1]);
@@ -525,9 +533,15 @@ float prefilter_r2(const fg_nq* nq, int arith, const int dim[3], float r_max)
         (1.0 + std::abs(nq->box.xy) + std::abs(nq->box.xz) + std::abs(nq->box.yz));
     const double delta = 2e-5 * (lmax + r_max) + 1e-6;
     if (!(r_max + delta < 0.5 * minp))
-        return 0.0f;
-    const double r = r_max + delta;
-    return static_cast<float>(r * r * (1.0 + 1e-6));
+        return pf;
+    const double ro = r_max + delta;
+    pf.out2 = static_cast<float>(ro * ro * (1.0 + 1e-6));
+    if (r_min == 0.0f && r_max > 2.0 * delta)
+    {
+        const double ri = r_max - delta;
+        pf.in2 = static_cast<float>(ri * ri * (1.0 - 1e-6));
+    }
+    return pf;
 }
 
 // Ball query -> NeighborList in reference order (count, scan, emit).
@@ -554,7 +568,7 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     p.exclude_ii = a.exclude_ii;
     p.arith = arith;
     p.nq = nqp;
-    const float pre_r2 = prefilter_r2(nq, arith, dim, a.r_max);
+    const Prefilter pf = prefilter(nq, arith, dim, a.r_max, a.r_min);
     DevBuf counts, offsets, scratch, heavy, heavy_n, over, over_n;
     counts.alloc(sizeof(uint32_t) * (nqp + 1));
     offsets.alloc(sizeof(uint64_t) * (nqp + 1));
@@ -564,8 +578,8 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (nqp + 1), s));
     FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
     reset_dev_err();
-    launch_cell(0, nq->dbox, view(g), qs.qg, p, pre_r2, counts.as<uint32_t>(), nullptr, nullptr, nullptr, nullptr,
-                over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s);
+    launch_cell(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, counts.as<uint32_t>(), nullptr, nullptr, nullptr,
+                nullptr, over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s);
     uint32_t n_over = 0;
     FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     sync();
@@ -597,7 +611,7 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     if (!by_distance)
     {
         FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
-        launch_cell(1, nq->dbox, view(g), qs.qg, p, pre_r2, counts.as<uint32_t>(), offsets.as<uint64_t>(),
+        launch_cell(1, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, counts.as<uint32_t>(), offsets.as<uint64_t>(),
                     out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(), over.as<uint32_t>(),
                     over_n.as<uint32_t>(), HistParams {}, nullptr, s);
         FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -1445,9 +1459,9 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
             over.alloc(sizeof(uint32_t) * (nqp + 1));
             over_n.alloc(sizeof(uint32_t));
             FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
-            launch_cell(2, nq->dbox, view(g), qs.qg, p, prefilter_r2(nq, p.arith, dim, a.r_max), nullptr, nullptr,
-                        nullptr, nullptr, nullptr, over.as<uint32_t>(), over_n.as<uint32_t>(), h,
-                        rdf->hist.as<unsigned long long>(), s);
+            const Prefilter pf = prefilter(nq, p.arith, dim, a.r_max, a.r_min);
+            launch_cell(2, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr,
+                        over.as<uint32_t>(), over_n.as<uint32_t>(), h, rdf->hist.as<unsigned long long>(), s);
             uint32_t n_over = 0;
             FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
             sync();

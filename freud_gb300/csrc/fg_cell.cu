@@ -1,26 +1,29 @@
-// Ball queries, block per home cell.
+// Ball queries, block per home cell, warp per query with compacted exact tests.
 //
 // A block takes one cell of the query grid and stages the candidate set shared by
 // all of its queries - the points of the 27 (9 in 2D) neighbouring cells, each
-// with its cell wrap - in shared memory once. Each warp then holds a chunk of 32
-// candidates in registers and sweeps the cell's queries (broadcast from shared
-// memory), so a candidate position is read from shared memory once per chunk
-// rather than once per query.
+// with its cell wrap - in shared memory once. Each warp then takes one query of
+// the cell at a time and scans the staged candidates 32 per step.
 //
 // Pair arithmetic is exact and identical to the warp-per-query kernels
-// (AABBQuery.cc:93,125 / LinkCell.cc:522). In wrap arithmetic a cheap prefilter
-// first rejects candidates whose cell-shifted distance exceeds r_max + delta; it
-// is only enabled when every periodic axis has >= 3 cells and r_max + delta is
-// below half the smallest plane distance, where the cell-derived image is the
-// minimum image of every possible bond.
+// (AABBQuery.cc:93,125 / LinkCell.cc:522). In wrap arithmetic the exact
+// box.wrap (three IEEE divisions) is expensive, so a cheap prefilter on the
+// cell-shifted positions classifies each candidate as certainly outside
+// (> r_max + delta), certainly inside (< r_max - delta) or undecided. Candidates
+// that need the exact test are appended to a per-warp queue in scan order and
+// tested 32 at a time, so the exact arithmetic runs with full lanes. The
+// prefilter is only enabled when every periodic axis has >= 3 cells and
+// r_max + delta is below half the smallest plane distance, where the
+// cell-derived image is the minimum image of every possible bond.
 //
-// COUNT: bonds per query. EMIT: the candidate set is sorted by point index once
-// per cell, so each query's accepted candidates come out in the reference's
-// (i, j) order (NeighborBond.h:80-95) without a per-query sort; the first sweep
-// stores one ballot mask per (query, chunk), an exclusive scan turns them into
-// write offsets, the second sweep writes the bonds. HIST: fused RDF binning.
-// Cells whose candidate set or query count exceed the shared-memory capacity
-// hand their queries to the warp-per-query kernels.
+// COUNT: bonds per query (candidates certainly inside need no exact test).
+// EMIT:  the staged candidates are sorted by point index once per cell, so the
+//        queue - and hence each query's accepted bonds - comes out in the
+//        reference's (i, j) order (NeighborBond.h:80-95); bonds are written at the
+//        query's offset as they are accepted, 32 consecutive slots at a time.
+// HIST:  fused RDF binning (RDF.cc:101-110, Histogram.h:152-174).
+// Cells whose candidate set exceeds the shared-memory capacity hand their queries
+// to the warp-per-query kernels.
 #include "fg_kernels.cuh"
 #include "fg_prof.cuh"
 
@@ -29,11 +32,9 @@ namespace fg {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int CWARPS = 16;
+constexpr int CWARPS = 8;
 constexpr int CTHREADS = CWARPS * 32;
-constexpr int CAP = 2048;         // staged candidates per cell
-constexpr int CHUNKS = CAP / 32;  // candidate chunks
-constexpr int QMAX = 96;          // queries per cell handled in shared memory (EMIT)
+constexpr int CAP = 2048; // staged candidates per cell
 constexpr int HIST_BINS_SMEM = 4096;
 
 enum CellMode
@@ -50,16 +51,12 @@ __device__ __forceinline__ int img_ax(int bits, int axis)
 
 struct CellShared
 {
-    float4 pos[CAP];               // x, y, z, packed image (AABB) / unused (wrap)
-    float4 ps[CAP];                // prefilter position (wrap arithmetic)
-    uint32_t j[CAP];               // point index
-    unsigned char wrap[CAP];       // cell wrap code (wx+1) + 3(wy+1) + 9(wz+1)
-    unsigned long long key[CAP];   // (j << 32) | slot for the per-cell sort (EMIT)
-    uint32_t mask[QMAX][CHUNKS];   // ballot per (query, chunk) (EMIT)
-    unsigned short moff[QMAX][CHUNKS]; // exclusive offsets of the masks (EMIT)
-    float4 q[QMAX];
-    uint32_t qi[QMAX];
-    uint32_t qcount[QMAX];
+    float4 pos[CAP];             // x, y, z, packed integer box image
+    float4 ps[CAP];              // prefilter position (wrap arithmetic)
+    uint32_t j[CAP];             // point index
+    unsigned char wrap[CAP];     // cell wrap code (wx+1) + 3(wy+1) + 9(wz+1)
+    unsigned long long key[CAP]; // (j << 32) | slot, sorted per cell (EMIT)
+    unsigned short queue[CWARPS][64];
     uint32_t item_start[32];
     uint32_t item_off[33];
     int item_wrap[32];
@@ -92,7 +89,7 @@ __device__ __forceinline__ bool exact_vec(const DevBox& b, const float (*img)[3]
     return true;
 }
 
-// Approximate in-box position shifted by integer lattice multiples (prefilter only).
+// Approximate position shifted by integer lattice multiples (prefilter only).
 __device__ __forceinline__ float3 shifted(const DevBox& b, float4 p, int sx, int sy, int sz)
 {
     float3 r;
@@ -103,19 +100,21 @@ __device__ __forceinline__ float3 shifted(const DevBox& b, float4 p, int sx, int
 }
 
 template<int MODE>
-__global__ void __launch_bounds__(CTHREADS, 1)
-    k_cell(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_r2, uint32_t* __restrict__ counts,
-           const uint64_t* __restrict__ offsets, uint2* __restrict__ ij, float* __restrict__ dist,
-           float* __restrict__ vec, uint32_t* overflow, uint32_t* overflow_n, HistParams h,
+__global__ void __launch_bounds__(CTHREADS, 2)
+    k_cell(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2,
+           uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets, uint2* __restrict__ ij,
+           float* __restrict__ dist, float* __restrict__ vec, uint32_t* overflow, uint32_t* overflow_n, HistParams h,
            unsigned long long* __restrict__ hist)
 {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     CellShared& S = *reinterpret_cast<CellShared*>(smem_raw);
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
-    const bool use_pre = pre_r2 > 0.0f;
+    const unsigned lt = (1u << lane) - 1u;
+    const bool use_pre = pre_out2 > 0.0f;
     const bool smem_hist = MODE == CM_HIST && h.bins <= HIST_BINS_SMEM;
+    unsigned short* queue = S.queue[warp];
 
     for (int t = tid; t < 81; t += CTHREADS)
     {
@@ -187,7 +186,7 @@ __global__ void __launch_bounds__(CTHREADS, 1)
         }
         __syncthreads();
         const uint32_t T = S.total;
-        if (T > CAP || (MODE != CM_HIST && nqc > QMAX))
+        if (T > CAP)
         {
             // hand this cell's queries to the warp-per-query kernel
             for (uint32_t k = tid; k < nqc; k += CTHREADS)
@@ -210,8 +209,9 @@ __global__ void __launch_bounds__(CTHREADS, 1)
             const uint32_t slot = S.item_start[s] + (t - S.item_off[s]);
             const float4 pp = g.cpos[slot];
             const int wr = S.item_wrap[s];
+            const uint32_t jj = g.cidx[slot];
             S.pos[t] = pp;
-            S.j[t] = g.cidx[slot];
+            S.j[t] = jj;
             S.wrap[t] = static_cast<unsigned char>(wr);
             if (use_pre)
             {
@@ -222,119 +222,86 @@ __global__ void __launch_bounds__(CTHREADS, 1)
             }
             if (MODE == CM_EMIT)
             {
-                S.key[t] = (static_cast<unsigned long long>(S.j[t]) << 32) | t;
+                S.key[t] = (static_cast<unsigned long long>(jj) << 32) | t;
             }
         }
-        const uint32_t nq_here = MODE == CM_HIST ? min(nqc, static_cast<uint32_t>(QMAX)) : nqc;
-        for (uint32_t k = tid; k < nq_here; k += CTHREADS)
-        {
-            S.q[k] = qg.cpos[q0 + k];
-            S.qi[k] = qg.cidx[q0 + k];
-            S.qcount[k] = 0;
-        }
-        uint32_t np2 = 32;
-        while (np2 < T)
-            np2 <<= 1;
         if (MODE == CM_EMIT)
         {
+            uint32_t np2 = 32;
+            while (np2 < T)
+                np2 <<= 1;
             for (uint32_t t = T + tid; t < np2; t += CTHREADS)
                 S.key[t] = ~0ull;
-        }
-        __syncthreads();
-        if (MODE == CM_EMIT)
-        {
+            __syncthreads();
             // bitonic sort of the staged candidates by point index
             for (uint32_t k = 2; k <= np2; k <<= 1)
             {
                 for (uint32_t jj = k >> 1; jj > 0; jj >>= 1)
                 {
-                    for (uint32_t e = tid; e < np2; e += CTHREADS)
+                    for (uint32_t e = tid; e < np2 / 2; e += CTHREADS)
                     {
-                        const uint32_t pe = e ^ jj;
-                        if (pe > e)
+                        // e indexes compare-exchange pairs: lower element of pair e
+                        const uint32_t lo = ((e & ~(jj - 1)) << 1) | (e & (jj - 1));
+                        const uint32_t hi = lo | jj;
+                        const bool up = (lo & k) == 0;
+                        const unsigned long long a = S.key[lo], cc = S.key[hi];
+                        if ((a > cc) == up)
                         {
-                            const bool up = (e & k) == 0;
-                            const unsigned long long a = S.key[e], cc = S.key[pe];
-                            if ((a > cc) == up)
-                            {
-                                S.key[e] = cc;
-                                S.key[pe] = a;
-                            }
+                            S.key[lo] = cc;
+                            S.key[hi] = a;
                         }
                     }
                     __syncthreads();
                 }
             }
         }
-        // ---- sweep: candidate chunk per warp, queries broadcast ----
+        __syncthreads();
+
+        // ---- warp per query ----
         const uint32_t nchunks = (T + 31) / 32;
-        const uint32_t nq_loop = MODE == CM_HIST ? nqc : nq_here;
-        for (uint32_t ch = warp; ch < nchunks; ch += CWARPS)
+        for (uint32_t qq = warp; qq < nqc; qq += CWARPS)
         {
-            const uint32_t e = ch * 32 + lane;
-            const bool live = e < T;
-            uint32_t t = e;
-            if (MODE == CM_EMIT && live)
-                t = static_cast<uint32_t>(S.key[e] & 0xffffffffull);
-            float4 pp = make_float4(0.f, 0.f, 0.f, 0.f);
-            float4 ps = make_float4(1e30f, 1e30f, 1e30f, 0.f);
-            uint32_t jidx = 0xffffffffu;
-            int wr = 13;
-            if (live)
-            {
-                pp = S.pos[t];
-                jidx = S.j[t];
-                wr = S.wrap[t];
-                if (use_pre)
-                    ps = S.ps[t];
-            }
-            for (uint32_t qq = 0; qq < nq_loop; ++qq)
-            {
-                float4 q;
-                uint32_t qi;
-                if (MODE != CM_HIST || qq < static_cast<uint32_t>(QMAX))
+            const float4 q = qg.cpos[q0 + qq];
+            const uint32_t qi = qg.cidx[q0 + qq];
+            const int qimg = __float_as_int(q.w);
+            const float3 qs = use_pre ? shifted(b, q, -img_ax(qimg, 0), -img_ax(qimg, 1), -img_ax(qimg, 2))
+                                      : make_float3(0.f, 0.f, 0.f);
+            uint32_t count = 0;
+            uint32_t qn = 0;
+            uint64_t out = MODE == CM_EMIT ? offsets[qi] : 0;
+
+            // exact test of the first n queued candidates (n <= 32), in queue order
+            auto process = [&](uint32_t n) {
+                bool acc = false;
+                float rx = 0.f, ry = 0.f, rz = 0.f, rsq = 0.f;
+                uint32_t t = 0;
+                if (lane < static_cast<int>(n))
                 {
-                    q = S.q[qq];
-                    qi = S.qi[qq];
-                }
-                else
-                {
-                    q = qg.cpos[q0 + qq];
-                    qi = qg.cidx[q0 + qq];
-                }
-                const int qimg = __float_as_int(q.w);
-                bool ok = false;
-                float rsq = 0.f;
-                if (live && !(p.exclude_ii && jidx == qi))
-                {
-                    bool cand = true;
-                    if (use_pre)
-                    {
-                        const float3 qs = shifted(b, q, -img_ax(qimg, 0), -img_ax(qimg, 1), -img_ax(qimg, 2));
-                        const float dx = ps.x - qs.x, dy = ps.y - qs.y, dz = ps.z - qs.z;
-                        cand = dx * dx + dy * dy + dz * dz <= pre_r2;
-                    }
-                    float rx, ry, rz;
-                    if (cand && exact_vec(b, S.img, p.arith, q, qimg, pp, wr, rx, ry, rz))
+                    t = queue[lane];
+                    if (MODE == CM_EMIT)
+                        t = static_cast<uint32_t>(S.key[t] & 0xffffffffull);
+                    if (exact_vec(b, S.img, p.arith, q, qimg, S.pos[t], S.wrap[t], rx, ry, rz))
                     {
                         rsq = dot3(rx, ry, rz);
-                        ok = rsq < p.r_max_sq && rsq >= p.r_min_sq;
+                        acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
                     }
                 }
-                const unsigned m = __ballot_sync(FULL, ok);
+                const unsigned am = __ballot_sync(FULL, acc);
                 if (MODE == CM_EMIT)
                 {
-                    if (lane == 0)
-                        S.mask[qq][ch] = m;
+                    if (acc)
+                    {
+                        const uint64_t o = out + count + __popc(am & lt);
+                        ij[o] = make_uint2(qi, S.j[t]);
+                        dist[o] = __fsqrt_rn(rsq);
+                        vec[3 * o] = rx;
+                        vec[3 * o + 1] = ry;
+                        vec[3 * o + 2] = rz;
+                    }
                 }
-                else if (MODE == CM_COUNT)
+                else if (MODE == CM_HIST)
                 {
-                    if (lane == 0 && m != 0)
-                        atomicAdd(&S.qcount[qq], static_cast<uint32_t>(__popc(m)));
-                }
-                else
-                {
-                    if (ok)
+                    if (acc)
                     {
                         const float d = __fsqrt_rn(rsq);
                         if (!(d < h.h_min || d >= h.h_max))
@@ -349,55 +316,70 @@ __global__ void __launch_bounds__(CTHREADS, 1)
                         }
                     }
                 }
-            }
-        }
-        __syncthreads();
-        if (MODE == CM_COUNT)
-        {
-            for (uint32_t k = tid; k < nqc; k += CTHREADS)
-                counts[S.qi[k]] = S.qcount[k];
-        }
-        else if (MODE == CM_EMIT)
-        {
-            // exclusive offsets of each query's masks over the chunks
-            for (uint32_t qq = tid; qq < nqc; qq += CTHREADS)
-            {
-                uint32_t run = 0;
-                for (uint32_t ch = 0; ch < nchunks; ++ch)
-                {
-                    S.moff[qq][ch] = static_cast<unsigned short>(run);
-                    run += __popc(S.mask[qq][ch]);
-                }
-                S.qcount[qq] = run;
-            }
-            __syncthreads();
-            for (uint32_t ch = warp; ch < nchunks; ch += CWARPS)
+                count += __popc(am);
+            };
+
+            for (uint32_t ch = 0; ch < nchunks; ++ch)
             {
                 const uint32_t e = ch * 32 + lane;
                 const bool live = e < T;
-                uint32_t t = live ? static_cast<uint32_t>(S.key[e] & 0xffffffffull) : 0;
-                const float4 pp = live ? S.pos[t] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const uint32_t jidx = live ? S.j[t] : 0;
-                const int wr = live ? S.wrap[t] : 13;
-                for (uint32_t qq = 0; qq < nqc; ++qq)
+                bool need = false;
+                bool inside = false;
+                if (live)
                 {
-                    const unsigned m = S.mask[qq][ch];
-                    if (m == 0)
-                        continue;
-                    if ((m >> lane) & 1u)
+                    const uint32_t t = MODE == CM_EMIT ? static_cast<uint32_t>(S.key[e] & 0xffffffffull) : e;
+                    if (!(p.exclude_ii && S.j[t] == qi))
                     {
-                        const float4 q = S.q[qq];
-                        float rx, ry, rz;
-                        exact_vec(b, S.img, p.arith, q, __float_as_int(q.w), pp, wr, rx, ry, rz);
-                        const uint32_t qi = S.qi[qq];
-                        const uint64_t o = offsets[qi] + S.moff[qq][ch] + __popc(m & ((1u << lane) - 1u));
-                        ij[o] = make_uint2(qi, jidx);
-                        dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
-                        vec[3 * o] = rx;
-                        vec[3 * o + 1] = ry;
-                        vec[3 * o + 2] = rz;
+                        if (use_pre)
+                        {
+                            const float4 ps = S.ps[t];
+                            const float dx = ps.x - qs.x, dy = ps.y - qs.y, dz = ps.z - qs.z;
+                            const float d2 = dx * dx + dy * dy + dz * dz;
+                            if (MODE == CM_COUNT && d2 < pre_in2)
+                                inside = true;
+                            else
+                                need = d2 <= pre_out2;
+                        }
+                        else
+                        {
+                            need = true;
+                        }
                     }
                 }
+                if (MODE == CM_COUNT)
+                {
+                    count += __popc(__ballot_sync(FULL, inside));
+                }
+                const unsigned nm = __ballot_sync(FULL, need);
+                if (need)
+                {
+                    queue[qn + __popc(nm & lt)] = static_cast<unsigned short>(e);
+                }
+                qn += __popc(nm);
+                __syncwarp();
+                if (qn >= 32)
+                {
+                    process(32);
+                    // move the remaining entries to the front of the queue
+                    const uint32_t rest = qn - 32;
+                    unsigned short v = 0;
+                    if (lane < static_cast<int>(rest))
+                        v = queue[32 + lane];
+                    __syncwarp();
+                    if (lane < static_cast<int>(rest))
+                        queue[lane] = v;
+                    __syncwarp();
+                    qn = rest;
+                }
+            }
+            if (qn > 0)
+            {
+                process(qn);
+                __syncwarp();
+            }
+            if (MODE == CM_COUNT && lane == 0)
+            {
+                counts[qi] = count;
             }
         }
         __syncthreads();
@@ -419,7 +401,8 @@ int cell_blocks(int ncell)
     cudaGetDevice(&dev);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return ncell < sms ? (ncell < 1 ? 1 : ncell) : sms;
+    const int want = 2 * sms;
+    return ncell < want ? (ncell < 1 ? 1 : ncell) : want;
 }
 
 template<int MODE> void configure()
@@ -440,9 +423,10 @@ size_t cell_smem_bytes()
     return sizeof(CellShared);
 }
 
-void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_r2,
-                 uint32_t* counts, const uint64_t* offsets, uint2* ij, float* dist, float* vec, uint32_t* overflow,
-                 uint32_t* overflow_n, const HistParams& h, unsigned long long* hist, cudaStream_t s)
+void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_out2,
+                 float pre_in2, uint32_t* counts, const uint64_t* offsets, uint2* ij, float* dist, float* vec,
+                 uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
+                 cudaStream_t s)
 {
     const int blocks = cell_blocks(qg.ncell);
     const size_t smem = sizeof(CellShared);
@@ -450,22 +434,22 @@ void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& q
     {
         configure<CM_COUNT>();
         ProfScope prof_("k_cell<COUNT>", s);
-        k_cell<CM_COUNT><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_r2, counts, offsets, ij, dist, vec, overflow,
-                                                         overflow_n, h, hist);
+        k_cell<CM_COUNT><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, offsets, ij, dist,
+                                                         vec, overflow, overflow_n, h, hist);
     }
     else if (mode == CM_EMIT)
     {
         configure<CM_EMIT>();
         ProfScope prof_("k_cell<EMIT>", s);
-        k_cell<CM_EMIT><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_r2, counts, offsets, ij, dist, vec, overflow,
-                                                        overflow_n, h, hist);
+        k_cell<CM_EMIT><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, offsets, ij, dist, vec,
+                                                        overflow, overflow_n, h, hist);
     }
     else
     {
         configure<CM_HIST>();
         ProfScope prof_("k_cell<HIST>", s);
-        k_cell<CM_HIST><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_r2, counts, offsets, ij, dist, vec, overflow,
-                                                        overflow_n, h, hist);
+        k_cell<CM_HIST><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, offsets, ij, dist, vec,
+                                                        overflow, overflow_n, h, hist);
     }
 }
 

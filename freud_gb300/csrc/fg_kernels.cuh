@@ -80,13 +80,16 @@ void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, c
                       const uint32_t* list = nullptr);
 
 // Block-per-cell ball kernels (mode 0 count, 1 emit in (i, j) order, 2 fused histogram).
-// qg is the cell-sorted query grid (same dims as g). Queries of cells that exceed the
-// shared-memory capacity are appended to overflow for the warp-per-query kernels.
-// pre_r2 > 0 enables the wrap-arithmetic prefilter with that squared radius.
+// qg is the cell-sorted query grid (same dims as g). Queries of cells whose candidate
+// set exceeds the shared-memory capacity are appended to overflow for the
+// warp-per-query kernels. pre_out2 > 0 enables the wrap-arithmetic prefilter
+// (candidates beyond sqrt(pre_out2) are rejected without the exact test);
+// pre_in2 > 0 lets the count pass accept candidates inside sqrt(pre_in2) unchecked.
 size_t cell_smem_bytes();
-void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_r2,
-                 uint32_t* counts, const uint64_t* offsets, uint2* ij, float* dist, float* vec, uint32_t* overflow,
-                 uint32_t* overflow_n, const HistParams& h, unsigned long long* hist, cudaStream_t s);
+void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_out2,
+                 float pre_in2, uint32_t* counts, const uint64_t* offsets, uint2* ij, float* dist, float* vec,
+                 uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
+                 cudaStream_t s);
 
 // Histogram of a distance array (RDF over a NeighborList).
 void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,
