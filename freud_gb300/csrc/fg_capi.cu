@@ -60,10 +60,29 @@ static void runtime_error(const std::string& m)
 static cudaStream_t g_user_stream = nullptr;
 static bool g_user_stream_set = false;
 
+static void keep_pool(int dev)
+{
+    // keep freed blocks in the stream-ordered pool for reuse across frames
+    static bool done[64] = {false};
+    if (dev >= 0 && dev < 64 && !done[dev])
+    {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+        {
+            uint64_t thr = std::numeric_limits<uint64_t>::max();
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        done[dev] = true;
+    }
+}
+
 static cudaStream_t stream()
 {
     if (g_user_stream_set)
     {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess)
+            keep_pool(dev);
         return g_user_stream;
     }
     static thread_local cudaStream_t own = nullptr;
@@ -74,13 +93,7 @@ static cudaStream_t stream()
     {
         FG_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
         own_dev = dev;
-        // keep freed blocks in the stream-ordered pool for reuse across frames
-        cudaMemPool_t pool;
-        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
-        {
-            uint64_t thr = std::numeric_limits<uint64_t>::max();
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-        }
+        keep_pool(dev);
     }
     return own;
 }
@@ -569,25 +582,36 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     p.arith = arith;
     p.nq = nqp;
     const Prefilter pf = prefilter(nq, arith, dim, a.r_max, a.r_min);
-    DevBuf counts, offsets, scratch, heavy, heavy_n, over, over_n;
+    DevBuf counts, offsets, scratch, heavy, heavy_n, over, over_n, gmask, gsorted;
     counts.alloc(sizeof(uint32_t) * (nqp + 1));
     offsets.alloc(sizeof(uint64_t) * (nqp + 1));
     scratch.alloc(scan_scratch_bytes(nqp + 1));
     over.alloc(sizeof(uint32_t) * (nqp + 1));
     over_n.alloc(sizeof(uint32_t));
+    const bool cellwise = !by_distance;
+    if (cellwise)
+    {
+        gmask.alloc(sizeof(uint32_t) * static_cast<size_t>(nqp) * CELL_CHUNKS);
+        gsorted.alloc(sizeof(uint32_t) * static_cast<size_t>(g.ncell) * CELL_CAP);
+    }
     FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (nqp + 1), s));
     FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
     reset_dev_err();
-    launch_cell(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, counts.as<uint32_t>(), nullptr, nullptr, nullptr,
-                nullptr, over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s);
-    uint32_t n_over = 0;
-    FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    sync();
+    uint32_t n_over = nqp;
+    const uint32_t* list = nullptr;
+    if (cellwise)
+    {
+        launch_cell_scan(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, counts.as<uint32_t>(), gmask.as<uint32_t>(),
+                         gsorted.as<uint32_t>(), over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s);
+        FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        sync();
+        list = over.as<uint32_t>();
+    }
     if (n_over > 0)
     {
         BallParams po = p;
         po.nq = n_over;
-        launch_ball_count(nq->dbox, view(g), qs.qpos, qs.qidx, po, counts.as<uint32_t>(), s, over.as<uint32_t>());
+        launch_ball_count(nq->dbox, view(g), qs.qpos, qs.qidx, po, counts.as<uint32_t>(), s, list);
     }
     scan_u32_to_u64(counts.as<uint32_t>(), offsets.as<uint64_t>(), nqp + 1, scratch.p, s);
     uint64_t total = 0;
@@ -606,23 +630,15 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     heavy.alloc(sizeof(uint32_t) * (nqp + 1));
     heavy_n.alloc(sizeof(uint32_t));
     FG_CUDA(cudaMemsetAsync(heavy_n.p, 0, sizeof(uint32_t), s));
-    const uint32_t* list = nullptr;
-    uint32_t nlist = nqp;
-    if (!by_distance)
+    if (cellwise)
     {
-        FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
-        launch_cell(1, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, counts.as<uint32_t>(), offsets.as<uint64_t>(),
-                    out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(), over.as<uint32_t>(),
-                    over_n.as<uint32_t>(), HistParams {}, nullptr, s);
-        FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        sync();
-        list = over.as<uint32_t>();
-        nlist = n_over;
+        launch_cell_emit(nq->dbox, view(g), qs.qg, p, gmask.as<uint32_t>(), gsorted.as<uint32_t>(),
+                         offsets.as<uint64_t>(), out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(), s);
     }
-    if (nlist > 0)
+    if (n_over > 0)
     {
         BallParams po = p;
-        po.nq = nlist;
+        po.nq = n_over;
         launch_ball_emit(nq->dbox, view(g), qs.qpos, qs.qidx, po, counts.as<uint32_t>(), offsets.as<uint64_t>(),
                          by_distance, out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(),
                          heavy.as<uint32_t>(), heavy_n.as<uint32_t>(), dev_err(), s, list);
@@ -1460,8 +1476,8 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
             over_n.alloc(sizeof(uint32_t));
             FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
             const Prefilter pf = prefilter(nq, p.arith, dim, a.r_max, a.r_min);
-            launch_cell(2, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr,
-                        over.as<uint32_t>(), over_n.as<uint32_t>(), h, rdf->hist.as<unsigned long long>(), s);
+            launch_cell_scan(1, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, nullptr, nullptr, nullptr,
+                             over.as<uint32_t>(), over_n.as<uint32_t>(), h, rdf->hist.as<unsigned long long>(), s);
             uint32_t n_over = 0;
             FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
             sync();

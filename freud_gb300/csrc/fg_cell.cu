@@ -1,27 +1,28 @@
-// Ball queries, block per home cell, warp per query with compacted exact tests.
+// Ball queries, block per home cell.
 //
 // A block takes one cell of the query grid and stages the candidate set shared by
 // all of its queries - the points of the 27 (9 in 2D) neighbouring cells, each
-// with its cell wrap - in shared memory once. Each warp then takes one query of
-// the cell at a time and scans the staged candidates 32 per step.
+// with its cell wrap - in shared memory once.
 //
 // Pair arithmetic is exact and identical to the warp-per-query kernels
 // (AABBQuery.cc:93,125 / LinkCell.cc:522). In wrap arithmetic the exact
-// box.wrap (three IEEE divisions) is expensive, so a cheap prefilter on the
-// cell-shifted positions classifies each candidate as certainly outside
-// (> r_max + delta), certainly inside (< r_max - delta) or undecided. Candidates
-// that need the exact test are appended to a per-warp queue in scan order and
-// tested 32 at a time, so the exact arithmetic runs with full lanes. The
-// prefilter is only enabled when every periodic axis has >= 3 cells and
-// r_max + delta is below half the smallest plane distance, where the
-// cell-derived image is the minimum image of every possible bond.
+// box.wrap (three IEEE divisions) is expensive, so a prefilter on cell-shifted
+// float positions classifies each (query, candidate) pair as certainly outside
+// (> r_max + delta), certainly inside (< r_max - delta, count pass only, r_min = 0)
+// or undecided; undecided pairs go to a per-warp queue and are tested exactly 32
+// at a time with full lanes. The prefilter is enabled only when every periodic
+// axis has >= 3 cells and r_max + delta is below half the smallest plane distance,
+// where the cell-derived image is the minimum image of every possible bond.
 //
-// COUNT: bonds per query (candidates certainly inside need no exact test).
-// EMIT:  the staged candidates are sorted by point index once per cell, so the
-//        queue - and hence each query's accepted bonds - comes out in the
-//        reference's (i, j) order (NeighborBond.h:80-95); bonds are written at the
-//        query's offset as they are accepted, 32 consecutive slots at a time.
-// HIST:  fused RDF binning (RDF.cc:101-110, Histogram.h:152-174).
+// SCAN (count pass of a NeighborList, or the fused RDF histogram): each warp
+// holds a chunk of 32 candidates in registers and sweeps the cell's queries,
+// broadcast from shared memory. For a NeighborList the staged candidates are
+// first sorted by point index; the pass stores that order per cell and one
+// acceptance mask per (query, 32-candidate chunk), and the bond count per query.
+// EMIT (write pass): warp per query; the set bits of its masks, in chunk order,
+// are exactly its bonds in the reference's (i, j) order (NeighborBond.h:80-95);
+// they are compacted 32 at a time, their exact vectors recomputed, and written
+// to 32 consecutive slots at the query's offset.
 // Cells whose candidate set exceeds the shared-memory capacity hand their queries
 // to the warp-per-query kernels.
 #include "fg_kernels.cuh"
@@ -32,16 +33,17 @@ namespace fg {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int CWARPS = 8;
-constexpr int CTHREADS = CWARPS * 32;
-constexpr int CAP = 2048; // staged candidates per cell
+constexpr int SWARPS = 8;
+constexpr int STHREADS = SWARPS * 32;
+constexpr int EWARPS = 8;
+constexpr int ETHREADS = EWARPS * 32;
+constexpr int QB = 64;              // queries per shared-memory batch in the scan pass
 constexpr int HIST_BINS_SMEM = 4096;
 
-enum CellMode
+enum ScanMode
 {
-    CM_COUNT = 0,
-    CM_EMIT = 1,
-    CM_HIST = 2,
+    SM_COUNT = 0,
+    SM_HIST = 1,
 };
 
 __device__ __forceinline__ int img_ax(int bits, int axis)
@@ -49,20 +51,35 @@ __device__ __forceinline__ int img_ax(int bits, int axis)
     return static_cast<int>(static_cast<int8_t>((bits >> (8 * axis)) & 0xff));
 }
 
-struct CellShared
+struct Items
 {
-    float4 pos[CAP];             // x, y, z, packed integer box image
-    float4 ps[CAP];              // prefilter position (wrap arithmetic)
-    uint32_t j[CAP];             // point index
-    unsigned char wrap[CAP];     // cell wrap code (wx+1) + 3(wy+1) + 9(wz+1)
-    unsigned long long key[CAP]; // (j << 32) | slot, sorted per cell (EMIT)
-    unsigned short queue[CWARPS][64];
-    uint32_t item_start[32];
-    uint32_t item_off[33];
-    int item_wrap[32];
-    float img[27][3];
+    uint32_t start[32];
+    uint32_t off[33];
+    int wrap[32];
     uint32_t total;
-    unsigned int hist[HIST_BINS_SMEM];
+};
+
+struct ScanShared
+{
+    union
+    {
+        float4 pos[CELL_CAP];           // x, y, z, packed integer box image (histogram pass)
+        uint32_t mask[QB][CELL_CHUNKS]; // acceptance per (query, chunk) in sorted order (count pass)
+    } u1;
+    union
+    {
+        unsigned long long key[CELL_CAP]; // (j << 32) | staged index (count pass sort)
+        unsigned int hist[HIST_BINS_SMEM]; // privatised RDF histogram (histogram pass)
+    } u2;
+    float4 ps[CELL_CAP];              // prefilter position (wrap arithmetic)
+    uint32_t j[CELL_CAP];             // point index
+    uint32_t slot[CELL_CAP];          // grid slot << 5 | cell wrap code
+    float4 q[QB];
+    float4 qs[QB];
+    uint32_t qi[QB];
+    uint32_t queue[SWARPS][64];       // undecided pairs: sorted index | query << 11
+    Items it;
+    float img[27][3];
 };
 
 // Exact pair vector (same arithmetic as the warp kernels). false: image outside +-1.
@@ -99,33 +116,88 @@ __device__ __forceinline__ float3 shifted(const DevBox& b, float4 p, int sx, int
     return r;
 }
 
+// Stencil items of cell c (warp 0 of the block): start, wrap and prefix offsets.
+__device__ void cell_items(const DevBox& b, const DevGrid& g, int arith, int c, Items& it, int lane)
+{
+    const int cz = c / (g.dim[0] * g.dim[1]);
+    const int cy = (c / g.dim[0]) % g.dim[1];
+    const int cx = c % g.dim[0];
+    uint32_t cnt = 0, st = 0;
+    int wr = 13;
+    const int nst = b.is2d ? 9 : 27;
+    if (lane < nst)
+    {
+        const int dx = lane % 3 - 1;
+        const int dy = (lane / 3) % 3 - 1;
+        const int dz = b.is2d ? 0 : lane / 9 - 1;
+        auto ok = [&](int d, int dim) {
+            if (arith == ARITH_AABB || dim >= 3)
+                return true;
+            return dim == 1 ? d == 0 : d >= 0;
+        };
+        if (ok(dx, g.dim[0]) && ok(dy, g.dim[1]) && (b.is2d || ok(dz, g.dim[2])))
+        {
+            const int ux = cx + dx, uy = cy + dy, uz = cz + dz;
+            const int wx = ux < 0 ? -1 : (ux >= g.dim[0] ? 1 : 0);
+            const int wy = uy < 0 ? -1 : (uy >= g.dim[1] ? 1 : 0);
+            const int wz = uz < 0 ? -1 : (uz >= g.dim[2] ? 1 : 0);
+            const int cell = (ux - wx * g.dim[0]) + g.dim[0] * ((uy - wy * g.dim[1]) + g.dim[1] * (uz - wz * g.dim[2]));
+            st = g.start[cell];
+            cnt = g.start[cell + 1] - st;
+            wr = (wx + 1) + 3 * (wy + 1) + 9 * (wz + 1);
+        }
+    }
+    uint32_t incl = cnt;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o)
+            incl += v;
+    }
+    it.start[lane] = st;
+    it.off[lane] = incl - cnt;
+    it.wrap[lane] = wr;
+    if (lane == 31)
+    {
+        it.off[32] = incl;
+        it.total = incl;
+    }
+}
+
+__device__ __forceinline__ int item_of(const Items& it, uint32_t t)
+{
+    int s = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1)
+    {
+        if (s + step < 32 && it.off[s + step] <= t)
+            s += step;
+    }
+    return s;
+}
+
 template<int MODE>
-__global__ void __launch_bounds__(CTHREADS, 2)
-    k_cell(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2,
-           uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets, uint2* __restrict__ ij,
-           float* __restrict__ dist, float* __restrict__ vec, uint32_t* overflow, uint32_t* overflow_n, HistParams h,
-           unsigned long long* __restrict__ hist)
+__global__ void __launch_bounds__(STHREADS, 2)
+    k_cell_scan(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2,
+                uint32_t* __restrict__ counts, uint32_t* __restrict__ gmask, uint32_t* __restrict__ gsorted,
+                uint32_t* overflow, uint32_t* overflow_n, HistParams h, unsigned long long* __restrict__ hist)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    CellShared& S = *reinterpret_cast<CellShared*>(smem_raw);
+    ScanShared& S = *reinterpret_cast<ScanShared*>(smem_raw);
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1u;
     const bool use_pre = pre_out2 > 0.0f;
-    const bool smem_hist = MODE == CM_HIST && h.bins <= HIST_BINS_SMEM;
-    unsigned short* queue = S.queue[warp];
+    const bool smem_hist = MODE == SM_HIST && h.bins <= HIST_BINS_SMEM;
+    uint32_t* queue = S.queue[warp];
 
-    for (int t = tid; t < 81; t += CTHREADS)
-    {
+    for (int t = tid; t < 81; t += STHREADS)
         S.img[t / 3][t % 3] = b.img[t / 3][t % 3];
-    }
-    if (MODE == CM_HIST && smem_hist)
+    if (MODE == SM_HIST && smem_hist)
     {
-        for (int t = tid; t < static_cast<int>(h.bins); t += CTHREADS)
-        {
-            S.hist[t] = 0;
-        }
+        for (int t = tid; t < static_cast<int>(h.bins); t += STHREADS)
+            S.u2.hist[t] = 0;
     }
     __syncthreads();
 
@@ -134,85 +206,30 @@ __global__ void __launch_bounds__(CTHREADS, 2)
         const uint32_t q0 = qg.start[c];
         const uint32_t nqc = qg.start[c + 1] - q0;
         if (nqc == 0)
-        {
             continue;
-        }
-        const int cz = c / (g.dim[0] * g.dim[1]);
-        const int cy = (c / g.dim[0]) % g.dim[1];
-        const int cx = c % g.dim[0];
-        // ---- stencil items and their offsets (warp 0) ----
         if (warp == 0)
-        {
-            uint32_t cnt = 0, st = 0;
-            int wr = 13;
-            const int nst = b.is2d ? 9 : 27;
-            if (lane < nst)
-            {
-                const int dx = lane % 3 - 1;
-                const int dy = (lane / 3) % 3 - 1;
-                const int dz = b.is2d ? 0 : lane / 9 - 1;
-                auto ok = [&](int d, int dim) {
-                    if (p.arith == ARITH_AABB || dim >= 3)
-                        return true;
-                    return dim == 1 ? d == 0 : d >= 0;
-                };
-                if (ok(dx, g.dim[0]) && ok(dy, g.dim[1]) && (b.is2d || ok(dz, g.dim[2])))
-                {
-                    const int ux = cx + dx, uy = cy + dy, uz = cz + dz;
-                    const int wx = ux < 0 ? -1 : (ux >= g.dim[0] ? 1 : 0);
-                    const int wy = uy < 0 ? -1 : (uy >= g.dim[1] ? 1 : 0);
-                    const int wz = uz < 0 ? -1 : (uz >= g.dim[2] ? 1 : 0);
-                    const int cell = (ux - wx * g.dim[0]) + g.dim[0] * ((uy - wy * g.dim[1]) + g.dim[1] * (uz - wz * g.dim[2]));
-                    st = g.start[cell];
-                    cnt = g.start[cell + 1] - st;
-                    wr = (wx + 1) + 3 * (wy + 1) + 9 * (wz + 1);
-                }
-            }
-            uint32_t incl = cnt;
-            for (int o = 1; o < 32; o <<= 1)
-            {
-                const uint32_t v = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o)
-                    incl += v;
-            }
-            S.item_start[lane] = st;
-            S.item_off[lane] = incl - cnt;
-            S.item_wrap[lane] = wr;
-            if (lane == 31)
-            {
-                S.item_off[32] = incl;
-                S.total = incl;
-            }
-        }
+            cell_items(b, g, p.arith, c, S.it, lane);
         __syncthreads();
-        const uint32_t T = S.total;
-        if (T > CAP)
+        const uint32_t T = S.it.total;
+        if (T > CELL_CAP)
         {
-            // hand this cell's queries to the warp-per-query kernel
-            for (uint32_t k = tid; k < nqc; k += CTHREADS)
-            {
+            for (uint32_t k = tid; k < nqc; k += STHREADS)
                 overflow[atomicAdd(overflow_n, 1u)] = q0 + k;
-            }
             __syncthreads();
             continue;
         }
         // ---- stage candidates ----
-        for (uint32_t t = tid; t < T; t += CTHREADS)
+        for (uint32_t t = tid; t < T; t += STHREADS)
         {
-            int s = 0;
-#pragma unroll
-            for (int step = 16; step >= 1; step >>= 1)
-            {
-                if (s + step < 32 && S.item_off[s + step] <= t)
-                    s += step;
-            }
-            const uint32_t slot = S.item_start[s] + (t - S.item_off[s]);
+            const int s = item_of(S.it, t);
+            const uint32_t slot = S.it.start[s] + (t - S.it.off[s]);
             const float4 pp = g.cpos[slot];
-            const int wr = S.item_wrap[s];
+            const int wr = S.it.wrap[s];
             const uint32_t jj = g.cidx[slot];
-            S.pos[t] = pp;
+            if (MODE == SM_HIST)
+                S.u1.pos[t] = pp;
             S.j[t] = jj;
-            S.wrap[t] = static_cast<unsigned char>(wr);
+            S.slot[t] = (slot << 5) | static_cast<uint32_t>(wr);
             if (use_pre)
             {
                 const int pim = __float_as_int(pp.w);
@@ -220,88 +237,93 @@ __global__ void __launch_bounds__(CTHREADS, 2)
                                           (wr / 9 - 1) - img_ax(pim, 2));
                 S.ps[t] = make_float4(sp.x, sp.y, sp.z, 0.0f);
             }
-            if (MODE == CM_EMIT)
-            {
-                S.key[t] = (static_cast<unsigned long long>(jj) << 32) | t;
-            }
+            if (MODE == SM_COUNT)
+                S.u2.key[t] = (static_cast<unsigned long long>(jj) << 32) | t;
         }
-        if (MODE == CM_EMIT)
+        uint32_t np2 = 32;
+        while (np2 < T)
+            np2 <<= 1;
+        if (MODE == SM_COUNT)
         {
-            uint32_t np2 = 32;
-            while (np2 < T)
-                np2 <<= 1;
-            for (uint32_t t = T + tid; t < np2; t += CTHREADS)
-                S.key[t] = ~0ull;
+            for (uint32_t t = T + tid; t < np2; t += STHREADS)
+                S.u2.key[t] = ~0ull;
             __syncthreads();
             // bitonic sort of the staged candidates by point index
             for (uint32_t k = 2; k <= np2; k <<= 1)
             {
                 for (uint32_t jj = k >> 1; jj > 0; jj >>= 1)
                 {
-                    for (uint32_t e = tid; e < np2 / 2; e += CTHREADS)
+                    for (uint32_t e = tid; e < np2 / 2; e += STHREADS)
                     {
-                        // e indexes compare-exchange pairs: lower element of pair e
                         const uint32_t lo = ((e & ~(jj - 1)) << 1) | (e & (jj - 1));
                         const uint32_t hi = lo | jj;
                         const bool up = (lo & k) == 0;
-                        const unsigned long long a = S.key[lo], cc = S.key[hi];
+                        const unsigned long long a = S.u2.key[lo], cc = S.u2.key[hi];
                         if ((a > cc) == up)
                         {
-                            S.key[lo] = cc;
-                            S.key[hi] = a;
+                            S.u2.key[lo] = cc;
+                            S.u2.key[hi] = a;
                         }
                     }
                     __syncthreads();
                 }
             }
+            // the sorted order (grid slot << 5 | wrap) is what the write pass replays
+            for (uint32_t e = tid; e < T; e += STHREADS)
+                gsorted[static_cast<size_t>(c) * CELL_CAP + e] = S.slot[static_cast<uint32_t>(S.u2.key[e] & 0xffffffffull)];
         }
         __syncthreads();
-
-        // ---- warp per query ----
         const uint32_t nchunks = (T + 31) / 32;
-        for (uint32_t qq = warp; qq < nqc; qq += CWARPS)
-        {
-            const float4 q = qg.cpos[q0 + qq];
-            const uint32_t qi = qg.cidx[q0 + qq];
-            const int qimg = __float_as_int(q.w);
-            const float3 qs = use_pre ? shifted(b, q, -img_ax(qimg, 0), -img_ax(qimg, 1), -img_ax(qimg, 2))
-                                      : make_float3(0.f, 0.f, 0.f);
-            uint32_t count = 0;
-            uint32_t qn = 0;
-            uint64_t out = MODE == CM_EMIT ? offsets[qi] : 0;
 
-            // exact test of the first n queued candidates (n <= 32), in queue order
+        for (uint32_t qb0 = 0; qb0 < nqc; qb0 += QB)
+        {
+            const uint32_t nb = min(static_cast<uint32_t>(QB), nqc - qb0);
+            for (uint32_t k = tid; k < nb; k += STHREADS)
+            {
+                const float4 q = qg.cpos[q0 + qb0 + k];
+                const int qim = __float_as_int(q.w);
+                S.q[k] = q;
+                S.qi[k] = qg.cidx[q0 + qb0 + k];
+                const float3 qs = use_pre ? shifted(b, q, -img_ax(qim, 0), -img_ax(qim, 1), -img_ax(qim, 2))
+                                          : make_float3(0.f, 0.f, 0.f);
+                S.qs[k] = make_float4(qs.x, qs.y, qs.z, 0.f);
+            }
+            if (MODE == SM_COUNT)
+            {
+                for (uint32_t k = tid; k < nb * CELL_CHUNKS; k += STHREADS)
+                    S.u1.mask[k / CELL_CHUNKS][k % CELL_CHUNKS] = 0u;
+            }
+            __syncthreads();
+            uint32_t qn = 0;
+
+            // exact test of the first n queued (candidate, query) pairs
             auto process = [&](uint32_t n) {
                 bool acc = false;
-                float rx = 0.f, ry = 0.f, rz = 0.f, rsq = 0.f;
-                uint32_t t = 0;
+                float rsq = 0.f;
+                uint32_t e = 0, qq = 0;
                 if (lane < static_cast<int>(n))
                 {
-                    t = queue[lane];
-                    if (MODE == CM_EMIT)
-                        t = static_cast<uint32_t>(S.key[t] & 0xffffffffull);
-                    if (exact_vec(b, S.img, p.arith, q, qimg, S.pos[t], S.wrap[t], rx, ry, rz))
+                    const uint32_t ent = queue[lane];
+                    e = ent & 0x7ffu;
+                    qq = ent >> 11;
+                    const uint32_t t = MODE == SM_COUNT ? static_cast<uint32_t>(S.u2.key[e] & 0xffffffffull) : e;
+                    const float4 q = S.q[qq];
+                    const float4 pp = MODE == SM_HIST ? S.u1.pos[t] : g.cpos[S.slot[t] >> 5];
+                    float rx, ry, rz;
+                    if (exact_vec(b, S.img, p.arith, q, __float_as_int(q.w), pp, static_cast<int>(S.slot[t] & 31u), rx,
+                                  ry, rz))
                     {
                         rsq = dot3(rx, ry, rz);
                         acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
                     }
                 }
-                const unsigned am = __ballot_sync(FULL, acc);
-                if (MODE == CM_EMIT)
+                if (acc)
                 {
-                    if (acc)
+                    if (MODE == SM_COUNT)
                     {
-                        const uint64_t o = out + count + __popc(am & lt);
-                        ij[o] = make_uint2(qi, S.j[t]);
-                        dist[o] = __fsqrt_rn(rsq);
-                        vec[3 * o] = rx;
-                        vec[3 * o + 1] = ry;
-                        vec[3 * o + 2] = rz;
+                        atomicOr(&S.u1.mask[qq][e >> 5], 1u << (e & 31u));
                     }
-                }
-                else if (MODE == CM_HIST)
-                {
-                    if (acc)
+                    else
                     {
                         const float d = __fsqrt_rn(rsq);
                         if (!(d < h.h_min || d >= h.h_max))
@@ -310,32 +332,38 @@ __global__ void __launch_bounds__(CTHREADS, 2)
                             if (bin == h.bins)
                                 bin = h.bins - 1;
                             if (smem_hist)
-                                atomicAdd(&S.hist[bin], 1u);
+                                atomicAdd(&S.u2.hist[bin], 1u);
                             else
                                 atomicAdd(&hist[bin], 1ull);
                         }
                     }
                 }
-                count += __popc(am);
             };
 
-            for (uint32_t ch = 0; ch < nchunks; ++ch)
+            for (uint32_t ch = warp; ch < nchunks; ch += SWARPS)
             {
                 const uint32_t e = ch * 32 + lane;
                 const bool live = e < T;
-                bool need = false;
-                bool inside = false;
+                const uint32_t t = (MODE == SM_COUNT && live) ? static_cast<uint32_t>(S.u2.key[e] & 0xffffffffull) : e;
+                float4 ps = make_float4(0.f, 0.f, 0.f, 0.f);
+                uint32_t jj = 0xffffffffu;
                 if (live)
                 {
-                    const uint32_t t = MODE == CM_EMIT ? static_cast<uint32_t>(S.key[e] & 0xffffffffull) : e;
-                    if (!(p.exclude_ii && S.j[t] == qi))
+                    jj = S.j[t];
+                    if (use_pre)
+                        ps = S.ps[t];
+                }
+                for (uint32_t qq = 0; qq < nb; ++qq)
+                {
+                    bool need = false, inside = false;
+                    if (live && !(p.exclude_ii && jj == S.qi[qq]))
                     {
                         if (use_pre)
                         {
-                            const float4 ps = S.ps[t];
+                            const float4 qs = S.qs[qq];
                             const float dx = ps.x - qs.x, dy = ps.y - qs.y, dz = ps.z - qs.z;
                             const float d2 = dx * dx + dy * dy + dz * dz;
-                            if (MODE == CM_COUNT && d2 < pre_in2)
+                            if (MODE == SM_COUNT && d2 < pre_in2)
                                 inside = true;
                             else
                                 need = d2 <= pre_out2;
@@ -345,24 +373,146 @@ __global__ void __launch_bounds__(CTHREADS, 2)
                             need = true;
                         }
                     }
+                    if (MODE == SM_COUNT)
+                    {
+                        const unsigned im = __ballot_sync(FULL, inside);
+                        if (lane == 0 && im != 0)
+                            atomicOr(&S.u1.mask[qq][ch], im);
+                    }
+                    const unsigned nm = __ballot_sync(FULL, need);
+                    if (need)
+                        queue[qn + __popc(nm & lt)] = e | (qq << 11);
+                    qn += __popc(nm);
+                    __syncwarp();
+                    if (qn >= 32)
+                    {
+                        process(32);
+                        const uint32_t rest = qn - 32;
+                        uint32_t v = 0;
+                        if (lane < static_cast<int>(rest))
+                            v = queue[32 + lane];
+                        __syncwarp();
+                        if (lane < static_cast<int>(rest))
+                            queue[lane] = v;
+                        __syncwarp();
+                        qn = rest;
+                    }
                 }
-                if (MODE == CM_COUNT)
+            }
+            if (qn > 0)
+                process(qn);
+            __syncthreads();
+            if (MODE == SM_COUNT)
+            {
+                // masks and counts of this query batch
+                for (uint32_t k = tid; k < nb; k += STHREADS)
                 {
-                    count += __popc(__ballot_sync(FULL, inside));
+                    uint32_t cnt = 0;
+                    uint32_t* dst = gmask + static_cast<size_t>(q0 + qb0 + k) * CELL_CHUNKS;
+                    for (uint32_t ch = 0; ch < nchunks; ++ch)
+                    {
+                        const uint32_t m = S.u1.mask[k][ch];
+                        dst[ch] = m;
+                        cnt += __popc(m);
+                    }
+                    counts[S.qi[k]] = cnt;
                 }
-                const unsigned nm = __ballot_sync(FULL, need);
-                if (need)
+                __syncthreads();
+            }
+        }
+    }
+    if (MODE == SM_HIST && smem_hist)
+    {
+        __syncthreads();
+        for (int bin = tid; bin < static_cast<int>(h.bins); bin += STHREADS)
+        {
+            if (S.u2.hist[bin] != 0)
+                atomicAdd(&hist[bin], static_cast<unsigned long long>(S.u2.hist[bin]));
+        }
+    }
+}
+
+struct EmitShared
+{
+    uint32_t sorted[CELL_CAP];
+    uint32_t queue[EWARPS][64];
+    Items it;
+    float img[27][3];
+};
+
+__global__ void __launch_bounds__(ETHREADS)
+    k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
+                const uint32_t* __restrict__ gsorted, const uint64_t* __restrict__ offsets, uint2* __restrict__ ij,
+                float* __restrict__ dist, float* __restrict__ vec)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    EmitShared& S = *reinterpret_cast<EmitShared*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t* queue = S.queue[warp];
+    for (int t = tid; t < 81; t += ETHREADS)
+        S.img[t / 3][t % 3] = b.img[t / 3][t % 3];
+    __syncthreads();
+    for (int c = blockIdx.x; c < qg.ncell; c += gridDim.x)
+    {
+        const uint32_t q0 = qg.start[c];
+        const uint32_t nqc = qg.start[c + 1] - q0;
+        if (nqc == 0)
+            continue;
+        if (warp == 0)
+            cell_items(b, g, p.arith, c, S.it, lane);
+        __syncthreads();
+        const uint32_t T = S.it.total;
+        if (T > CELL_CAP)
+        {
+            __syncthreads();
+            continue; // written by the warp-per-query kernel
+        }
+        for (uint32_t e = tid; e < T; e += ETHREADS)
+            S.sorted[e] = gsorted[static_cast<size_t>(c) * CELL_CAP + e];
+        __syncthreads();
+        const uint32_t nchunks = (T + 31) / 32;
+        for (uint32_t qq = warp; qq < nqc; qq += EWARPS)
+        {
+            const float4 q = qg.cpos[q0 + qq];
+            const uint32_t qi = qg.cidx[q0 + qq];
+            const int qimg = __float_as_int(q.w);
+            const uint32_t* mrow = gmask + static_cast<size_t>(q0 + qq) * CELL_CHUNKS;
+            const uint64_t out = offsets[qi];
+            uint32_t written = 0;
+            uint32_t qn = 0;
+            auto process = [&](uint32_t n) {
+                if (lane < static_cast<int>(n))
                 {
-                    queue[qn + __popc(nm & lt)] = static_cast<unsigned short>(e);
+                    const uint32_t ent = S.sorted[queue[lane]];
+                    const uint32_t slot = ent >> 5;
+                    float rx, ry, rz;
+                    exact_vec(b, S.img, p.arith, q, qimg, g.cpos[slot], static_cast<int>(ent & 31u), rx, ry, rz);
+                    const uint64_t o = out + written + lane;
+                    ij[o] = make_uint2(qi, g.cidx[slot]);
+                    dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
+                    vec[3 * o] = rx;
+                    vec[3 * o + 1] = ry;
+                    vec[3 * o + 2] = rz;
                 }
-                qn += __popc(nm);
+                written += n;
+            };
+            for (uint32_t ch = 0; ch < nchunks; ++ch)
+            {
+                const uint32_t m = mrow[ch];
+                if (m == 0)
+                    continue;
+                if ((m >> lane) & 1u)
+                    queue[qn + __popc(m & lt)] = ch * 32 + lane;
+                qn += __popc(m);
                 __syncwarp();
                 if (qn >= 32)
                 {
                     process(32);
-                    // move the remaining entries to the front of the queue
                     const uint32_t rest = qn - 32;
-                    unsigned short v = 0;
+                    uint32_t v = 0;
                     if (lane < static_cast<int>(rest))
                         v = queue[32 + lane];
                     __syncwarp();
@@ -373,45 +523,27 @@ __global__ void __launch_bounds__(CTHREADS, 2)
                 }
             }
             if (qn > 0)
-            {
                 process(qn);
-                __syncwarp();
-            }
-            if (MODE == CM_COUNT && lane == 0)
-            {
-                counts[qi] = count;
-            }
+            __syncwarp();
         }
         __syncthreads();
-    }
-    if (MODE == CM_HIST && smem_hist)
-    {
-        __syncthreads();
-        for (int bin = tid; bin < static_cast<int>(h.bins); bin += CTHREADS)
-        {
-            if (S.hist[bin] != 0)
-                atomicAdd(&hist[bin], static_cast<unsigned long long>(S.hist[bin]));
-        }
     }
 }
 
-int cell_blocks(int ncell)
+int sm_count_cell()
 {
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int want = 2 * sms;
-    return ncell < want ? (ncell < 1 ? 1 : ncell) : want;
+    return sms;
 }
 
-template<int MODE> void configure()
+template<typename K> void configure(K kernel, size_t bytes, bool& done)
 {
-    static bool done = false;
     if (!done)
     {
-        cudaFuncSetAttribute(k_cell<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(sizeof(CellShared)));
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
         done = true;
     }
 }
@@ -420,37 +552,46 @@ template<int MODE> void configure()
 
 size_t cell_smem_bytes()
 {
-    return sizeof(CellShared);
+    return sizeof(ScanShared);
 }
 
-void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_out2,
-                 float pre_in2, uint32_t* counts, const uint64_t* offsets, uint2* ij, float* dist, float* vec,
-                 uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
-                 cudaStream_t s)
+void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
+                      float pre_out2, float pre_in2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
+                      uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
+                      cudaStream_t s)
 {
-    const int blocks = cell_blocks(qg.ncell);
-    const size_t smem = sizeof(CellShared);
-    if (mode == CM_COUNT)
+    const int want = 2 * sm_count_cell();
+    const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
+    const size_t smem = sizeof(ScanShared);
+    if (!hist_mode)
     {
-        configure<CM_COUNT>();
-        ProfScope prof_("k_cell<COUNT>", s);
-        k_cell<CM_COUNT><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, offsets, ij, dist,
-                                                         vec, overflow, overflow_n, h, hist);
-    }
-    else if (mode == CM_EMIT)
-    {
-        configure<CM_EMIT>();
-        ProfScope prof_("k_cell<EMIT>", s);
-        k_cell<CM_EMIT><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, offsets, ij, dist, vec,
-                                                        overflow, overflow_n, h, hist);
+        static bool done = false;
+        configure(k_cell_scan<SM_COUNT>, smem, done);
+        ProfScope prof_("k_cell_scan<COUNT>", s);
+        k_cell_scan<SM_COUNT><<<blocks, STHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, gmask, gsorted,
+                                                             overflow, overflow_n, h, hist);
     }
     else
     {
-        configure<CM_HIST>();
-        ProfScope prof_("k_cell<HIST>", s);
-        k_cell<CM_HIST><<<blocks, CTHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, offsets, ij, dist, vec,
-                                                        overflow, overflow_n, h, hist);
+        static bool done = false;
+        configure(k_cell_scan<SM_HIST>, smem, done);
+        ProfScope prof_("k_cell_scan<HIST>", s);
+        k_cell_scan<SM_HIST><<<blocks, STHREADS, smem, s>>>(box, g, qg, p, pre_out2, 0.0f, counts, gmask, gsorted,
+                                                            overflow, overflow_n, h, hist);
     }
+}
+
+void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
+                      const uint32_t* gmask, const uint32_t* gsorted, const uint64_t* offsets, uint2* ij, float* dist,
+                      float* vec, cudaStream_t s)
+{
+    const int want = 6 * sm_count_cell();
+    const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
+    const size_t smem = sizeof(EmitShared);
+    static bool done = false;
+    configure(k_cell_emit, smem, done);
+    ProfScope prof_("k_cell_emit", s);
+    k_cell_emit<<<blocks, ETHREADS, smem, s>>>(box, g, qg, p, gmask, gsorted, offsets, ij, dist, vec);
 }
 
 } // namespace fg

@@ -79,17 +79,25 @@ void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, c
                       const BallParams& p, const HistParams& h, unsigned long long* hist, cudaStream_t s,
                       const uint32_t* list = nullptr);
 
-// Block-per-cell ball kernels (mode 0 count, 1 emit in (i, j) order, 2 fused histogram).
-// qg is the cell-sorted query grid (same dims as g). Queries of cells whose candidate
-// set exceeds the shared-memory capacity are appended to overflow for the
-// warp-per-query kernels. pre_out2 > 0 enables the wrap-arithmetic prefilter
-// (candidates beyond sqrt(pre_out2) are rejected without the exact test);
-// pre_in2 > 0 lets the count pass accept candidates inside sqrt(pre_in2) unchecked.
+// Block-per-cell ball kernels. qg is the cell-sorted query grid (same dims as g).
+// Queries of cells whose candidate set exceeds CELL_CAP are appended to overflow
+// for the warp-per-query kernels. pre_out2 > 0 enables the wrap-arithmetic
+// prefilter (pairs beyond sqrt(pre_out2) are rejected without the exact test);
+// pre_in2 > 0 lets the count pass accept pairs inside sqrt(pre_in2) unchecked.
+// Scan pass (hist_mode 0): counts per query, acceptance masks gmask[nq][CELL_CHUNKS]
+// (by sorted query position) and each cell's candidates sorted by point index,
+// gsorted[ncell][CELL_CAP] (grid slot << 5 | wrap). hist_mode 1: fused histogram.
+// Emit pass: writes each query's bonds, in (i, j) order, at offsets[i].
+constexpr int CELL_CAP = 2048;
+constexpr int CELL_CHUNKS = CELL_CAP / 32;
 size_t cell_smem_bytes();
-void launch_cell(int mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_out2,
-                 float pre_in2, uint32_t* counts, const uint64_t* offsets, uint2* ij, float* dist, float* vec,
-                 uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
-                 cudaStream_t s);
+void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
+                      float pre_out2, float pre_in2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
+                      uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
+                      cudaStream_t s);
+void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
+                      const uint32_t* gmask, const uint32_t* gsorted, const uint64_t* offsets, uint2* ij, float* dist,
+                      float* vec, cudaStream_t s);
 
 // Histogram of a distance array (RDF over a NeighborList).
 void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,
