@@ -39,10 +39,10 @@ WORKLOAD = "large_n_nlist_rdf"
 L2_BYTES = 129 * 1024 * 1024
 
 
-def c2_system(seed=2024):
-    """102^3 simple-cubic lattice, spacing 1, N(0, 0.1) jitter, wrapped into L = 102."""
-    n1 = 102
-    L = 102.0
+def c2_system(seed=2024, n1=102):
+    """n1^3 simple-cubic lattice (102^3 by default), spacing 1, N(0, 0.1) jitter,
+    wrapped into the periodic cube of side L = n1."""
+    L = float(n1)
     g = np.arange(n1, dtype=np.float64) - n1 / 2.0
     x, y, z = np.meshgrid(g, g, g, indexing="ij")
     pts = np.stack([x.ravel(), y.ravel(), z.ravel()], 1)
@@ -152,7 +152,7 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return 0
-    L, pts = c2_system()
+    L, pts = c2_system(n1=args.n_side)
     vals = []
     desc = cores = None
     for _ in range(args.warmup):
@@ -181,6 +181,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-side", type=int, default=102,
+                    help="lattice points per side; 102 is the benchmark workload, smaller sizes are for profiling")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -203,7 +205,7 @@ def main():
     _lib.set_stream(stream.cuda_stream)
     torch.cuda.set_stream(stream)
 
-    L, pts_host = c2_system(seed=2024 + rank)
+    L, pts_host = c2_system(seed=2024 + rank, n1=args.n_side)
     n = len(pts_host)
     d_pts = torch.from_numpy(pts_host).cuda()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -315,7 +317,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "pair evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered 102^3 lattice)",
-            "config": {"workload": WORKLOAD, "n_points": n, "box_L": L, "cell_width": 3.0, "r_max": 3.0,
+            "config": {"workload": WORKLOAD if args.n_side == 102 else "%s_n%d" % (WORKLOAD, args.n_side), "n_points": n, "box_L": L, "cell_width": 3.0, "r_max": 3.0,
                        "bins": 300, "bonds_per_step": bonds, "l2": "flushed between steps (258 MB write)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,

@@ -421,8 +421,14 @@ void build_grid(const DevBox& db, const float* dpts, uint32_t n, const int dim[3
     FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (g.ncell + 1), s));
     launch_assign(db, dpts, n, dim, cell_of.as<uint32_t>(), rank.as<uint32_t>(), counts.as<uint32_t>(), s);
     scan_u32_to_u32(counts.as<uint32_t>(), g.start.as<uint32_t>(), g.ncell + 1, scratch.p, s);
-    launch_scatter(db, dpts, n, cell_of.as<uint32_t>(), rank.as<uint32_t>(), g.start.as<uint32_t>(), g.cpos.as<float4>(),
-                   g.cidx.as<uint32_t>(), s);
+    DevBuf cpos0, cidx0;
+    cpos0.alloc(sizeof(float4) * n);
+    cidx0.alloc(sizeof(uint32_t) * n);
+    launch_scatter(db, dpts, n, cell_of.as<uint32_t>(), rank.as<uint32_t>(), g.start.as<uint32_t>(),
+                   cpos0.as<float4>(), cidx0.as<uint32_t>(), s);
+    // cells sorted by point index, so candidate sets are unions of sorted runs
+    launch_sort_cells(g.start.as<uint32_t>(), g.ncell, cpos0.as<float4>(), cidx0.as<uint32_t>(), g.cpos.as<float4>(),
+                      g.cidx.as<uint32_t>(), s);
     FG_CUDA(cudaGetLastError());
 }
 

@@ -2,29 +2,32 @@
 //
 // A block takes one cell of the query grid and stages the candidate set shared by
 // all of its queries - the points of the 27 (9 in 2D) neighbouring cells, each
-// with its cell wrap - in shared memory once.
+// with its cell wrap - in shared memory.
 //
 // Pair arithmetic is exact and identical to the warp-per-query kernels
 // (AABBQuery.cc:93,125 / LinkCell.cc:522). In wrap arithmetic the exact
 // box.wrap (three IEEE divisions) is expensive, so a prefilter on cell-shifted
 // float positions classifies each (query, candidate) pair as certainly outside
-// (> r_max + delta), certainly inside (< r_max - delta, count pass only, r_min = 0)
+// (> r_max + delta), certainly inside (< r_max - delta; count pass with r_min = 0)
 // or undecided; undecided pairs go to a per-warp queue and are tested exactly 32
 // at a time with full lanes. The prefilter is enabled only when every periodic
 // axis has >= 3 cells and r_max + delta is below half the smallest plane distance,
 // where the cell-derived image is the minimum image of every possible bond.
 //
-// SCAN (count pass of a NeighborList, or the fused RDF histogram): each warp
-// holds a chunk of 32 candidates in registers and sweeps the cell's queries,
-// broadcast from shared memory. For a NeighborList the staged candidates are
-// first sorted by point index; the pass stores that order per cell and one
-// acceptance mask per (query, 32-candidate chunk), and the bond count per query.
-// EMIT (write pass): warp per query; the set bits of its masks, in chunk order,
-// are exactly its bonds in the reference's (i, j) order (NeighborBond.h:80-95);
-// they are compacted 32 at a time, their exact vectors recomputed, and written
-// to 32 consecutive slots at the query's offset.
-// Cells whose candidate set exceeds the shared-memory capacity hand their queries
-// to the warp-per-query kernels.
+// Scan pass: each warp holds a chunk of 32 candidates in registers and sweeps
+// the cell's queries, broadcast from shared memory.
+//  - count (NeighborList): grid cells are stored sorted by point index, so the
+//    staged candidates are <= 27 sorted runs; five levels of pairwise merges
+//    (rank by binary search) give the cell's candidates in index order. The pass
+//    stores that order per cell, one acceptance mask per (query, 32-candidate
+//    chunk) and the bond count per query. Cells with more than CELL_CAP
+//    candidates hand their queries to the warp-per-query kernels.
+//  - histogram (fused RDF): no ordering; the candidate set is processed in tiles
+//    of CELL_CAP, so dense cells stay on this path.
+// Write pass: warp per query; the set bits of its masks, in chunk order, are its
+// bonds in the reference's (i, j) order (NeighborBond.h:80-95); they are
+// compacted 32 at a time, their exact vectors recomputed and written to 32
+// consecutive slots at the query's offset.
 #include "fg_kernels.cuh"
 #include "fg_prof.cuh"
 
@@ -37,7 +40,7 @@ constexpr int SWARPS = 8;
 constexpr int STHREADS = SWARPS * 32;
 constexpr int EWARPS = 8;
 constexpr int ETHREADS = EWARPS * 32;
-constexpr int QB = 64;              // queries per shared-memory batch in the scan pass
+constexpr int QB = 64; // queries per shared-memory batch in the scan pass
 constexpr int HIST_BINS_SMEM = 4096;
 
 enum ScanMode
@@ -63,17 +66,18 @@ struct ScanShared
 {
     union
     {
-        float4 pos[CELL_CAP];           // x, y, z, packed integer box image (histogram pass)
-        uint32_t mask[QB][CELL_CHUNKS]; // acceptance per (query, chunk) in sorted order (count pass)
-    } u1;
-    union
-    {
-        unsigned long long key[CELL_CAP]; // (j << 32) | staged index (count pass sort)
+        struct
+        {
+            unsigned long long a[CELL_CAP]; // merge ping-pong buffers: (j << 32) | staged index
+            unsigned long long b[CELL_CAP];
+        } keys;
         unsigned int hist[HIST_BINS_SMEM]; // privatised RDF histogram (histogram pass)
-    } u2;
+    } u;
     float4 ps[CELL_CAP];              // prefilter position (wrap arithmetic)
+    float4 pos[CELL_CAP];             // candidate position (histogram pass)
     uint32_t j[CELL_CAP];             // point index
     uint32_t slot[CELL_CAP];          // grid slot << 5 | cell wrap code
+    uint32_t mask[QB][CELL_CHUNKS];   // acceptance per (query, chunk) in sorted order (count pass)
     float4 q[QB];
     float4 qs[QB];
     uint32_t qi[QB];
@@ -116,7 +120,7 @@ __device__ __forceinline__ float3 shifted(const DevBox& b, float4 p, int sx, int
     return r;
 }
 
-// Stencil items of cell c (warp 0 of the block): start, wrap and prefix offsets.
+// Stencil items of cell c (run by one warp): start, wrap and prefix offsets.
 __device__ void cell_items(const DevBox& b, const DevGrid& g, int arith, int c, Items& it, int lane)
 {
     const int cz = c / (g.dim[0] * g.dim[1]);
@@ -176,8 +180,24 @@ __device__ __forceinline__ int item_of(const Items& it, uint32_t t)
     return s;
 }
 
+// Number of keys in src[lo, hi) smaller than key (keys are distinct).
+__device__ __forceinline__ uint32_t rank_in(const unsigned long long* src, uint32_t lo, uint32_t hi,
+                                            unsigned long long key)
+{
+    uint32_t a = lo, z = hi;
+    while (a < z)
+    {
+        const uint32_t m = (a + z) >> 1;
+        if (src[m] < key)
+            a = m + 1;
+        else
+            z = m;
+    }
+    return a - lo;
+}
+
 template<int MODE>
-__global__ void __launch_bounds__(STHREADS, 2)
+__global__ void __launch_bounds__(STHREADS, 3)
     k_cell_scan(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2,
                 uint32_t* __restrict__ counts, uint32_t* __restrict__ gmask, uint32_t* __restrict__ gsorted,
                 uint32_t* overflow, uint32_t* overflow_n, HistParams h, unsigned long long* __restrict__ hist)
@@ -197,7 +217,7 @@ __global__ void __launch_bounds__(STHREADS, 2)
     if (MODE == SM_HIST && smem_hist)
     {
         for (int t = tid; t < static_cast<int>(h.bins); t += STHREADS)
-            S.u2.hist[t] = 0;
+            S.u.hist[t] = 0;
     }
     __syncthreads();
 
@@ -211,213 +231,218 @@ __global__ void __launch_bounds__(STHREADS, 2)
             cell_items(b, g, p.arith, c, S.it, lane);
         __syncthreads();
         const uint32_t T = S.it.total;
-        if (T > CELL_CAP)
+        if (MODE == SM_COUNT && T > CELL_CAP)
         {
             for (uint32_t k = tid; k < nqc; k += STHREADS)
                 overflow[atomicAdd(overflow_n, 1u)] = q0 + k;
             __syncthreads();
             continue;
         }
-        // ---- stage candidates ----
-        for (uint32_t t = tid; t < T; t += STHREADS)
+        const uint32_t ntiles = MODE == SM_COUNT ? 1u : (T + CELL_CAP - 1) / CELL_CAP;
+        for (uint32_t tile = 0; tile < ntiles; ++tile)
         {
-            const int s = item_of(S.it, t);
-            const uint32_t slot = S.it.start[s] + (t - S.it.off[s]);
-            const float4 pp = g.cpos[slot];
-            const int wr = S.it.wrap[s];
-            const uint32_t jj = g.cidx[slot];
-            if (MODE == SM_HIST)
-                S.u1.pos[t] = pp;
-            S.j[t] = jj;
-            S.slot[t] = (slot << 5) | static_cast<uint32_t>(wr);
-            if (use_pre)
+            const uint32_t t0 = tile * CELL_CAP;
+            const uint32_t TT = min(static_cast<uint32_t>(CELL_CAP), T - t0);
+            // ---- stage candidates [t0, t0 + TT) ----
+            for (uint32_t tl = tid; tl < TT; tl += STHREADS)
             {
-                const int pim = __float_as_int(pp.w);
-                const float3 sp = shifted(b, pp, (wr % 3 - 1) - img_ax(pim, 0), ((wr / 3) % 3 - 1) - img_ax(pim, 1),
-                                          (wr / 9 - 1) - img_ax(pim, 2));
-                S.ps[t] = make_float4(sp.x, sp.y, sp.z, 0.0f);
-            }
-            if (MODE == SM_COUNT)
-                S.u2.key[t] = (static_cast<unsigned long long>(jj) << 32) | t;
-        }
-        uint32_t np2 = 32;
-        while (np2 < T)
-            np2 <<= 1;
-        if (MODE == SM_COUNT)
-        {
-            for (uint32_t t = T + tid; t < np2; t += STHREADS)
-                S.u2.key[t] = ~0ull;
-            __syncthreads();
-            // bitonic sort of the staged candidates by point index
-            for (uint32_t k = 2; k <= np2; k <<= 1)
-            {
-                for (uint32_t jj = k >> 1; jj > 0; jj >>= 1)
+                const uint32_t t = t0 + tl;
+                const int s = item_of(S.it, t);
+                const uint32_t slot = S.it.start[s] + (t - S.it.off[s]);
+                const float4 pp = g.cpos[slot];
+                const int wr = S.it.wrap[s];
+                const uint32_t jj = g.cidx[slot];
+                S.j[tl] = jj;
+                S.slot[tl] = (slot << 5) | static_cast<uint32_t>(wr);
+                if (MODE == SM_HIST)
+                    S.pos[tl] = pp;
+                if (use_pre)
                 {
-                    for (uint32_t e = tid; e < np2 / 2; e += STHREADS)
+                    const int pim = __float_as_int(pp.w);
+                    const float3 sp = shifted(b, pp, (wr % 3 - 1) - img_ax(pim, 0), ((wr / 3) % 3 - 1) - img_ax(pim, 1),
+                                              (wr / 9 - 1) - img_ax(pim, 2));
+                    S.ps[tl] = make_float4(sp.x, sp.y, sp.z, 0.0f);
+                }
+                if (MODE == SM_COUNT)
+                    S.u.keys.a[tl] = (static_cast<unsigned long long>(jj) << 32) | tl;
+            }
+            const unsigned long long* order = nullptr; // sorted keys (count pass)
+            if (MODE == SM_COUNT)
+            {
+                __syncthreads();
+                // merge the <= 32 sorted runs (one per stencil item) pairwise, 5 levels
+                unsigned long long* src = S.u.keys.a;
+                unsigned long long* dst = S.u.keys.b;
+                for (int L = 0; L < 5; ++L)
+                {
+                    for (uint32_t e = tid; e < T; e += STHREADS)
                     {
-                        const uint32_t lo = ((e & ~(jj - 1)) << 1) | (e & (jj - 1));
-                        const uint32_t hi = lo | jj;
-                        const bool up = (lo & k) == 0;
-                        const unsigned long long a = S.u2.key[lo], cc = S.u2.key[hi];
-                        if ((a > cc) == up)
-                        {
-                            S.u2.key[lo] = cc;
-                            S.u2.key[hi] = a;
-                        }
+                        const int r = item_of(S.it, e) >> L;
+                        const int pr = r ^ 1;
+                        const uint32_t lo_r = S.it.off[min(r << L, 32)];
+                        const uint32_t lo_p = S.it.off[min(pr << L, 32)];
+                        const uint32_t hi_p = S.it.off[min((pr + 1) << L, 32)];
+                        const unsigned long long key = src[e];
+                        const uint32_t out = min(lo_r, lo_p) + (e - lo_r) + rank_in(src, lo_p, hi_p, key);
+                        dst[out] = key;
                     }
                     __syncthreads();
+                    unsigned long long* tmp = src;
+                    src = dst;
+                    dst = tmp;
                 }
-            }
-            // the sorted order (grid slot << 5 | wrap) is what the write pass replays
-            for (uint32_t e = tid; e < T; e += STHREADS)
-                gsorted[static_cast<size_t>(c) * CELL_CAP + e] = S.slot[static_cast<uint32_t>(S.u2.key[e] & 0xffffffffull)];
-        }
-        __syncthreads();
-        const uint32_t nchunks = (T + 31) / 32;
-
-        for (uint32_t qb0 = 0; qb0 < nqc; qb0 += QB)
-        {
-            const uint32_t nb = min(static_cast<uint32_t>(QB), nqc - qb0);
-            for (uint32_t k = tid; k < nb; k += STHREADS)
-            {
-                const float4 q = qg.cpos[q0 + qb0 + k];
-                const int qim = __float_as_int(q.w);
-                S.q[k] = q;
-                S.qi[k] = qg.cidx[q0 + qb0 + k];
-                const float3 qs = use_pre ? shifted(b, q, -img_ax(qim, 0), -img_ax(qim, 1), -img_ax(qim, 2))
-                                          : make_float3(0.f, 0.f, 0.f);
-                S.qs[k] = make_float4(qs.x, qs.y, qs.z, 0.f);
-            }
-            if (MODE == SM_COUNT)
-            {
-                for (uint32_t k = tid; k < nb * CELL_CHUNKS; k += STHREADS)
-                    S.u1.mask[k / CELL_CHUNKS][k % CELL_CHUNKS] = 0u;
+                order = src;
+                // the sorted order (grid slot << 5 | wrap) is what the write pass replays
+                for (uint32_t e = tid; e < T; e += STHREADS)
+                    gsorted[static_cast<size_t>(c) * CELL_CAP + e] = S.slot[static_cast<uint32_t>(order[e] & 0xffffffffull)];
             }
             __syncthreads();
-            uint32_t qn = 0;
+            const uint32_t nchunks = (TT + 31) / 32;
 
-            // exact test of the first n queued (candidate, query) pairs
-            auto process = [&](uint32_t n) {
-                bool acc = false;
-                float rsq = 0.f;
-                uint32_t e = 0, qq = 0;
-                if (lane < static_cast<int>(n))
+            for (uint32_t qb0 = 0; qb0 < nqc; qb0 += QB)
+            {
+                const uint32_t nb = min(static_cast<uint32_t>(QB), nqc - qb0);
+                for (uint32_t k = tid; k < nb; k += STHREADS)
                 {
-                    const uint32_t ent = queue[lane];
-                    e = ent & 0x7ffu;
-                    qq = ent >> 11;
-                    const uint32_t t = MODE == SM_COUNT ? static_cast<uint32_t>(S.u2.key[e] & 0xffffffffull) : e;
-                    const float4 q = S.q[qq];
-                    const float4 pp = MODE == SM_HIST ? S.u1.pos[t] : g.cpos[S.slot[t] >> 5];
-                    float rx, ry, rz;
-                    if (exact_vec(b, S.img, p.arith, q, __float_as_int(q.w), pp, static_cast<int>(S.slot[t] & 31u), rx,
-                                  ry, rz))
-                    {
-                        rsq = dot3(rx, ry, rz);
-                        acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
-                    }
+                    const float4 q = qg.cpos[q0 + qb0 + k];
+                    const int qim = __float_as_int(q.w);
+                    S.q[k] = q;
+                    S.qi[k] = qg.cidx[q0 + qb0 + k];
+                    const float3 qs = use_pre ? shifted(b, q, -img_ax(qim, 0), -img_ax(qim, 1), -img_ax(qim, 2))
+                                              : make_float3(0.f, 0.f, 0.f);
+                    S.qs[k] = make_float4(qs.x, qs.y, qs.z, 0.f);
                 }
-                if (acc)
-                {
-                    if (MODE == SM_COUNT)
+                __syncthreads();
+                uint32_t qn = 0;
+
+                // exact test of the first n queued (candidate, query) pairs
+                auto process = [&](uint32_t n) {
+                    bool acc = false;
+                    float rsq = 0.f;
+                    uint32_t e = 0, qq = 0;
+                    if (lane < static_cast<int>(n))
                     {
-                        atomicOr(&S.u1.mask[qq][e >> 5], 1u << (e & 31u));
-                    }
-                    else
-                    {
-                        const float d = __fsqrt_rn(rsq);
-                        if (!(d < h.h_min || d >= h.h_max))
+                        const uint32_t ent = queue[lane];
+                        e = ent & 0x7ffu;
+                        qq = ent >> 11;
+                        const uint32_t t = MODE == SM_COUNT ? static_cast<uint32_t>(order[e] & 0xffffffffull) : e;
+                        const float4 q = S.q[qq];
+                        const uint32_t sl = S.slot[t];
+                        const float4 pp = MODE == SM_HIST ? S.pos[t] : g.cpos[sl >> 5];
+                        float rx, ry, rz;
+                        if (exact_vec(b, S.img, p.arith, q, __float_as_int(q.w), pp, static_cast<int>(sl & 31u), rx, ry,
+                                      rz))
                         {
-                            uint32_t bin = static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
-                            if (bin == h.bins)
-                                bin = h.bins - 1;
-                            if (smem_hist)
-                                atomicAdd(&S.u2.hist[bin], 1u);
-                            else
-                                atomicAdd(&hist[bin], 1ull);
+                            rsq = dot3(rx, ry, rz);
+                            acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
                         }
                     }
-                }
-            };
-
-            for (uint32_t ch = warp; ch < nchunks; ch += SWARPS)
-            {
-                const uint32_t e = ch * 32 + lane;
-                const bool live = e < T;
-                const uint32_t t = (MODE == SM_COUNT && live) ? static_cast<uint32_t>(S.u2.key[e] & 0xffffffffull) : e;
-                float4 ps = make_float4(0.f, 0.f, 0.f, 0.f);
-                uint32_t jj = 0xffffffffu;
-                if (live)
-                {
-                    jj = S.j[t];
-                    if (use_pre)
-                        ps = S.ps[t];
-                }
-                for (uint32_t qq = 0; qq < nb; ++qq)
-                {
-                    bool need = false, inside = false;
-                    if (live && !(p.exclude_ii && jj == S.qi[qq]))
+                    if (acc)
                     {
+                        if (MODE == SM_COUNT)
+                        {
+                            atomicOr(&S.mask[qq][e >> 5], 1u << (e & 31u));
+                        }
+                        else
+                        {
+                            const float d = __fsqrt_rn(rsq);
+                            if (!(d < h.h_min || d >= h.h_max))
+                            {
+                                uint32_t bin = static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
+                                if (bin == h.bins)
+                                    bin = h.bins - 1;
+                                if (smem_hist)
+                                    atomicAdd(&S.u.hist[bin], 1u);
+                                else
+                                    atomicAdd(&hist[bin], 1ull);
+                            }
+                        }
+                    }
+                };
+
+                for (uint32_t ch = warp; ch < nchunks; ch += SWARPS)
+                {
+                    const uint32_t e = ch * 32 + lane;
+                    const bool live = e < TT;
+                    const uint32_t t = (MODE == SM_COUNT && live) ? static_cast<uint32_t>(order[e] & 0xffffffffull) : e;
+                    float4 ps = make_float4(3e30f, 3e30f, 3e30f, 0.f);
+                    uint32_t jj = 0xffffffffu;
+                    if (live)
+                    {
+                        jj = S.j[t];
+                        if (use_pre)
+                            ps = S.ps[t];
+                    }
+                    for (uint32_t qq = 0; qq < nb; ++qq)
+                    {
+                        const bool ok = live && !(p.exclude_ii && jj == S.qi[qq]);
+                        bool need = ok;
+                        bool inside = false;
                         if (use_pre)
                         {
                             const float4 qs = S.qs[qq];
                             const float dx = ps.x - qs.x, dy = ps.y - qs.y, dz = ps.z - qs.z;
                             const float d2 = dx * dx + dy * dy + dz * dz;
-                            if (MODE == SM_COUNT && d2 < pre_in2)
-                                inside = true;
-                            else
-                                need = d2 <= pre_out2;
+                            inside = MODE == SM_COUNT && ok && d2 < pre_in2;
+                            need = ok && !inside && d2 <= pre_out2;
                         }
-                        else
+                        if (MODE == SM_COUNT)
                         {
-                            need = true;
+                            const unsigned im = __ballot_sync(FULL, inside);
+                            if (lane == 0)
+                                S.mask[qq][ch] = im;
+                        }
+                        const unsigned nm = __ballot_sync(FULL, need);
+                        if (nm != 0)
+                        {
+                            if (need)
+                                queue[qn + __popc(nm & lt)] = e | (qq << 11);
+                            qn += __popc(nm);
+                            __syncwarp();
+                            if (qn >= 32)
+                            {
+                                process(32);
+                                const uint32_t rest = qn - 32;
+                                uint32_t v = 0;
+                                if (lane < static_cast<int>(rest))
+                                    v = queue[32 + lane];
+                                __syncwarp();
+                                if (lane < static_cast<int>(rest))
+                                    queue[lane] = v;
+                                __syncwarp();
+                                qn = rest;
+                            }
                         }
                     }
-                    if (MODE == SM_COUNT)
+                    if (MODE == SM_COUNT && qn > 0)
                     {
-                        const unsigned im = __ballot_sync(FULL, inside);
-                        if (lane == 0 && im != 0)
-                            atomicOr(&S.u1.mask[qq][ch], im);
-                    }
-                    const unsigned nm = __ballot_sync(FULL, need);
-                    if (need)
-                        queue[qn + __popc(nm & lt)] = e | (qq << 11);
-                    qn += __popc(nm);
-                    __syncwarp();
-                    if (qn >= 32)
-                    {
-                        process(32);
-                        const uint32_t rest = qn - 32;
-                        uint32_t v = 0;
-                        if (lane < static_cast<int>(rest))
-                            v = queue[32 + lane];
+                        // flush before the chunk's masks can be read by another warp
+                        process(qn);
                         __syncwarp();
-                        if (lane < static_cast<int>(rest))
-                            queue[lane] = v;
-                        __syncwarp();
-                        qn = rest;
+                        qn = 0;
                     }
                 }
-            }
-            if (qn > 0)
-                process(qn);
-            __syncthreads();
-            if (MODE == SM_COUNT)
-            {
-                // masks and counts of this query batch
-                for (uint32_t k = tid; k < nb; k += STHREADS)
+                if (qn > 0)
                 {
-                    uint32_t cnt = 0;
-                    uint32_t* dst = gmask + static_cast<size_t>(q0 + qb0 + k) * CELL_CHUNKS;
-                    for (uint32_t ch = 0; ch < nchunks; ++ch)
-                    {
-                        const uint32_t m = S.u1.mask[k][ch];
-                        dst[ch] = m;
-                        cnt += __popc(m);
-                    }
-                    counts[S.qi[k]] = cnt;
+                    process(qn);
+                    __syncwarp();
                 }
                 __syncthreads();
+                if (MODE == SM_COUNT)
+                {
+                    // masks and counts of this query batch: warp per query, lane per chunk
+                    for (uint32_t k = warp; k < nb; k += SWARPS)
+                    {
+                        const uint32_t m = lane < static_cast<int>(nchunks) ? S.mask[k][lane] : 0u;
+                        gmask[static_cast<size_t>(q0 + qb0 + k) * CELL_CHUNKS + lane] = m;
+                        uint32_t cnt = __popc(m);
+                        for (int o = 16; o > 0; o >>= 1)
+                            cnt += __shfl_xor_sync(FULL, cnt, o);
+                        if (lane == 0)
+                            counts[S.qi[k]] = cnt;
+                    }
+                    __syncthreads();
+                }
             }
         }
     }
@@ -426,8 +451,8 @@ __global__ void __launch_bounds__(STHREADS, 2)
         __syncthreads();
         for (int bin = tid; bin < static_cast<int>(h.bins); bin += STHREADS)
         {
-            if (S.u2.hist[bin] != 0)
-                atomicAdd(&hist[bin], static_cast<unsigned long long>(S.u2.hist[bin]));
+            if (S.u.hist[bin] != 0)
+                atomicAdd(&hist[bin], static_cast<unsigned long long>(S.u.hist[bin]));
         }
     }
 }
@@ -479,7 +504,8 @@ __global__ void __launch_bounds__(ETHREADS)
             const float4 q = qg.cpos[q0 + qq];
             const uint32_t qi = qg.cidx[q0 + qq];
             const int qimg = __float_as_int(q.w);
-            const uint32_t* mrow = gmask + static_cast<size_t>(q0 + qq) * CELL_CHUNKS;
+            // lane k holds the mask word of chunk k
+            const uint32_t mword = lane < static_cast<int>(nchunks) ? gmask[static_cast<size_t>(q0 + qq) * CELL_CHUNKS + lane] : 0u;
             const uint64_t out = offsets[qi];
             uint32_t written = 0;
             uint32_t qn = 0;
@@ -499,13 +525,14 @@ __global__ void __launch_bounds__(ETHREADS)
                 }
                 written += n;
             };
-            for (uint32_t ch = 0; ch < nchunks; ++ch)
+            unsigned live_chunks = __ballot_sync(FULL, mword != 0);
+            while (live_chunks != 0)
             {
-                const uint32_t m = mrow[ch];
-                if (m == 0)
-                    continue;
+                const int ch = __ffs(live_chunks) - 1;
+                live_chunks &= live_chunks - 1;
+                const uint32_t m = __shfl_sync(FULL, mword, ch);
                 if ((m >> lane) & 1u)
-                    queue[qn + __popc(m & lt)] = ch * 32 + lane;
+                    queue[qn + __popc(m & lt)] = static_cast<uint32_t>(ch) * 32u + lane;
                 qn += __popc(m);
                 __syncwarp();
                 if (qn >= 32)
@@ -560,7 +587,7 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
                       uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
                       cudaStream_t s)
 {
-    const int want = 2 * sm_count_cell();
+    const int want = 3 * sm_count_cell();
     const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
     const size_t smem = sizeof(ScanShared);
     if (!hist_mode)

@@ -334,4 +334,112 @@ void launch_segments_from_offsets(const uint32_t* counts, const uint64_t* offset
     }
 }
 
+// ---------------------------------------------------------------------------
+// Sort the points of every cell by point index (cells of up to SORT_CELL_MAX
+// points; larger cells are left in scatter order and never reach the per-cell
+// merge, whose candidate capacity they exceed). A home cell's candidate set is
+// then a union of runs already sorted by index.
+// ---------------------------------------------------------------------------
+constexpr int SORT_CELL_MAX = 1024;
+constexpr int SORT_WARPS = 4;
+
+// Reads the scatter-ordered (cpos_in, cidx_in) and writes every cell's points
+// sorted by point index to (cpos_out, cidx_out). Cells larger than SORT_CELL_MAX
+// are copied in scatter order.
+__global__ void __launch_bounds__(SORT_WARPS * 32)
+    k_sort_cells(const uint32_t* __restrict__ start, int ncell, const float4* __restrict__ cpos_in,
+                 const uint32_t* __restrict__ cidx_in, float4* __restrict__ cpos_out, uint32_t* __restrict__ cidx_out)
+{
+    __shared__ unsigned long long s_key[SORT_WARPS][SORT_CELL_MAX];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    unsigned long long* key = s_key[warp];
+    for (int c = blockIdx.x * SORT_WARPS + warp; c < ncell; c += gridDim.x * SORT_WARPS)
+    {
+        const uint32_t b0 = start[c];
+        const uint32_t n = start[c + 1] - b0;
+        if (n == 0)
+            continue;
+        if (n > static_cast<uint32_t>(SORT_CELL_MAX))
+        {
+            for (uint32_t e = lane; e < n; e += 32)
+            {
+                cpos_out[b0 + e] = cpos_in[b0 + e];
+                cidx_out[b0 + e] = cidx_in[b0 + e];
+            }
+            continue;
+        }
+        if (n <= 32)
+        {
+            // register bitonic sort over the warp on (index << 32 | slot) keys
+            unsigned long long k = lane < static_cast<int>(n)
+                ? ((static_cast<unsigned long long>(cidx_in[b0 + lane]) << 32) | static_cast<unsigned>(lane))
+                : ~0ull;
+            for (int kk = 2; kk <= 32; kk <<= 1)
+            {
+                for (int j = kk >> 1; j > 0; j >>= 1)
+                {
+                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, k, j);
+                    const bool up = (lane & kk) == 0;
+                    const bool lower = (lane & j) == 0;
+                    const bool take = lower ? (up ? o < k : o > k) : (up ? o > k : o < k);
+                    if (take)
+                        k = o;
+                }
+            }
+            if (lane < static_cast<int>(n))
+            {
+                cpos_out[b0 + lane] = cpos_in[b0 + static_cast<uint32_t>(k & 0xffffffffull)];
+                cidx_out[b0 + lane] = static_cast<uint32_t>(k >> 32);
+            }
+            continue;
+        }
+        uint32_t np2 = 64;
+        while (np2 < n)
+            np2 <<= 1;
+        for (uint32_t e = lane; e < np2; e += 32)
+            key[e] = e < n ? ((static_cast<unsigned long long>(cidx_in[b0 + e]) << 32) | e) : ~0ull;
+        __syncwarp();
+        for (uint32_t kk = 2; kk <= np2; kk <<= 1)
+        {
+            for (uint32_t j = kk >> 1; j > 0; j >>= 1)
+            {
+                for (uint32_t e = lane; e < np2 / 2; e += 32)
+                {
+                    const uint32_t lo = ((e & ~(j - 1)) << 1) | (e & (j - 1));
+                    const uint32_t hi = lo | j;
+                    const bool up = (lo & kk) == 0;
+                    const unsigned long long a = key[lo], c2 = key[hi];
+                    if ((a > c2) == up)
+                    {
+                        key[lo] = c2;
+                        key[hi] = a;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        for (uint32_t e = lane; e < n; e += 32)
+        {
+            cpos_out[b0 + e] = cpos_in[b0 + static_cast<uint32_t>(key[e] & 0xffffffffull)];
+            cidx_out[b0 + e] = static_cast<uint32_t>(key[e] >> 32);
+        }
+        __syncwarp();
+    }
+}
+
+void launch_sort_cells(const uint32_t* start, int ncell, const float4* cpos_in, const uint32_t* cidx_in,
+                       float4* cpos_out, uint32_t* cidx_out, cudaStream_t s)
+{
+    if (ncell == 0)
+    {
+        return;
+    }
+    const int blocks = grid_for(static_cast<size_t>(ncell) * 32, SORT_WARPS * 32);
+    {
+        ProfScope prof_("k_sort_cells", s);
+        k_sort_cells<<<blocks, SORT_WARPS * 32, 0, s>>>(start, ncell, cpos_in, cidx_in, cpos_out, cidx_out);
+    }
+}
+
 } // namespace fg

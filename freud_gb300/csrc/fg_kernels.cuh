@@ -36,6 +36,9 @@ void launch_assign(const DevBox& box, const float* pts, uint32_t n, const int di
                    uint32_t* rank, uint32_t* cell_count, cudaStream_t s);
 void launch_scatter(const DevBox& box, const float* pts, uint32_t n, const uint32_t* cell_of,
                     const uint32_t* rank, const uint32_t* start, float4* cpos, uint32_t* cidx, cudaStream_t s);
+// Every cell's points sorted by point index (cells of up to 1024 points).
+void launch_sort_cells(const uint32_t* start, int ncell, const float4* cpos_in, const uint32_t* cidx_in,
+                       float4* cpos_out, uint32_t* cidx_out, cudaStream_t s);
 
 // Exclusive scans. scratch must hold scan_scratch_bytes(n) bytes.
 size_t scan_scratch_bytes(size_t n);
@@ -80,15 +83,16 @@ void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, c
                       const uint32_t* list = nullptr);
 
 // Block-per-cell ball kernels. qg is the cell-sorted query grid (same dims as g).
-// Queries of cells whose candidate set exceeds CELL_CAP are appended to overflow
-// for the warp-per-query kernels. pre_out2 > 0 enables the wrap-arithmetic
+// In the count pass, queries of cells whose candidate set exceeds CELL_CAP are
+// appended to overflow for the warp-per-query kernels; the histogram pass tiles
+// large candidate sets instead. pre_out2 > 0 enables the wrap-arithmetic
 // prefilter (pairs beyond sqrt(pre_out2) are rejected without the exact test);
 // pre_in2 > 0 lets the count pass accept pairs inside sqrt(pre_in2) unchecked.
 // Scan pass (hist_mode 0): counts per query, acceptance masks gmask[nq][CELL_CHUNKS]
 // (by sorted query position) and each cell's candidates sorted by point index,
 // gsorted[ncell][CELL_CAP] (grid slot << 5 | wrap). hist_mode 1: fused histogram.
 // Emit pass: writes each query's bonds, in (i, j) order, at offsets[i].
-constexpr int CELL_CAP = 2048;
+constexpr int CELL_CAP = 1024;
 constexpr int CELL_CHUNKS = CELL_CAP / 32;
 size_t cell_smem_bytes();
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,

@@ -195,6 +195,34 @@ def test_small_box_few_cells(freud):
     assert_nlist_equal(nl, ij, d, v)
 
 
+def test_aabb_two_cells_per_axis(freud):
+    # AABB arithmetic with two cells per axis: each cell appears twice in the
+    # stencil (two images), so the candidate set holds every point twice
+    box, pts = random_box_points(freud, 5.0, 300, 13, (0.1, 0.0, 0.0))
+    nq = freud.locality.AABBQuery(box, pts)
+    nl = nq.query(pts, dict(r_max=2.2, exclude_ii=True)).toNeighborList()
+    ij, d, v = O.query(box, pts, r_max=2.2, exclude_ii=True, arith=O.ARITH_AABB)
+    assert_nlist_equal(nl, ij, d, v)
+    rdf = freud.density.RDF(50, 2.2).compute(nq, neighbors={"r_max": 2.2})
+    np.testing.assert_array_equal(rdf.bin_counts_u64, O.hist(d, 50, 2.2))
+
+
+def test_dense_blob_histogram(freud):
+    # a dense blob: home cells with more candidates than the shared-memory tile
+    rs = np.random.RandomState(21)
+    box = freud.box.Box.cube(40.0)
+    pts = np.concatenate([rs.normal(0, 1.5, (6000, 3)), rs.uniform(-20, 20, (4000, 3))]).astype(np.float32)
+    pts = box.wrap(pts)
+    rdf = freud.density.RDF(120, 3.0).compute((box, pts))
+    np.testing.assert_array_equal(rdf.bin_counts_u64, O.rdf_counts_query(box, pts, 120, 3.0))
+    lc = freud.locality.LinkCell(box, pts, 3.0)
+    nl = lc.query(pts, dict(r_max=3.0, exclude_ii=True)).toNeighborList()
+    ij, d, v = O.query(box, pts, r_max=3.0, exclude_ii=True, arith=O.ARITH_WRAP)
+    assert_nlist_equal(nl, ij, d, v)
+    rdf2 = freud.density.RDF(120, 3.0).compute(lc, neighbors={"r_max": 3.0})
+    np.testing.assert_array_equal(rdf2.bin_counts_u64, O.hist(d, 120, 3.0))
+
+
 def test_empty_result(freud):
     box, pts = random_box_points(freud, 10.0, 100, 1)
     nq = freud.locality.AABBQuery(box, pts)
