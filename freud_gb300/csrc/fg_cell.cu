@@ -77,6 +77,7 @@ struct ScanShared
     float4 pos[CELL_CAP];             // candidate position (histogram pass)
     uint32_t j[CELL_CAP];             // point index
     uint32_t slot[CELL_CAP];          // grid slot << 5 | cell wrap code
+    unsigned char run[CELL_CAP];      // stencil item (sorted run) of each staged position
     uint32_t mask[QB][CELL_CHUNKS];   // acceptance per (query, chunk) in sorted order (count pass)
     float4 q[QB];
     float4 qs[QB];
@@ -254,6 +255,7 @@ __global__ void __launch_bounds__(STHREADS, 3)
                 const uint32_t jj = g.cidx[slot];
                 S.j[tl] = jj;
                 S.slot[tl] = (slot << 5) | static_cast<uint32_t>(wr);
+                S.run[tl] = static_cast<unsigned char>(s);
                 if (MODE == SM_HIST)
                     S.pos[tl] = pp;
                 if (use_pre)
@@ -277,7 +279,7 @@ __global__ void __launch_bounds__(STHREADS, 3)
                 {
                     for (uint32_t e = tid; e < T; e += STHREADS)
                     {
-                        const int r = item_of(S.it, e) >> L;
+                        const int r = static_cast<int>(S.run[e]) >> L;
                         const int pr = r ^ 1;
                         const uint32_t lo_r = S.it.off[min(r << L, 32)];
                         const uint32_t lo_p = S.it.off[min(pr << L, 32)];
@@ -375,7 +377,8 @@ __global__ void __launch_bounds__(STHREADS, 3)
                     }
                     for (uint32_t qq = 0; qq < nb; ++qq)
                     {
-                        const bool ok = live && !(p.exclude_ii && jj == S.qi[qq]);
+                        // count pass: self bonds are removed per query after the sweep
+                        const bool ok = live && (MODE == SM_COUNT || !(p.exclude_ii && jj == S.qi[qq]));
                         bool need = ok;
                         bool inside = false;
                         if (use_pre)
@@ -430,6 +433,22 @@ __global__ void __launch_bounds__(STHREADS, 3)
                 __syncthreads();
                 if (MODE == SM_COUNT)
                 {
+                    if (p.exclude_ii)
+                    {
+                        // drop the bonds whose point index equals the query index
+                        // (NeighborQuery exclude_ii); equal indices are adjacent in the sorted keys
+                        for (uint32_t k = tid; k < nb; k += STHREADS)
+                        {
+                            const unsigned long long lo_key = static_cast<unsigned long long>(S.qi[k]) << 32;
+                            uint32_t e = rank_in(order, 0, T, lo_key);
+                            while (e < T && (order[e] >> 32) == S.qi[k])
+                            {
+                                atomicAnd(&S.mask[k][e >> 5], ~(1u << (e & 31u)));
+                                ++e;
+                            }
+                        }
+                        __syncthreads();
+                    }
                     // masks and counts of this query batch: warp per query, lane per chunk
                     for (uint32_t k = warp; k < nb; k += SWARPS)
                     {
@@ -459,7 +478,9 @@ __global__ void __launch_bounds__(STHREADS, 3)
 
 struct EmitShared
 {
-    uint32_t sorted[CELL_CAP];
+    float4 pos[CELL_CAP];  // candidate positions in sorted order
+    uint32_t j[CELL_CAP];  // point index in sorted order
+    unsigned char wrap[CELL_CAP];
     uint32_t queue[EWARPS][64];
     Items it;
     float img[27][3];
@@ -496,7 +517,12 @@ __global__ void __launch_bounds__(ETHREADS)
             continue; // written by the warp-per-query kernel
         }
         for (uint32_t e = tid; e < T; e += ETHREADS)
-            S.sorted[e] = gsorted[static_cast<size_t>(c) * CELL_CAP + e];
+        {
+            const uint32_t ent = gsorted[static_cast<size_t>(c) * CELL_CAP + e];
+            S.pos[e] = g.cpos[ent >> 5];
+            S.j[e] = g.cidx[ent >> 5];
+            S.wrap[e] = static_cast<unsigned char>(ent & 31u);
+        }
         __syncthreads();
         const uint32_t nchunks = (T + 31) / 32;
         for (uint32_t qq = warp; qq < nqc; qq += EWARPS)
@@ -512,12 +538,11 @@ __global__ void __launch_bounds__(ETHREADS)
             auto process = [&](uint32_t n) {
                 if (lane < static_cast<int>(n))
                 {
-                    const uint32_t ent = S.sorted[queue[lane]];
-                    const uint32_t slot = ent >> 5;
+                    const uint32_t e = queue[lane];
                     float rx, ry, rz;
-                    exact_vec(b, S.img, p.arith, q, qimg, g.cpos[slot], static_cast<int>(ent & 31u), rx, ry, rz);
+                    exact_vec(b, S.img, p.arith, q, qimg, S.pos[e], static_cast<int>(S.wrap[e]), rx, ry, rz);
                     const uint64_t o = out + written + lane;
-                    ij[o] = make_uint2(qi, g.cidx[slot]);
+                    ij[o] = make_uint2(qi, S.j[e]);
                     dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
                     vec[3 * o] = rx;
                     vec[3 * o + 1] = ry;
