@@ -375,7 +375,68 @@ __global__ void __launch_bounds__(STHREADS, 3)
                         if (use_pre)
                             ps = S.ps[t];
                     }
-                    for (uint32_t qq = 0; qq < nb; ++qq)
+                    // queue the undecided pairs of one query (warp-uniform nm != 0)
+                    auto append = [&](bool need, unsigned nm, uint32_t qq) {
+                        if (need)
+                            queue[qn + __popc(nm & lt)] = e | (qq << 11);
+                        qn += __popc(nm);
+                        __syncwarp();
+                        if (qn >= 32)
+                        {
+                            process(32);
+                            const uint32_t rest = qn - 32;
+                            uint32_t v = 0;
+                            if (lane < static_cast<int>(rest))
+                                v = queue[32 + lane];
+                            __syncwarp();
+                            if (lane < static_cast<int>(rest))
+                                queue[lane] = v;
+                            __syncwarp();
+                            qn = rest;
+                        }
+                    };
+                    uint32_t qq = 0;
+                    if (use_pre)
+                    {
+                        // four queries per step: independent distance tests and ballots
+                        for (; qq + 4 <= nb; qq += 4)
+                        {
+                            bool ok[4], in[4], nd[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                            {
+                                const float4 qs = S.qs[qq + k];
+                                const float dx = ps.x - qs.x, dy = ps.y - qs.y, dz = ps.z - qs.z;
+                                const float d2 = dx * dx + dy * dy + dz * dz;
+                                ok[k] = live && (MODE == SM_COUNT || !(p.exclude_ii && jj == S.qi[qq + k]));
+                                in[k] = MODE == SM_COUNT && ok[k] && d2 < pre_in2;
+                                nd[k] = ok[k] && !in[k] && d2 <= pre_out2;
+                            }
+                            if (MODE == SM_COUNT)
+                            {
+                                unsigned im[4];
+#pragma unroll
+                                for (int k = 0; k < 4; ++k)
+                                    im[k] = __ballot_sync(FULL, in[k]);
+                                if (lane < 4)
+                                    S.mask[qq + lane][ch] = lane == 0 ? im[0] : (lane == 1 ? im[1] : (lane == 2 ? im[2] : im[3]));
+                            }
+                            unsigned nm[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                nm[k] = __ballot_sync(FULL, nd[k]);
+                            if ((nm[0] | nm[1] | nm[2] | nm[3]) != 0)
+                            {
+#pragma unroll
+                                for (int k = 0; k < 4; ++k)
+                                {
+                                    if (nm[k] != 0)
+                                        append(nd[k], nm[k], qq + k);
+                                }
+                            }
+                        }
+                    }
+                    for (; qq < nb; ++qq)
                     {
                         // count pass: self bonds are removed per query after the sweep
                         const bool ok = live && (MODE == SM_COUNT || !(p.exclude_ii && jj == S.qi[qq]));
@@ -397,25 +458,7 @@ __global__ void __launch_bounds__(STHREADS, 3)
                         }
                         const unsigned nm = __ballot_sync(FULL, need);
                         if (nm != 0)
-                        {
-                            if (need)
-                                queue[qn + __popc(nm & lt)] = e | (qq << 11);
-                            qn += __popc(nm);
-                            __syncwarp();
-                            if (qn >= 32)
-                            {
-                                process(32);
-                                const uint32_t rest = qn - 32;
-                                uint32_t v = 0;
-                                if (lane < static_cast<int>(rest))
-                                    v = queue[32 + lane];
-                                __syncwarp();
-                                if (lane < static_cast<int>(rest))
-                                    queue[lane] = v;
-                                __syncwarp();
-                                qn = rest;
-                            }
-                        }
+                            append(need, nm, qq);
                     }
                     if (MODE == SM_COUNT && qn > 0)
                     {
@@ -525,13 +568,28 @@ __global__ void __launch_bounds__(ETHREADS)
         }
         __syncthreads();
         const uint32_t nchunks = (T + 31) / 32;
+        // one-ahead prefetch of each warp's next query (position, index, mask row)
+        float4 q_n = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t qi_n = 0, mw_n = 0;
+        if (static_cast<uint32_t>(warp) < nqc)
+        {
+            q_n = qg.cpos[q0 + warp];
+            qi_n = qg.cidx[q0 + warp];
+            mw_n = lane < static_cast<int>(nchunks) ? gmask[static_cast<size_t>(q0 + warp) * CELL_CHUNKS + lane] : 0u;
+        }
         for (uint32_t qq = warp; qq < nqc; qq += EWARPS)
         {
-            const float4 q = qg.cpos[q0 + qq];
-            const uint32_t qi = qg.cidx[q0 + qq];
+            const float4 q = q_n;
+            const uint32_t qi = qi_n;
+            const uint32_t mword = mw_n;
             const int qimg = __float_as_int(q.w);
-            // lane k holds the mask word of chunk k
-            const uint32_t mword = lane < static_cast<int>(nchunks) ? gmask[static_cast<size_t>(q0 + qq) * CELL_CHUNKS + lane] : 0u;
+            if (qq + EWARPS < nqc)
+            {
+                q_n = qg.cpos[q0 + qq + EWARPS];
+                qi_n = qg.cidx[q0 + qq + EWARPS];
+                mw_n = lane < static_cast<int>(nchunks)
+                    ? gmask[static_cast<size_t>(q0 + qq + EWARPS) * CELL_CHUNKS + lane] : 0u;
+            }
             const uint64_t out = offsets[qi];
             uint32_t written = 0;
             uint32_t qn = 0;
