@@ -90,6 +90,7 @@ SIGNATURES = {
     "fg_steinhardt_compute": [P, P, P, pargs],
     "fg_steinhardt_num_particles": [P, pu32],
     "fg_steinhardt_get": [P, P, P, P, P],
+    "fg_rdf_histogram_noalloc": [pbox, P, u32, f32, f32, u32, i32, i32, P, P],
 }
 _RESTYPES = {"fg_last_error": ctypes.c_char_p, "fg_version": ctypes.c_int}
 

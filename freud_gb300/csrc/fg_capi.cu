@@ -13,6 +13,7 @@
 #include <limits>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -1832,6 +1833,161 @@ fg_status fg_steinhardt_get(const fg_steinhardt* st, float* ql, float* particle_
         if (order)
             std::memcpy(order, st->order.data(), sizeof(float) * st->order.size());
         sync();
+    });
+}
+
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free fused RDF histogram.
+//
+// For callers that cannot allocate device memory themselves or through this
+// library: code running inside a framework that owns every device allocation
+// (a simulation engine's analysis plugin handed device pointers, a custom
+// allocator that forbids cudaMalloc/cudaMallocAsync mid-run, or work recorded
+// into a CUDA graph by someone else). All scratch lives in one file-scope device
+// array of fixed size, g_noalloc_scratch, held by every GPU that loads this
+// library until the process exits. Host code never dereferences the array's
+// name: its device address is obtained with cudaGetSymbolAddress, once per
+// device, on the first call made with that device current (so that first call
+// should come before any stream capture). Every call shares the array and it
+// keeps the last call's contents; calls that overlap on the GPU race on it.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_POINTS = 1u << 16;                  // 65,536 points
+constexpr uint32_t NOALLOC_MAX_CELLS = 2u * NOALLOC_MAX_POINTS + 64u; // grid_dims keeps <= 2N + 64 cells
+constexpr size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+constexpr size_t NA_CELL_OF = 0;
+constexpr size_t NA_RANK = align256(NA_CELL_OF + 4ull * NOALLOC_MAX_POINTS);
+constexpr size_t NA_COUNTS = align256(NA_RANK + 4ull * NOALLOC_MAX_POINTS);
+constexpr size_t NA_START = align256(NA_COUNTS + 4ull * (NOALLOC_MAX_CELLS + 1));
+constexpr size_t NA_CPOS0 = align256(NA_START + 4ull * (NOALLOC_MAX_CELLS + 1));
+constexpr size_t NA_CIDX0 = align256(NA_CPOS0 + 16ull * NOALLOC_MAX_POINTS);
+constexpr size_t NA_CPOS = align256(NA_CIDX0 + 4ull * NOALLOC_MAX_POINTS);
+constexpr size_t NA_CIDX = align256(NA_CPOS + 16ull * NOALLOC_MAX_POINTS);
+constexpr size_t NA_SCAN = align256(NA_CIDX + 4ull * NOALLOC_MAX_POINTS);
+constexpr size_t NA_SCAN_BYTES = 8192; // scan_scratch_bytes(NOALLOC_MAX_CELLS + 1) is ~1.3 KB
+constexpr size_t NA_OVER = align256(NA_SCAN + NA_SCAN_BYTES);
+constexpr size_t NOALLOC_SCRATCH_BYTES = align256(NA_OVER + 64);
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch for the current device (looked up once per device).
+unsigned char* noalloc_scratch()
+{
+    int dev = 0;
+    FG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64)
+        runtime_error("device ordinal out of range for the allocation-free entry point");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr)
+    {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || ptr == nullptr)
+            throw Error(FG_ERR_CUDA, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(ptr);
+    }
+    return g_noalloc_ptr[dev];
+}
+
+} // namespace
+
+extern "C" {
+
+fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points, uint32_t n, float r_max, float r_min,
+                                   uint32_t bins, int exclude_ii, int kind, unsigned long long* device_counts,
+                                   void* cuda_stream)
+{
+    return guard([&] {
+        require(box, "box");
+        require(device_points, "device_points");
+        require(device_counts, "device_counts");
+        if (n == 0)
+            value_error("Cannot create a NeighborQuery with 0 particles.");
+        if (n > NOALLOC_MAX_POINTS)
+            value_error("fg_rdf_histogram_noalloc handles at most " + std::to_string(NOALLOC_MAX_POINTS) +
+                        " points (its scratch is a fixed " + std::to_string(NOALLOC_SCRATCH_BYTES) +
+                        "-byte device array); got " + std::to_string(n));
+        if (bins == 0)
+            value_error("RDF requires a nonzero number of bins.");
+        if (r_max <= 0.0f)
+            value_error("RDF requires r_max to be positive.");
+        if (r_min < 0.0f)
+            value_error("RDF requires r_min to be non-negative.");
+        if (r_max <= r_min)
+            value_error("RDF requires that r_max must be greater than r_min.");
+        if (kind < FG_NQ_RAWPOINTS || kind > FG_NQ_LINKCELL)
+            value_error("unknown neighbour-query kind");
+        const HostBox hb = to_host_box(box);
+        if (kind != FG_NQ_RAWPOINTS)
+            check_periodic(hb);
+        const int arith = kind == FG_NQ_LINKCELL ? ARITH_WRAP : ARITH_AABB;
+        float pd[3];
+        nearest_plane(hb, pd);
+        if (arith == ARITH_AABB &&
+            (pd[0] <= r_max * 2.0 || pd[1] <= r_max * 2.0 || (!hb.is2d && pd[2] <= r_max * 2.0)))
+            runtime_error("The AABBQuery r_max is too large for this box.");
+        const DevBox db = make_devbox(hb);
+        int dim[3];
+        grid_dims(hb, r_max * (1.0f + 1e-5f), n, dim);
+        const int ncell = dim[0] * dim[1] * dim[2];
+        if (static_cast<uint32_t>(ncell) > NOALLOC_MAX_CELLS)
+            runtime_error("cell grid larger than the allocation-free scratch");
+
+        unsigned char* base = noalloc_scratch();
+        cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+        uint32_t* cell_of = reinterpret_cast<uint32_t*>(base + NA_CELL_OF);
+        uint32_t* rank = reinterpret_cast<uint32_t*>(base + NA_RANK);
+        uint32_t* counts = reinterpret_cast<uint32_t*>(base + NA_COUNTS);
+        uint32_t* start = reinterpret_cast<uint32_t*>(base + NA_START);
+        float4* cpos0 = reinterpret_cast<float4*>(base + NA_CPOS0);
+        uint32_t* cidx0 = reinterpret_cast<uint32_t*>(base + NA_CIDX0);
+        float4* cpos = reinterpret_cast<float4*>(base + NA_CPOS);
+        uint32_t* cidx = reinterpret_cast<uint32_t*>(base + NA_CIDX);
+        void* scan_scratch = base + NA_SCAN;
+        uint32_t* over = reinterpret_cast<uint32_t*>(base + NA_OVER);
+        if (scan_scratch_bytes(static_cast<size_t>(ncell) + 1) > NA_SCAN_BYTES)
+            runtime_error("scan scratch larger than reserved");
+
+        // the cell counts start at zero; the output is this frame's counts
+        FG_CUDA(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (ncell + 1), s));
+        FG_CUDA(cudaMemsetAsync(over, 0, 64, s));
+        FG_CUDA(cudaMemsetAsync(device_counts, 0, sizeof(unsigned long long) * bins, s));
+        launch_assign(db, device_points, n, dim, cell_of, rank, counts, s);
+        scan_u32_to_u32(counts, start, static_cast<size_t>(ncell) + 1, scan_scratch, s);
+        launch_scatter(db, device_points, n, cell_of, rank, start, cpos0, cidx0, s);
+        launch_sort_cells(start, ncell, cpos0, cidx0, cpos, cidx, s);
+        DevGrid g;
+        g.dim[0] = dim[0];
+        g.dim[1] = dim[1];
+        g.dim[2] = dim[2];
+        g.ncell = ncell;
+        g.start = start;
+        g.cpos = cpos;
+        g.cidx = cidx;
+        BallParams p;
+        p.r_max_sq = fmul(r_max, r_max);
+        p.r_min_sq = 0.0f;
+        p.exclude_ii = exclude_ii != 0;
+        p.arith = arith;
+        p.nq = n;
+        HistParams h;
+        h.h_min = r_min;
+        h.h_max = r_max;
+        h.h_inv = fdiv(1.0f, fdiv(fsub(r_max, r_min), static_cast<float>(bins)));
+        h.bins = bins;
+        // a stub NeighborQuery carrying the box for the prefilter rule
+        fg_nq probe;
+        probe.box = hb;
+        const Prefilter pf = prefilter(&probe, arith, dim, r_max, 0.0f);
+        launch_cell_scan(1, db, g, g, p, pf.out2, 0.0f, nullptr, nullptr, nullptr, over, over + 1, h, device_counts, s);
+        FG_CUDA(cudaGetLastError());
     });
 }
 

@@ -183,6 +183,26 @@ fg_status fg_steinhardt_num_particles(const fg_steinhardt* st, uint32_t* out);
  * Any output may be NULL. */
 fg_status fg_steinhardt_get(const fg_steinhardt* st, float* ql, float* particle_order, float* qlm, float* order);
 
+/* ---- Allocation-free RDF histogram -----------------------------------------
+ * No counterpart in the reference (freud has no device code). For callers that
+ * may not allocate device memory - an analysis plugin inside a simulation engine
+ * that owns every device allocation, or code under an allocator that forbids
+ * cudaMalloc - this computes the uint64 RDF bin counts of one frame (the ball
+ * query of radius r_max with bins over [r_min, r_max), as
+ * RDF(bins, r_max, r_min).compute((box, points)) does, fused) without allocating
+ * anything: its scratch is a fixed file-scope device array of about 3.7 MB that
+ * every GPU loading the library holds until exit, which limits n to 65,536 points
+ * (larger n is rejected with FG_ERR_VALUE). device_points (n x 3 float32) and
+ * device_counts (bins uint64, overwritten) are the caller's device buffers.
+ * kind: FG_NQ_RAWPOINTS / FG_NQ_AABB (AABB arithmetic) or FG_NQ_LINKCELL (wrap).
+ * Work is enqueued on cuda_stream (NULL: the legacy default stream) and the call
+ * returns without synchronising. The first call on each device looks up the
+ * scratch array's device address, so make it before any stream capture. All
+ * calls share the scratch: calls that overlap on the GPU race. */
+fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points, uint32_t n, float r_max,
+                                   float r_min, uint32_t bins, int exclude_ii, int kind,
+                                   unsigned long long* device_counts, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
