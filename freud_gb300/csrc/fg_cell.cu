@@ -396,6 +396,81 @@ __global__ void __launch_bounds__(STHREADS, 3)
                         }
                     };
                     uint32_t qq = 0;
+                    if (p.arith == ARITH_AABB)
+                    {
+                        // AABB arithmetic is cheap, so every pair is tested exactly in place:
+                        // r = p_j - (q + image_k) with k = n_j - wrap - n_q. For queries inside
+                        // the box (n_q = 0) the image depends on the candidate only.
+                        float4 pp = make_float4(0.f, 0.f, 0.f, 0.f);
+                        int wr = 13, kx = 0, ky = 0, kz = 0;
+                        if (live)
+                        {
+                            const uint32_t sl = S.slot[t];
+                            pp = MODE == SM_HIST ? S.pos[t] : g.cpos[sl >> 5];
+                            wr = static_cast<int>(sl & 31u);
+                            const int pim = __float_as_int(pp.w);
+                            kx = img_ax(pim, 0) - (wr % 3 - 1);
+                            ky = img_ax(pim, 1) - ((wr / 3) % 3 - 1);
+                            kz = img_ax(pim, 2) - (wr / 9 - 1);
+                        }
+                        const bool inimg = live && kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1;
+                        float ix = 0.f, iy = 0.f, iz = 0.f;
+                        if (inimg)
+                        {
+                            const float* iv = S.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
+                            ix = iv[0];
+                            iy = iv[1];
+                            iz = iv[2];
+                        }
+                        for (; qq < nb; ++qq)
+                        {
+                            const float4 q = S.q[qq];
+                            const int qimg = __float_as_int(q.w);
+                            const bool ok = MODE == SM_COUNT || !(p.exclude_ii && jj == S.qi[qq]);
+                            bool acc = false;
+                            float rsq = 0.f;
+                            if (qimg == 0)
+                            {
+                                if (inimg && ok)
+                                {
+                                    const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, ix));
+                                    const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iy));
+                                    const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iz));
+                                    rsq = dot3(rx, ry, rz);
+                                    acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
+                                }
+                            }
+                            else if (live && ok)
+                            {
+                                float rx, ry, rz;
+                                if (exact_vec(b, S.img, p.arith, q, qimg, pp, wr, rx, ry, rz))
+                                {
+                                    rsq = dot3(rx, ry, rz);
+                                    acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
+                                }
+                            }
+                            if (MODE == SM_COUNT)
+                            {
+                                const unsigned am = __ballot_sync(FULL, acc);
+                                if (lane == 0)
+                                    S.mask[qq][ch] = am;
+                            }
+                            else if (acc)
+                            {
+                                const float d = __fsqrt_rn(rsq);
+                                if (!(d < h.h_min || d >= h.h_max))
+                                {
+                                    uint32_t bin = static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
+                                    if (bin == h.bins)
+                                        bin = h.bins - 1;
+                                    if (smem_hist)
+                                        atomicAdd(&S.u.hist[bin], 1u);
+                                    else
+                                        atomicAdd(&hist[bin], 1ull);
+                                }
+                            }
+                        }
+                    }
                     if (use_pre)
                     {
                         // four queries per step: independent distance tests and ballots
