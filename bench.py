@@ -52,6 +52,57 @@ def c2_system(seed=2024, n1=102):
     return L, pts.astype(np.float32)
 
 
+def c1_system(seed=1):
+    """10,000 points uniform in a periodic cube of side 21.544 (number density 1)."""
+    L = 21.544
+    rng = np.random.default_rng(seed)
+    pts = rng.uniform(-L / 2, L / 2, (10000, 3)).astype(np.float32)
+    return L, pts
+
+
+def c3_system(seed=3):
+    """FCC crystal 4 * 40^3 = 256,000 points, lattice constant 1.5874 (density 1),
+    seeded N(0, 0.05) displacements, periodic cube of side 63.496."""
+    a, nc = 1.5874, 40
+    L = a * nc
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]], np.float64)
+    g = np.arange(nc, dtype=np.float64)
+    cells = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 1, 3)
+    pts = ((cells + basis[None]) * a).reshape(-1, 3) - L / 2
+    rng = np.random.default_rng(seed)
+    pts = pts + rng.normal(0.0, 0.05, pts.shape)
+    pts = (pts + L / 2) % L - L / 2
+    return np.float32(L), pts.astype(np.float32)
+
+
+def c4_frames(freud, seed=4, nframes=64, density=0.85):
+    """64 frames, N uniform-integer in [5,000, 500,000], points uniform in
+    fractional coordinates at number density 0.85; 90% cubic boxes, 10%
+    triclinic (xy = 0.2, xz = 0.1, yz = 0)."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(5000, 500001, nframes)
+    tric = np.zeros(nframes, bool)
+    tric[rng.permutation(nframes)[:int(round(0.1 * nframes))]] = True
+    frames = []
+    for n, t in zip(ns, tric):
+        L = float((n / density) ** (1.0 / 3.0))
+        box = freud.box.Box(L, L, L, 0.2 if t else 0.0, 0.1 if t else 0.0, 0.0)
+        frac = rng.random((int(n), 3))
+        frames.append((box, box.make_absolute(frac).astype(np.float32)))
+    return frames
+
+
+def c5_system(seed=5):
+    """4,096 isotropic Gaussian blobs (sigma 2.0, 1,024 points each) with centres
+    uniform in a periodic cube of side 256: 4,194,304 points."""
+    L = 256.0
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.0, L, (4096, 3))
+    pts = (centres[:, None, :] + rng.normal(0.0, 2.0, (4096, 1024, 3))).reshape(-1, 3)
+    pts = (pts % L) - L / 2
+    return L, pts.astype(np.float32)
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -141,6 +192,182 @@ def cpu_baseline(L, pts, r_max=3.0, bins=300, target_s=12.0, threads=None):
                           "first %d of %d query points against all points" % (m2, len(pts))), threads, dt
 
 
+def _median_wall(fn, steps, warmup):
+    for _ in range(warmup):
+        fn()
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts)
+
+
+def _device_ms(_lib, fn, steps):
+    """Median device time of fn's kernels per call (CUDA events the library records
+    on its stream around each launch) and the launches per call."""
+    _lib.profile_enable(True)
+    l0 = _lib.launch_count()
+    for _ in range(steps):
+        fn()
+    prof = _lib.profile_report()
+    launches = (_lib.launch_count() - l0) / steps
+    _lib.profile_enable(False)
+    kern = {k: v for k, v in prof.items() if not k.startswith("graph:")}
+    graphs = {k: v for k, v in prof.items() if k.startswith("graph:")}
+    ms = (sum(v[1] for v in kern.values()) + sum(v[1] for v in graphs.values())) / steps
+    top = max(prof.items(), key=lambda kv: kv[1][1])[0] if prof else None
+    return ms, launches, top
+
+
+def measure_c1(freud, _lib, steps, warmup, cpu=True):
+    """Plain RDF: RDF(200, 4.0).compute((box, points)), 10,000 uniform points."""
+    L, pts = c1_system()
+    box = freud.box.Box.cube(L)
+    rdf = freud.density.RDF(200, 4.0)
+
+    def step():
+        rdf.compute((box, pts))
+        return rdf.bin_counts_u64
+
+    pairs = int(step().sum())
+    t = _median_wall(step, steps, warmup)
+    dev_ms, launches, top = _device_ms(_lib, step, steps)
+    out = {"workload": "plain_rdf_n10000_L21.544_rmax4_bins200", "pairs": pairs, "e2e_ms": t * 1e3,
+           "e2e": pairs / t, "device_ms": dev_ms, "device": pairs / (dev_ms / 1e3), "unit": "pair evals/s",
+           "launches_per_step": launches, "top_kernel": top}
+    if cpu:
+        from oracle import oracle as O
+
+        bx = (L, L, L, 0.0, 0.0, 0.0, 0.0)
+        threads = os.cpu_count() or 1
+        ts = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            O.rdf_counts_query(bx, pts, 200, 4.0, arith=O.ARITH_AABB, threads=threads)
+            ts.append(time.perf_counter() - t0)
+        out["cpu_baseline"] = {"value": pairs / statistics.median(ts), "unit": "pair evals/s", "cores": threads,
+                               "kind": "port", "sample": "whole workload, median of 5"}
+    return out
+
+
+def measure_c3(freud, _lib, steps, warmup, cpu=True):
+    """Steinhardt([4, 6, 8, 10, 12], average, wl, wl_normalize) with 12 nearest
+    neighbours on a 256,000-point noisy FCC crystal."""
+    L, pts = c3_system()
+    box = freud.box.Box.cube(float(L))
+    st = freud.order.Steinhardt([4, 6, 8, 10, 12], average=True, wl=True, wl_normalize=True)
+
+    def step():
+        st.compute((box, pts), neighbors={"num_neighbors": 12})
+        return st.particle_order
+
+    step()
+    t = _median_wall(step, steps, warmup)
+    dev_ms, launches, top = _device_ms(_lib, step, steps)
+    n = len(pts)
+    out = {"workload": "steinhardt_fcc_256000_k12_l4-12_ave_wl", "particles": n, "e2e_ms": t * 1e3, "e2e": n / t,
+           "device_ms": dev_ms, "device": n / (dev_ms / 1e3), "unit": "particles/s", "launches_per_step": launches,
+           "top_kernel": top}
+    if cpu:
+        from oracle import oracle as O
+
+        bx = (float(L),) * 3 + (0.0, 0.0, 0.0, 0.0)
+        m = 32000
+        t0 = time.perf_counter()
+        ij, d, v = O.query(bx, pts, query_points=pts[:m], num_neighbors=12, exclude_ii=True)
+        tq = time.perf_counter() - t0
+        ij_all, d_all, _ = O.query(bx, pts, num_neighbors=12, exclude_ii=True)
+        t0 = time.perf_counter()
+        O.steinhardt([4, 6, 8, 10, 12], bx, pts, ij_all, d_all, average=True, wl=True, wl_normalize=True)
+        ts = time.perf_counter() - t0
+        per_particle = tq / m + ts / n
+        out["cpu_baseline"] = {"value": 1.0 / per_particle, "unit": "particles/s", "cores": os.cpu_count() or 1,
+                               "kind": "port",
+                               "sample": "kNN query of %d query points (all threads) + FP64 Steinhardt of all %d "
+                                         "particles (1 thread)" % (m, n)}
+    return out
+
+
+def measure_c4(freud, _lib, steps, warmup):
+    """64 uneven frames: RDF(200, 4.0) accumulated over the frames (reset=False)
+    plus Steinhardt(6, average=True) on r_max = 1.5 ball neighbours, per frame
+    (plain) and as one FrameBatch (batched), both through the public API with
+    host points, results read back every step."""
+    frames = c4_frames(freud)
+    n_total = sum(len(p) for _, p in frames)
+    rdf = freud.density.RDF(200, 4.0)
+    st = freud.order.Steinhardt(6, average=True)
+
+    def plain():
+        for f, (box, p) in enumerate(frames):
+            rdf.compute((box, p), reset=(f == 0))
+            st.compute((box, p), neighbors={"r_max": 1.5})
+            st.ql
+        return rdf.bin_counts_u64
+
+    def batched():
+        batch = freud.locality.FrameBatch(frames)
+        rdf.compute(batch)
+        st.compute(batch, neighbors={"r_max": 1.5})
+        st.ql
+        return rdf.bin_counts_u64
+
+    ref = plain()
+    got = batched()
+    assert np.array_equal(ref, got), "batched RDF counts differ from the per-frame path"
+    pairs = int(got.sum())
+    k = max(1, min(steps, 5))
+    t_plain = _median_wall(plain, k, 1)
+    t_batch = _median_wall(batched, k, max(1, warmup))
+    dev_plain, l_plain, top_plain = _device_ms(_lib, plain, 2)
+    dev_batch, l_batch, top_batch = _device_ms(_lib, batched, 2)
+    return {"workload": "batched_uneven_64_frames_rdf_rmax4_bins200_steinhardt6_rmax1.5", "frames": len(frames),
+            "particles": n_total, "pairs": pairs,
+            "plain": {"e2e_ms": t_plain * 1e3, "pair_evals_per_s": pairs / t_plain, "particles_per_s": n_total / t_plain,
+                      "device_ms": dev_plain, "launches_per_step": l_plain, "top_kernel": top_plain},
+            "batched": {"e2e_ms": t_batch * 1e3, "pair_evals_per_s": pairs / t_batch,
+                        "particles_per_s": n_total / t_batch, "device_ms": dev_batch, "launches_per_step": l_batch,
+                        "top_kernel": top_batch},
+            "speedup_e2e": t_plain / t_batch, "speedup_device": dev_plain / dev_batch if dev_batch else None,
+            "autotune": _lib.autotune_report().strip().splitlines()[-1:] }
+
+
+def measure_c5(freud, _lib, steps, warmup):
+    """4,194,304 points in 4,096 Gaussian blobs: RDF(500, 5.0) with uint64 counts
+    and FP64 normalisation, Steinhardt(6) on r_max = 1.2 ball neighbours."""
+    L, pts = c5_system()
+    box = freud.box.Box.cube(L)
+    rdf = freud.density.RDF(500, 5.0)
+    st = freud.order.Steinhardt(6)
+
+    def step():
+        rdf.compute((box, pts))
+        c = rdf.bin_counts_u64
+        st.compute((box, pts), neighbors={"r_max": 1.2})
+        st.ql
+        return c
+
+    c = step()
+    pairs = int(c.sum())
+    k = max(1, min(steps, 3))
+    t = _median_wall(step, k, 1)
+    dev_ms, launches, top = _device_ms(_lib, step, 1)
+    g32, g64 = rdf.rdf.astype(np.float64), rdf.rdf_fp64
+    nz = g64 > 0
+    # occupancy skew of the r_max = 5 cell grid (51^3 cells)
+    nc = int(L // 5.0)
+    idx = np.floor((pts.astype(np.float64) + L / 2) / L * nc).astype(np.int64) % nc
+    occ = np.bincount((idx[:, 0] * nc + idx[:, 1]) * nc + idx[:, 2], minlength=nc ** 3)
+    return {"workload": "blobs_4096x1024_L256_rdf_rmax5_bins500_steinhardt6_rmax1.2", "particles": len(pts),
+            "pairs": pairs, "pairs_above_2^32": pairs >= 2 ** 32, "e2e_ms": t * 1e3, "e2e": pairs / t,
+            "device_ms": dev_ms, "device": pairs / (dev_ms / 1e3), "unit": "pair evals/s (RDF + Steinhardt step)",
+            "launches_per_step": launches, "top_kernel": top,
+            "rdf_f32_vs_fp64_max_rel": float(np.max(np.abs(g32[nz] - g64[nz]) / g64[nz])),
+            "cell_occupancy": {"mean": float(occ.mean()), "max": int(occ.max()),
+                               "skew_max_over_mean": float(occ.max() / occ.mean())}}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -181,6 +408,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the plain-RDF, Steinhardt, batched-frames and stress workloads")
     ap.add_argument("--n-side", type=int, default=102,
                     help="lattice points per side; 102 is the benchmark workload, smaller sizes are for profiling")
     args = ap.parse_args()
@@ -268,7 +497,7 @@ def main():
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else (None, (0, 0.0))
     dom_name, (dom_n, dom_ms) = dom
     per_launch_ms = dom_ms / max(dom_n, 1)
-    if dom_name is not None and "EMIT" in dom_name:
+    if dom_name is not None and ("EMIT" in dom_name or "emit" in dom_name):
         alg_bytes = 12.0 * n + 24.0 * bonds  # positions read + (i,j) 8 B + distance 4 B + vector 12 B per bond
         alg_desc = "12*N + 24*B (positions read; (i,j), distance, vector written; weights are lazy)"
     elif dom_name is not None and "COUNT" in dom_name:
@@ -281,6 +510,12 @@ def main():
         alg_bytes = 12.0 * n
         alg_desc = "12*N"
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+    # the whole NeighborList build (grid + scan + write passes) against its output bytes
+    build_names = ("k_assign", "k_scatter", "k_sort_cells", "k_tile_scan", "k_tile_sums", "k_cell_scan<COUNT>",
+                   "k_cell_emit", "k_seg_from_offsets")
+    build_ms = sum(v[1] for k, v in prof.items() if k.startswith(build_names)) / max(args.steps, 1)
+    build_bytes = 12.0 * n + 24.0 * bonds
+    build_gbs = build_bytes / (build_ms / 1e3) / 1e9 if build_ms > 0 else 0.0
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
@@ -312,6 +547,21 @@ def main():
         cpu = {"value": v, "unit": "pair evals/s", "cores": cores, "kind": "port", "sample": desc,
                "seconds": round(dt, 2)}
 
+    # ---- the other workloads (rank 0, N=1): plain RDF, Steinhardt, batched frames, stress
+    secondary = None
+    if rank == 0 and world == 1 and not args.no_secondary:
+        secondary = {}
+        for name, fn in (("plain_rdf", lambda: measure_c1(freud, _lib, args.steps, args.warmup,
+                                                            cpu=not args.no_cpu_baseline)),
+                         ("steinhardt", lambda: measure_c3(freud, _lib, args.steps, args.warmup,
+                                                            cpu=not args.no_cpu_baseline)),
+                         ("batched_frames", lambda: measure_c4(freud, _lib, args.steps, args.warmup)),
+                         ("precision_stress", lambda: measure_c5(freud, _lib, args.steps, args.warmup))):
+            try:
+                secondary[name] = fn()
+            except Exception as e:  # report, do not hide, a failing secondary workload
+                secondary[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "pair evals/s", "n_gpus": world, "steps": args.steps,
@@ -324,7 +574,11 @@ def main():
                          "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                          "algorithmic_bytes": alg_desc, "launch_ms": per_launch_ms},
+            "roofline_build": {"bound": "hbm", "what": "NeighborList build: grid + scan + write passes",
+                               "achieved": build_gbs, "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
+                               "algorithmic_bytes": "12*N + 24*B", "ms_per_step": build_ms},
             "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in sorted(prof.items())},
+            "secondary": secondary,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "pair evals/s", "h2d_bytes_per_step": int(12 * n),
                     "d2h_bytes_per_step": int(300 * 4)},

@@ -91,6 +91,17 @@ SIGNATURES = {
     "fg_steinhardt_num_particles": [P, pu32],
     "fg_steinhardt_get": [P, P, P, P, P],
     "fg_rdf_histogram_noalloc": [pbox, P, u32, f32, f32, u32, i32, i32, P, P],
+    "fg_frames_create": [P, P, P, u32, PP],
+    "fg_frames_create_device": [P, P, P, u32, PP],
+    "fg_frames_set_points": [P, P],
+    "fg_frames_destroy": [P],
+    "fg_frames_info": [P, pu32, pu64],
+    "fg_rdf_accumulate_frames": [P, P, pargs],
+    "fg_steinhardt_compute_frames": [P, P, pargs],
+    "fg_steinhardt_num_frames": [P, pu32],
+    "fg_batch_set_config": [i32, i32, i32],
+    "fg_autotune_report": [ctypes.c_char_p, ctypes.c_size_t],
+    "fg_set_graphs": [i32],
 }
 _RESTYPES = {"fg_last_error": ctypes.c_char_p, "fg_version": ctypes.c_int}
 
@@ -138,6 +149,21 @@ def profile_report():
         name, n, ms = line.rsplit(" ", 2)
         out[name] = (int(n), float(ms))
     return out
+
+
+def autotune_report():
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(lib.fg_autotune_report(buf, len(buf)))
+    return buf.value.decode()
+
+
+def set_batch_config(shell=0, warps=8, copies=1):
+    """Force the batched RDF kernel's launch shape (shell=0: autotune)."""
+    check(lib.fg_batch_set_config(int(shell), int(warps), int(copies)))
+
+
+def set_graphs(enable):
+    check(lib.fg_set_graphs(int(bool(enable))))
 
 
 def set_stream(stream_ptr):

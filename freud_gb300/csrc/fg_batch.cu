@@ -1,0 +1,636 @@
+// Batched frames: every frame of a batch of uneven-N frames in one launch per
+// stage.
+//
+// Grid build: one counting sort over the concatenated points, each point placed
+// by its own frame's box (exact makeFractional, Box.h:243-255), so the cells of
+// all frames form one array of offsets.
+//
+// Fused RDF histogram: persistent blocks pull runs of cells from a device work
+// counter; a block reloads the frame's box when the frame changes, stages the
+// candidate set of the home cell (the (2s + 1)^3 stencil, s = shell, gathered
+// as x-row segments so each segment is one contiguous slot range) with each
+// candidate's image vector already resolved for queries inside the box, and
+// sweeps the cell's queries over it: 32 candidates per warp in registers,
+// queries broadcast from shared memory, the exact AABB pair test
+// (AABBQuery.cc:93,125) and binning (Histogram.h:327-351) into privatised
+// shared histograms, flushed once per block with 64-bit atomics.
+//
+// Steinhardt neighbours: thread per query over the 27-cell stencil, count then
+// fill; the bonds of a frame batch feed the existing qlm / average / wl kernels
+// over the concatenated rows, and the system sums are taken per frame.
+#include "fg_batch.cuh"
+#include "fg_prof.cuh"
+
+namespace fg {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int BT_TILE = 1024;   // staged candidates per tile
+constexpr int BT_QB = 64;       // queries per shared-memory batch
+constexpr int BT_ITEMS = 96;    // stencil items: up to 32 rows x 3 x-segments
+constexpr int BT_HIST = 2048;   // shared histogram words (all copies)
+constexpr int BT_CHUNK = 4;     // cells per work-counter pop
+
+// Largest f with base[f] <= x (base[0] = 0 <= x < base[nframes]).
+__device__ __forceinline__ uint32_t frame_of(const uint32_t* __restrict__ base, uint32_t nframes, uint32_t x)
+{
+    uint32_t lo = 0, hi = nframes;
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(base + mid) <= x)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_frames_assign(const FrameDesc* __restrict__ fd, const uint32_t* __restrict__ pt_base,
+                                uint32_t nframes, const float* __restrict__ pts, uint32_t n,
+                                uint32_t* __restrict__ cell_of, uint32_t* __restrict__ rank, float4* __restrict__ pos4,
+                                uint32_t* __restrict__ cell_count)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const FrameDesc& F = fd[frame_of(pt_base, nframes, i)];
+        const float x = pts[3 * (size_t) i];
+        const float y = pts[3 * (size_t) i + 1];
+        const float z = pts[3 * (size_t) i + 2];
+        const int dim[3] = {F.dim[0], F.dim[1], F.dim[2]};
+        int cx, cy, cz, img;
+        point_cell(F.b, dim, x, y, z, cx, cy, cz, img);
+        const uint32_t cell = F.cell_base + static_cast<uint32_t>(cx + dim[0] * (cy + dim[1] * cz));
+        cell_of[i] = cell;
+        rank[i] = atomicAdd(&cell_count[cell], 1u);
+        pos4[i] = make_float4(x, y, F.b.is2d ? 0.0f : z, __int_as_float(img));
+    }
+}
+
+__global__ void k_frames_scatter(uint32_t n, const uint32_t* __restrict__ cell_of, const uint32_t* __restrict__ rank,
+                                 const float4* __restrict__ pos4, const uint32_t* __restrict__ start,
+                                 float4* __restrict__ cpos, uint32_t* __restrict__ cidx)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t pos = start[cell_of[i]] + rank[i];
+        cpos[pos] = pos4[i];
+        cidx[pos] = i;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused histogram
+// ---------------------------------------------------------------------------
+
+struct BItems
+{
+    uint32_t start[BT_ITEMS];
+    uint32_t off[BT_ITEMS + 1];
+    int wrap[BT_ITEMS];
+};
+
+struct HistShared
+{
+    float4 pos[BT_TILE];        // candidate position, w = packed integer image
+    float4 iv[BT_TILE];         // image vector for queries inside the box; w = 1 if |k| <= 1
+    uint32_t j[BT_TILE];        // global point index
+    unsigned char wr[BT_TILE];  // cell wrap code (wx + 1) + 3 (wy + 1) + 9 (wz + 1)
+    float4 q[BT_QB];
+    uint32_t qi[BT_QB];
+    BItems it;
+    DevBox box;
+    int dim[3];
+    int shell;
+    uint32_t cell_base;
+    uint32_t work;
+    uint32_t hist[BT_HIST];
+};
+
+// Stencil items of local cell c (run by one warp): lane = one (dy, dz) row of
+// the (2s + 1)-wide stencil, split into up to three x-segments by wrap. Each
+// unwrapped cell offset maps to exactly one (cell, wrap) pair because every
+// periodic axis has at least s cells.
+__device__ void frame_items(const HistShared& S, const uint32_t* __restrict__ start, int c, BItems& it, int lane)
+{
+    const int d0 = S.dim[0], d1 = S.dim[1], d2 = S.dim[2];
+    const int cz = c / (d0 * d1);
+    const int cy = (c / d0) % d1;
+    const int cx = c % d0;
+    const int s = S.shell;
+    const int w = 2 * s + 1;
+    const int nrows = S.box.is2d ? w : w * w;
+    uint32_t st[3] = {0u, 0u, 0u}, cnt[3] = {0u, 0u, 0u};
+    int wc[3] = {13, 13, 13};
+    if (lane < nrows)
+    {
+        const int dy = lane % w - s;
+        const int dz = S.box.is2d ? 0 : lane / w - s;
+        const int uy = cy + dy, uz = cz + dz;
+        const int wy = uy < 0 ? -1 : (uy >= d1 ? 1 : 0);
+        const int wz = uz < 0 ? -1 : (uz >= d2 ? 1 : 0);
+        const int row = d0 * ((uy - wy * d1) + d1 * (uz - wz * d2));
+        const int x0 = cx - s, x1 = cx + s;
+        const int lo[3] = {x0 + d0, max(x0, 0), 0};
+        const int hi[3] = {x0 < 0 ? d0 - 1 : -1, min(x1, d0 - 1), x1 >= d0 ? x1 - d0 : -1};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            if (lo[k] <= hi[k])
+            {
+                const uint32_t base = S.cell_base + static_cast<uint32_t>(row);
+                st[k] = start[base + lo[k]];
+                cnt[k] = start[base + hi[k] + 1] - st[k];
+                wc[k] = k + 3 * (wy + 1) + 9 * (wz + 1);
+            }
+        }
+    }
+    const uint32_t tot = cnt[0] + cnt[1] + cnt[2];
+    uint32_t incl = tot;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o)
+            incl += v;
+    }
+    uint32_t off = incl - tot;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        it.start[3 * lane + k] = st[k];
+        it.off[3 * lane + k] = off;
+        it.wrap[3 * lane + k] = wc[k];
+        off += cnt[k];
+    }
+    if (lane == 31)
+        it.off[BT_ITEMS] = incl;
+}
+
+__device__ __forceinline__ int bitem_of(const BItems& it, uint32_t t)
+{
+    int s = 0;
+#pragma unroll
+    for (int step = 64; step >= 1; step >>= 1)
+    {
+        if (s + step < BT_ITEMS && it.off[s + step] <= t)
+            s += step;
+    }
+    return s;
+}
+
+template<int WARPS, int COPIES>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_frames_hist(BatchGrid g, BallParams p, HistParams h, uint32_t cell_limit, uint32_t* __restrict__ queue,
+                  unsigned long long* __restrict__ hist)
+{
+    constexpr int THREADS = WARPS * 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HistShared& S = *reinterpret_cast<HistShared*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    const bool smem_hist = h.bins * COPIES <= static_cast<uint32_t>(BT_HIST);
+    uint32_t* my_hist = S.hist + (warp % COPIES) * h.bins;
+
+    if (smem_hist)
+    {
+        for (uint32_t t = tid; t < h.bins * COPIES; t += THREADS)
+            S.hist[t] = 0;
+    }
+    int cur_frame = -1;
+    __syncthreads();
+
+    for (;;)
+    {
+        if (tid == 0)
+            S.work = atomicAdd(queue, static_cast<uint32_t>(BT_CHUNK));
+        __syncthreads();
+        const uint32_t c0 = S.work;
+        __syncthreads();
+        if (c0 >= cell_limit)
+            break;
+        const uint32_t c1 = min(c0 + static_cast<uint32_t>(BT_CHUNK), cell_limit);
+        for (uint32_t c = c0; c < c1; ++c)
+        {
+            const uint32_t q0 = g.start[c];
+            const uint32_t nqc = g.start[c + 1] - q0;
+            if (nqc == 0)
+                continue;
+            const int f = static_cast<int>(frame_of(g.cell_base, g.nframes, c));
+            if (f != cur_frame)
+            {
+                // block-uniform: every thread walks the same cells; all threads
+                // have passed the previous cell's final barrier
+                cur_frame = f;
+                const FrameDesc& F = g.fd[f];
+                const int* src = reinterpret_cast<const int*>(&F.b);
+                int* dst = reinterpret_cast<int*>(&S.box);
+                for (int t = tid; t < static_cast<int>(sizeof(DevBox) / sizeof(int)); t += THREADS)
+                    dst[t] = src[t];
+                if (tid == 0)
+                {
+                    S.dim[0] = F.dim[0];
+                    S.dim[1] = F.dim[1];
+                    S.dim[2] = F.dim[2];
+                    S.shell = F.shell;
+                    S.cell_base = F.cell_base;
+                }
+                __syncthreads();
+            }
+            if (warp == 0)
+                frame_items(S, g.start, static_cast<int>(c - S.cell_base), S.it, lane);
+            __syncthreads();
+            const uint32_t T = S.it.off[BT_ITEMS];
+            for (uint32_t t0 = 0; t0 < T; t0 += BT_TILE)
+            {
+                const uint32_t TT = min(static_cast<uint32_t>(BT_TILE), T - t0);
+                for (uint32_t tl = tid; tl < TT; tl += THREADS)
+                {
+                    const uint32_t t = t0 + tl;
+                    const int s = bitem_of(S.it, t);
+                    const uint32_t slot = S.it.start[s] + (t - S.it.off[s]);
+                    const float4 pp = g.cpos[slot];
+                    const int wr = S.it.wrap[s];
+                    const int pim = __float_as_int(pp.w);
+                    const int kx = img_ax(pim, 0) - (wr % 3 - 1);
+                    const int ky = img_ax(pim, 1) - ((wr / 3) % 3 - 1);
+                    const int kz = img_ax(pim, 2) - (wr / 9 - 1);
+                    float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1)
+                    {
+                        const float* v = S.box.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
+                        iv = make_float4(v[0], v[1], v[2], 1.0f);
+                    }
+                    S.pos[tl] = pp;
+                    S.iv[tl] = iv;
+                    S.j[tl] = g.cidx[slot];
+                    S.wr[tl] = static_cast<unsigned char>(wr);
+                }
+                const uint32_t nchunks = (TT + 31) / 32;
+                for (uint32_t qb0 = 0; qb0 < nqc; qb0 += BT_QB)
+                {
+                    const uint32_t nb = min(static_cast<uint32_t>(BT_QB), nqc - qb0);
+                    __syncthreads();
+                    for (uint32_t k = tid; k < nb; k += THREADS)
+                    {
+                        S.q[k] = g.cpos[q0 + qb0 + k];
+                        S.qi[k] = g.cidx[q0 + qb0 + k];
+                    }
+                    __syncthreads();
+                    for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
+                    {
+                        const uint32_t e = ch * 32 + lane;
+                        const bool live = e < TT;
+                        float4 pp = make_float4(0.f, 0.f, 0.f, 0.f);
+                        float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                        uint32_t jj = 0xffffffffu;
+                        int wr = 13;
+                        if (live)
+                        {
+                            pp = S.pos[e];
+                            iv = S.iv[e];
+                            jj = S.j[e];
+                            wr = S.wr[e];
+                        }
+                        const bool valid = iv.w != 0.0f;
+#pragma unroll 4
+                        for (uint32_t qq = 0; qq < nb; ++qq)
+                        {
+                            const float4 q = S.q[qq];
+                            const int qimg = __float_as_int(q.w);
+                            const bool ok = !(p.exclude_ii && jj == S.qi[qq]);
+                            bool acc = false;
+                            float rsq = 0.f;
+                            if (qimg == 0)
+                            {
+                                if (valid && ok)
+                                {
+                                    const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, iv.x));
+                                    const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iv.y));
+                                    const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iv.z));
+                                    rsq = dot3(rx, ry, rz);
+                                    acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
+                                }
+                            }
+                            else if (live && ok)
+                            {
+                                // query outside the box: k = n_j - n_q - wrap
+                                const int pim = __float_as_int(pp.w);
+                                const int kx = img_ax(pim, 0) - img_ax(qimg, 0) - (wr % 3 - 1);
+                                const int ky = img_ax(pim, 1) - img_ax(qimg, 1) - ((wr / 3) % 3 - 1);
+                                const int kz = img_ax(pim, 2) - img_ax(qimg, 2) - (wr / 9 - 1);
+                                if (kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1)
+                                {
+                                    const float* v = S.box.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
+                                    const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, v[0]));
+                                    const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, v[1]));
+                                    const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, v[2]));
+                                    rsq = dot3(rx, ry, rz);
+                                    acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
+                                }
+                            }
+                            if (acc)
+                            {
+                                const float d = __fsqrt_rn(rsq);
+                                if (!(d < h.h_min || d >= h.h_max))
+                                {
+                                    uint32_t bin = static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
+                                    if (bin == h.bins)
+                                        bin = h.bins - 1;
+                                    if (smem_hist)
+                                        atomicAdd(&my_hist[bin], 1u);
+                                    else
+                                        atomicAdd(&hist[bin], 1ull);
+                                }
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+    }
+    if (smem_hist)
+    {
+        __syncthreads();
+        for (uint32_t bin = tid; bin < h.bins; bin += THREADS)
+        {
+            uint32_t v = 0;
+#pragma unroll
+            for (int k = 0; k < COPIES; ++k)
+                v += S.hist[k * h.bins + bin];
+            if (v != 0)
+                atomicAdd(&hist[bin], static_cast<unsigned long long>(v));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Steinhardt neighbours (thread per query, 27-cell stencil of r_max cells)
+// ---------------------------------------------------------------------------
+
+template<bool FILL>
+__global__ void __launch_bounds__(128)
+    k_frames_ball(BatchGrid g, BallParams p, uint32_t n, uint32_t* __restrict__ counts,
+                  const uint64_t* __restrict__ offsets, uint2* __restrict__ ij, float* __restrict__ dist,
+                  float* __restrict__ vec)
+{
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    {
+        const float4 q = g.cpos[t];
+        const uint32_t i = g.cidx[t];
+        const uint32_t c = g.cell_of[i];
+        const FrameDesc& F = g.fd[frame_of(g.cell_base, g.nframes, c)];
+        const int d0 = F.dim[0], d1 = F.dim[1], d2 = F.dim[2];
+        const int lc = static_cast<int>(c - F.cell_base);
+        const int cz = lc / (d0 * d1);
+        const int cy = (lc / d0) % d1;
+        const int cx = lc % d0;
+        const int qimg = __float_as_int(q.w);
+        const int nst = F.b.is2d ? 9 : 27;
+        uint32_t cnt = 0;
+        const uint64_t o = FILL ? offsets[i] : 0;
+        for (int s = 0; s < nst; ++s)
+        {
+            const int ux = cx + s % 3 - 1;
+            const int uy = cy + (s / 3) % 3 - 1;
+            const int uz = cz + (F.b.is2d ? 0 : s / 9 - 1);
+            const int wx = ux < 0 ? -1 : (ux >= d0 ? 1 : 0);
+            const int wy = uy < 0 ? -1 : (uy >= d1 ? 1 : 0);
+            const int wz = uz < 0 ? -1 : (uz >= d2 ? 1 : 0);
+            const uint32_t cell =
+                F.cell_base + static_cast<uint32_t>((ux - wx * d0) + d0 * ((uy - wy * d1) + d1 * (uz - wz * d2)));
+            const uint32_t a = g.start[cell], b = g.start[cell + 1];
+            for (uint32_t u = a; u < b; ++u)
+            {
+                const uint32_t j = g.cidx[u];
+                if (p.exclude_ii && j == i)
+                    continue;
+                const float4 pp = g.cpos[u];
+                const int pim = __float_as_int(pp.w);
+                const int kx = img_ax(pim, 0) - img_ax(qimg, 0) - wx;
+                const int ky = img_ax(pim, 1) - img_ax(qimg, 1) - wy;
+                const int kz = img_ax(pim, 2) - img_ax(qimg, 2) - wz;
+                if (kx < -1 || kx > 1 || ky < -1 || ky > 1 || kz < -1 || kz > 1)
+                    continue;
+                const float* v = F.b.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
+                const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, v[0]));
+                const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, v[1]));
+                const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, v[2]));
+                const float rsq = dot3(rx, ry, rz);
+                if (rsq < p.r_max_sq && rsq >= p.r_min_sq)
+                {
+                    if (FILL)
+                    {
+                        const uint64_t e = o + cnt;
+                        ij[e] = make_uint2(i, j);
+                        dist[e] = __fsqrt_rn(rsq);
+                        float dx, dy, dz;
+                        box_wrap(F.b, __fsub_rn(pp.x, q.x), __fsub_rn(pp.y, q.y), __fsub_rn(pp.z, q.z), dx, dy, dz);
+                        vec[3 * e] = dx;
+                        vec[3 * e + 1] = dy;
+                        vec[3 * e + 2] = dz;
+                    }
+                    ++cnt;
+                }
+            }
+        }
+        if (!FILL)
+            counts[i] = cnt;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-frame system sums
+// ---------------------------------------------------------------------------
+
+__global__ void k_frames_sys(const uint32_t* __restrict__ pt_base, StLs ls, int stride, const float2* __restrict__ src,
+                             double* __restrict__ partial)
+{
+    const uint32_t f = blockIdx.x;
+    const uint32_t split = blockIdx.y;
+    const uint32_t r_lo = pt_base[f];
+    const uint32_t nf = pt_base[f + 1] - r_lo;
+    const uint32_t per = (nf + FRAME_SYS_SPLIT - 1) / FRAME_SYS_SPLIT;
+    const uint32_t r0 = r_lo + min(nf, split * per);
+    const uint32_t r1 = r_lo + min(nf, (split + 1) * per);
+    for (int col = threadIdx.x; col < stride; col += blockDim.x)
+    {
+        // column -> (l index, m slot)
+        int k = 0, m = col;
+        while (k < ls.nl - 1 && m >= 2 * ls.l[k] + 1)
+        {
+            m -= 2 * ls.l[k] + 1;
+            ++k;
+        }
+        const int nm = 2 * ls.l[k] + 1;
+        const float2* base = src + ls.qlm_offset[k] + m;
+        double sr = 0.0, si = 0.0, cr = 0.0, ci = 0.0;
+        for (uint32_t r = r0; r < r1; ++r)
+        {
+            const float2 v = base[static_cast<size_t>(r) * nm];
+            const double yr = static_cast<double>(v.x) / nf - cr;
+            const double tr = sr + yr;
+            cr = (tr - sr) - yr;
+            sr = tr;
+            const double yi = static_cast<double>(v.y) / nf - ci;
+            const double ti = si + yi;
+            ci = (ti - si) - yi;
+            si = ti;
+        }
+        double* out = partial + ((static_cast<size_t>(f) * FRAME_SYS_SPLIT + split) * stride + col) * 2;
+        out[0] = sr;
+        out[1] = si;
+    }
+}
+
+__global__ void k_frames_sys_final(uint32_t nframes, int stride, const double* __restrict__ partial,
+                                   double* __restrict__ sys)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nframes * static_cast<uint32_t>(stride))
+        return;
+    const uint32_t f = t / stride;
+    const uint32_t col = t % stride;
+    double sr = 0.0, si = 0.0, cr = 0.0, ci = 0.0;
+    for (int k = 0; k < FRAME_SYS_SPLIT; ++k)
+    {
+        const double* v = partial + ((static_cast<size_t>(f) * FRAME_SYS_SPLIT + k) * stride + col) * 2;
+        const double yr = v[0] - cr;
+        const double tr = sr + yr;
+        cr = (tr - sr) - yr;
+        sr = tr;
+        const double yi = v[1] - ci;
+        const double ti = si + yi;
+        ci = (ti - si) - yi;
+        si = ti;
+    }
+    sys[2 * static_cast<size_t>(t)] = sr;
+    sys[2 * static_cast<size_t>(t) + 1] = si;
+}
+
+int grid_blocks(size_t n, int threads)
+{
+    size_t b = (n + threads - 1) / threads;
+    if (b > 152 * 32)
+        b = 152 * 32;
+    return b < 1 ? 1 : static_cast<int>(b);
+}
+
+int sms()
+{
+    static int v = 0;
+    if (v == 0)
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        if (v <= 0)
+            v = 1;
+    }
+    return v;
+}
+
+template<int WARPS, int COPIES>
+void hist_launch(const BatchGrid& g, const BallParams& p, const HistParams& h, uint32_t cell_limit, uint32_t* queue,
+                 unsigned long long* hist, cudaStream_t s)
+{
+    const size_t smem = sizeof(HistShared);
+    static bool attr = false;
+    static int per_sm = 1;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_frames_hist<WARPS, COPIES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_frames_hist<WARPS, COPIES>, WARPS * 32, smem);
+        if (per_sm < 1)
+            per_sm = 1;
+        attr = true;
+    }
+    const uint32_t blocks = std::min<uint32_t>(static_cast<uint32_t>(sms() * per_sm),
+                                               std::max<uint32_t>(1u, (cell_limit + BT_CHUNK - 1) / BT_CHUNK));
+    ProfScope prof_("k_frames_hist", s);
+    k_frames_hist<WARPS, COPIES><<<blocks, WARPS * 32, smem, s>>>(g, p, h, cell_limit, queue, hist);
+}
+
+} // namespace
+
+void launch_frames_assign(const FrameDesc* fd, const uint32_t* pt_base, uint32_t nframes, const float* pts, uint32_t n,
+                          uint32_t* cell_of, uint32_t* rank, float4* pos4, uint32_t* cell_count, cudaStream_t s)
+{
+    if (n == 0)
+        return;
+    ProfScope prof_("k_frames_assign", s);
+    k_frames_assign<<<grid_blocks(n, 256), 256, 0, s>>>(fd, pt_base, nframes, pts, n, cell_of, rank, pos4, cell_count);
+}
+
+void launch_frames_scatter(uint32_t n, const uint32_t* cell_of, const uint32_t* rank, const float4* pos4,
+                           const uint32_t* start, float4* cpos, uint32_t* cidx, cudaStream_t s)
+{
+    if (n == 0)
+        return;
+    ProfScope prof_("k_frames_scatter", s);
+    k_frames_scatter<<<grid_blocks(n, 256), 256, 0, s>>>(n, cell_of, rank, pos4, start, cpos, cidx);
+}
+
+size_t frames_hist_smem_bytes()
+{
+    return sizeof(HistShared);
+}
+
+void launch_frames_hist(const BatchHistConfig& cfg, const BatchGrid& g, const BallParams& p, const HistParams& h,
+                        uint32_t cell_limit, uint32_t* queue, unsigned long long* hist, cudaStream_t s)
+{
+    if (cell_limit == 0)
+        return;
+    if (cfg.warps == 4)
+    {
+        if (cfg.copies == 2)
+            hist_launch<4, 2>(g, p, h, cell_limit, queue, hist, s);
+        else
+            hist_launch<4, 1>(g, p, h, cell_limit, queue, hist, s);
+    }
+    else
+    {
+        if (cfg.copies == 2)
+            hist_launch<8, 2>(g, p, h, cell_limit, queue, hist, s);
+        else
+            hist_launch<8, 1>(g, p, h, cell_limit, queue, hist, s);
+    }
+}
+
+void launch_frames_ball_count(const BatchGrid& g, const BallParams& p, uint32_t n, uint32_t* counts, cudaStream_t s)
+{
+    if (n == 0)
+        return;
+    ProfScope prof_("k_frames_ball<COUNT>", s);
+    k_frames_ball<false><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, counts, nullptr, nullptr, nullptr, nullptr);
+}
+
+void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n, const uint64_t* offsets, uint2* ij,
+                             float* dist, float* vec, cudaStream_t s)
+{
+    if (n == 0)
+        return;
+    ProfScope prof_("k_frames_ball<FILL>", s);
+    k_frames_ball<true><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, nullptr, offsets, ij, dist, vec);
+}
+
+void launch_frames_sys(const uint32_t* pt_base, uint32_t nframes, const StLs& ls, int stride, const float2* src,
+                       double* partial, double* sys, cudaStream_t s)
+{
+    if (nframes == 0)
+        return;
+    {
+        ProfScope prof_("k_frames_sys", s);
+        k_frames_sys<<<dim3(nframes, FRAME_SYS_SPLIT), 64, 0, s>>>(pt_base, ls, stride, src, partial);
+    }
+    {
+        const uint32_t t = nframes * static_cast<uint32_t>(stride);
+        ProfScope prof_("k_frames_sys_final", s);
+        k_frames_sys_final<<<(t + 127) / 128, 128, 0, s>>>(nframes, stride, partial, sys);
+    }
+}
+
+} // namespace fg

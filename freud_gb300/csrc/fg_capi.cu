@@ -7,6 +7,7 @@
 // RDF.cc:25-42; NeighborList.cc:51-82, 286-307). All device work is issued on one
 // stream; every entry point synchronises before returning.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -19,8 +20,10 @@
 #include <vector>
 
 #include "../../include/freud_gb300.h"
+#include "fg_batch.cuh"
 #include "fg_kernels.cuh"
 #include "fg_nlist.cuh"
+#include "fg_prof.cuh"
 #include "fg_steinhardt.cuh"
 
 namespace fg {
@@ -339,7 +342,8 @@ struct fg_steinhardt
     size_t stride = 0; // sum of (2l + 1)
     DevBuf qlm, qlm_ave, ql, ql_ave, wlv, sys;
     std::vector<DevBuf> w3j;
-    std::vector<float> order;
+    std::vector<float> order; // frames x n_l
+    uint32_t frames = 1;
     bool computed = false;
 };
 
@@ -1719,6 +1723,37 @@ fg_status fg_steinhardt_destroy(fg_steinhardt* st)
     });
 }
 
+// Steinhardt::normalizeSystem (Steinhardt.cc:291-327), in double, from the FP64
+// system qlm sums of one frame (complex, every l's m in column order).
+static void normalize_system(const fg_steinhardt* st, const double* sys, float* order)
+{
+    size_t col = 0;
+    for (int k = 0; k < st->st.nl; ++k)
+    {
+        const int l = st->st.l[k];
+        const double nf = 4.0 * M_PI / (2 * l + 1);
+        double acc = 0.0;
+        for (int m = 0; m < 2 * l + 1; ++m)
+            acc += sys[2 * (col + m)] * sys[2 * (col + m)] + sys[2 * (col + m) + 1] * sys[2 * (col + m) + 1];
+        const double qsys = std::sqrt(acc * nf);
+        if (st->wl)
+        {
+            double v = reduce_w3j_host(&sys[2 * col], l, wigner3j_table(l));
+            if (st->wl_normalize)
+            {
+                const double w = std::sqrt(nf) / qsys;
+                v *= w * w * w;
+            }
+            order[k] = static_cast<float>(v);
+        }
+        else
+        {
+            order[k] = static_cast<float>(qsys);
+        }
+        col += 2 * l + 1;
+    }
+}
+
 fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nlist, const fg_query_args* args)
 {
     return guard([&] {
@@ -1736,6 +1771,7 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
         ensure_segments(nl);
         const uint32_t n = nq->n;
         st->n = n;
+        st->frames = 1;
         // per-l offsets in one buffer
         size_t off = 0;
         for (int k = 0; k < st->st.nl; ++k)
@@ -1773,33 +1809,8 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
         std::vector<double> sys(2 * st->stride);
         FG_CUDA(cudaMemcpyAsync(sys.data(), st->sys.p, sizeof(double) * 2 * st->stride, cudaMemcpyDeviceToHost, s));
         sync();
-        // Steinhardt::normalizeSystem (Steinhardt.cc:291-327), in double
         st->order.assign(st->st.nl, 0.0f);
-        size_t col = 0;
-        for (int k = 0; k < st->st.nl; ++k)
-        {
-            const int l = st->st.l[k];
-            const double nf = 4.0 * M_PI / (2 * l + 1);
-            double acc = 0.0;
-            for (int m = 0; m < 2 * l + 1; ++m)
-                acc += sys[2 * (col + m)] * sys[2 * (col + m)] + sys[2 * (col + m) + 1] * sys[2 * (col + m) + 1];
-            const double qsys = std::sqrt(acc * nf);
-            if (st->wl)
-            {
-                double v = reduce_w3j_host(&sys[2 * col], l, wigner3j_table(l));
-                if (st->wl_normalize)
-                {
-                    const double w = std::sqrt(nf) / qsys;
-                    v *= w * w * w;
-                }
-                st->order[k] = static_cast<float>(v);
-            }
-            else
-            {
-                st->order[k] = static_cast<float>(qsys);
-            }
-            col += 2 * l + 1;
-        }
+        normalize_system(st, sys.data(), st->order.data());
         st->computed = true;
     });
 }
@@ -1989,6 +2000,645 @@ fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points
         launch_cell_scan(1, db, g, g, p, pf.out2, 0.0f, nullptr, nullptr, nullptr, over, over + 1, h, device_counts, s);
         FG_CUDA(cudaGetLastError());
     });
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched frames
+//
+// A batch is F frames of uneven N ((box, points) systems, AABB arithmetic as for
+// RawPoints) held on the device once. RDF and Steinhardt over the batch run
+// every frame in one launch per stage (fg_batch.cu) instead of one pipeline
+// per frame, with the device-side sequence of each call recorded once as a
+// CUDA graph and replayed while the batch layout and buffers stay the same.
+// The histogram kernel's launch shape (stencil shell, warps per block, shared
+// histogram copies) is chosen by timing the candidates on the first batch of
+// each kind (density, r_max, bins) the process sees.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+bool g_graphs_enabled = true;
+std::mutex g_tune_mu;
+std::map<std::string, BatchHistConfig> g_tuned;
+std::string g_tune_log;
+BatchHistConfig g_forced {0, 0, 0};
+
+struct GraphCache
+{
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> key;
+    uint64_t launches = 0;
+    GraphCache() = default;
+    GraphCache(const GraphCache&) = delete;
+    GraphCache& operator=(const GraphCache&) = delete;
+    ~GraphCache()
+    {
+        if (exec != nullptr)
+            cudaGraphExecDestroy(exec);
+    }
+};
+
+uint64_t fbits(float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, sizeof(u));
+    return u;
+}
+
+// Runs body on the library stream, through a CUDA graph recorded on the first
+// call with this key (body must only enqueue stream work on preallocated
+// buffers). The legacy / per-thread default streams cannot be captured: there
+// body runs directly.
+template<typename F> void run_graph(GraphCache& gc, const std::vector<uint64_t>& key, const char* name, F&& body)
+{
+    cudaStream_t s = stream();
+    const bool capturable = g_graphs_enabled && s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
+    if (!capturable)
+    {
+        body();
+        return;
+    }
+    if (gc.exec == nullptr || gc.key != key)
+    {
+        if (gc.exec != nullptr)
+        {
+            cudaGraphExecDestroy(gc.exec);
+            gc.exec = nullptr;
+        }
+        FG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+        prof_begin_capture();
+        try
+        {
+            body();
+        }
+        catch (...)
+        {
+            prof_end_capture();
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(s, &g);
+            if (g != nullptr)
+                cudaGraphDestroy(g);
+            throw;
+        }
+        const uint64_t n = prof_end_capture();
+        cudaGraph_t graph = nullptr;
+        FG_CUDA(cudaStreamEndCapture(s, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&gc.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        FG_CUDA(e);
+        gc.key = key;
+        gc.launches = n;
+    }
+    prof_add_launches(gc.launches);
+    ProfScope prof_(name, s, false);
+    FG_CUDA(cudaGraphLaunch(gc.exec, s));
+}
+
+// Cell grid of a batch for one cell width rule (r_max / shell), with its buffers.
+struct BatchGridBufs
+{
+    uint64_t id = 0; // unique per grid built in this process (graph keys)
+    float r_max = 0.0f;
+    int shell = 0;
+    uint32_t ncell = 0;
+    std::vector<FrameDesc> fd_host;
+    std::vector<uint32_t> cell_base_host;
+    DevBuf fd, cell_base, counts, start, cell_of, rank, pos4, cpos0, cidx0, cpos, cidx, scan;
+};
+
+} // namespace
+
+struct fg_frames
+{
+    std::vector<HostBox> boxes;
+    std::vector<uint32_t> n;       // points per frame
+    std::vector<uint32_t> pt_base; // nframes + 1
+    uint32_t total = 0;
+    DevBuf own;
+    const float* dpts = nullptr;
+    DevBuf d_pt_base;
+    std::vector<std::unique_ptr<BatchGridBufs>> grids;
+    // RDF workspace
+    DevBuf queue;
+    GraphCache rdf_graph;
+    // Steinhardt workspace
+    DevBuf st_counts, st_offsets, st_scan, st_ij, st_dist, st_vec, st_seg, st_partial, st_sys;
+    GraphCache st_graph_a, st_graph_b;
+};
+
+namespace {
+
+// Grid of the batch for (r_max, shell): per-frame dims from the nearest-plane
+// distances (at least `shell` cells on every periodic axis, else that frame
+// falls back to shell 1 with r_max cells).
+BatchGridBufs& batch_grid(fg_frames* fr, float r_max, int shell)
+{
+    for (auto& g : fr->grids)
+    {
+        if (g->r_max == r_max && g->shell == shell)
+            return *g;
+    }
+    if (fr->grids.size() >= 4)
+        fr->grids.erase(fr->grids.begin());
+    static std::atomic<uint64_t> next_id {1};
+    auto g = std::make_unique<BatchGridBufs>();
+    g->id = next_id.fetch_add(1);
+    g->r_max = r_max;
+    g->shell = shell;
+    const uint32_t F = static_cast<uint32_t>(fr->n.size());
+    g->fd_host.resize(F);
+    g->cell_base_host.resize(F + 1);
+    uint64_t cells = 0;
+    for (uint32_t f = 0; f < F; ++f)
+    {
+        const HostBox& hb = fr->boxes[f];
+        int sh = shell;
+        int dim[3];
+        grid_dims(hb, fdiv(r_max, static_cast<float>(sh)) * (1.0f + 1e-5f), fr->n[f], dim);
+        if (sh > 1 && (dim[0] < sh || dim[1] < sh || (!hb.is2d && dim[2] < sh)))
+        {
+            sh = 1;
+            grid_dims(hb, r_max * (1.0f + 1e-5f), fr->n[f], dim);
+        }
+        FrameDesc& d = g->fd_host[f];
+        d.b = make_devbox(hb);
+        d.dim[0] = dim[0];
+        d.dim[1] = dim[1];
+        d.dim[2] = dim[2];
+        d.shell = sh;
+        d.cell_base = static_cast<uint32_t>(cells);
+        d.ncell = static_cast<uint32_t>(dim[0] * dim[1] * dim[2]);
+        d.pt_base = fr->pt_base[f];
+        d.n = fr->n[f];
+        g->cell_base_host[f] = static_cast<uint32_t>(cells);
+        cells += d.ncell;
+        if (cells >= (1ull << 31))
+            runtime_error("the batch's cell grid exceeds 2^31 cells");
+    }
+    g->cell_base_host[F] = static_cast<uint32_t>(cells);
+    g->ncell = static_cast<uint32_t>(cells);
+    cudaStream_t s = stream();
+    const uint32_t n = fr->total;
+    g->fd.alloc(sizeof(FrameDesc) * F);
+    g->cell_base.alloc(sizeof(uint32_t) * (F + 1));
+    g->counts.alloc(sizeof(uint32_t) * (g->ncell + 1));
+    g->start.alloc(sizeof(uint32_t) * (g->ncell + 1));
+    g->cell_of.alloc(sizeof(uint32_t) * n);
+    g->rank.alloc(sizeof(uint32_t) * n);
+    g->pos4.alloc(sizeof(float4) * n);
+    g->cpos0.alloc(sizeof(float4) * n);
+    g->cidx0.alloc(sizeof(uint32_t) * n);
+    g->cpos.alloc(sizeof(float4) * n);
+    g->cidx.alloc(sizeof(uint32_t) * n);
+    g->scan.alloc(scan_scratch_bytes(static_cast<size_t>(g->ncell) + 1));
+    FG_CUDA(cudaMemcpyAsync(g->fd.p, g->fd_host.data(), sizeof(FrameDesc) * F, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(g->cell_base.p, g->cell_base_host.data(), sizeof(uint32_t) * (F + 1),
+                            cudaMemcpyHostToDevice, s));
+    sync(); // the host tables are pageable
+    fr->grids.push_back(std::move(g));
+    return *fr->grids.back();
+}
+
+// Enqueues the grid build (capturable: stream work on preallocated buffers only).
+void enqueue_grid_build(fg_frames* fr, BatchGridBufs& g, cudaStream_t s)
+{
+    const uint32_t F = static_cast<uint32_t>(fr->n.size());
+    FG_CUDA(cudaMemsetAsync(g.counts.p, 0, sizeof(uint32_t) * (g.ncell + 1), s));
+    launch_frames_assign(g.fd.as<FrameDesc>(), fr->d_pt_base.as<uint32_t>(), F, fr->dpts, fr->total,
+                         g.cell_of.as<uint32_t>(), g.rank.as<uint32_t>(), g.pos4.as<float4>(), g.counts.as<uint32_t>(),
+                         s);
+    scan_u32_to_u32(g.counts.as<uint32_t>(), g.start.as<uint32_t>(), static_cast<size_t>(g.ncell) + 1, g.scan.p, s);
+    launch_frames_scatter(fr->total, g.cell_of.as<uint32_t>(), g.rank.as<uint32_t>(), g.pos4.as<float4>(),
+                          g.start.as<uint32_t>(), g.cpos0.as<float4>(), g.cidx0.as<uint32_t>(), s);
+    launch_sort_cells(g.start.as<uint32_t>(), static_cast<int>(g.ncell), g.cpos0.as<float4>(), g.cidx0.as<uint32_t>(),
+                      g.cpos.as<float4>(), g.cidx.as<uint32_t>(), s);
+}
+
+BatchGrid batch_view(const fg_frames* fr, const BatchGridBufs& g)
+{
+    BatchGrid v;
+    v.fd = g.fd.as<FrameDesc>();
+    v.cell_base = g.cell_base.as<uint32_t>();
+    v.nframes = static_cast<uint32_t>(fr->n.size());
+    v.ncell = g.ncell;
+    v.start = g.start.as<uint32_t>();
+    v.cpos = g.cpos.as<float4>();
+    v.cidx = g.cidx.as<uint32_t>();
+    v.cell_of = g.cell_of.as<uint32_t>();
+    return v;
+}
+
+// Ball-query arguments of a batch call: checks shared with the per-frame path.
+fg_query_args batch_args(const fg_frames* fr, const fg_query_args* args)
+{
+    fg_query_args a = *args;
+    validate_args(a);
+    if (a.mode != FG_MODE_BALL)
+        value_error("batched frames support ball queries (r_max) only");
+    for (const HostBox& hb : fr->boxes)
+    {
+        check_periodic(hb);
+        float pd[3];
+        nearest_plane(hb, pd);
+        // updateImageVectors(r_max, true), NeighborQuery.h:504-509
+        if (pd[0] <= a.r_max * 2.0 || pd[1] <= a.r_max * 2.0 || (!hb.is2d && pd[2] <= a.r_max * 2.0))
+            runtime_error("The AABBQuery r_max is too large for this box.");
+    }
+    return a;
+}
+
+std::string tune_key(const fg_frames* fr, float r_max, uint32_t bins)
+{
+    double vol = 0.0;
+    bool any2d = false;
+    for (size_t f = 0; f < fr->boxes.size(); ++f)
+    {
+        const HostBox& b = fr->boxes[f];
+        vol += b.is2d ? static_cast<double>(b.L[0]) * b.L[1] : static_cast<double>(b.L[0]) * b.L[1] * b.L[2];
+        any2d = any2d || b.is2d;
+    }
+    const double per_cell = vol > 0.0 ? fr->total / vol * std::pow(static_cast<double>(r_max), any2d ? 2.0 : 3.0)
+                                      : 0.0;
+    const int dens = per_cell > 0.0 ? static_cast<int>(std::lround(2.0 * std::log2(per_cell))) : -99;
+    return std::string(any2d ? "2d" : "3d") + " pts_per_rmax_cell~2^" + std::to_string(dens / 2.0) +
+           " bins_le_" + std::to_string(bins <= 1024 ? 1024 : (bins <= 2048 ? 2048 : 1 << 30));
+}
+
+// Chooses the histogram kernel's launch shape for this batch (cached per key):
+// each candidate runs on the cells of the first frames (up to ~2^20 points) into
+// a scratch histogram, best of three, timed with events on the stream.
+BatchHistConfig tuned_config(fg_frames* fr, const BallParams& p, const HistParams& h, float r_max)
+{
+    if (g_forced.shell != 0)
+        return g_forced;
+    const std::string key = tune_key(fr, r_max, h.bins);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end())
+            return it->second;
+    }
+    cudaStream_t s = stream();
+    // sample: the first frames, at least one, up to about 2^20 points
+    const uint32_t F = static_cast<uint32_t>(fr->n.size());
+    uint32_t nf = 1;
+    while (nf < F && fr->pt_base[nf] < (1u << 20))
+        ++nf;
+    DevBuf scratch_hist;
+    scratch_hist.alloc(sizeof(unsigned long long) * h.bins);
+    if (fr->queue.bytes < sizeof(uint32_t))
+        fr->queue.alloc(sizeof(uint32_t));
+    cudaEvent_t e0, e1;
+    FG_CUDA(cudaEventCreate(&e0));
+    FG_CUDA(cudaEventCreate(&e1));
+    BatchHistConfig best {1, 8, 1};
+    float best_ms = std::numeric_limits<float>::infinity();
+    std::string log = "rdf_frames [" + key + "]:";
+    for (int shell = 1; shell <= 2; ++shell)
+    {
+        BatchGridBufs& g = batch_grid(fr, r_max, shell);
+        enqueue_grid_build(fr, g, s);
+        const uint32_t limit = g.cell_base_host[nf];
+        const BatchGrid v = batch_view(fr, g);
+        for (int warps : {4, 8})
+        {
+            for (int copies : {1, 2})
+            {
+                const BatchHistConfig cfg {shell, warps, copies};
+                float ms = std::numeric_limits<float>::infinity();
+                for (int rep = 0; rep < 3; ++rep)
+                {
+                    FG_CUDA(cudaMemsetAsync(fr->queue.p, 0, sizeof(uint32_t), s));
+                    FG_CUDA(cudaMemsetAsync(scratch_hist.p, 0, sizeof(unsigned long long) * h.bins, s));
+                    FG_CUDA(cudaEventRecord(e0, s));
+                    launch_frames_hist(cfg, v, p, h, limit, fr->queue.as<uint32_t>(), scratch_hist.as<unsigned long long>(),
+                                       s);
+                    FG_CUDA(cudaEventRecord(e1, s));
+                    FG_CUDA(cudaEventSynchronize(e1));
+                    float t = 0.0f;
+                    FG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+                    ms = std::min(ms, t);
+                }
+                char buf[96];
+                std::snprintf(buf, sizeof(buf), " s%d/w%d/c%d=%.3fms", shell, warps, copies, ms);
+                log += buf;
+                if (ms < best_ms)
+                {
+                    best_ms = ms;
+                    best = cfg;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    FG_CUDA(cudaGetLastError());
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), " -> s%d/w%d/c%d\n", best.shell, best.warps, best.copies);
+    log += buf;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[key] = best;
+    g_tune_log += log;
+    return best;
+}
+
+void check_frames_points(const fg_box* boxes, const uint64_t* offsets, uint32_t n_frames)
+{
+    require(boxes, "boxes");
+    require(offsets, "frame_offsets");
+    if (n_frames == 0)
+        value_error("a frame batch needs at least one frame");
+    if (offsets[0] != 0)
+        value_error("frame_offsets[0] must be 0");
+    for (uint32_t f = 0; f < n_frames; ++f)
+    {
+        if (offsets[f + 1] <= offsets[f])
+            value_error("Cannot create a NeighborQuery with 0 particles.");
+    }
+    if (offsets[n_frames] >= (1ull << 32))
+        value_error("a frame batch holds fewer than 2^32 points");
+}
+
+fg_frames* new_frames(const fg_box* boxes, const uint64_t* offsets, uint32_t n_frames)
+{
+    check_frames_points(boxes, offsets, n_frames);
+    auto fr = std::make_unique<fg_frames>();
+    fr->boxes.resize(n_frames);
+    fr->n.resize(n_frames);
+    fr->pt_base.resize(n_frames + 1);
+    for (uint32_t f = 0; f < n_frames; ++f)
+    {
+        fr->boxes[f] = to_host_box(&boxes[f]);
+        fr->n[f] = static_cast<uint32_t>(offsets[f + 1] - offsets[f]);
+        fr->pt_base[f] = static_cast<uint32_t>(offsets[f]);
+    }
+    fr->pt_base[n_frames] = static_cast<uint32_t>(offsets[n_frames]);
+    fr->total = fr->pt_base[n_frames];
+    fr->d_pt_base.alloc(sizeof(uint32_t) * (n_frames + 1));
+    FG_CUDA(cudaMemcpyAsync(fr->d_pt_base.p, fr->pt_base.data(), sizeof(uint32_t) * (n_frames + 1),
+                            cudaMemcpyHostToDevice, stream()));
+    return fr.release();
+}
+
+} // namespace
+
+extern "C" {
+
+fg_status fg_frames_create(const fg_box* boxes, const float* points, const uint64_t* frame_offsets, uint32_t n_frames,
+                           fg_frames** out)
+{
+    return guard([&] {
+        require(out, "out");
+        require(points, "points");
+        std::unique_ptr<fg_frames> fr(new_frames(boxes, frame_offsets, n_frames));
+        upload_points(points, fr->total, fr->own);
+        fr->dpts = fr->own.as<float>();
+        sync();
+        *out = fr.release();
+    });
+}
+
+fg_status fg_frames_create_device(const fg_box* boxes, const float* device_points, const uint64_t* frame_offsets,
+                                  uint32_t n_frames, fg_frames** out)
+{
+    return guard([&] {
+        require(out, "out");
+        require(device_points, "device_points");
+        std::unique_ptr<fg_frames> fr(new_frames(boxes, frame_offsets, n_frames));
+        fr->dpts = device_points;
+        sync();
+        *out = fr.release();
+    });
+}
+
+fg_status fg_frames_set_points(fg_frames* fr, const float* points)
+{
+    return guard([&] {
+        require(fr, "frames");
+        require(points, "points");
+        if (fr->own.p == nullptr)
+            value_error("fg_frames_set_points needs a batch created from host points");
+        FG_CUDA(cudaMemcpyAsync(fr->own.p, points, sizeof(float) * 3 * static_cast<size_t>(fr->total),
+                                cudaMemcpyHostToDevice, stream()));
+        sync();
+    });
+}
+
+fg_status fg_frames_destroy(fg_frames* fr)
+{
+    return guard([&] {
+        delete fr;
+        sync();
+    });
+}
+
+fg_status fg_frames_info(const fg_frames* fr, uint32_t* n_frames, uint64_t* n_points)
+{
+    return guard([&] {
+        require(fr, "frames");
+        if (n_frames)
+            *n_frames = static_cast<uint32_t>(fr->n.size());
+        if (n_points)
+            *n_points = fr->total;
+    });
+}
+
+fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_args* args)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        require(fr, "frames");
+        require(args, "args");
+        const fg_query_args a = batch_args(fr, args);
+        cudaStream_t s = stream();
+        const HistParams h = hist_params(rdf);
+        BallParams p;
+        p.r_max_sq = fmul(a.r_max, a.r_max);
+        p.r_min_sq = fmul(a.r_min, a.r_min);
+        p.exclude_ii = a.exclude_ii;
+        p.arith = ARITH_AABB;
+        p.nq = fr->total;
+        if (fr->queue.bytes < sizeof(uint32_t))
+            fr->queue.alloc(sizeof(uint32_t));
+        const BatchHistConfig cfg = tuned_config(fr, p, h, a.r_max);
+        BatchGridBufs& g = batch_grid(fr, a.r_max, cfg.shell);
+        const BatchGrid v = batch_view(fr, g);
+        const std::vector<uint64_t> key = {reinterpret_cast<uint64_t>(rdf->hist.p), g.id,
+                                           reinterpret_cast<uint64_t>(fr->dpts), static_cast<uint64_t>(cfg.shell),
+                                           static_cast<uint64_t>(cfg.warps), static_cast<uint64_t>(cfg.copies),
+                                           fbits(a.r_max), fbits(a.r_min), static_cast<uint64_t>(a.exclude_ii),
+                                           static_cast<uint64_t>(h.bins), fbits(h.h_min), fbits(h.h_max)};
+        run_graph(fr->rdf_graph, key, "graph:rdf_frames", [&] {
+            enqueue_grid_build(fr, g, s);
+            FG_CUDA(cudaMemsetAsync(fr->queue.p, 0, sizeof(uint32_t), s));
+            launch_frames_hist(cfg, v, p, h, g.ncell, fr->queue.as<uint32_t>(), rdf->hist.as<unsigned long long>(), s);
+        });
+        FG_CUDA(cudaGetLastError());
+        sync();
+        // F accumulate calls: the frame count grows by F, box and N are the last frame's
+        rdf->frames += static_cast<uint32_t>(fr->n.size());
+        rdf->box = fr->boxes.back();
+        rdf->n_points = fr->n.back();
+        rdf->n_query = fr->n.back();
+    });
+}
+
+fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_args* args)
+{
+    return guard([&] {
+        require(st, "steinhardt");
+        require(fr, "frames");
+        require(args, "args");
+        const fg_query_args a = batch_args(fr, args);
+        cudaStream_t s = stream();
+        const uint32_t P = fr->total;
+        const uint32_t F = static_cast<uint32_t>(fr->n.size());
+        BallParams p;
+        p.r_max_sq = fmul(a.r_max, a.r_max);
+        p.r_min_sq = fmul(a.r_min, a.r_min);
+        p.exclude_ii = a.exclude_ii;
+        p.arith = ARITH_AABB;
+        p.nq = P;
+        BatchGridBufs& g = batch_grid(fr, a.r_max, 1);
+        const BatchGrid v = batch_view(fr, g);
+        fr->st_counts.alloc(sizeof(uint32_t) * (P + 1));
+        fr->st_offsets.alloc(sizeof(uint64_t) * (P + 1));
+        fr->st_scan.alloc(scan_scratch_bytes(static_cast<size_t>(P) + 1));
+        // phase 1: grid, bond counts, offsets
+        const std::vector<uint64_t> key_a = {g.id, reinterpret_cast<uint64_t>(fr->dpts),
+                                             reinterpret_cast<uint64_t>(fr->st_counts.p),
+                                             reinterpret_cast<uint64_t>(fr->st_offsets.p),
+                                             reinterpret_cast<uint64_t>(fr->st_scan.p), fbits(a.r_max), fbits(a.r_min),
+                                             static_cast<uint64_t>(a.exclude_ii)};
+        run_graph(fr->st_graph_a, key_a, "graph:steinhardt_frames_count", [&] {
+            enqueue_grid_build(fr, g, s);
+            FG_CUDA(cudaMemsetAsync(fr->st_counts.p, 0, sizeof(uint32_t) * (P + 1), s));
+            launch_frames_ball_count(v, p, P, fr->st_counts.as<uint32_t>(), s);
+            scan_u32_to_u64(fr->st_counts.as<uint32_t>(), fr->st_offsets.as<uint64_t>(), static_cast<size_t>(P) + 1,
+                            fr->st_scan.p, s);
+        });
+        uint64_t nb = 0;
+        FG_CUDA(cudaMemcpyAsync(&nb, fr->st_offsets.as<uint64_t>() + P, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        sync();
+        if (nb >= (1ull << 32))
+            runtime_error("a batched Steinhardt neighbour list holds fewer than 2^32 bonds");
+        // phase 2: bonds, qlm, average, per-frame system sums, wl
+        st->n = P;
+        st->frames = F;
+        size_t off = 0;
+        for (int k = 0; k < st->st.nl; ++k)
+        {
+            st->st.qlm_offset[k] = off;
+            off += static_cast<size_t>(P) * (2 * st->st.l[k] + 1);
+        }
+        const int stride = static_cast<int>(st->stride);
+        fr->st_ij.alloc(sizeof(uint2) * std::max<uint64_t>(nb, 1));
+        fr->st_dist.alloc(sizeof(float) * std::max<uint64_t>(nb, 1));
+        fr->st_vec.alloc(sizeof(float) * 3 * std::max<uint64_t>(nb, 1));
+        fr->st_seg.alloc(sizeof(uint32_t) * (P + 1));
+        fr->st_partial.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * FRAME_SYS_SPLIT * stride);
+        fr->st_sys.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * stride);
+        st->qlm.alloc(sizeof(float2) * std::max<size_t>(off, 1));
+        st->ql.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
+        if (st->average)
+        {
+            st->qlm_ave.alloc(sizeof(float2) * std::max<size_t>(off, 1));
+            st->ql_ave.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
+        }
+        if (st->wl)
+            st->wlv.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
+        std::vector<uint64_t> key_b = {
+            g.id, nb, reinterpret_cast<uint64_t>(fr->st_ij.p),
+            reinterpret_cast<uint64_t>(fr->st_dist.p), reinterpret_cast<uint64_t>(fr->st_vec.p),
+            reinterpret_cast<uint64_t>(fr->st_seg.p), reinterpret_cast<uint64_t>(fr->st_partial.p),
+            reinterpret_cast<uint64_t>(fr->st_sys.p), reinterpret_cast<uint64_t>(st->qlm.p),
+            reinterpret_cast<uint64_t>(st->ql.p), reinterpret_cast<uint64_t>(st->qlm_ave.p),
+            reinterpret_cast<uint64_t>(st->ql_ave.p), reinterpret_cast<uint64_t>(st->wlv.p),
+            reinterpret_cast<uint64_t>(st), fbits(a.r_max), fbits(a.r_min), static_cast<uint64_t>(a.exclude_ii),
+            static_cast<uint64_t>(st->average), static_cast<uint64_t>(st->wl), static_cast<uint64_t>(st->wl_normalize)};
+        for (int k = 0; k < st->st.nl; ++k)
+        {
+            key_b.push_back(static_cast<uint64_t>(st->st.l[k]));
+            key_b.push_back(reinterpret_cast<uint64_t>(st->w3j[k].p));
+        }
+        run_graph(fr->st_graph_b, key_b, "graph:steinhardt_frames", [&] {
+            launch_frames_ball_fill(v, p, P, fr->st_offsets.as<uint64_t>(), fr->st_ij.as<uint2>(), fr->st_dist.as<float>(),
+                                    fr->st_vec.as<float>(), s);
+            launch_segments_from_offsets(fr->st_counts.as<uint32_t>(), fr->st_offsets.as<uint64_t>(), P,
+                                         fr->st_seg.as<uint32_t>(), s);
+            launch_qlm(g.fd_host[0].b, fr->dpts, P, fr->st_ij.as<uint2>(), fr->st_dist.as<float>(), nullptr,
+                       fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st, 0, st->qlm.as<float2>(),
+                       st->ql.as<float>(), s, fr->st_vec.as<float>());
+            const float2* src = st->qlm.as<float2>();
+            const float* qn = st->ql.as<float>();
+            if (st->average)
+            {
+                launch_ave(P, fr->st_ij.as<uint2>(), fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st,
+                           st->qlm.as<float2>(), st->qlm_ave.as<float2>(), st->ql_ave.as<float>(), s);
+                src = st->qlm_ave.as<float2>();
+                qn = st->ql_ave.as<float>();
+            }
+            launch_frames_sys(fr->d_pt_base.as<uint32_t>(), F, st->st, stride, src, fr->st_partial.as<double>(),
+                              fr->st_sys.as<double>(), s);
+            if (st->wl)
+            {
+                for (int k = 0; k < st->st.nl; ++k)
+                    launch_wl(P, st->st, k, src, st->w3j[k].as<float>(), qn, st->wl_normalize ? 1 : 0,
+                              st->wlv.as<float>(), s);
+            }
+        });
+        FG_CUDA(cudaGetLastError());
+        std::vector<double> sys(2 * static_cast<size_t>(F) * stride);
+        FG_CUDA(cudaMemcpyAsync(sys.data(), fr->st_sys.p, sizeof(double) * sys.size(), cudaMemcpyDeviceToHost, s));
+        sync();
+        st->order.assign(static_cast<size_t>(F) * st->st.nl, 0.0f);
+        for (uint32_t f = 0; f < F; ++f)
+            normalize_system(st, &sys[2 * static_cast<size_t>(f) * stride], &st->order[static_cast<size_t>(f) * st->st.nl]);
+        st->computed = true;
+    });
+}
+
+fg_status fg_steinhardt_num_frames(const fg_steinhardt* st, uint32_t* out)
+{
+    return guard([&] {
+        require(st, "steinhardt");
+        require(out, "out");
+        *out = st->frames;
+    });
+}
+
+fg_status fg_batch_set_config(int shell, int warps_per_block, int hist_copies)
+{
+    return guard([&] {
+        if (shell == 0)
+        {
+            g_forced = BatchHistConfig {0, 0, 0};
+            return;
+        }
+        if (shell < 1 || shell > 2 || (warps_per_block != 4 && warps_per_block != 8) ||
+            (hist_copies != 1 && hist_copies != 2))
+            value_error("batch config: shell 1 or 2, 4 or 8 warps per block, 1 or 2 histogram copies");
+        g_forced = BatchHistConfig {shell, warps_per_block, hist_copies};
+    });
+}
+
+fg_status fg_set_graphs(int enable)
+{
+    g_graphs_enabled = enable != 0;
+    return FG_OK;
+}
+
+fg_status fg_autotune_report(char* buf, size_t len)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    if (buf != nullptr && len > 0)
+    {
+        std::strncpy(buf, g_tune_log.c_str(), len - 1);
+        buf[len - 1] = 0;
+    }
+    return g_tune_log.size() + 1 > len ? FG_ERR_VALUE : FG_OK;
 }
 
 } // extern "C"

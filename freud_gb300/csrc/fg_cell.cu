@@ -49,11 +49,6 @@ enum ScanMode
     SM_HIST = 1,
 };
 
-__device__ __forceinline__ int img_ax(int bits, int axis)
-{
-    return static_cast<int>(static_cast<int8_t>((bits >> (8 * axis)) & 0xff));
-}
-
 struct Items
 {
     uint32_t start[32];

@@ -11,38 +11,6 @@
 
 namespace fg {
 
-__device__ __forceinline__ int pack_image(int nx, int ny, int nz)
-{
-    return (nx & 0xff) | ((ny & 0xff) << 8) | ((nz & 0xff) << 16);
-}
-
-__device__ __forceinline__ int clamp_img(float n)
-{
-    return n < -100.0f ? -100 : (n > 100.0f ? 100 : static_cast<int>(n));
-}
-
-// Wrapped cell coordinate and integer image of a point (fractional coordinate
-// f = n + u with n = floor(f), u in [0, 1)).
-__device__ __forceinline__ void point_cell(const DevBox& b, const int dim[3], float x, float y, float z,
-                                           int& cx, int& cy, int& cz, int& img)
-{
-    float fx, fy, fz;
-    make_fractional(b, x, y, z, fx, fy, fz);
-    const float nx = floorf(fx);
-    const float ny = floorf(fy);
-    const float nz = floorf(fz);
-    const float ux = __fsub_rn(fx, nx);
-    const float uy = __fsub_rn(fy, ny);
-    const float uz = __fsub_rn(fz, nz);
-    cx = min(static_cast<int>(ux * static_cast<float>(dim[0])), dim[0] - 1);
-    cy = min(static_cast<int>(uy * static_cast<float>(dim[1])), dim[1] - 1);
-    cz = b.is2d ? 0 : min(static_cast<int>(uz * static_cast<float>(dim[2])), dim[2] - 1);
-    cx = max(cx, 0);
-    cy = max(cy, 0);
-    cz = max(cz, 0);
-    img = pack_image(clamp_img(nx), clamp_img(ny), b.is2d ? 0 : clamp_img(nz));
-}
-
 __global__ void k_assign(DevBox b, const float* __restrict__ pts, uint32_t n, int dx, int dy, int dz,
                          uint32_t* __restrict__ cell_of, uint32_t* __restrict__ rank,
                          uint32_t* __restrict__ cell_count)

@@ -28,6 +28,8 @@ struct Stat
     double ms = 0.0;
 };
 std::map<std::string, Stat> g_stats;
+thread_local bool g_capturing = false;
+thread_local uint64_t g_captured = 0;
 
 void drain_locked()
 {
@@ -50,7 +52,32 @@ void drain_locked()
 
 void prof_count_launch()
 {
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (g_capturing)
+        ++g_captured;
+    else
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+void prof_begin_capture()
+{
+    g_capturing = true;
+    g_captured = 0;
+}
+
+uint64_t prof_end_capture()
+{
+    g_capturing = false;
+    return g_captured;
+}
+
+bool prof_capturing()
+{
+    return g_capturing;
+}
+
+void prof_add_launches(uint64_t n)
+{
+    g_launches.fetch_add(n, std::memory_order_relaxed);
 }
 
 bool prof_enabled()

@@ -38,7 +38,8 @@ template<int LANES>
 __global__ void __launch_bounds__(128)
     k_qlm(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
           const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
-          const uint32_t* __restrict__ cnt, StLs ls, int weighted, float2* __restrict__ qlm_out, float* __restrict__ ql_out)
+          const uint32_t* __restrict__ cnt, const float* __restrict__ bvec, StLs ls, int weighted,
+          float2* __restrict__ qlm_out, float* __restrict__ ql_out)
 {
     const int lane = threadIdx.x & 31;
     const int sub = lane % LANES;               // m owned by this thread
@@ -67,10 +68,19 @@ __global__ void __launch_bounds__(128)
             const uint32_t b1 = b0 + cnt[i];
             for (uint32_t e = b0; e < b1; ++e)
             {
-                const uint32_t j = ij[e].y;
                 float dx, dy, dz;
-                box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pix), __fsub_rn(pts[3 * (size_t) j + 1], piy),
-                         __fsub_rn(pts[3 * (size_t) j + 2], piz), dx, dy, dz);
+                if (bvec != nullptr)
+                {
+                    dx = bvec[3 * (size_t) e];
+                    dy = bvec[3 * (size_t) e + 1];
+                    dz = bvec[3 * (size_t) e + 2];
+                }
+                else
+                {
+                    const uint32_t j = ij[e].y;
+                    box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pix), __fsub_rn(pts[3 * (size_t) j + 1], piy),
+                             __fsub_rn(pts[3 * (size_t) j + 2], piz), dx, dy, dz);
+                }
                 const float w = weighted ? weights[e] : 1.0f;
                 const float d = dist[e];
                 float ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
@@ -388,7 +398,7 @@ static int lanes_for(int max_l)
 
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
-                float2* qlm, float* ql, cudaStream_t s)
+                float2* qlm, float* ql, cudaStream_t s, const float* bond_vec)
 {
     if (n == 0)
     {
@@ -402,17 +412,17 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
     if (lanes == 8)
         {
             ProfScope prof_("k_qlm<8>", s);
-            k_qlm<8><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql);
+            k_qlm<8><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
         }
     else if (lanes == 16)
         {
             ProfScope prof_("k_qlm<16>", s);
-            k_qlm<16><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql);
+            k_qlm<16><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
         }
     else
         {
             ProfScope prof_("k_qlm<32>", s);
-            k_qlm<32><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql);
+            k_qlm<32><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
         }
 }
 

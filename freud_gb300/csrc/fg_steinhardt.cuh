@@ -24,9 +24,12 @@ struct StLs
 };
 
 void st_upload_tables(cudaStream_t s);
+// bond_vec (optional, 3 floats per bond): the bond vectors box.wrap(p_j - p_i)
+// precomputed per bond (batched frames, where the box differs per particle);
+// without it they are computed here from pts and box.
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
-                float2* qlm, float* ql, cudaStream_t s);
+                float2* qlm, float* ql, cudaStream_t s, const float* bond_vec = nullptr);
 void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
                 const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s);
 void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float* w3j_dev, const float* qnorm,

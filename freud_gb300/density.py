@@ -9,7 +9,7 @@ import numpy as np
 
 from . import _lib
 from .box import Box
-from .locality import NeighborList, _SpatialHistogram1D
+from .locality import FrameBatch, NeighborList, _QueryArgs, _SpatialHistogram1D
 from .util import _Compute
 
 
@@ -54,6 +54,16 @@ class RDF(_SpatialHistogram1D):
         """Accumulate the pair distances of one frame (reset=False keeps adding frames)."""
         if reset:
             self._reset()
+        if isinstance(system, FrameBatch):
+            # every frame in one pass: same counts as one compute(reset=False) per frame
+            if query_points is not None or isinstance(neighbors, NeighborList):
+                raise ValueError("a FrameBatch is queried against itself; query_points and NeighborList "
+                                 "neighbors are not supported")
+            query_args = self.default_query_args if neighbors is None else dict(neighbors)
+            query_args.setdefault("exclude_ii", True)
+            qargs = _QueryArgs.from_dict(query_args)
+            _lib.check(_lib.lib.fg_rdf_accumulate_frames(self._h, system._h, ctypes.byref(qargs._c())))
+            return self
         nq, nlist, qargs, l_query_points, num_query_points = self._preprocess_arguments(
             system, query_points, neighbors)
         qp = np.ascontiguousarray(l_query_points, dtype=np.float32)

@@ -258,6 +258,96 @@ class LinkCell(NeighborQuery):
         return out.value
 
 
+class FrameBatch:
+    """Many (box, points) systems of uneven N held on the GPU together, so a
+    compute runs over every frame in one launch per stage instead of one
+    pipeline per frame. ``RDF.compute(batch, reset=False)`` equals calling
+    ``RDF.compute((box, points), reset=False)`` frame by frame, and
+    ``Steinhardt.compute(batch, neighbors)`` computes every frame with its own
+    neighbours (per-particle outputs concatenated in frame order, ``order`` per
+    frame). Frames use AABB pair arithmetic, as (box, points) systems do.
+
+    Args:
+        frames: iterable of (box, points) systems (or objects with ``box`` and
+            ``points``), each with at least one point.
+    """
+
+    def __init__(self, frames):
+        boxes, pts = [], []
+        for system in frames:
+            if hasattr(system, "box") and hasattr(system, "points"):
+                system = (system.box, system.points)
+            box, points = system
+            b = _convert_box(box)
+            boxes.append(b._c_box())
+            pts.append(_convert_array(points, shape=(None, 3)))
+        self._init(boxes, pts)
+
+    def _init(self, boxes, pts):
+        if len(boxes) == 0:
+            raise ValueError("a FrameBatch needs at least one frame")
+        self._offsets = np.zeros(len(boxes) + 1, dtype=np.uint64)
+        self._offsets[1:] = np.cumsum([len(p) for p in pts])
+        self._boxes = (_lib.fg_box * len(boxes))(*boxes)
+        self._points = np.ascontiguousarray(np.concatenate(pts, axis=0), dtype=np.float32)
+        h = _lib.ctypes.c_void_p()
+        _lib.check(_lib.lib.fg_frames_create(self._boxes, _lib.ptr(self._points), _lib.ptr(self._offsets),
+                                             len(boxes), _lib.ctypes.byref(h)))
+        self._handle = _lib.Handle(h, _lib.lib.fg_frames_destroy)
+
+    @classmethod
+    def from_device(cls, boxes, device_points_ptr, frame_offsets, keepalive=None):
+        """A batch over points already on the GPU: ``device_points_ptr`` is the
+        address of a contiguous (total, 3) float32 device array (e.g.
+        ``tensor.data_ptr()``), ``frame_offsets`` the F + 1 ascending point
+        offsets. ``keepalive`` (e.g. the tensor) is held by the batch."""
+        self = cls.__new__(cls)
+        c_boxes = [_convert_box(b)._c_box() for b in boxes]
+        offs = np.asarray(frame_offsets, dtype=np.uint64)
+        if len(offs) != len(c_boxes) + 1:
+            raise ValueError("frame_offsets needs one more entry than boxes")
+        if len(c_boxes) == 0:
+            raise ValueError("a FrameBatch needs at least one frame")
+        self._offsets = np.ascontiguousarray(offs)
+        self._boxes = (_lib.fg_box * len(c_boxes))(*c_boxes)
+        self._points = None
+        self._keepalive = keepalive
+        h = _lib.ctypes.c_void_p()
+        _lib.check(_lib.lib.fg_frames_create_device(self._boxes, _lib.ctypes.c_void_p(device_points_ptr),
+                                                    _lib.ptr(self._offsets), len(c_boxes), _lib.ctypes.byref(h)))
+        self._handle = _lib.Handle(h, _lib.lib.fg_frames_destroy)
+        return self
+
+    @property
+    def _h(self):
+        return self._handle.value
+
+    @property
+    def num_frames(self):
+        return len(self._offsets) - 1
+
+    @property
+    def frame_offsets(self):
+        return self._offsets.copy()
+
+    @property
+    def num_points(self):
+        """Points per frame."""
+        return np.diff(self._offsets).astype(np.int64)
+
+    def box(self, f):
+        b = self._boxes[f]
+        return Box(b.Lx, b.Ly, b.Lz, b.xy, b.xz, b.yz, bool(b.is2D))
+
+    def set_points(self, points):
+        """New positions (same frames and N) for a batch built from host points."""
+        pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        if self._points is None or pts.shape != self._points.shape:
+            raise ValueError("set_points needs the same total number of points as the batch")
+        self._points = pts
+        _lib.check(_lib.lib.fg_frames_set_points(self._h, _lib.ptr(pts)))
+
+
 class NeighborList:
     """Bonds between query points and points, sorted by query point index
     (freud/locality.py:443-751). Arrays are device-resident; properties return

@@ -7,7 +7,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .locality import _PairCompute
+from .locality import FrameBatch, NeighborList, _QueryArgs, _PairCompute
 from .util import _Compute
 
 
@@ -62,6 +62,16 @@ class Steinhardt(_PairCompute):
         return self._ls[0] if len(self._ls) == 1 else list(self._ls)
 
     def compute(self, system, neighbors=None):
+        if isinstance(system, FrameBatch):
+            # every frame with its own ball query; order is per frame
+            if neighbors is None or isinstance(neighbors, NeighborList):
+                raise ValueError("a FrameBatch needs ball query arguments as neighbors, e.g. {'r_max': 1.5}")
+            query_args = dict(neighbors)
+            query_args.setdefault("exclude_ii", True)
+            qargs = _QueryArgs.from_dict(query_args)
+            _lib.check(_lib.lib.fg_steinhardt_compute_frames(self._h, system._h, ctypes.byref(qargs._c())))
+            self._cache = None
+            return self
         nq, nlist, qargs, _qp, _nqp = self._preprocess_arguments(system, neighbors=neighbors)
         _lib.check(_lib.lib.fg_steinhardt_compute(self._h, nq._h, None if nlist is None else nlist._h,
                                                   ctypes.byref(qargs._c())))
@@ -78,7 +88,9 @@ class Steinhardt(_PairCompute):
             ql = np.zeros((n, nl), np.float32)
             po = np.zeros((n, nl), np.float32)
             qlm = np.zeros(n * stride * 2, np.float32)
-            order = np.zeros(nl, np.float32)
+            nf = ctypes.c_uint32()
+            _lib.check(_lib.lib.fg_steinhardt_num_frames(self._h, ctypes.byref(nf)))
+            order = np.zeros(nf.value * nl, np.float32)
             _lib.check(_lib.lib.fg_steinhardt_get(self._h, _lib.ptr(ql), _lib.ptr(po), _lib.ptr(qlm),
                                                   _lib.ptr(order)))
             qc = qlm.view(np.complex64)
@@ -87,12 +99,16 @@ class Steinhardt(_PairCompute):
                 m = 2 * l + 1
                 per_l.append(qc[off:off + n * m].reshape(n, m))
                 off += n * m
+            if nf.value > 1:
+                order = order.reshape(nf.value, nl)
             self._cache = {"ql": ql, "po": po, "qlm": per_l, "order": order}
         return self._cache
 
     @_Compute._computed_property
     def order(self):
         order = self._outputs()["order"]
+        if order.ndim == 2:
+            return order[:, 0] if order.shape[1] == 1 else order
         return order[0] if len(order) == 1 else order
 
     @_Compute._computed_property

@@ -69,6 +69,7 @@ typedef struct fg_nq fg_nq;
 typedef struct fg_nlist fg_nlist;
 typedef struct fg_rdf fg_rdf;
 typedef struct fg_steinhardt fg_steinhardt;
+typedef struct fg_frames fg_frames;
 
 /* Library */
 const char* fg_last_error(void);
@@ -202,6 +203,46 @@ fg_status fg_steinhardt_get(const fg_steinhardt* st, float* ql, float* particle_
 fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points, uint32_t n, float r_max,
                                    float r_min, uint32_t bins, int exclude_ii, int kind,
                                    unsigned long long* device_counts, void* cuda_stream);
+
+/* ---- Batched frames ----------------------------------------------------------
+ * No single counterpart in the reference: a batch stands for a sequence of
+ * (box, points) systems (RawPoints, NeighborQuery.h / RawPoints.h:30-77) that a
+ * freud user passes one per compute call, e.g. RDF.compute(system, reset=False)
+ * over a trajectory (BondHistogramCompute.h:115-126). The batch holds F frames of
+ * uneven N on the device; points are concatenated frame after frame
+ * (frame_offsets: F + 1 ascending point offsets, offsets[0] = 0, every frame
+ * non-empty) and point indices in every per-point output are global (into the
+ * concatenation). boxes: F periodic boxes. Pair arithmetic is AABB arithmetic
+ * (AABBQuery.cc:93,125), as for a (box, points) system. */
+fg_status fg_frames_create(const fg_box* boxes, const float* points, const uint64_t* frame_offsets, uint32_t n_frames,
+                           fg_frames** out);
+/* As fg_frames_create with the caller's device points (borrowed, not copied). */
+fg_status fg_frames_create_device(const fg_box* boxes, const float* device_points, const uint64_t* frame_offsets,
+                                  uint32_t n_frames, fg_frames** out);
+/* New positions for a batch created from host points (same frames and N). */
+fg_status fg_frames_set_points(fg_frames* frames, const float* points);
+fg_status fg_frames_destroy(fg_frames* frames);
+fg_status fg_frames_info(const fg_frames* frames, uint32_t* n_frames, uint64_t* n_points);
+/* Same result as F calls of RDF::accumulate (RDF.cc:101-110) with a ball query
+ * (args: mode ball, r_max, r_min, exclude_ii) on each frame in order: bin counts
+ * summed, frame counter += F, box and N of the last frame. */
+fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* frames, const fg_query_args* args);
+/* Steinhardt::compute (Steinhardt.cc:85-118) of every frame with its own ball
+ * query (args as above). Per-particle outputs (fg_steinhardt_get) cover all
+ * points in batch order; the order output holds n_frames x n_l values. */
+fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* frames, const fg_query_args* args);
+/* Frames covered by the last compute (1 after fg_steinhardt_compute). */
+fg_status fg_steinhardt_num_frames(const fg_steinhardt* st, uint32_t* out);
+/* Launch shape of the batched RDF kernel: shell 1 (27 cells of width >= r_max)
+ * or 2 (125 cells of width >= r_max / 2), 4 or 8 warps per block, 1 or 2
+ * privatised shared histograms per block. shell 0 (default) = autotuned: the
+ * candidates are timed on the first batch of each kind and the fastest is kept. */
+fg_status fg_batch_set_config(int shell, int warps_per_block, int hist_copies);
+/* Text log of the autotuner's measurements and choices. */
+fg_status fg_autotune_report(char* buf, size_t len);
+/* Batched calls record their device work as CUDA graphs and replay them (1,
+ * default) or launch it directly (0). */
+fg_status fg_set_graphs(int enable);
 
 #ifdef __cplusplus
 }
