@@ -213,11 +213,9 @@ def _device_ms(_lib, fn, steps):
     prof = _lib.profile_report()
     launches = (_lib.launch_count() - l0) / steps
     _lib.profile_enable(False)
-    kern = {k: v for k, v in prof.items() if not k.startswith("graph:")}
-    graphs = {k: v for k, v in prof.items() if k.startswith("graph:")}
-    ms = (sum(v[1] for v in kern.values()) + sum(v[1] for v in graphs.values())) / steps
-    top = max(prof.items(), key=lambda kv: kv[1][1])[0] if prof else None
-    return ms, launches, top
+    ms = sum(v[1] for v in prof.values()) / steps
+    per = {k: round(v[1] / steps, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    return ms, launches, per
 
 
 def measure_c1(freud, _lib, steps, warmup, cpu=True):
@@ -235,7 +233,7 @@ def measure_c1(freud, _lib, steps, warmup, cpu=True):
     dev_ms, launches, top = _device_ms(_lib, step, steps)
     out = {"workload": "plain_rdf_n10000_L21.544_rmax4_bins200", "pairs": pairs, "e2e_ms": t * 1e3,
            "e2e": pairs / t, "device_ms": dev_ms, "device": pairs / (dev_ms / 1e3), "unit": "pair evals/s",
-           "launches_per_step": launches, "top_kernel": top}
+           "launches_per_step": launches, "kernels_ms_per_step": top}
     if cpu:
         from oracle import oracle as O
 
@@ -268,7 +266,7 @@ def measure_c3(freud, _lib, steps, warmup, cpu=True):
     n = len(pts)
     out = {"workload": "steinhardt_fcc_256000_k12_l4-12_ave_wl", "particles": n, "e2e_ms": t * 1e3, "e2e": n / t,
            "device_ms": dev_ms, "device": n / (dev_ms / 1e3), "unit": "particles/s", "launches_per_step": launches,
-           "top_kernel": top}
+           "kernels_ms_per_step": top}
     if cpu:
         from oracle import oracle as O
 
@@ -325,10 +323,10 @@ def measure_c4(freud, _lib, steps, warmup):
     return {"workload": "batched_uneven_64_frames_rdf_rmax4_bins200_steinhardt6_rmax1.5", "frames": len(frames),
             "particles": n_total, "pairs": pairs,
             "plain": {"e2e_ms": t_plain * 1e3, "pair_evals_per_s": pairs / t_plain, "particles_per_s": n_total / t_plain,
-                      "device_ms": dev_plain, "launches_per_step": l_plain, "top_kernel": top_plain},
+                      "device_ms": dev_plain, "launches_per_step": l_plain, "kernels_ms_per_step": top_plain},
             "batched": {"e2e_ms": t_batch * 1e3, "pair_evals_per_s": pairs / t_batch,
                         "particles_per_s": n_total / t_batch, "device_ms": dev_batch, "launches_per_step": l_batch,
-                        "top_kernel": top_batch},
+                        "kernels_ms_per_step": top_batch},
             "speedup_e2e": t_plain / t_batch, "speedup_device": dev_plain / dev_batch if dev_batch else None,
             "autotune": _lib.autotune_report().strip().splitlines()[-1:] }
 
@@ -362,7 +360,7 @@ def measure_c5(freud, _lib, steps, warmup):
     return {"workload": "blobs_4096x1024_L256_rdf_rmax5_bins500_steinhardt6_rmax1.2", "particles": len(pts),
             "pairs": pairs, "pairs_above_2^32": pairs >= 2 ** 32, "e2e_ms": t * 1e3, "e2e": pairs / t,
             "device_ms": dev_ms, "device": pairs / (dev_ms / 1e3), "unit": "pair evals/s (RDF + Steinhardt step)",
-            "launches_per_step": launches, "top_kernel": top,
+            "launches_per_step": launches, "kernels_ms_per_step": top,
             "rdf_f32_vs_fp64_max_rel": float(np.max(np.abs(g32[nz] - g64[nz]) / g64[nz])),
             "cell_occupancy": {"mean": float(occ.mean()), "max": int(occ.max()),
                                "skew_max_over_mean": float(occ.max() / occ.mean())}}
@@ -401,6 +399,25 @@ def run_reference(args):
     return 0
 
 
+def run_only(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    from freud_gb300 import _lib
+
+    import freud_gb300 as freud
+
+    stream = torch.cuda.Stream()
+    _lib.set_stream(stream.cuda_stream)
+    torch.cuda.set_stream(stream)
+    fns = {"plain_rdf": lambda: measure_c1(freud, _lib, args.steps, args.warmup, cpu=False),
+           "steinhardt": lambda: measure_c3(freud, _lib, args.steps, args.warmup, cpu=False),
+           "batched_frames": lambda: measure_c4(freud, _lib, args.steps, args.warmup),
+           "precision_stress": lambda: measure_c5(freud, _lib, args.steps, args.warmup)}
+    print(json.dumps({"only": args.only, "result": fns[args.only]()}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -412,9 +429,13 @@ def main():
                     help="skip the plain-RDF, Steinhardt, batched-frames and stress workloads")
     ap.add_argument("--n-side", type=int, default=102,
                     help="lattice points per side; 102 is the benchmark workload, smaller sizes are for profiling")
+    ap.add_argument("--only", default=None, choices=["plain_rdf", "steinhardt", "batched_frames", "precision_stress"],
+                    help="run one of the other workloads alone and print its result (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_only(args)
 
     import torch
 

@@ -445,17 +445,24 @@ __global__ void __launch_bounds__(128)
 // Per-frame system sums
 // ---------------------------------------------------------------------------
 
-__global__ void k_frames_sys(const uint32_t* __restrict__ pt_base, StLs ls, int stride, const float2* __restrict__ src,
-                             double* __restrict__ partial)
+// Rows [r0, r1) of one frame split, warp per column: each lane keeps an FP64
+// running sum over every 32nd row (at most FRAME_SYS_ROWS / 32 values, so the
+// rounding is far below the float32 inputs' own), then a fixed shuffle tree;
+// lane 0 writes partial[f][split][col].
+__global__ void __launch_bounds__(256)
+    k_frames_sys(const uint32_t* __restrict__ pt_base, StLs ls, int stride, int splits,
+                 const float2* __restrict__ src, double* __restrict__ partial)
 {
     const uint32_t f = blockIdx.x;
     const uint32_t split = blockIdx.y;
     const uint32_t r_lo = pt_base[f];
     const uint32_t nf = pt_base[f + 1] - r_lo;
-    const uint32_t per = (nf + FRAME_SYS_SPLIT - 1) / FRAME_SYS_SPLIT;
+    const uint32_t per = (nf + splits - 1) / splits;
     const uint32_t r0 = r_lo + min(nf, split * per);
     const uint32_t r1 = r_lo + min(nf, (split + 1) * per);
-    for (int col = threadIdx.x; col < stride; col += blockDim.x)
+    const int lane = threadIdx.x & 31;
+    const int warps = blockDim.x >> 5;
+    for (int col = threadIdx.x >> 5; col < stride; col += warps)
     {
         // column -> (l index, m slot)
         int k = 0, m = col;
@@ -466,48 +473,57 @@ __global__ void k_frames_sys(const uint32_t* __restrict__ pt_base, StLs ls, int 
         }
         const int nm = 2 * ls.l[k] + 1;
         const float2* base = src + ls.qlm_offset[k] + m;
-        double sr = 0.0, si = 0.0, cr = 0.0, ci = 0.0;
-        for (uint32_t r = r0; r < r1; ++r)
+        double sr = 0.0, si = 0.0;
+        for (uint32_t r = r0 + lane; r < r1; r += 32)
         {
             const float2 v = base[static_cast<size_t>(r) * nm];
-            const double yr = static_cast<double>(v.x) / nf - cr;
-            const double tr = sr + yr;
-            cr = (tr - sr) - yr;
-            sr = tr;
-            const double yi = static_cast<double>(v.y) / nf - ci;
-            const double ti = si + yi;
-            ci = (ti - si) - yi;
-            si = ti;
+            sr += static_cast<double>(v.x);
+            si += static_cast<double>(v.y);
         }
-        double* out = partial + ((static_cast<size_t>(f) * FRAME_SYS_SPLIT + split) * stride + col) * 2;
-        out[0] = sr;
-        out[1] = si;
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0)
+        {
+            double* out = partial + ((static_cast<size_t>(f) * splits + split) * stride + col) * 2;
+            out[0] = sr;
+            out[1] = si;
+        }
     }
 }
 
-__global__ void k_frames_sys_final(uint32_t nframes, int stride, const double* __restrict__ partial,
-                                   double* __restrict__ sys)
+// Block per frame, warp per column: the split sums reduced by lanes (every 32nd
+// split) and a fixed shuffle tree (the same order every run), divided by n_f.
+__global__ void __launch_bounds__(256)
+    k_frames_sys_final(const uint32_t* __restrict__ pt_base, int stride, int splits,
+                       const double* __restrict__ partial, double* __restrict__ sys)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nframes * static_cast<uint32_t>(stride))
-        return;
-    const uint32_t f = t / stride;
-    const uint32_t col = t % stride;
-    double sr = 0.0, si = 0.0, cr = 0.0, ci = 0.0;
-    for (int k = 0; k < FRAME_SYS_SPLIT; ++k)
+    const uint32_t f = blockIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int warps = blockDim.x >> 5;
+    const double nf = static_cast<double>(pt_base[f + 1] - pt_base[f]);
+    for (int col = threadIdx.x >> 5; col < stride; col += warps)
     {
-        const double* v = partial + ((static_cast<size_t>(f) * FRAME_SYS_SPLIT + k) * stride + col) * 2;
-        const double yr = v[0] - cr;
-        const double tr = sr + yr;
-        cr = (tr - sr) - yr;
-        sr = tr;
-        const double yi = v[1] - ci;
-        const double ti = si + yi;
-        ci = (ti - si) - yi;
-        si = ti;
+        double sr = 0.0, si = 0.0;
+        for (int k = lane; k < splits; k += 32)
+        {
+            const double* v = partial + ((static_cast<size_t>(f) * splits + k) * stride + col) * 2;
+            sr += v[0];
+            si += v[1];
+        }
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0)
+        {
+            sys[2 * (static_cast<size_t>(f) * stride + col)] = nf > 0.0 ? sr / nf : 0.0;
+            sys[2 * (static_cast<size_t>(f) * stride + col) + 1] = nf > 0.0 ? si / nf : 0.0;
+        }
     }
-    sys[2 * static_cast<size_t>(t)] = sr;
-    sys[2 * static_cast<size_t>(t) + 1] = si;
 }
 
 int grid_blocks(size_t n, int threads)
@@ -617,19 +633,25 @@ void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n
     k_frames_ball<true><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, nullptr, offsets, ij, dist, vec);
 }
 
-void launch_frames_sys(const uint32_t* pt_base, uint32_t nframes, const StLs& ls, int stride, const float2* src,
-                       double* partial, double* sys, cudaStream_t s)
+int frames_sys_splits(uint32_t max_rows)
+{
+    const uint32_t want = (max_rows + FRAME_SYS_ROWS - 1) / FRAME_SYS_ROWS;
+    return static_cast<int>(std::min<uint32_t>(std::max<uint32_t>(want, 1u), 65535u));
+}
+
+void launch_frames_sys(const uint32_t* pt_base, uint32_t nframes, uint32_t max_rows, const StLs& ls, int stride,
+                       const float2* src, double* partial, double* sys, cudaStream_t s)
 {
     if (nframes == 0)
         return;
+    const int splits = frames_sys_splits(max_rows);
     {
         ProfScope prof_("k_frames_sys", s);
-        k_frames_sys<<<dim3(nframes, FRAME_SYS_SPLIT), 64, 0, s>>>(pt_base, ls, stride, src, partial);
+        k_frames_sys<<<dim3(nframes, splits), 256, 0, s>>>(pt_base, ls, stride, splits, src, partial);
     }
     {
-        const uint32_t t = nframes * static_cast<uint32_t>(stride);
         ProfScope prof_("k_frames_sys_final", s);
-        k_frames_sys_final<<<(t + 127) / 128, 128, 0, s>>>(nframes, stride, partial, sys);
+        k_frames_sys_final<<<nframes, 256, 0, s>>>(pt_base, stride, splits, partial, sys);
     }
 }
 

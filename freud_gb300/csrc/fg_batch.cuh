@@ -74,11 +74,15 @@ void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n
                              float* dist, float* vec, cudaStream_t s);
 
 // Per-frame FP64 system sums of the per-l (n, 2l + 1) qlm layout: sys[f][col]
-// (complex, col running over every l's m) = sum over the frame's rows of
-// qlm / n_f, compensated, reduced in a fixed order. partial holds
-// nframes * FRAME_SYS_SPLIT * stride * 2 doubles.
-constexpr int FRAME_SYS_SPLIT = 64;
-void launch_frames_sys(const uint32_t* pt_base, uint32_t nframes, const StLs& ls, int stride, const float2* src,
-                       double* partial, double* sys, cudaStream_t s);
+// (complex, col running over every l's m) = (FP64 sum over the frame's rows) /
+// n_f: FP64 running sums over runs of at most FRAME_SYS_ROWS rows (a warp per
+// column, fixed shuffle trees), then a fixed tree over the runs, so results do
+// not depend on scheduling. max_rows is the
+// largest frame; partial holds nframes * frames_sys_splits(max_rows) * stride * 2
+// doubles.
+constexpr uint32_t FRAME_SYS_ROWS = 512;
+int frames_sys_splits(uint32_t max_rows);
+void launch_frames_sys(const uint32_t* pt_base, uint32_t nframes, uint32_t max_rows, const StLs& ls, int stride,
+                       const float2* src, double* partial, double* sys, cudaStream_t s);
 
 } // namespace fg

@@ -898,6 +898,10 @@ double reduce_w3j_host(const double* q, int l, const std::vector<double>& w)
 
 } // namespace
 
+namespace fg {
+bool steinhardt_ball_single(fg_steinhardt* st, fg_nq* nq, const fg_query_args* args);
+}
+
 extern "C" {
 
 const char* fg_last_error(void)
@@ -1697,6 +1701,10 @@ fg_status fg_steinhardt_create(const uint32_t* ls, uint32_t n_l, int average, in
             st->st.norm[k] = static_cast<float>(4.0 * M_PI / (2 * ls[k] + 1));
             st->stride += 2 * ls[k] + 1;
         }
+        for (uint32_t k = 0; k < n_l; ++k)
+            st->st.sorted_k[k] = static_cast<int>(k);
+        std::stable_sort(st->st.sorted_k, st->st.sorted_k + n_l,
+                         [&](int a, int b) { return st->st.l[a] < st->st.l[b]; });
         st_upload_tables(stream());
         for (uint32_t k = 0; k < n_l; ++k)
         {
@@ -1760,6 +1768,12 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
         require(st, "steinhardt");
         require(nq, "nq");
         cudaStream_t s = stream();
+        if (nlist == nullptr)
+        {
+            require(args, "args");
+            if (steinhardt_ball_single(st, nq, args))
+                return;
+        }
         fg_nlist own;
         const fg_nlist* nl = nlist;
         if (nl == nullptr)
@@ -1796,9 +1810,15 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
             src = st->qlm_ave.as<float2>();
             qn = st->ql_ave.as<float>();
         }
+        // system qlm: the frame-sum kernel over this single frame
         st->sys.alloc(sizeof(double) * 2 * st->stride);
-        FG_CUDA(cudaMemsetAsync(st->sys.p, 0, sizeof(double) * 2 * st->stride, s));
-        launch_sys(n, st->st, src, st->sys.as<double>(), s);
+        const uint32_t rows[2] = {0u, n};
+        DevBuf d_rows, partial;
+        d_rows.alloc(sizeof(rows));
+        FG_CUDA(cudaMemcpyAsync(d_rows.p, rows, sizeof(rows), cudaMemcpyHostToDevice, s));
+        partial.alloc(sizeof(double) * 2 * static_cast<size_t>(frames_sys_splits(n)) * st->stride);
+        launch_frames_sys(d_rows.as<uint32_t>(), 1, n, st->st, static_cast<int>(st->stride), src, partial.as<double>(),
+                          st->sys.as<double>(), s);
         if (st->wl)
         {
             st->wlv.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(n) * st->st.nl, 1));
@@ -2051,10 +2071,12 @@ uint64_t fbits(float f)
 // call with this key (body must only enqueue stream work on preallocated
 // buffers). The legacy / per-thread default streams cannot be captured: there
 // body runs directly.
-template<typename F> void run_graph(GraphCache& gc, const std::vector<uint64_t>& key, const char* name, F&& body)
+template<typename F>
+void run_graph(GraphCache& gc, bool allow, const std::vector<uint64_t>& key, const char* name, F&& body)
 {
     cudaStream_t s = stream();
-    const bool capturable = g_graphs_enabled && s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
+    const bool capturable =
+        allow && g_graphs_enabled && s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread;
     if (!capturable)
     {
         body();
@@ -2112,6 +2134,7 @@ struct BatchGridBufs
 
 struct fg_frames
 {
+    bool graphs = true; // record/replay CUDA graphs (off for one-off internal batches)
     std::vector<HostBox> boxes;
     std::vector<uint32_t> n;       // points per frame
     std::vector<uint32_t> pt_base; // nframes + 1
@@ -2470,7 +2493,7 @@ fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_ar
                                            static_cast<uint64_t>(cfg.warps), static_cast<uint64_t>(cfg.copies),
                                            fbits(a.r_max), fbits(a.r_min), static_cast<uint64_t>(a.exclude_ii),
                                            static_cast<uint64_t>(h.bins), fbits(h.h_min), fbits(h.h_max)};
-        run_graph(fr->rdf_graph, key, "graph:rdf_frames", [&] {
+        run_graph(fr->rdf_graph, fr->graphs, key, "graph:rdf_frames", [&] {
             enqueue_grid_build(fr, g, s);
             FG_CUDA(cudaMemsetAsync(fr->queue.p, 0, sizeof(uint32_t), s));
             launch_frames_hist(cfg, v, p, h, g.ncell, fr->queue.as<uint32_t>(), rdf->hist.as<unsigned long long>(), s);
@@ -2485,13 +2508,9 @@ fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_ar
     });
 }
 
-fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_args* args)
+static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_args& a)
 {
-    return guard([&] {
-        require(st, "steinhardt");
-        require(fr, "frames");
-        require(args, "args");
-        const fg_query_args a = batch_args(fr, args);
+    {
         cudaStream_t s = stream();
         const uint32_t P = fr->total;
         const uint32_t F = static_cast<uint32_t>(fr->n.size());
@@ -2512,7 +2531,7 @@ fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const f
                                              reinterpret_cast<uint64_t>(fr->st_offsets.p),
                                              reinterpret_cast<uint64_t>(fr->st_scan.p), fbits(a.r_max), fbits(a.r_min),
                                              static_cast<uint64_t>(a.exclude_ii)};
-        run_graph(fr->st_graph_a, key_a, "graph:steinhardt_frames_count", [&] {
+        run_graph(fr->st_graph_a, fr->graphs, key_a, "graph:steinhardt_frames_count", [&] {
             enqueue_grid_build(fr, g, s);
             FG_CUDA(cudaMemsetAsync(fr->st_counts.p, 0, sizeof(uint32_t) * (P + 1), s));
             launch_frames_ball_count(v, p, P, fr->st_counts.as<uint32_t>(), s);
@@ -2538,7 +2557,8 @@ fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const f
         fr->st_dist.alloc(sizeof(float) * std::max<uint64_t>(nb, 1));
         fr->st_vec.alloc(sizeof(float) * 3 * std::max<uint64_t>(nb, 1));
         fr->st_seg.alloc(sizeof(uint32_t) * (P + 1));
-        fr->st_partial.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * FRAME_SYS_SPLIT * stride);
+        const uint32_t max_rows = *std::max_element(fr->n.begin(), fr->n.end());
+        fr->st_partial.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * frames_sys_splits(max_rows) * stride);
         fr->st_sys.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * stride);
         st->qlm.alloc(sizeof(float2) * std::max<size_t>(off, 1));
         st->ql.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
@@ -2563,7 +2583,7 @@ fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const f
             key_b.push_back(static_cast<uint64_t>(st->st.l[k]));
             key_b.push_back(reinterpret_cast<uint64_t>(st->w3j[k].p));
         }
-        run_graph(fr->st_graph_b, key_b, "graph:steinhardt_frames", [&] {
+        run_graph(fr->st_graph_b, fr->graphs, key_b, "graph:steinhardt_frames", [&] {
             launch_frames_ball_fill(v, p, P, fr->st_offsets.as<uint64_t>(), fr->st_ij.as<uint2>(), fr->st_dist.as<float>(),
                                     fr->st_vec.as<float>(), s);
             launch_segments_from_offsets(fr->st_counts.as<uint32_t>(), fr->st_offsets.as<uint64_t>(), P,
@@ -2580,8 +2600,8 @@ fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const f
                 src = st->qlm_ave.as<float2>();
                 qn = st->ql_ave.as<float>();
             }
-            launch_frames_sys(fr->d_pt_base.as<uint32_t>(), F, st->st, stride, src, fr->st_partial.as<double>(),
-                              fr->st_sys.as<double>(), s);
+            launch_frames_sys(fr->d_pt_base.as<uint32_t>(), F, max_rows, st->st, stride, src,
+                              fr->st_partial.as<double>(), fr->st_sys.as<double>(), s);
             if (st->wl)
             {
                 for (int k = 0; k < st->st.nl; ++k)
@@ -2597,6 +2617,17 @@ fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const f
         for (uint32_t f = 0; f < F; ++f)
             normalize_system(st, &sys[2 * static_cast<size_t>(f) * stride], &st->order[static_cast<size_t>(f) * st->st.nl]);
         st->computed = true;
+    }
+}
+
+fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_args* args)
+{
+    return guard([&] {
+        require(st, "steinhardt");
+        require(fr, "frames");
+        require(args, "args");
+        const fg_query_args a = batch_args(fr, args);
+        steinhardt_frames(st, fr, a);
     });
 }
 
@@ -2642,3 +2673,34 @@ fg_status fg_autotune_report(char* buf, size_t len)
 }
 
 } // extern "C"
+
+namespace fg {
+
+// Steinhardt of one (box, points) system with its own ball query (nlist ==
+// NULL, AABB arithmetic, periodic box): the frames path with one frame. The
+// reference sums each particle's bonds in query-iterator order here
+// (Steinhardt.cc:136-147 with loopOverNeighborsIterator), not in NeighborList
+// order, so no sorted list is built.
+bool steinhardt_ball_single(fg_steinhardt* st, fg_nq* nq, const fg_query_args* args)
+{
+    if (nq->kind == FG_NQ_LINKCELL || !(nq->box.periodic[0] && nq->box.periodic[1] && nq->box.periodic[2]))
+        return false;
+    fg_query_args a = *args;
+    validate_args(a);
+    if (a.mode != FG_MODE_BALL)
+        return false;
+    fg_frames fr;
+    fr.graphs = false;
+    fr.boxes.push_back(nq->box);
+    fr.n.push_back(nq->n);
+    fr.pt_base = {0u, nq->n};
+    fr.total = nq->n;
+    fr.dpts = nq->dpts;
+    fr.d_pt_base.alloc(sizeof(uint32_t) * 2);
+    FG_CUDA(cudaMemcpyAsync(fr.d_pt_base.p, fr.pt_base.data(), sizeof(uint32_t) * 2, cudaMemcpyHostToDevice, stream()));
+    const fg_query_args checked = batch_args(&fr, &a);
+    steinhardt_frames(st, &fr, checked);
+    return true;
+}
+
+} // namespace fg

@@ -535,28 +535,45 @@ __global__ void k_hist_distances(const float* __restrict__ dist, uint64_t nb, Hi
     }
     __syncthreads();
     unsigned int* my = s_hist + ((threadIdx.x >> 5) % HIST_COPIES) * HIST_SMEM_BINS;
-    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-    for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < nb; e += stride)
-    {
-        const float d = dist[e];
+    auto add = [&](float d) {
         if (d < h.h_min || d >= h.h_max)
-        {
-            continue;
-        }
+            return;
         uint32_t bin = static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
         if (bin == h.bins)
-        {
             bin = h.bins - 1;
-        }
         if (smem_hist)
-        {
             atomicAdd(&my[bin], 1u);
-        }
         else
-        {
             atomicAdd(&hist[bin], 1ull);
+    };
+    // 16-byte loads, two in flight per thread: scalar head up to the first
+    // 16-byte boundary, float4 body, scalar tail
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    const uint64_t gtid = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    const uint64_t mis = (reinterpret_cast<uintptr_t>(dist) >> 2) & 3u;
+    const uint64_t head = mis == 0 ? 0 : (4 - mis < nb ? 4 - mis : nb);
+    if (gtid < head)
+        add(dist[gtid]);
+    const uint64_t n4 = (nb - head) / 4;
+    const float4* d4 = reinterpret_cast<const float4*>(dist + head);
+    for (uint64_t e = gtid; e < n4; e += 2 * stride)
+    {
+        const float4 a = d4[e];
+        const float4 b = e + stride < n4 ? d4[e + stride] : make_float4(-1.0f, -1.0f, -1.0f, -1.0f);
+        add(a.x);
+        add(a.y);
+        add(a.z);
+        add(a.w);
+        if (e + stride < n4)
+        {
+            add(b.x);
+            add(b.y);
+            add(b.z);
+            add(b.w);
         }
     }
+    for (uint64_t e = head + 4 * n4 + gtid; e < nb; e += stride)
+        add(dist[e]);
     if (smem_hist)
     {
         __syncthreads();

@@ -16,7 +16,8 @@
 // reduces ql over the particle's lanes with shuffles.
 // k_ave: the same mapping gathers the neighbours' qlm (Steinhardt.cc:224-289).
 // k_wl: thread per (particle, l), Wigner-3j triple sum with compensated float sum.
-// k_sys: FP64 column sums of qlm (or averaged qlm) / N for the system order.
+// The FP64 system sums (qlm or averaged qlm over the particles, divided by N)
+// are taken by the per-frame column-sum kernels of fg_batch.cu.
 #include <cmath>
 #include <cstdint>
 
@@ -34,40 +35,68 @@ __constant__ float c_K[ST_MAX_L + 1];                    // Q_m^m prefactors
 __constant__ float c_a[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // a_lm at [l*(L+1)+m]
 __constant__ float c_b[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // b_lm
 
-template<int LANES>
+template<int LANES, int NL>
 __global__ void __launch_bounds__(128)
     k_qlm(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
           const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
           const uint32_t* __restrict__ cnt, const float* __restrict__ bvec, StLs ls, int weighted,
           float2* __restrict__ qlm_out, float* __restrict__ ql_out)
 {
+    // recurrence coefficients staged once per block (lanes read different m)
+    __shared__ float s_a[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
+    __shared__ float s_b[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
+    __shared__ float s_K[ST_MAX_L + 1];
+    for (int t = threadIdx.x; t <= ls.max_l * (ST_MAX_L + 1) + ST_MAX_L; t += blockDim.x)
+    {
+        s_a[t] = c_a[t];
+        s_b[t] = c_b[t];
+    }
+    for (int t = threadIdx.x; t <= ST_MAX_L; t += blockDim.x)
+        s_K[t] = c_K[t];
+    __syncthreads();
+
     const int lane = threadIdx.x & 31;
     const int sub = lane % LANES;               // m owned by this thread
     const int group = lane / LANES;             // particle slot within the warp
     const int groups_per_block = blockDim.x / LANES;
     const unsigned gmask = LANES == 32 ? FULL : (((1u << LANES) - 1u) << (group * LANES));
     const int m = sub;
-    (void) group;
+    const float sgn = (m & 1) ? -1.0f : 1.0f;
+    // slot kk holds the kk-th smallest requested l
+    int lt[NL];
+#pragma unroll
+    for (int kk = 0; kk < NL; ++kk)
+        lt[kk] = kk < ls.nl ? ls.l[ls.sorted_k[kk]] : -1;
+    const int lmax = ls.max_l;
+    const float km = m <= lmax ? s_K[m] : 0.0f;
+    const float c1 = sqrtf(2.0f * m + 3.0f);
     for (uint32_t i = blockIdx.x * groups_per_block + threadIdx.x / LANES; i < n; i += gridDim.x * groups_per_block)
     {
-        const bool live = true;
-        float acc_re[ST_MAX_NL][2];
-        float acc_im[ST_MAX_NL][2];
+        float acc_re[NL][2];
+        float acc_im[NL][2];
 #pragma unroll
-        for (int k = 0; k < ST_MAX_NL; ++k)
+        for (int k = 0; k < NL; ++k)
         {
             acc_re[k][0] = acc_re[k][1] = acc_im[k][0] = acc_im[k][1] = 0.0f;
         }
         float tw = 0.0f;
-        if (live && m <= ls.max_l)
+        const uint32_t b0 = seg[i];
+        const uint32_t nbond = cnt[i];
+        float pix = 0.f, piy = 0.f, piz = 0.f;
+        if (bvec == nullptr)
         {
-            const float pix = pts[3 * (size_t) i];
-            const float piy = pts[3 * (size_t) i + 1];
-            const float piz = pts[3 * (size_t) i + 2];
-            const uint32_t b0 = seg[i];
-            const uint32_t b1 = b0 + cnt[i];
-            for (uint32_t e = b0; e < b1; ++e)
+            pix = pts[3 * (size_t) i];
+            piy = pts[3 * (size_t) i + 1];
+            piz = pts[3 * (size_t) i + 2];
+        }
+        // bonds in batches of LANES: lane t computes the geometry of bond base + t
+        // (independent loads in flight), then the group walks the batch with shuffles
+        for (uint32_t base = 0; base < nbond; base += LANES)
+        {
+            float g_ct = 1.0f, g_st = 0.0f, g_cp = 1.0f, g_sp = 0.0f, g_w = 0.0f;
+            if (base + sub < nbond)
             {
+                const uint32_t e = b0 + base + sub;
                 float dx, dy, dz;
                 if (bvec != nullptr)
                 {
@@ -81,89 +110,103 @@ __global__ void __launch_bounds__(128)
                     box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pix), __fsub_rn(pts[3 * (size_t) j + 1], piy),
                              __fsub_rn(pts[3 * (size_t) j + 2], piz), dx, dy, dz);
                 }
-                const float w = weighted ? weights[e] : 1.0f;
+                g_w = weighted ? weights[e] : 1.0f;
                 const float d = dist[e];
-                float ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
-                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                g_ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
+                g_st = sqrtf(fmaxf(0.0f, 1.0f - g_ct * g_ct));
                 const float rho = sqrtf(dx * dx + dy * dy);
-                float cp = 1.0f, sp = 0.0f;
                 if (rho > 0.0f)
                 {
-                    cp = dx / rho;
-                    sp = dy / rho;
+                    g_cp = dx / rho;
+                    g_sp = dy / rho;
                 }
-                // e^{i m phi} and sin^m(theta)
+            }
+            const uint32_t nb_here = min(static_cast<uint32_t>(LANES), nbond - base);
+            for (uint32_t t = 0; t < nb_here; ++t)
+            {
+                const float ct = __shfl_sync(gmask, g_ct, t, LANES);
+                const float st = __shfl_sync(gmask, g_st, t, LANES);
+                const float cp = __shfl_sync(gmask, g_cp, t, LANES);
+                const float sp = __shfl_sync(gmask, g_sp, t, LANES);
+                const float w = __shfl_sync(gmask, g_w, t, LANES);
+                // One loop of lmax steps for every lane: the first m steps build
+                // e^{i m phi} and sin^m(theta); the rest run the normalised Legendre
+                // recurrence in l divided by K_m sin^m(theta):
+                //   R_m = 1, R_{m+1} = sqrt(2m+3) x R_m, R_l = a_lm (x R_{l-1} - b_lm R_{l-2})
+                // so Q_l^m = K_m sin^m(theta) R_l and no lane waits on another.
                 float em_re = 1.0f, em_im = 0.0f, sm = 1.0f;
-                for (int t = 0; t < m; ++t)
+                float r_cur = 1.0f, r_prev = 0.0f;
+                float R[NL];
+#pragma unroll
+                for (int kk = 0; kk < NL; ++kk)
+                    R[kk] = lt[kk] == m ? 1.0f : 0.0f;
+                int l = m;
+                for (int s = 0; s < lmax; ++s)
                 {
-                    const float nr = em_re * cp - em_im * sp;
-                    em_im = em_re * sp + em_im * cp;
-                    em_re = nr;
-                    sm *= st;
-                }
-                float q_lm2 = 0.0f;
-                float q_lm1 = c_K[m] * sm; // Q_m^m
-                // advance over the requested ls (ascending) while running the recurrence in l
-                for (int l = m; l <= ls.max_l; ++l)
-                {
-                    float q;
-                    if (l == m)
+                    if (s < m)
                     {
-                        q = q_lm1;
-                    }
-                    else if (l == m + 1)
-                    {
-                        q = sqrtf(2.0f * m + 3.0f) * ct * q_lm1;
-                        q_lm2 = q_lm1;
-                        q_lm1 = q;
+                        const float nr = em_re * cp - em_im * sp;
+                        em_im = em_re * sp + em_im * cp;
+                        em_re = nr;
+                        sm *= st;
                     }
                     else
                     {
-                        q = c_a[l * (ST_MAX_L + 1) + m] * (ct * q_lm1 - c_b[l * (ST_MAX_L + 1) + m] * q_lm2);
-                        q_lm2 = q_lm1;
-                        q_lm1 = q;
-                    }
+                        ++l;
+                        const float r = l == m + 1
+                            ? c1 * ct * r_cur
+                            : s_a[l * (ST_MAX_L + 1) + m] * (ct * r_cur - s_b[l * (ST_MAX_L + 1) + m] * r_prev);
+                        r_prev = r_cur;
+                        r_cur = r;
 #pragma unroll
-                    for (int k = 0; k < ST_MAX_NL; ++k)
-                    {
-                        if (k < ls.nl && ls.l[k] == l)
+                        for (int kk = 0; kk < NL; ++kk)
                         {
-                            const float yr = w * q * em_re;
-                            const float yi = w * q * em_im;
-                            acc_re[k][0] += yr;
-                            acc_im[k][0] += yi;
-                            // Y_l^{-m} = (-1)^m conj(Y_l^m)
-                            const float sgn = (m & 1) ? -1.0f : 1.0f;
-                            acc_re[k][1] += sgn * yr;
-                            acc_im[k][1] -= sgn * yi;
+                            if (lt[kk] == l)
+                                R[kk] = r;
                         }
                     }
+                }
+                const float pf = w * km * sm;
+                const float wre = pf * em_re;
+                const float wim = pf * em_im;
+#pragma unroll
+                for (int kk = 0; kk < NL; ++kk)
+                {
+                    const float yr = R[kk] * wre;
+                    const float yi = R[kk] * wim;
+                    acc_re[kk][0] += yr;
+                    acc_im[kk][0] += yi;
+                    // Y_l^{-m} = (-1)^m conj(Y_l^m)
+                    acc_re[kk][1] += sgn * yr;
+                    acc_im[kk][1] -= sgn * yi;
                 }
                 tw += w;
             }
         }
-        // normalise, write, and reduce ql over the particle's lanes
+        // normalise, write, and reduce ql over the particle's lanes (slot kk holds
+        // the kk-th smallest l, whose caller index is k)
 #pragma unroll
-        for (int k = 0; k < ST_MAX_NL; ++k)
+        for (int kk = 0; kk < NL; ++kk)
         {
-            if (k >= ls.nl)
+            if (kk >= ls.nl)
             {
                 break;
             }
-            const int l = ls.l[k];
+            const int k = ls.sorted_k[kk];
+            const int lk = lt[kk];
             float part = 0.0f;
-            if (live && m <= l)
+            if (m <= lk)
             {
-                const float qr = acc_re[k][0] / tw;
-                const float qi = acc_im[k][0] / tw;
-                float2* row = qlm_out + ls.qlm_offset[k] + static_cast<size_t>(i) * (2 * l + 1);
+                const float qr = acc_re[kk][0] / tw;
+                const float qi = acc_im[kk][0] / tw;
+                float2* row = qlm_out + ls.qlm_offset[k] + static_cast<size_t>(i) * (2 * lk + 1);
                 row[m] = make_float2(qr, qi);
                 part = qr * qr + qi * qi;
                 if (m > 0)
                 {
-                    const float nr = acc_re[k][1] / tw;
-                    const float ni = acc_im[k][1] / tw;
-                    row[l + m] = make_float2(nr, ni);
+                    const float nr = acc_re[kk][1] / tw;
+                    const float ni = acc_im[kk][1] / tw;
+                    row[lk + m] = make_float2(nr, ni);
                     part += nr * nr + ni * ni;
                 }
             }
@@ -171,7 +214,7 @@ __global__ void __launch_bounds__(128)
             {
                 part += __shfl_xor_sync(gmask, part, o, LANES);
             }
-            if (live && sub == 0)
+            if (sub == 0)
             {
                 ql_out[static_cast<size_t>(i) * ls.nl + k] = sqrtf(part * ls.norm[k]);
             }
@@ -179,7 +222,9 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-// Neighbour averaging: ave(i) = (sum_j qlm(j) + qlm(i)) / (1 + n_i).
+// Neighbour averaging: ave(i) = (sum_j qlm(j) + qlm(i)) / (1 + n_i). Per l, the
+// neighbour indices of LANES bonds are loaded at once (one per lane) and
+// broadcast, so the row gathers do not wait on the index loads one by one.
 template<int LANES>
 __global__ void __launch_bounds__(128)
     k_ave(uint32_t n, const uint2* __restrict__ ij, const uint32_t* __restrict__ seg, const uint32_t* __restrict__ cnt,
@@ -191,60 +236,62 @@ __global__ void __launch_bounds__(128)
     const int groups_per_block = blockDim.x / LANES;
     const unsigned gmask = LANES == 32 ? FULL : (((1u << LANES) - 1u) << (group * LANES));
     const int m = sub;
-    (void) group;
     for (uint32_t i = blockIdx.x * groups_per_block + threadIdx.x / LANES; i < n; i += gridDim.x * groups_per_block)
     {
-        const bool live = true;
-        const uint32_t b0 = live ? seg[i] : 0;
-        const uint32_t b1 = live ? b0 + cnt[i] : 0;
-#pragma unroll
-        for (int k = 0; k < ST_MAX_NL; ++k)
+        const uint32_t b0 = seg[i];
+        const uint32_t nbond = cnt[i];
+        const float cntf = static_cast<float>(1u + nbond);
+        for (int k = 0; k < ls.nl; ++k)
         {
-            if (k >= ls.nl)
-            {
-                break;
-            }
             const int l = ls.l[k];
-            float part = 0.0f;
-            if (live && m <= l)
+            const float2* base_k = qlm + ls.qlm_offset[k];
+            float pr = 0.f, pim = 0.f, nr = 0.f, nim = 0.f;
+            for (uint32_t base = 0; base < nbond; base += LANES)
             {
-                const float2* base = qlm + ls.qlm_offset[k];
-                float pr = 0.f, pim = 0.f, nr = 0.f, nim = 0.f;
-                for (uint32_t e = b0; e < b1; ++e)
+                const uint32_t jl = base + sub < nbond ? ij[b0 + base + sub].y : 0u;
+                const uint32_t nb_here = min(static_cast<uint32_t>(LANES), nbond - base);
+                for (uint32_t t = 0; t < nb_here; ++t)
                 {
-                    const float2* rj = base + static_cast<size_t>(ij[e].y) * (2 * l + 1);
-                    const float2 a = rj[m];
-                    pr += a.x;
-                    pim += a.y;
-                    if (m > 0)
+                    const uint32_t j = __shfl_sync(gmask, jl, t, LANES);
+                    if (m <= l)
                     {
-                        const float2 c = rj[l + m];
-                        nr += c.x;
-                        nim += c.y;
+                        const float2* rj = base_k + static_cast<size_t>(j) * (2 * l + 1);
+                        const float2 a = rj[m];
+                        pr += a.x;
+                        pim += a.y;
+                        if (m > 0)
+                        {
+                            const float2 c = rj[l + m];
+                            nr += c.x;
+                            nim += c.y;
+                        }
                     }
                 }
-                const float2* ri = base + static_cast<size_t>(i) * (2 * l + 1);
-                const float cntf = static_cast<float>(1u + (b1 - b0));
+            }
+            float part = 0.0f;
+            if (m <= l)
+            {
+                const float2* ri = base_k + static_cast<size_t>(i) * (2 * l + 1);
                 const float2 a = ri[m];
-                pr = (pr + a.x) / cntf;
-                pim = (pim + a.y) / cntf;
+                const float qr = (pr + a.x) / cntf;
+                const float qi = (pim + a.y) / cntf;
                 float2* out = ave + ls.qlm_offset[k] + static_cast<size_t>(i) * (2 * l + 1);
-                out[m] = make_float2(pr, pim);
-                part = pr * pr + pim * pim;
+                out[m] = make_float2(qr, qi);
+                part = qr * qr + qi * qi;
                 if (m > 0)
                 {
                     const float2 c = ri[l + m];
-                    nr = (nr + c.x) / cntf;
-                    nim = (nim + c.y) / cntf;
-                    out[l + m] = make_float2(nr, nim);
-                    part += nr * nr + nim * nim;
+                    const float vr = (nr + c.x) / cntf;
+                    const float vi = (nim + c.y) / cntf;
+                    out[l + m] = make_float2(vr, vi);
+                    part += vr * vr + vi * vi;
                 }
             }
             for (int o = LANES / 2; o > 0; o >>= 1)
             {
                 part += __shfl_xor_sync(gmask, part, o, LANES);
             }
-            if (live && sub == 0)
+            if (sub == 0)
             {
                 ql_ave[static_cast<size_t>(i) * ls.nl + k] = sqrtf(part * ls.norm[k]);
             }
@@ -306,36 +353,6 @@ __global__ void __launch_bounds__(128)
 }
 
 // FP64 column sums: sys[c] += sum_i src[i, c] / n over a row range, compensated.
-__global__ void k_sys(uint32_t n, int ncols, size_t offset, const float2* __restrict__ src, double* sys)
-{
-    const int c = threadIdx.x;
-    if (c >= ncols)
-    {
-        return;
-    }
-    const uint32_t rows_per_block = (n + gridDim.x - 1) / gridDim.x;
-    const uint32_t r0 = blockIdx.x * rows_per_block;
-    const uint32_t r1 = min(n, r0 + rows_per_block);
-    double sr = 0.0, si = 0.0, cr = 0.0, ci = 0.0;
-    for (uint32_t r = r0; r < r1; ++r)
-    {
-        const float2 v = src[offset + static_cast<size_t>(r) * ncols + c];
-        const double yr = static_cast<double>(v.x) / n - cr;
-        const double tr = sr + yr;
-        cr = (tr - sr) - yr;
-        sr = tr;
-        const double yi = static_cast<double>(v.y) / n - ci;
-        const double ti = si + yi;
-        ci = (ti - si) - yi;
-        si = ti;
-    }
-    if (r1 > r0)
-    {
-        atomicAdd(&sys[2 * c], sr);
-        atomicAdd(&sys[2 * c + 1], si);
-    }
-}
-
 int sm_count()
 {
     int dev = 0;
@@ -409,21 +426,44 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
     uint32_t blocks = (n + groups - 1) / groups;
     const uint32_t cap = static_cast<uint32_t>(sm_count()) * 16;
     blocks = blocks < cap ? blocks : cap;
+    const int nlt = ls.nl <= 1 ? 1 : (ls.nl <= 2 ? 2 : (ls.nl <= 5 ? 5 : ST_MAX_NL));
+    auto go = [&](auto kernel, const char* name) {
+        ProfScope prof_(name, s);
+        kernel<<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
+    };
     if (lanes == 8)
-        {
-            ProfScope prof_("k_qlm<8>", s);
-            k_qlm<8><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
-        }
+    {
+        if (nlt == 1)
+            go(k_qlm<8, 1>, "k_qlm<8>");
+        else if (nlt == 2)
+            go(k_qlm<8, 2>, "k_qlm<8>");
+        else if (nlt == 5)
+            go(k_qlm<8, 5>, "k_qlm<8>");
+        else
+            go(k_qlm<8, ST_MAX_NL>, "k_qlm<8>");
+    }
     else if (lanes == 16)
-        {
-            ProfScope prof_("k_qlm<16>", s);
-            k_qlm<16><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
-        }
+    {
+        if (nlt == 1)
+            go(k_qlm<16, 1>, "k_qlm<16>");
+        else if (nlt == 2)
+            go(k_qlm<16, 2>, "k_qlm<16>");
+        else if (nlt == 5)
+            go(k_qlm<16, 5>, "k_qlm<16>");
+        else
+            go(k_qlm<16, ST_MAX_NL>, "k_qlm<16>");
+    }
     else
-        {
-            ProfScope prof_("k_qlm<32>", s);
-            k_qlm<32><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
-        }
+    {
+        if (nlt == 1)
+            go(k_qlm<32, 1>, "k_qlm<32>");
+        else if (nlt == 2)
+            go(k_qlm<32, 2>, "k_qlm<32>");
+        else if (nlt == 5)
+            go(k_qlm<32, 5>, "k_qlm<32>");
+        else
+            go(k_qlm<32, ST_MAX_NL>, "k_qlm<32>");
+    }
 }
 
 void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
@@ -478,23 +518,5 @@ void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float
     }
 }
 
-void launch_sys(uint32_t n, const StLs& ls, const float2* src, double* sys, cudaStream_t s)
-{
-    if (n == 0)
-    {
-        return;
-    }
-    size_t col_off = 0;
-    for (int k = 0; k < ls.nl; ++k)
-    {
-        const int nm = 2 * ls.l[k] + 1;
-        const uint32_t blocks = static_cast<uint32_t>(sm_count()) * 4;
-        {
-            ProfScope prof_("k_sys", s);
-            k_sys<<<blocks, 64, 0, s>>>(n, nm, ls.qlm_offset[k], src, sys + 2 * col_off);
-        }
-        col_off += nm;
-    }
-}
 
 } // namespace fg

@@ -21,6 +21,7 @@ struct StLs
     int l[ST_MAX_NL];
     size_t qlm_offset[ST_MAX_NL]; // in float2 units
     float norm[ST_MAX_NL];        // float(4 pi / (2l + 1))
+    int sorted_k[ST_MAX_NL];      // k indices ordered by ascending l
 };
 
 void st_upload_tables(cudaStream_t s);
@@ -34,6 +35,5 @@ void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t
                 const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s);
 void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float* w3j_dev, const float* qnorm,
                int normalize, float* wl, cudaStream_t s);
-void launch_sys(uint32_t n, const StLs& ls, const float2* src, double* sys, cudaStream_t s);
 
 } // namespace fg

@@ -78,52 +78,64 @@ class Steinhardt(_PairCompute):
         self._cache = None
         return self
 
-    def _outputs(self):
+    def _dims(self):
+        n = ctypes.c_uint32()
+        _lib.check(_lib.lib.fg_steinhardt_num_particles(self._h, ctypes.byref(n)))
+        nf = ctypes.c_uint32()
+        _lib.check(_lib.lib.fg_steinhardt_num_frames(self._h, ctypes.byref(nf)))
+        return n.value, nf.value, len(self._ls)
+
+    def _fetch(self, key):
+        """One output array, copied from the device on first access after a compute."""
         if self._cache is None:
-            n = ctypes.c_uint32()
-            _lib.check(_lib.lib.fg_steinhardt_num_particles(self._h, ctypes.byref(n)))
-            n = n.value
-            nl = len(self._ls)
+            self._cache = {}
+        if key in self._cache:
+            return self._cache[key]
+        n, nf, nl = self._dims()
+        if key == "ql":
+            out = np.zeros((n, nl), np.float32)
+            _lib.check(_lib.lib.fg_steinhardt_get(self._h, _lib.ptr(out), None, None, None))
+        elif key == "po":
+            out = np.zeros((n, nl), np.float32)
+            _lib.check(_lib.lib.fg_steinhardt_get(self._h, None, _lib.ptr(out), None, None))
+        elif key == "order":
+            out = np.zeros(nf * nl, np.float32)
+            _lib.check(_lib.lib.fg_steinhardt_get(self._h, None, None, None, _lib.ptr(out)))
+            if nf > 1:
+                out = out.reshape(nf, nl)
+        else:
             stride = sum(2 * l + 1 for l in self._ls)
-            ql = np.zeros((n, nl), np.float32)
-            po = np.zeros((n, nl), np.float32)
             qlm = np.zeros(n * stride * 2, np.float32)
-            nf = ctypes.c_uint32()
-            _lib.check(_lib.lib.fg_steinhardt_num_frames(self._h, ctypes.byref(nf)))
-            order = np.zeros(nf.value * nl, np.float32)
-            _lib.check(_lib.lib.fg_steinhardt_get(self._h, _lib.ptr(ql), _lib.ptr(po), _lib.ptr(qlm),
-                                                  _lib.ptr(order)))
+            _lib.check(_lib.lib.fg_steinhardt_get(self._h, None, None, _lib.ptr(qlm), None))
             qc = qlm.view(np.complex64)
-            per_l, off = [], 0
+            out, off = [], 0
             for l in self._ls:
                 m = 2 * l + 1
-                per_l.append(qc[off:off + n * m].reshape(n, m))
+                out.append(qc[off:off + n * m].reshape(n, m))
                 off += n * m
-            if nf.value > 1:
-                order = order.reshape(nf.value, nl)
-            self._cache = {"ql": ql, "po": po, "qlm": per_l, "order": order}
-        return self._cache
+        self._cache[key] = out
+        return out
 
     @_Compute._computed_property
     def order(self):
-        order = self._outputs()["order"]
+        order = self._fetch("order")
         if order.ndim == 2:
             return order[:, 0] if order.shape[1] == 1 else order
         return order[0] if len(order) == 1 else order
 
     @_Compute._computed_property
     def particle_order(self):
-        p = self._outputs()["po"]
+        p = self._fetch("po")
         return np.ravel(p) if p.shape[1] == 1 else p
 
     @_Compute._computed_property
     def ql(self):
-        q = self._outputs()["ql"]
+        q = self._fetch("ql")
         return np.ravel(q) if q.shape[1] == 1 else q
 
     @_Compute._computed_property
     def particle_harmonics(self):
-        qlm = self._outputs()["qlm"]
+        qlm = self._fetch("qlm")
         return qlm if len(qlm) > 1 else qlm[0]
 
     def __repr__(self):

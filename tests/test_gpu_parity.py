@@ -233,10 +233,11 @@ def test_empty_result(freud):
 
 
 def test_steinhardt_vs_fp64_oracle(freud):
-    """Ql within 1e-5 relative of the FP64 oracle. Wl: |dw| <= 1e-5 |w| + 2e-6 M, where
-    M is the sum of the magnitudes of the Wigner-3j terms (the float32 qlm feeding
-    the sum carry ~1e-7 relative error, which the cancellation in the sum amplifies
-    by M / |w|); where M / |w| is small this is a 1e-5 relative bound."""
+    """Ql within 1e-5 relative of the FP64 oracle. Wl: |dw| <= 1e-5 (|w| + M), where M
+    is the sum of the magnitudes of the Wigner-3j terms: 1e-5 relative to the scale of
+    the summands. The float32 Ylm / qlm feeding the sum carry ~1e-7 to 1e-6 relative
+    error, which the cancellation in the sum amplifies by M / |w| (W10 of near-perfect
+    FCC nearly cancels); where M / |w| is small this is a 1e-5 relative bound."""
     from golden.make_golden import fcc
 
     box, pts = fcc(6, 1.5874, 0.05, 77)
@@ -251,7 +252,7 @@ def test_steinhardt_vs_fp64_oracle(freud):
     err = np.abs(st.particle_order - w)
     print("max |dw| / |w| per l:", np.max(err / np.abs(w), axis=0))
     print("max |dw| / M per l:", np.max(err / mag, axis=0))
-    assert np.all(err <= 1e-5 * np.abs(w) + 2e-6 * mag)
+    assert np.all(err <= 1e-5 * (np.abs(w) + mag))
     st2 = freud.order.Steinhardt(ls)
     st2.compute((fbox, pts), neighbors={"num_neighbors": 12})
     o2 = O.steinhardt(ls, box, pts, ij, d)
