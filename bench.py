@@ -92,13 +92,13 @@ def c4_frames(freud, seed=4, nframes=64, density=0.85):
     return frames
 
 
-def c5_system(seed=5):
+def c5_system(seed=5, blobs=4096, L=256.0):
     """4,096 isotropic Gaussian blobs (sigma 2.0, 1,024 points each) with centres
-    uniform in a periodic cube of side 256: 4,194,304 points."""
-    L = 256.0
+    uniform in a periodic cube of side 256: 4,194,304 points (a smaller profiling
+    case keeps the blob density: 512 blobs in L = 128)."""
     rng = np.random.default_rng(seed)
-    centres = rng.uniform(0.0, L, (4096, 3))
-    pts = (centres[:, None, :] + rng.normal(0.0, 2.0, (4096, 1024, 3))).reshape(-1, 3)
+    centres = rng.uniform(0.0, L, (blobs, 3))
+    pts = (centres[:, None, :] + rng.normal(0.0, 2.0, (blobs, 1024, 3))).reshape(-1, 3)
     pts = (pts % L) - L / 2
     return L, pts.astype(np.float32)
 
@@ -287,12 +287,12 @@ def measure_c3(freud, _lib, steps, warmup, cpu=True):
     return out
 
 
-def measure_c4(freud, _lib, steps, warmup):
+def measure_c4(freud, _lib, steps, warmup, nframes=64):
     """64 uneven frames: RDF(200, 4.0) accumulated over the frames (reset=False)
     plus Steinhardt(6, average=True) on r_max = 1.5 ball neighbours, per frame
     (plain) and as one FrameBatch (batched), both through the public API with
     host points, results read back every step."""
-    frames = c4_frames(freud)
+    frames = c4_frames(freud, nframes=nframes)
     n_total = sum(len(p) for _, p in frames)
     rdf = freud.density.RDF(200, 4.0)
     st = freud.order.Steinhardt(6, average=True)
@@ -320,7 +320,8 @@ def measure_c4(freud, _lib, steps, warmup):
     t_batch = _median_wall(batched, k, max(1, warmup))
     dev_plain, l_plain, top_plain = _device_ms(_lib, plain, 2)
     dev_batch, l_batch, top_batch = _device_ms(_lib, batched, 2)
-    return {"workload": "batched_uneven_64_frames_rdf_rmax4_bins200_steinhardt6_rmax1.5", "frames": len(frames),
+    return {"workload": "batched_uneven_%d_frames_rdf_rmax4_bins200_steinhardt6_rmax1.5" % len(frames),
+            "frames": len(frames),
             "particles": n_total, "pairs": pairs,
             "plain": {"e2e_ms": t_plain * 1e3, "pair_evals_per_s": pairs / t_plain, "particles_per_s": n_total / t_plain,
                       "device_ms": dev_plain, "launches_per_step": l_plain, "kernels_ms_per_step": top_plain},
@@ -331,10 +332,10 @@ def measure_c4(freud, _lib, steps, warmup):
             "autotune": _lib.autotune_report().strip().splitlines()[-1:] }
 
 
-def measure_c5(freud, _lib, steps, warmup):
+def measure_c5(freud, _lib, steps, warmup, small=False):
     """4,194,304 points in 4,096 Gaussian blobs: RDF(500, 5.0) with uint64 counts
     and FP64 normalisation, Steinhardt(6) on r_max = 1.2 ball neighbours."""
-    L, pts = c5_system()
+    L, pts = c5_system(blobs=512, L=128.0) if small else c5_system()
     box = freud.box.Box.cube(L)
     rdf = freud.density.RDF(500, 5.0)
     st = freud.order.Steinhardt(6)
@@ -357,7 +358,8 @@ def measure_c5(freud, _lib, steps, warmup):
     nc = int(L // 5.0)
     idx = np.floor((pts.astype(np.float64) + L / 2) / L * nc).astype(np.int64) % nc
     occ = np.bincount((idx[:, 0] * nc + idx[:, 1]) * nc + idx[:, 2], minlength=nc ** 3)
-    return {"workload": "blobs_4096x1024_L256_rdf_rmax5_bins500_steinhardt6_rmax1.2", "particles": len(pts),
+    return {"workload": "blobs_%dx1024_L%d_rdf_rmax5_bins500_steinhardt6_rmax1.2" % (len(pts) // 1024, int(L)),
+            "particles": len(pts),
             "pairs": pairs, "pairs_above_2^32": pairs >= 2 ** 32, "e2e_ms": t * 1e3, "e2e": pairs / t,
             "device_ms": dev_ms, "device": pairs / (dev_ms / 1e3), "unit": "pair evals/s (RDF + Steinhardt step)",
             "launches_per_step": launches, "kernels_ms_per_step": top,
@@ -412,8 +414,8 @@ def run_only(args):
     torch.cuda.set_stream(stream)
     fns = {"plain_rdf": lambda: measure_c1(freud, _lib, args.steps, args.warmup, cpu=False),
            "steinhardt": lambda: measure_c3(freud, _lib, args.steps, args.warmup, cpu=False),
-           "batched_frames": lambda: measure_c4(freud, _lib, args.steps, args.warmup),
-           "precision_stress": lambda: measure_c5(freud, _lib, args.steps, args.warmup)}
+           "batched_frames": lambda: measure_c4(freud, _lib, args.steps, args.warmup, 8 if args.small else 64),
+           "precision_stress": lambda: measure_c5(freud, _lib, args.steps, args.warmup, args.small)}
     print(json.dumps({"only": args.only, "result": fns[args.only]()}), flush=True)
     return 0
 
@@ -431,6 +433,8 @@ def main():
                     help="lattice points per side; 102 is the benchmark workload, smaller sizes are for profiling")
     ap.add_argument("--only", default=None, choices=["plain_rdf", "steinhardt", "batched_frames", "precision_stress"],
                     help="run one of the other workloads alone and print its result (profiling)")
+    ap.add_argument("--small", action="store_true",
+                    help="with --only: the profiling-size case (8 frames; 512 blobs in L = 128)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -6,7 +6,7 @@ CUDA library; there is no CPU fallback.
 
 from . import box, data, density, locality, order, parallel
 from .box import Box
-from .locality import AABBQuery, FrameBatch, LinkCell, NeighborList
+from .locality import AABBQuery, CellQuery, FrameBatch, LinkCell, NeighborList
 
 __version__ = "0.1.0"
 

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libfreud_gb300.so")
 
 FG_OK, FG_ERR_VALUE, FG_ERR_RUNTIME, FG_ERR_INDEX, FG_ERR_CUDA, FG_ERR_MEMORY = range(6)
 MODE_NONE, MODE_BALL, MODE_NEAREST = 0, 1, 2
-NQ_RAWPOINTS, NQ_AABB, NQ_LINKCELL = 0, 1, 2
+NQ_RAWPOINTS, NQ_AABB, NQ_LINKCELL, NQ_CELLQUERY = 0, 1, 2, 3
 DEFAULT_NUM_NEIGHBORS = 0xFFFFFFFF
 
 

@@ -299,6 +299,10 @@ struct GridEntry
     int dim[3];
     int ncell;
     DevBuf start, cpos, cidx;
+    // ghost grid of a CellQuery (r_cut = the query's r_max)
+    bool ghost = false;
+    float r_cut = 0.0f;
+    GhostParams gp {};
 };
 
 struct fg_nq
@@ -311,6 +315,7 @@ struct fg_nq
     const float* dpts;
     DevBuf own;
     std::vector<std::unique_ptr<GridEntry>> grids;
+    std::vector<std::unique_ptr<GridEntry>> ghost_grids; // CellQuery, per r_cut
 };
 
 struct fg_nlist
@@ -461,11 +466,18 @@ DevGrid view(const GridEntry& g)
     d.start = g.start.as<uint32_t>();
     d.cpos = g.cpos.as<float4>();
     d.cidx = g.cidx.as<uint32_t>();
+    if (g.ghost)
+    {
+        d.ghost = 1;
+        for (int a = 0; a < 3; ++a)
+            d.gmin[a] = g.gp.gmin[a];
+        d.ginv = g.gp.ginv;
+    }
     return d;
 }
 
-// QueryArgs validation and mode inference (NeighborQuery.h:195-228, 278-292).
-void validate_args(fg_query_args& a)
+// Mode inference and the mode's required arguments (NeighborQuery.h:195-228, 278-292).
+void infer_mode(fg_query_args& a)
 {
     if (a.mode == FG_MODE_NONE)
     {
@@ -493,11 +505,113 @@ void validate_args(fg_query_args& a)
     {
         runtime_error("Unknown mode");
     }
-    // per-point iterator checks (NeighborQuery.h:315-329)
+}
+
+// QueryArgs validation: inference, then the per-point iterator checks
+// (NeighborQuery.h:315-329).
+void validate_args(fg_query_args& a)
+{
+    infer_mode(a);
     if (a.r_max <= 0.0f)
         value_error("NeighborQuery requires r_max to be positive.");
     if (a.r_max <= a.r_min)
         value_error("NeighborQuery requires that r_max must be greater than r_min.");
+}
+
+// CellQuery::validateQueryArgs (CellQuery.h:173-199): ball queries only, 2 r_max
+// below every nearest-plane distance, then its own r_max checks.
+void validate_cellquery_args(const HostBox& box, fg_query_args& a)
+{
+    infer_mode(a);
+    if (a.mode == FG_MODE_NEAREST)
+        runtime_error("CellQuery only supports ball queries (r_max), not nearest queries (num_neighbors). Use "
+                      "AABBQuery for nearest neighbor queries.");
+    float pd[3];
+    nearest_plane(box, pd);
+    if (pd[0] <= a.r_max * 2.0f || pd[1] <= a.r_max * 2.0f || (!box.is2d && pd[2] <= a.r_max * 2.0f))
+        runtime_error("The CellQuery r_max is too large for this box.");
+    if (a.r_max <= 0.0f)
+        value_error("r_max must be positive.");
+    if (a.r_max <= a.r_min)
+        value_error("r_max must be greater than r_min.");
+}
+
+// CellQuery::setupGrid (CellQuery.h:143-167) in float, plus the ghost rule's
+// fractional r_cut and lattice vectors (CellQuery.cc:92-98).
+GhostParams ghost_setup(const HostBox& b, const DevBox& db, float r_cut)
+{
+    GhostParams gp;
+    gp.b = db;
+    gp.ginv = fdiv(1.0f, r_cut);
+    const float wx = fadd(fadd(b.L[0], fmul(b.L[1], std::abs(b.xy))), fmul(b.L[2], std::abs(b.xz)));
+    const float wy = fadd(b.L[1], fmul(b.L[2], std::abs(b.yz)));
+    const float wz = b.L[2];
+    gp.dim[0] = static_cast<int>(fmul(wx, gp.ginv)) + 3;
+    gp.dim[1] = static_cast<int>(fmul(wy, gp.ginv)) + 3;
+    gp.dim[2] = static_cast<int>(fmul(wz, gp.ginv)) + 3;
+    const float bmx = fadd(fmul(b.L[1], std::min(0.0f, b.xy)), fmul(b.L[2], std::min(0.0f, b.xz)));
+    const float bmy = fmul(b.L[2], std::min(0.0f, b.yz));
+    // Box::makeAbsolute({0, 0, 0}) (Box.h:212-222)
+    float ax = fadd(db.lo[0], fmul(0.0f, b.L[0]));
+    float ay = fadd(db.lo[1], fmul(0.0f, b.L[1]));
+    float az = fadd(db.lo[2], fmul(0.0f, b.L[2]));
+    ax = fadd(ax, fadd(fmul(b.xy, ay), fmul(b.xz, az)));
+    ay = fadd(ay, fmul(b.yz, az));
+    if (b.is2d)
+        az = 0.0f;
+    gp.gmin[0] = fadd(fsub(bmx, r_cut), ax);
+    gp.gmin[1] = fadd(fsub(bmy, r_cut), ay);
+    gp.gmin[2] = fadd(-r_cut, az);
+    float pd[3];
+    nearest_plane(b, pd);
+    for (int a = 0; a < 3; ++a)
+        gp.fr[a] = fdiv(r_cut, pd[a]);
+    const float lat[3][3] = {{b.L[0], 0.0f, 0.0f},
+                             {fmul(b.L[1], b.xy), b.L[1], 0.0f},
+                             {b.is2d ? 0.0f : fmul(b.L[2], b.xz), b.is2d ? 0.0f : fmul(b.L[2], b.yz),
+                              b.is2d ? 0.0f : b.L[2]}};
+    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c)
+            gp.lat[i][c] = lat[i][c];
+    return gp;
+}
+
+// Counting sort of points (with_ghosts: and their ghosts) into the ghost grid.
+void build_ghost_grid(const GhostParams& gp, const float* dpts, uint32_t n, int with_ghosts, GridEntry& g)
+{
+    cudaStream_t s = stream();
+    g.ghost = true;
+    g.gp = gp;
+    g.dim[0] = gp.dim[0];
+    g.dim[1] = gp.dim[1];
+    g.dim[2] = gp.dim[2];
+    const size_t ncell = static_cast<size_t>(gp.dim[0]) * gp.dim[1] * gp.dim[2];
+    if (ncell >= (1ull << 31))
+        runtime_error("The CellQuery grid is too large.");
+    g.ncell = static_cast<int>(ncell);
+    DevBuf copy_cell, copy_rank, counts, scratch, cpos0, cidx0;
+    copy_cell.alloc(sizeof(uint32_t) * 8 * static_cast<size_t>(n));
+    copy_rank.alloc(sizeof(uint32_t) * 8 * static_cast<size_t>(n));
+    counts.alloc(sizeof(uint32_t) * (ncell + 2));
+    g.start.alloc(sizeof(uint32_t) * (ncell + 2));
+    scratch.alloc(scan_scratch_bytes(ncell + 2));
+    FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (ncell + 2), s));
+    launch_ghost_count(gp, dpts, n, with_ghosts, copy_cell.as<uint32_t>(), copy_rank.as<uint32_t>(),
+                       counts.as<uint32_t>(), s);
+    scan_u32_to_u32(counts.as<uint32_t>(), g.start.as<uint32_t>(), ncell + 2, scratch.p, s);
+    uint32_t total = 0;
+    FG_CUDA(cudaMemcpyAsync(&total, g.start.as<uint32_t>() + ncell + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    sync();
+    cpos0.alloc(sizeof(float4) * std::max<uint32_t>(total, 1));
+    cidx0.alloc(sizeof(uint32_t) * std::max<uint32_t>(total, 1));
+    g.cpos.alloc(sizeof(float4) * std::max<uint32_t>(total, 1));
+    g.cidx.alloc(sizeof(uint32_t) * std::max<uint32_t>(total, 1));
+    launch_ghost_scatter(gp, dpts, n, with_ghosts, copy_cell.as<uint32_t>(), copy_rank.as<uint32_t>(),
+                         g.start.as<uint32_t>(), cpos0.as<float4>(), cidx0.as<uint32_t>(), s);
+    // cells sorted by point index, so candidate sets are unions of sorted runs
+    launch_sort_cells(g.start.as<uint32_t>(), g.ncell + 1, cpos0.as<float4>(), cidx0.as<uint32_t>(),
+                      g.cpos.as<float4>(), g.cidx.as<uint32_t>(), s);
+    FG_CUDA(cudaGetLastError());
 }
 
 void check_periodic(const HostBox& b)
@@ -568,11 +682,40 @@ Prefilter prefilter(const fg_nq* nq, int arith, const int dim[3], float r_max, f
     return pf;
 }
 
+// The CellQuery ghost grid for r_cut (cached on the NeighborQuery; the
+// reference rebuilds it for every query, CellQuery.cc:26-30).
+GridEntry& nq_ghost_grid(fg_nq* nq, float r_cut)
+{
+    for (auto& g : nq->ghost_grids)
+    {
+        if (g->r_cut == r_cut)
+            return *g;
+    }
+    if (nq->ghost_grids.size() >= 2)
+        nq->ghost_grids.erase(nq->ghost_grids.begin());
+    nq->ghost_grids.push_back(std::make_unique<GridEntry>());
+    GridEntry& g = *nq->ghost_grids.back();
+    g.r_cut = r_cut;
+    build_ghost_grid(ghost_setup(nq->box, nq->dbox, r_cut), nq->dpts, nq->n, 1, g);
+    return g;
+}
+
+// Query points (the object's points when dq is NULL) in the cells of a ghost
+// grid; points outside the grid go to the bucket past the last cell.
+void make_ghost_query_set(fg_nq* nq, const GridEntry& g, const float* dq, uint32_t nqp, QuerySet& qs)
+{
+    build_ghost_grid(g.gp, dq != nullptr ? dq : nq->dpts, nqp, 0, qs.own);
+    qs.qpos = qs.own.cpos.as<float4>();
+    qs.qidx = qs.own.cidx.as<uint32_t>();
+    qs.qg = view(qs.own);
+}
+
 // Ball query -> NeighborList in reference order (count, scan, emit).
 void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a, int by_distance, fg_nlist& out)
 {
     cudaStream_t s = stream();
-    const int arith = nq->kind == FG_NQ_LINKCELL ? ARITH_WRAP : ARITH_AABB;
+    const int arith =
+        nq->kind == FG_NQ_LINKCELL ? ARITH_WRAP : (nq->kind == FG_NQ_CELLQUERY ? ARITH_GHOST : ARITH_AABB);
     if (arith == ARITH_AABB)
     {
         // updateImageVectors(r_max, true), NeighborQuery.h:504-509
@@ -582,10 +725,23 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
             runtime_error("The AABBQuery r_max is too large for this box.");
     }
     int dim[3];
-    grid_dims(nq->box, a.r_max * (1.0f + 1e-5f), nq->n, dim);
-    GridEntry& g = nq_grid(nq, dim);
     QuerySet qs;
-    make_query_set(nq, g, dq, nqp, qs);
+    GridEntry* gptr = nullptr;
+    if (arith == ARITH_GHOST)
+    {
+        gptr = &nq_ghost_grid(nq, a.r_max);
+        dim[0] = gptr->dim[0];
+        dim[1] = gptr->dim[1];
+        dim[2] = gptr->dim[2];
+        make_ghost_query_set(nq, *gptr, dq, nqp, qs);
+    }
+    else
+    {
+        grid_dims(nq->box, a.r_max * (1.0f + 1e-5f), nq->n, dim);
+        gptr = &nq_grid(nq, dim);
+        make_query_set(nq, *gptr, dq, nqp, qs);
+    }
+    GridEntry& g = *gptr;
     BallParams p;
     p.r_max_sq = fmul(a.r_max, a.r_max);
     p.r_min_sq = fmul(a.r_min, a.r_min);
@@ -779,7 +935,10 @@ void run_query(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args* ar
     fg_query_args a = *args;
     if (nq->kind != FG_NQ_RAWPOINTS)
         check_periodic(nq->box);
-    validate_args(a);
+    if (nq->kind == FG_NQ_CELLQUERY)
+        validate_cellquery_args(nq->box, a);
+    else
+        validate_args(a);
     if (a.mode == FG_MODE_BALL)
         ball_nlist(nq, dq, nqp, a, by_distance, out);
     else
@@ -809,7 +968,7 @@ void upload_points(const float* host, uint32_t n, DevBuf& buf)
 
 void nq_init(fg_nq* nq, const fg_box* box, uint32_t n, int kind, float cell_width, const float* host_pts_for_check)
 {
-    if (kind < FG_NQ_RAWPOINTS || kind > FG_NQ_LINKCELL)
+    if (kind < FG_NQ_RAWPOINTS || kind > FG_NQ_CELLQUERY)
         value_error("unknown neighbour-query kind");
     if (n == 0)
         value_error("Cannot create a NeighborQuery with 0 particles.");
@@ -1464,10 +1623,14 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
         fg_query_args a = *args;
         if (nq->kind != FG_NQ_RAWPOINTS)
             check_periodic(nq->box);
-        validate_args(a);
+        if (nq->kind == FG_NQ_CELLQUERY)
+            validate_cellquery_args(nq->box, a);
+        else
+            validate_args(a);
         if (a.mode == FG_MODE_BALL)
         {
-            const int arith = nq->kind == FG_NQ_LINKCELL ? ARITH_WRAP : ARITH_AABB;
+            const int arith =
+                nq->kind == FG_NQ_LINKCELL ? ARITH_WRAP : (nq->kind == FG_NQ_CELLQUERY ? ARITH_GHOST : ARITH_AABB);
             if (arith == ARITH_AABB)
             {
                 float pd[3];
@@ -1476,10 +1639,23 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
                     runtime_error("The AABBQuery r_max is too large for this box.");
             }
             int dim[3];
-            grid_dims(nq->box, a.r_max * (1.0f + 1e-5f), nq->n, dim);
-            GridEntry& g = nq_grid(nq, dim);
             QuerySet qs;
-            make_query_set(nq, g, dq, nqp, qs);
+            GridEntry* gptr = nullptr;
+            if (arith == ARITH_GHOST)
+            {
+                gptr = &nq_ghost_grid(nq, a.r_max);
+                dim[0] = gptr->dim[0];
+                dim[1] = gptr->dim[1];
+                dim[2] = gptr->dim[2];
+                make_ghost_query_set(nq, *gptr, dq, nqp, qs);
+            }
+            else
+            {
+                grid_dims(nq->box, a.r_max * (1.0f + 1e-5f), nq->n, dim);
+                gptr = &nq_grid(nq, dim);
+                make_query_set(nq, *gptr, dq, nqp, qs);
+            }
+            GridEntry& g = *gptr;
             BallParams p;
             p.r_max_sq = fmul(a.r_max, a.r_max);
             p.r_min_sq = fmul(a.r_min, a.r_min);
@@ -2683,7 +2859,8 @@ namespace fg {
 // order, so no sorted list is built.
 bool steinhardt_ball_single(fg_steinhardt* st, fg_nq* nq, const fg_query_args* args)
 {
-    if (nq->kind == FG_NQ_LINKCELL || !(nq->box.periodic[0] && nq->box.periodic[1] && nq->box.periodic[2]))
+    if ((nq->kind != FG_NQ_RAWPOINTS && nq->kind != FG_NQ_AABB) ||
+        !(nq->box.periodic[0] && nq->box.periodic[1] && nq->box.periodic[2]))
         return false;
     fg_query_args a = *args;
     validate_args(a);

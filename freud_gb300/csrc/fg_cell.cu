@@ -91,6 +91,13 @@ __device__ __forceinline__ bool exact_vec(const DevBox& b, const float (*img)[3]
         box_wrap(b, __fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z), rx, ry, rz);
         return true;
     }
+    if (arith == ARITH_GHOST)
+    {
+        rx = __fsub_rn(p.x, q.x);
+        ry = __fsub_rn(p.y, q.y);
+        rz = __fsub_rn(p.z, q.z);
+        return true;
+    }
     const int pimg = __float_as_int(p.w);
     const int kx = img_ax(pimg, 0) - img_ax(qimg, 0) - (wrap % 3 - 1);
     const int ky = img_ax(pimg, 1) - img_ax(qimg, 1) - ((wrap / 3) % 3 - 1);
@@ -124,8 +131,22 @@ __device__ void cell_items(const DevBox& b, const DevGrid& g, int arith, int c, 
     const int cx = c % g.dim[0];
     uint32_t cnt = 0, st = 0;
     int wr = 13;
-    const int nst = b.is2d ? 9 : 27;
-    if (lane < nst)
+    // the ghost grid has real cells in z (3 layers in 2D) and no wrap: the 27
+    // neighbours clipped to the grid (CellIterator.h:105-146)
+    const int nst = (b.is2d && arith != ARITH_GHOST) ? 9 : 27;
+    if (arith == ARITH_GHOST && lane < 27)
+    {
+        const int ux = cx + lane % 3 - 1;
+        const int uy = cy + (lane / 3) % 3 - 1;
+        const int uz = cz + lane / 9 - 1;
+        if (ux >= 0 && uy >= 0 && uz >= 0 && ux < g.dim[0] && uy < g.dim[1] && uz < g.dim[2])
+        {
+            const int cell = ux + g.dim[0] * (uy + g.dim[1] * uz);
+            st = g.start[cell];
+            cnt = g.start[cell + 1] - st;
+        }
+    }
+    else if (lane < nst)
     {
         const int dx = lane % 3 - 1;
         const int dy = (lane / 3) % 3 - 1;
@@ -391,6 +412,45 @@ __global__ void __launch_bounds__(STHREADS, 3)
                         }
                     };
                     uint32_t qq = 0;
+                    if (p.arith == ARITH_GHOST)
+                    {
+                        // stored copies: r = g - q, every pair tested in place
+                        float4 pp = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (live)
+                            pp = MODE == SM_HIST ? S.pos[t] : g.cpos[S.slot[t] >> 5];
+                        for (; qq < nb; ++qq)
+                        {
+                            const float4 q = S.q[qq];
+                            const bool ok = live && (MODE == SM_COUNT || !(p.exclude_ii && jj == S.qi[qq]));
+                            bool acc = false;
+                            float rsq = 0.f;
+                            if (ok)
+                            {
+                                rsq = dot3(__fsub_rn(pp.x, q.x), __fsub_rn(pp.y, q.y), __fsub_rn(pp.z, q.z));
+                                acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
+                            }
+                            if (MODE == SM_COUNT)
+                            {
+                                const unsigned am = __ballot_sync(FULL, acc);
+                                if (lane == 0)
+                                    S.mask[qq][ch] = am;
+                            }
+                            else if (acc)
+                            {
+                                const float d = __fsqrt_rn(rsq);
+                                if (!(d < h.h_min || d >= h.h_max))
+                                {
+                                    uint32_t bin = static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
+                                    if (bin == h.bins)
+                                        bin = h.bins - 1;
+                                    if (smem_hist)
+                                        atomicAdd(&S.u.hist[bin], 1u);
+                                    else
+                                        atomicAdd(&hist[bin], 1ull);
+                                }
+                            }
+                        }
+                    }
                     if (p.arith == ARITH_AABB)
                     {
                         // AABB arithmetic is cheap, so every pair is tested exactly in place:

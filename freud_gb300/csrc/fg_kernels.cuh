@@ -13,6 +13,7 @@ enum Arith : int
 {
     ARITH_AABB = 0, // r = p_j - (q + image)   AABBQuery.cc:93,125 (also RawPoints, the default)
     ARITH_WRAP = 1, // r = box.wrap(p_j - q)   LinkCell.cc:522
+    ARITH_GHOST = 2, // r = g_j - q, g_j a stored copy (point or ghost)   CellIterator.h:173
 };
 
 // Cell-sorted view of a point set: points reordered by cell, with cell offsets.
@@ -23,7 +24,34 @@ struct DevGrid
     const uint32_t* start; // ncell + 1 exclusive offsets
     const float4* cpos;    // positions sorted by cell; w = packed integer box image
     const uint32_t* cidx;  // original point index of each sorted slot
+    // Ghost grid (ARITH_GHOST): axis-aligned cells of width 1 / ginv from gmin,
+    // no wrap; a cell of position p is floor((p - gmin) * ginv) (CellQuery.h:53-59)
+    int ghost = 0;
+    float gmin[3] = {0.0f, 0.0f, 0.0f};
+    float ginv = 0.0f;
 };
+
+// Ghost grid of a CellQuery (CellQuery.h:143-167, 218-299; CellQuery.cc:55-137):
+// every point plus the ghost copies p + shift of points within r_cut (in
+// fractional units fr) of a box face, on a padded axis-aligned grid.
+struct GhostParams
+{
+    DevBox b;
+    float fr[3];     // r_cut / nearest-plane distance, per axis
+    float lat[3][3]; // lattice vectors (Box::getLatticeVector), lat[2] = 0 in 2D
+    float gmin[3];
+    float ginv;      // 1 / r_cut
+    int dim[3];
+};
+// with_ghosts = 1: point grid (point + ghosts; copies outside the grid dropped).
+// with_ghosts = 0: query grid (the point only; outside the grid -> bucket cell
+// dim[0] * dim[1] * dim[2], which the kernels never visit).
+// cell_count: ncell + 2 entries, zeroed. copy_cell / copy_rank: 8 per point.
+void launch_ghost_count(const GhostParams& gp, const float* pts, uint32_t n, int with_ghosts, uint32_t* copy_cell,
+                        uint32_t* copy_rank, uint32_t* cell_count, cudaStream_t s);
+void launch_ghost_scatter(const GhostParams& gp, const float* pts, uint32_t n, int with_ghosts,
+                          const uint32_t* copy_cell, const uint32_t* copy_rank, const uint32_t* start, float4* cpos,
+                          uint32_t* cidx, cudaStream_t s);
 
 // Per-query staging capacity of the warp-per-query emit kernel; queries with more
 // bonds are written by the block-per-query kernel.

@@ -52,6 +52,27 @@ struct Stencil
 __device__ __forceinline__ void query_cell(const DevBox& b, const DevGrid& g, float4 q, int& cx, int& cy, int& cz,
                                            int& img)
 {
+    if (g.ghost)
+    {
+        // ghost grid: axis-aligned cell, cx = -1 outside the grid (no bonds,
+        // CellIterator.h:52-57)
+        const float fx = floorf(__fmul_rn(__fsub_rn(q.x, g.gmin[0]), g.ginv));
+        const float fy = floorf(__fmul_rn(__fsub_rn(q.y, g.gmin[1]), g.ginv));
+        const float fz = floorf(__fmul_rn(__fsub_rn(q.z, g.gmin[2]), g.ginv));
+        img = 0;
+        if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f && fx < static_cast<float>(g.dim[0])
+            && fy < static_cast<float>(g.dim[1]) && fz < static_cast<float>(g.dim[2]))
+        {
+            cx = static_cast<int>(fx);
+            cy = static_cast<int>(fy);
+            cz = static_cast<int>(fz);
+        }
+        else
+        {
+            cx = cy = cz = -1;
+        }
+        return;
+    }
     float fx, fy, fz;
     make_fractional(b, q.x, q.y, q.z, fx, fy, fz);
     const float nx = floorf(fx);
@@ -87,7 +108,23 @@ __device__ __forceinline__ Stencil build_stencil(const DevBox& b, const DevGrid&
     st.count = 0;
     st.wrap = 13;
     const int nst = b.is2d ? 9 : 27;
-    if (lane < nst)
+    if (arith == ARITH_GHOST)
+    {
+        // no wrap: the 27 neighbours clipped to the grid; none for a query outside it
+        if (lane < 27 && cx >= 0)
+        {
+            const int ux = cx + lane % 3 - 1;
+            const int uy = cy + (lane / 3) % 3 - 1;
+            const int uz = cz + lane / 9 - 1;
+            if (ux >= 0 && uy >= 0 && uz >= 0 && ux < g.dim[0] && uy < g.dim[1] && uz < g.dim[2])
+            {
+                const int cell = ux + g.dim[0] * (uy + g.dim[1] * uz);
+                st.start = g.start[cell];
+                st.count = g.start[cell + 1] - st.start;
+            }
+        }
+    }
+    else if (lane < nst)
     {
         const int dx = lane % 3 - 1;
         const int dy = (lane / 3) % 3 - 1;
@@ -152,6 +189,13 @@ __device__ __forceinline__ bool pair_vector(const DevBox& b, const float (*img)[
     if (arith == ARITH_WRAP)
     {
         box_wrap(b, __fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z), rx, ry, rz);
+        return true;
+    }
+    if (arith == ARITH_GHOST)
+    {
+        rx = __fsub_rn(p.x, q.x);
+        ry = __fsub_rn(p.y, q.y);
+        rz = __fsub_rn(p.z, q.z);
         return true;
     }
     const int pimg = __float_as_int(p.w);

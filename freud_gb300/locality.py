@@ -258,6 +258,16 @@ class LinkCell(NeighborQuery):
         return out.value
 
 
+class CellQuery(NeighborQuery):
+    """Neighbour queries with freud's CellQuery arithmetic (freud/locality.py:900-921):
+    the points plus ghost copies of those within r_max of a box face, on a padded
+    axis-aligned grid of r_max cells; r = g_j - q (CellIterator.h:173). Ball
+    queries (r_max) only."""
+
+    def __init__(self, box, points):
+        self._init(box, points, _lib.NQ_CELLQUERY)
+
+
 class FrameBatch:
     """Many (box, points) systems of uneven N held on the GPU together, so a
     compute runs over every frame in one launch per stage instead of one

@@ -64,6 +64,7 @@ typedef struct fg_query_args
 #define FG_NQ_RAWPOINTS 0
 #define FG_NQ_AABB 1
 #define FG_NQ_LINKCELL 2
+#define FG_NQ_CELLQUERY 3 /* freud::locality::CellQuery (CellQuery.h:30-318): ball queries only */
 
 typedef struct fg_nq fg_nq;
 typedef struct fg_nlist fg_nlist;

@@ -19,7 +19,8 @@ mkdir -p "$OUT"
 CXX="${CXX:-g++}"
 FLAGS=(-O3 -ffp-contract=off -std=c++17 -fPIC -shared -w
        -I"$HERE/ref_shim" -I"$SRC/box" -I"$SRC/util" -I"$SRC/locality" -I"$SRC/density" -I"$SRC/order")
-SOURCES=("$SRC/locality/LinkCell.cc" "$SRC/locality/AABBQuery.cc" "$SRC/locality/NeighborList.cc"
+SOURCES=("$SRC/locality/LinkCell.cc" "$SRC/locality/AABBQuery.cc" "$SRC/locality/CellQuery.cc"
+         "$SRC/locality/NeighborList.cc"
          "$SRC/locality/NeighborComputeFunctional.cc" "$SRC/density/RDF.cc" "$SRC/order/Steinhardt.cc"
          "$SRC/order/Wigner3j.cc" "$HERE/ref_harness.cpp")
 OBJS=()

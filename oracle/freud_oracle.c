@@ -33,6 +33,7 @@
 
 #define OFG_ARITH_AABB 0 /* r = p_j - (q + image)  (AABBQuery / RawPoints) */
 #define OFG_ARITH_WRAP 1 /* r = wrap(p_j - q)      (LinkCell) */
+#define OFG_ARITH_GHOST 2 /* r = g_j - q, g_j the point or a ghost copy (CellQuery) */
 
 typedef struct
 {
@@ -617,6 +618,179 @@ static void run_query(qctx* c, int nthreads)
     free(args);
 }
 
+/* ------------------------------------------------------------------------- */
+/* CellQuery: ghost copies on a padded axis-aligned grid                      */
+/* ------------------------------------------------------------------------- */
+
+typedef struct
+{
+    float fr[3];     /* r_cut / nearest-plane distance (CellQuery.cc:94) */
+    float lat[3][3]; /* Box::getLatticeVector (Box.h:503-518) */
+    float minp[3];   /* CellQuery::setupGrid (CellQuery.h:143-167) */
+    float inv;
+    int dim[3];
+} oghost;
+
+static void ghost_setup(const obox* b, float r_cut, oghost* G)
+{
+    G->inv = 1.0f / r_cut;
+    const float wx = (b->L[0] + b->L[1] * fabsf(b->xy)) + b->L[2] * fabsf(b->xz);
+    const float wy = b->L[1] + b->L[2] * fabsf(b->yz);
+    const float wz = b->L[2];
+    G->dim[0] = (int) (wx * G->inv) + 3;
+    G->dim[1] = (int) (wy * G->inv) + 3;
+    G->dim[2] = (int) (wz * G->inv) + 3;
+    const float bmx = b->L[1] * fminf(0.0f, b->xy) + b->L[2] * fminf(0.0f, b->xz);
+    const float bmy = b->L[2] * fminf(0.0f, b->yz);
+    const float zero[3] = {0.0f, 0.0f, 0.0f};
+    float a[3];
+    make_absolute(b, zero, a);
+    G->minp[0] = (bmx - r_cut) + a[0];
+    G->minp[1] = (bmy - r_cut) + a[1];
+    G->minp[2] = -r_cut + a[2];
+    float pd[3];
+    nearest_plane(b, pd);
+    for (int d = 0; d < 3; ++d)
+        G->fr[d] = r_cut / pd[d];
+    G->lat[0][0] = b->L[0];
+    G->lat[0][1] = 0.0f;
+    G->lat[0][2] = 0.0f;
+    G->lat[1][0] = b->L[1] * b->xy;
+    G->lat[1][1] = b->L[1];
+    G->lat[1][2] = 0.0f;
+    G->lat[2][0] = b->is2d ? 0.0f : b->L[2] * b->xz;
+    G->lat[2][1] = b->is2d ? 0.0f : b->L[2] * b->yz;
+    G->lat[2][2] = b->is2d ? 0.0f : b->L[2];
+}
+
+/* cell_idx_xyz + getCellIdxSafe (CellQuery.h:53-75); 0 outside the grid */
+static int ghost_cell(const oghost* G, const float* p, int* c)
+{
+    for (int d = 0; d < 3; ++d)
+    {
+        const float f = floorf((p[d] - G->minp[d]) * G->inv);
+        if (!(f >= 0.0f && f < (float) G->dim[d]))
+            return 0;
+        c[d] = (int) f;
+    }
+    return 1;
+}
+
+/* The copies of point p: ghosts (faces, edges, corner; CellQuery.h:218-299),
+ * then p itself. Returns the count (<= 8). */
+static int ghost_copies(const obox* b, const oghost* G, const float* p, float out[8][3])
+{
+    int n = 0;
+    float f[3];
+    make_fractional(b, p, f);
+    const int dx = (int) (f[0] <= G->fr[0]) - (int) ((double) f[0] >= 1.0 - (double) G->fr[0]);
+    const int dy = (int) (f[1] <= G->fr[1]) - (int) ((double) f[1] >= 1.0 - (double) G->fr[1]);
+    int dz = (int) (f[2] <= G->fr[2]) - (int) ((double) f[2] >= 1.0 - (double) G->fr[2]);
+    if (b->is2d)
+        dz = 0;
+    if (dx != 0 || dy != 0 || dz != 0)
+    {
+        const int sites[7][3] = {{dx, 0, 0}, {0, dy, 0}, {0, 0, dz}, {dx, dy, 0}, {dx, 0, dz}, {0, dy, dz}, {dx, dy, dz}};
+        const int use[7] = {dx != 0, dy != 0, dz != 0, dx != 0 && dy != 0, dx != 0 && dz != 0, dy != 0 && dz != 0,
+                            dx != 0 && dy != 0 && dz != 0};
+        for (int s = 0; s < 7; ++s)
+        {
+            if (!use[s])
+                continue;
+            float sh[3] = {0.0f, 0.0f, 0.0f};
+            for (int a = 0; a < 3; ++a)
+            {
+                if (sites[s][a] != 0)
+                {
+                    for (int c = 0; c < 3; ++c)
+                        sh[c] += sites[s][a] == 1 ? G->lat[a][c] : -G->lat[a][c];
+                }
+            }
+            for (int c = 0; c < 3; ++c)
+                out[n][c] = p[c] + sh[c];
+            ++n;
+        }
+    }
+    out[n][0] = p[0];
+    out[n][1] = p[1];
+    out[n][2] = p[2];
+    return n + 1;
+}
+
+/* CellQueryBallIterator (CellIterator.h:35-185): the copies in the 27 cells around
+ * the query's cell (clipped to the grid; no bonds for a query outside it), pair
+ * vector g - q, the reference ball test, exclude_ii on the real index. */
+static void ghost_bonds(const obox* b, const float* pts, uint32_t n, const float* qpts, uint32_t nq, float r_max,
+                        float r_min, int exclude_ii, obonds* out)
+{
+    oghost G;
+    ghost_setup(b, r_max, &G);
+    const size_t ncell = (size_t) G.dim[0] * G.dim[1] * G.dim[2];
+    uint32_t* cnt = (uint32_t*) calloc(ncell + 1, sizeof(uint32_t));
+    float (*cp)[3] = (float (*)[3]) malloc(sizeof(float) * 3 * 8 * (size_t) (n ? n : 1));
+    uint32_t* cj = (uint32_t*) malloc(sizeof(uint32_t) * 8 * (size_t) (n ? n : 1));
+    uint32_t* cc = (uint32_t*) malloc(sizeof(uint32_t) * 8 * (size_t) (n ? n : 1));
+    size_t nc = 0;
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        float copies[8][3];
+        const int k = ghost_copies(b, &G, pts + 3 * (size_t) i, copies);
+        for (int t = 0; t < k; ++t)
+        {
+            int c[3];
+            if (!ghost_cell(&G, copies[t], c))
+                continue;
+            const size_t cell = ((size_t) c[2] * G.dim[1] + c[1]) * G.dim[0] + c[0];
+            memcpy(cp[nc], copies[t], sizeof(float) * 3);
+            cj[nc] = i;
+            cc[nc] = (uint32_t) cell;
+            cnt[cell + 1]++;
+            ++nc;
+        }
+    }
+    for (size_t c = 0; c < ncell; ++c)
+        cnt[c + 1] += cnt[c];
+    uint32_t* fill = (uint32_t*) malloc(sizeof(uint32_t) * (ncell ? ncell : 1));
+    memcpy(fill, cnt, sizeof(uint32_t) * ncell);
+    uint32_t* order = (uint32_t*) malloc(sizeof(uint32_t) * (nc ? nc : 1));
+    for (size_t t = 0; t < nc; ++t)
+        order[fill[cc[t]]++] = (uint32_t) t;
+    const float rmax_sq = r_max * r_max;
+    const float rmin_sq = r_min * r_min;
+    for (uint32_t i = 0; i < nq; ++i)
+    {
+        const float* q = qpts + 3 * (size_t) i;
+        int qc[3];
+        if (!ghost_cell(&G, q, qc))
+            continue;
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx)
+                {
+                    const int x = qc[0] + dx, y = qc[1] + dy, z = qc[2] + dz;
+                    if (x < 0 || y < 0 || z < 0 || x >= G.dim[0] || y >= G.dim[1] || z >= G.dim[2])
+                        continue;
+                    const size_t cell = ((size_t) z * G.dim[1] + y) * G.dim[0] + x;
+                    for (uint32_t u = cnt[cell]; u < cnt[cell + 1]; ++u)
+                    {
+                        const uint32_t t = order[u];
+                        if (exclude_ii && cj[t] == i)
+                            continue;
+                        float r[3] = {cp[t][0] - q[0], cp[t][1] - q[1], cp[t][2] - q[2]};
+                        const float rsq = dot3(r);
+                        if (rsq < rmax_sq && rsq >= rmin_sq)
+                            bonds_push(out, i, cj[t], sqrtf(rsq), r);
+                    }
+                }
+    }
+    free(cnt);
+    free(cp);
+    free(cj);
+    free(cc);
+    free(fill);
+    free(order);
+}
+
 /* Neighbour query producing a NeighborList in reference order
  * (NeighborQuery.h:434-481): sorted by (i, j, weight, distance), or by
  * (i, distance, j, weight) when sort_by_distance. k == 0 selects a ball query.
@@ -627,6 +801,18 @@ int ofg_query(const float* box7, const float* pts, uint32_t n, const float* qpts
 {
     obox box;
     box_init(&box, box7);
+    if (arith == OFG_ARITH_GHOST)
+    {
+        obonds all = {0, 0, 0};
+        ghost_bonds(&box, pts, n, qpts, nq, r_max, r_min, exclude_ii, &all);
+        ofg_nlist* nl = (ofg_nlist*) malloc(sizeof(ofg_nlist));
+        nl->n = all.n;
+        nl->b = all.b ? all.b : (obond*) malloc(sizeof(obond));
+        qsort(nl->b, nl->n, sizeof(obond), sort_by_distance ? cmp_dist : cmp_tuple);
+        *nbonds_out = nl->n;
+        *handle_out = nl;
+        return 0;
+    }
     qctx c;
     memset(&c, 0, sizeof(c));
     c.box = &box;
@@ -709,6 +895,21 @@ int ofg_rdf_query(const float* box7, const float* pts, uint32_t n, const float* 
 {
     obox box;
     box_init(&box, box7);
+    if (arith == OFG_ARITH_GHOST)
+    {
+        obonds all = {0, 0, 0};
+        ghost_bonds(&box, pts, n, qpts, nq, q_r_max, q_r_min, exclude_ii, &all);
+        const float bw = (r_max - r_min) / (float) bins;
+        const float inv = 1.0f / bw;
+        for (size_t t = 0; t < all.n; ++t)
+        {
+            const int64_t bb = hist_bin(all.b[t].d, r_min, r_max, inv, bins);
+            if (bb >= 0)
+                counts[bb]++;
+        }
+        free(all.b);
+        return 0;
+    }
     qctx c;
     memset(&c, 0, sizeof(c));
     c.box = &box;

@@ -17,7 +17,7 @@ _SRC = os.path.join(_HERE, "freud_oracle.c")
 _LIB = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 
-ARITH_AABB, ARITH_WRAP = 0, 1
+ARITH_AABB, ARITH_WRAP, ARITH_GHOST = 0, 1, 2
 
 
 def build(force=False):

@@ -16,7 +16,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_ref", "libfreud_ref.so")
 _lib = None
 
-KIND_RAW, KIND_AABB, KIND_LINKCELL = 0, 1, 2
+KIND_RAW, KIND_AABB, KIND_LINKCELL, KIND_CELLQUERY = 0, 1, 2, 3
 MODE_INFER, MODE_BALL, MODE_NEAREST = 0, 1, 2
 DEFAULT_NUM_NEIGHBORS = 0xFFFFFFFF
 

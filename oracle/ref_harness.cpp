@@ -10,6 +10,7 @@
 //   freud/locality/LinkCell.cc:222-260        LinkCell::LinkCell
 //   freud/locality/AABBQuery.cc:18-24         AABBQuery::AABBQuery
 //   freud/locality/RawPoints.h:30-77          RawPoints (default (box, points) path)
+//   freud/locality/CellQuery.cc:17-137        CellQuery (ghost-particle grid, ball queries)
 //   freud/locality/NeighborList.cc:51-82      NeighborList from arrays
 //   freud/density/RDF.cc:25-110               RDF ctor / accumulate / reduce
 //   freud/order/Steinhardt.cc:85-118          Steinhardt::compute
@@ -21,6 +22,7 @@
 #include <vector>
 
 #include "AABBQuery.h"
+#include "CellQuery.h"
 #include "Box.h"
 #include "LinkCell.h"
 #include "NeighborList.h"
@@ -63,6 +65,10 @@ std::shared_ptr<NeighborQuery> make_nq(int kind, const Box& box, const float* pt
     if (kind == 0)
     {
         return std::make_shared<RawPoints>(box, p, n);
+    }
+    if (kind == 3)
+    {
+        return std::make_shared<CellQuery>(box, p, n);
     }
     if (kind == 1)
     {
@@ -107,7 +113,7 @@ std::shared_ptr<NeighborList> nlist_from(unsigned nbonds, const unsigned* ij, un
 
 extern "C" {
 
-// kind: 0 = RawPoints (AABB arithmetic), 1 = AABBQuery, 2 = LinkCell(cell_width)
+// kind: 0 = RawPoints (AABB arithmetic), 1 = AABBQuery, 2 = LinkCell(cell_width), 3 = CellQuery
 // mode: 0 = infer, 1 = ball, 2 = nearest
 void* ref_query(int kind, const float* box6, int is2d, const float* pts, unsigned n, float cell_width,
                 const float* qpts, unsigned nq, int mode, unsigned num_neighbors, float r_max, float r_min,

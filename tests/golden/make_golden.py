@@ -81,6 +81,35 @@ def main():
             save(name + ("_bydist" if by_dist else ""), box=np.asarray(box, np.float32), points=pts, kind=kind,
                  r_max=np.float32(r_max), r_min=np.float32(r_min), cell_width=np.float32(cw), ij=ij, d=d, v=v)
 
+    # CellQuery (ghost copies; third arithmetic): cubic / triclinic with some points
+    # outside the box (their copies beyond the padded grid are dropped) / 2D
+    def spill_system(L, n, seed, tilt, spill):
+        rs = np.random.RandomState(seed)
+        f = rs.random_sample((n, 3)) * (1 + 2 * spill) - spill
+        box = (L, L, L, tilt[0], tilt[1], tilt[2], 0)
+        return box, absolute(box, f)
+
+    cq_cases = [
+        ("ball_cq_cubic", random_system(8.0, 400, 61), 2.0, 0.0),
+        ("ball_cq_triclinic_spill", spill_system(9.0, 400, 62, (0.3, -0.2, 0.1), 0.06), 2.2, 0.4),
+        ("ball_cq_2d", random_system(10.0, 300, 63, (0.25, 0, 0), is2d=True), 1.7, 0.0),
+    ]
+    for name, (box, pts), r_max, r_min in cq_cases:
+        for by_dist in (False, True):
+            ij, d, w, v = R.query(R.KIND_CELLQUERY, box, pts, pts, mode=R.MODE_BALL, r_max=r_max, r_min=r_min,
+                                  exclude_ii=True, sort_by_distance=by_dist)
+            save(name + ("_bydist" if by_dist else ""), box=np.asarray(box, np.float32), points=pts,
+                 kind=R.KIND_CELLQUERY, r_max=np.float32(r_max), r_min=np.float32(r_min), ij=ij, d=d, v=v)
+    box, pts = random_system(8.0, 300, 64, (0.1, 0.2, 0.0))
+    _, qpts = spill_system(8.0, 120, 65, (0.1, 0.2, 0.0), 0.1)
+    ij, d, w, v = R.query(R.KIND_CELLQUERY, box, pts, qpts, mode=R.MODE_BALL, r_max=1.9, exclude_ii=False)
+    save("ball_cq_query_points", box=np.asarray(box, np.float32), points=pts, query_points=qpts,
+         kind=R.KIND_CELLQUERY, r_max=np.float32(1.9), ij=ij, d=d, v=v)
+    box, pts = random_system(9.0, 800, 66, (0.2, 0.0, 0.1))
+    c, g, nr = R.rdf(90, 2.5, [(box, pts)], kind=R.KIND_CELLQUERY)
+    save("rdf_cellquery", box=np.asarray(box, np.float32), points=pts, bins=90, r_max=np.float32(2.5), counts=c,
+         rdf=g, n_r=nr)
+
     # query points different from the points
     box, pts = random_system(8.0, 300, 21)
     _, qpts = random_system(8.0, 100, 22)

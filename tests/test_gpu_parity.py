@@ -10,8 +10,8 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-KIND_CLASS = {0: "_RawPoints", 1: "AABBQuery", 2: "LinkCell"}
-ARITH = {0: O.ARITH_AABB, 1: O.ARITH_AABB, 2: O.ARITH_WRAP}
+KIND_CLASS = {0: "_RawPoints", 1: "AABBQuery", 2: "LinkCell", 3: "CellQuery"}
+ARITH = {0: O.ARITH_AABB, 1: O.ARITH_AABB, 2: O.ARITH_WRAP, 3: O.ARITH_GHOST}
 
 
 def box_of(freud, b):
@@ -19,6 +19,8 @@ def box_of(freud, b):
 
 
 def make_nq(freud, kind, box, pts, cell_width=0.0):
+    if kind == 3:
+        return freud.locality.CellQuery(box, pts)
     if kind == 2:
         return freud.locality.LinkCell(box, pts, cell_width)
     if kind == 1:
@@ -116,7 +118,7 @@ def random_box_points(freud, L, n, seed, tilt=(0, 0, 0), is2d=False):
     return box, box.make_absolute(f)
 
 
-@pytest.mark.parametrize("kind", [0, 2])
+@pytest.mark.parametrize("kind", [0, 2, 3])
 @pytest.mark.parametrize("tilt", [(0, 0, 0), (0.2, 0.1, 0.0), (-0.4, 0.3, 0.2)])
 def test_ball_vs_oracle_medium(freud, kind, tilt):
     box, pts = random_box_points(freud, 24.0, 20000, 7, tilt)
@@ -258,3 +260,58 @@ def test_steinhardt_vs_fp64_oracle(freud):
     o2 = O.steinhardt(ls, box, pts, ij, d)
     np.testing.assert_allclose(st2.ql, o2["ql"], rtol=1e-5)
     np.testing.assert_allclose(np.atleast_1d(st2.order), o2["order"], rtol=1e-5)
+
+
+# ---- CellQuery (ghost copies; third pair arithmetic) -----------------------------------
+
+def test_rdf_cellquery_golden(freud):
+    g = load_golden("rdf_cellquery")
+    box = box_of(freud, g["box"])
+    rdf = freud.density.RDF(int(g["bins"]), float(g["r_max"]))
+    rdf.compute(freud.locality.CellQuery(box, g["points"]))
+    np.testing.assert_array_equal(rdf.bin_counts, g["counts"])
+    np.testing.assert_array_equal(rdf.rdf, g["rdf"])
+    np.testing.assert_array_equal(rdf.n_r, g["n_r"])
+
+
+@pytest.mark.parametrize("spill", [0.0, 0.08])
+def test_cellquery_points_outside_box(freud, spill):
+    """Points up to 8% of the box outside it: their copies beyond the padded grid are
+    dropped, as the reference drops them; query points partly outside the grid."""
+    rs = np.random.RandomState(5)
+    box = freud.box.Box(14.0, 13.0, 15.0, 0.3, -0.2, 0.1)
+    pts = box.make_absolute(rs.random_sample((6000, 3)) * (1 + 2 * spill) - spill).astype(np.float32)
+    qp = box.make_absolute(rs.random_sample((900, 3)) * 1.3 - 0.15).astype(np.float32)
+    nq = freud.locality.CellQuery(box, pts)
+    nl = nq.query(pts, dict(r_max=2.6, r_min=0.3, exclude_ii=True)).toNeighborList()
+    assert_nlist_equal(nl, *O.query(box, pts, r_max=2.6, r_min=0.3, exclude_ii=True, arith=O.ARITH_GHOST))
+    nl = nq.query(qp, dict(r_max=2.6)).toNeighborList(sort_by_distance=True)
+    assert_nlist_equal(nl, *O.query(box, pts, query_points=qp, r_max=2.6, arith=O.ARITH_GHOST,
+                                    sort_by_distance=True))
+    counts = O.rdf_counts_query(box, pts, 100, 2.6, arith=O.ARITH_GHOST)
+    rdf = freud.density.RDF(100, 2.6).compute(nq)
+    np.testing.assert_array_equal(rdf.bin_counts_u64, counts)
+
+
+def test_cellquery_dense_cells(freud):
+    """Dense clusters (> 1024 candidates per cell) take the warp-per-query path."""
+    rs = np.random.RandomState(8)
+    box = freud.box.Box.cube(20.0)
+    centres = rs.random_sample((6, 3)) * 20 - 10
+    pts = (centres[:, None, :] + rs.normal(0, 0.6, (6, 700, 3))).reshape(-1, 3)
+    pts = box.wrap(pts.astype(np.float32)).astype(np.float32)
+    nq = freud.locality.CellQuery(box, pts)
+    nl = nq.query(pts, dict(r_max=2.0, exclude_ii=True)).toNeighborList()
+    assert_nlist_equal(nl, *O.query(box, pts, r_max=2.0, exclude_ii=True, arith=O.ARITH_GHOST))
+
+
+def test_cellquery_errors(freud):
+    box = freud.box.Box.cube(10.0)
+    pts = np.zeros((4, 3), np.float32)
+    nq = freud.locality.CellQuery(box, pts)
+    with pytest.raises(RuntimeError, match="only supports ball queries"):
+        nq.query(pts, dict(num_neighbors=2)).toNeighborList()
+    with pytest.raises(RuntimeError, match="CellQuery r_max is too large"):
+        nq.query(pts, dict(r_max=5.5)).toNeighborList()
+    with pytest.raises(ValueError, match="r_max must be greater than r_min"):
+        nq.query(pts, dict(r_max=1.0, r_min=2.0)).toNeighborList()

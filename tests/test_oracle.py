@@ -9,7 +9,7 @@ from conftest import golden_names, load_golden
 
 from oracle import oracle as O
 
-ARITH = {0: O.ARITH_AABB, 1: O.ARITH_AABB, 2: O.ARITH_WRAP}
+ARITH = {0: O.ARITH_AABB, 1: O.ARITH_AABB, 2: O.ARITH_WRAP, 3: O.ARITH_GHOST}
 
 
 @pytest.mark.parametrize("name", golden_names("ball_"))
@@ -45,6 +45,12 @@ def test_rdf_plain_matches_reference():
     rdf, nr = O.rdf_reduce(c, float(g["r_max"]), 0.0, 1, len(g["points"]), len(g["points"]), vol)
     np.testing.assert_array_equal(rdf, g["rdf"])
     np.testing.assert_array_equal(nr, g["n_r"])
+
+
+def test_rdf_cellquery_matches_reference():
+    g = load_golden("rdf_cellquery")
+    c = O.rdf_counts_query(g["box"], g["points"], int(g["bins"]), float(g["r_max"]), arith=O.ARITH_GHOST)
+    np.testing.assert_array_equal(c.astype(np.uint32), g["counts"])
 
 
 def test_rdf_frames_matches_reference():
