@@ -354,6 +354,17 @@ def measure_c5(freud, _lib, steps, warmup, small=False):
     dev_ms, launches, top = _device_ms(_lib, step, 1)
     g32, g64 = rdf.rdf.astype(np.float64), rdf.rdf_fp64
     nz = g64 > 0
+    # Steinhardt error against the FP64 oracle on the first 16,384 particles (their
+    # q6 needs only their own bonds: no averaging)
+    from oracle import oracle as O
+
+    m = min(16384, len(pts))
+    bx = (L, L, L, 0.0, 0.0, 0.0, 0.0)
+    ij, d, _ = O.query(bx, pts, query_points=pts[:m], r_max=1.2, exclude_ii=True, arith=O.ARITH_AABB)
+    ref = O.steinhardt([6], bx, pts, ij, d)["ql"][:m, 0]
+    got = np.asarray(st.ql, np.float64)[:m]
+    ok = np.isfinite(ref)
+    ql_err = float(np.max(np.abs(got[ok] - ref[ok]) / np.abs(ref[ok])))
     # occupancy skew of the r_max = 5 cell grid (51^3 cells)
     nc = int(L // 5.0)
     idx = np.floor((pts.astype(np.float64) + L / 2) / L * nc).astype(np.int64) % nc
@@ -364,6 +375,7 @@ def measure_c5(freud, _lib, steps, warmup, small=False):
             "device_ms": dev_ms, "device": pairs / (dev_ms / 1e3), "unit": "pair evals/s (RDF + Steinhardt step)",
             "launches_per_step": launches, "kernels_ms_per_step": top,
             "rdf_f32_vs_fp64_max_rel": float(np.max(np.abs(g32[nz] - g64[nz]) / g64[nz])),
+            "q6_vs_fp64_oracle_max_rel": ql_err, "q6_checked_particles": int(m),
             "cell_occupancy": {"mean": float(occ.mean()), "max": int(occ.max()),
                                "skew_max_over_mean": float(occ.max() / occ.mean())}}
 

@@ -373,8 +373,7 @@ __global__ void __launch_bounds__(WARPS * 32)
 template<bool FILL>
 __global__ void __launch_bounds__(128)
     k_frames_ball(BatchGrid g, BallParams p, uint32_t n, uint32_t* __restrict__ counts,
-                  const uint64_t* __restrict__ offsets, uint2* __restrict__ ij, float* __restrict__ dist,
-                  float* __restrict__ vec)
+                  const uint64_t* __restrict__ offsets, uint32_t* __restrict__ bj, float4* __restrict__ bvd)
 {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
     {
@@ -424,13 +423,10 @@ __global__ void __launch_bounds__(128)
                     if (FILL)
                     {
                         const uint64_t e = o + cnt;
-                        ij[e] = make_uint2(i, j);
-                        dist[e] = __fsqrt_rn(rsq);
                         float dx, dy, dz;
                         box_wrap(F.b, __fsub_rn(pp.x, q.x), __fsub_rn(pp.y, q.y), __fsub_rn(pp.z, q.z), dx, dy, dz);
-                        vec[3 * e] = dx;
-                        vec[3 * e + 1] = dy;
-                        vec[3 * e + 2] = dz;
+                        bj[e] = j;
+                        bvd[e] = make_float4(dx, dy, dz, __fsqrt_rn(rsq));
                     }
                     ++cnt;
                 }
@@ -621,16 +617,16 @@ void launch_frames_ball_count(const BatchGrid& g, const BallParams& p, uint32_t 
     if (n == 0)
         return;
     ProfScope prof_("k_frames_ball<COUNT>", s);
-    k_frames_ball<false><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, counts, nullptr, nullptr, nullptr, nullptr);
+    k_frames_ball<false><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, counts, nullptr, nullptr, nullptr);
 }
 
-void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n, const uint64_t* offsets, uint2* ij,
-                             float* dist, float* vec, cudaStream_t s)
+void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n, const uint64_t* offsets,
+                             uint32_t* bond_j, float4* bond_vd, cudaStream_t s)
 {
     if (n == 0)
         return;
     ProfScope prof_("k_frames_ball<FILL>", s);
-    k_frames_ball<true><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, nullptr, offsets, ij, dist, vec);
+    k_frames_ball<true><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, nullptr, offsets, bond_j, bond_vd);
 }
 
 int frames_sys_splits(uint32_t max_rows)

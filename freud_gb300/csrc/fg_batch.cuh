@@ -67,11 +67,11 @@ void launch_frames_hist(const BatchHistConfig& cfg, const BatchGrid& g, const Ba
 
 // Ball query over every frame (grid of r_max cells, shell 1), thread per query.
 // Count pass: counts[i] = bonds of point i. Fill pass: bonds of point i at
-// offsets[i] in candidate order: (i, j), distance, and the Steinhardt bond
-// vector box.wrap(p_j - p_i) (Steinhardt.cc:155).
+// offsets[i] in candidate order: the neighbour index j and one float4 holding the
+// Steinhardt bond vector box.wrap(p_j - p_i) (Steinhardt.cc:155) and the distance.
 void launch_frames_ball_count(const BatchGrid& g, const BallParams& p, uint32_t n, uint32_t* counts, cudaStream_t s);
-void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n, const uint64_t* offsets, uint2* ij,
-                             float* dist, float* vec, cudaStream_t s);
+void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n, const uint64_t* offsets,
+                             uint32_t* bond_j, float4* bond_vd, cudaStream_t s);
 
 // Per-frame FP64 system sums of the per-l (n, 2l + 1) qlm layout: sys[f][col]
 // (complex, col running over every l's m) = (FP64 sum over the frame's rows) /

@@ -347,6 +347,7 @@ struct fg_steinhardt
     size_t stride = 0; // sum of (2l + 1)
     DevBuf qlm, qlm_ave, ql, ql_ave, wlv, sys;
     std::vector<DevBuf> w3j;
+    std::vector<std::vector<double>> w3j_host; // per l, for the system Wl (computed once)
     std::vector<float> order; // frames x n_l
     uint32_t frames = 1;
     bool computed = false;
@@ -1059,6 +1060,7 @@ double reduce_w3j_host(const double* q, int l, const std::vector<double>& w)
 
 namespace fg {
 bool steinhardt_ball_single(fg_steinhardt* st, fg_nq* nq, const fg_query_args* args);
+bool rdf_ball_single(fg_rdf* rdf, fg_nq* nq, const float* dq, const fg_query_args* args);
 }
 
 extern "C" {
@@ -1608,6 +1610,10 @@ static HistParams hist_params(const fg_rdf* r)
     return h;
 }
 
+// Single-frame (box, points) RDFs through the frames kernels (1) or the
+// block-per-cell kernel of the NeighborQuery's own grid (0).
+static bool g_rdf_single_frames = true;
+
 static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp, const fg_nlist* nlist,
                            const fg_query_args* args)
 {
@@ -1616,6 +1622,10 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
     if (nlist != nullptr)
     {
         launch_hist_distances(nlist->dist.as<float>(), nlist->nb, h, rdf->hist.as<unsigned long long>(), s);
+    }
+    else if (g_rdf_single_frames && rdf_ball_single(rdf, nq, dq, args))
+    {
+        return; // frame counter, box and N updated by the frames path
     }
     else
     {
@@ -1885,9 +1895,11 @@ fg_status fg_steinhardt_create(const uint32_t* ls, uint32_t n_l, int average, in
         for (uint32_t k = 0; k < n_l; ++k)
         {
             DevBuf b;
+            st->w3j_host.emplace_back();
             if (st->wl)
             {
                 const std::vector<double> w = wigner3j_table(static_cast<int>(ls[k]));
+                st->w3j_host.back() = w;
                 std::vector<float> f(w.begin(), w.end());
                 b.alloc(sizeof(float) * f.size());
                 FG_CUDA(cudaMemcpyAsync(b.p, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice, stream()));
@@ -1922,7 +1934,7 @@ static void normalize_system(const fg_steinhardt* st, const double* sys, float* 
         const double qsys = std::sqrt(acc * nf);
         if (st->wl)
         {
-            double v = reduce_w3j_host(&sys[2 * col], l, wigner3j_table(l));
+            double v = reduce_w3j_host(&sys[2 * col], l, st->w3j_host[k]);
             if (st->wl_normalize)
             {
                 const double w = std::sqrt(nf) / qsys;
@@ -2323,7 +2335,7 @@ struct fg_frames
     DevBuf queue;
     GraphCache rdf_graph;
     // Steinhardt workspace
-    DevBuf st_counts, st_offsets, st_scan, st_ij, st_dist, st_vec, st_seg, st_partial, st_sys;
+    DevBuf st_counts, st_offsets, st_scan, st_j, st_vd, st_seg, st_partial, st_sys;
     GraphCache st_graph_a, st_graph_b;
 };
 
@@ -2499,7 +2511,13 @@ BatchHistConfig tuned_config(fg_frames* fr, const BallParams& p, const HistParam
     {
         BatchGridBufs& g = batch_grid(fr, r_max, shell);
         enqueue_grid_build(fr, g, s);
-        const uint32_t limit = g.cell_base_host[nf];
+        uint32_t limit = g.cell_base_host[nf];
+        if (nf == 1 && fr->n[0] > (1u << 20))
+        {
+            // one large frame: a slab of its cells (cells run z-major, so the same
+            // fraction of the box for either stencil)
+            limit = static_cast<uint32_t>(static_cast<double>(limit) * (1u << 20) / fr->n[0]) + 1;
+        }
         const BatchGrid v = batch_view(fr, g);
         for (int warps : {4, 8})
         {
@@ -2644,13 +2662,9 @@ fg_status fg_frames_info(const fg_frames* fr, uint32_t* n_frames, uint64_t* n_po
     });
 }
 
-fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_args* args)
+static void rdf_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_args& a)
 {
-    return guard([&] {
-        require(rdf, "rdf");
-        require(fr, "frames");
-        require(args, "args");
-        const fg_query_args a = batch_args(fr, args);
+    {
         cudaStream_t s = stream();
         const HistParams h = hist_params(rdf);
         BallParams p;
@@ -2681,6 +2695,17 @@ fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_ar
         rdf->box = fr->boxes.back();
         rdf->n_points = fr->n.back();
         rdf->n_query = fr->n.back();
+    }
+}
+
+fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_args* args)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        require(fr, "frames");
+        require(args, "args");
+        const fg_query_args a = batch_args(fr, args);
+        rdf_frames(rdf, fr, a);
     });
 }
 
@@ -2729,9 +2754,8 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
             off += static_cast<size_t>(P) * (2 * st->st.l[k] + 1);
         }
         const int stride = static_cast<int>(st->stride);
-        fr->st_ij.alloc(sizeof(uint2) * std::max<uint64_t>(nb, 1));
-        fr->st_dist.alloc(sizeof(float) * std::max<uint64_t>(nb, 1));
-        fr->st_vec.alloc(sizeof(float) * 3 * std::max<uint64_t>(nb, 1));
+        fr->st_j.alloc(sizeof(uint32_t) * std::max<uint64_t>(nb, 1));
+        fr->st_vd.alloc(sizeof(float4) * std::max<uint64_t>(nb, 1));
         fr->st_seg.alloc(sizeof(uint32_t) * (P + 1));
         const uint32_t max_rows = *std::max_element(fr->n.begin(), fr->n.end());
         fr->st_partial.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * frames_sys_splits(max_rows) * stride);
@@ -2746,8 +2770,7 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
         if (st->wl)
             st->wlv.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
         std::vector<uint64_t> key_b = {
-            g.id, nb, reinterpret_cast<uint64_t>(fr->st_ij.p),
-            reinterpret_cast<uint64_t>(fr->st_dist.p), reinterpret_cast<uint64_t>(fr->st_vec.p),
+            g.id, nb, reinterpret_cast<uint64_t>(fr->st_j.p), reinterpret_cast<uint64_t>(fr->st_vd.p),
             reinterpret_cast<uint64_t>(fr->st_seg.p), reinterpret_cast<uint64_t>(fr->st_partial.p),
             reinterpret_cast<uint64_t>(fr->st_sys.p), reinterpret_cast<uint64_t>(st->qlm.p),
             reinterpret_cast<uint64_t>(st->ql.p), reinterpret_cast<uint64_t>(st->qlm_ave.p),
@@ -2760,19 +2783,20 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
             key_b.push_back(reinterpret_cast<uint64_t>(st->w3j[k].p));
         }
         run_graph(fr->st_graph_b, fr->graphs, key_b, "graph:steinhardt_frames", [&] {
-            launch_frames_ball_fill(v, p, P, fr->st_offsets.as<uint64_t>(), fr->st_ij.as<uint2>(), fr->st_dist.as<float>(),
-                                    fr->st_vec.as<float>(), s);
+            launch_frames_ball_fill(v, p, P, fr->st_offsets.as<uint64_t>(), fr->st_j.as<uint32_t>(),
+                                    fr->st_vd.as<float4>(), s);
             launch_segments_from_offsets(fr->st_counts.as<uint32_t>(), fr->st_offsets.as<uint64_t>(), P,
                                          fr->st_seg.as<uint32_t>(), s);
-            launch_qlm(g.fd_host[0].b, fr->dpts, P, fr->st_ij.as<uint2>(), fr->st_dist.as<float>(), nullptr,
-                       fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st, 0, st->qlm.as<float2>(),
-                       st->ql.as<float>(), s, fr->st_vec.as<float>());
+            launch_qlm(g.fd_host[0].b, fr->dpts, P, nullptr, nullptr, nullptr, fr->st_seg.as<uint32_t>(),
+                       fr->st_counts.as<uint32_t>(), st->st, 0, st->qlm.as<float2>(), st->ql.as<float>(), s,
+                       fr->st_vd.as<float4>());
             const float2* src = st->qlm.as<float2>();
             const float* qn = st->ql.as<float>();
             if (st->average)
             {
-                launch_ave(P, fr->st_ij.as<uint2>(), fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st,
-                           st->qlm.as<float2>(), st->qlm_ave.as<float2>(), st->ql_ave.as<float>(), s);
+                launch_ave(P, nullptr, fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st,
+                           st->qlm.as<float2>(), st->qlm_ave.as<float2>(), st->ql_ave.as<float>(), s,
+                           fr->st_j.as<uint32_t>());
                 src = st->qlm_ave.as<float2>();
                 qn = st->ql_ave.as<float>();
             }
@@ -2857,6 +2881,33 @@ namespace fg {
 // reference sums each particle's bonds in query-iterator order here
 // (Steinhardt.cc:136-147 with loopOverNeighborsIterator), not in NeighborList
 // order, so no sorted list is built.
+// RDF of one (box, points) system with its own ball query (nlist == NULL, the
+// points as query points, AABB arithmetic, periodic box): the frames path with
+// one frame - one grid build and the persistent histogram kernel with the
+// autotuned launch shape. Returns false (caller takes the general path) otherwise.
+bool rdf_ball_single(fg_rdf* rdf, fg_nq* nq, const float* dq, const fg_query_args* args)
+{
+    if (dq != nullptr || (nq->kind != FG_NQ_RAWPOINTS && nq->kind != FG_NQ_AABB) ||
+        !(nq->box.periodic[0] && nq->box.periodic[1] && nq->box.periodic[2]))
+        return false;
+    fg_query_args a = *args;
+    validate_args(a);
+    if (a.mode != FG_MODE_BALL)
+        return false;
+    fg_frames fr;
+    fr.graphs = false;
+    fr.boxes.push_back(nq->box);
+    fr.n.push_back(nq->n);
+    fr.pt_base = {0u, nq->n};
+    fr.total = nq->n;
+    fr.dpts = nq->dpts;
+    fr.d_pt_base.alloc(sizeof(uint32_t) * 2);
+    FG_CUDA(cudaMemcpyAsync(fr.d_pt_base.p, fr.pt_base.data(), sizeof(uint32_t) * 2, cudaMemcpyHostToDevice, stream()));
+    const fg_query_args checked = batch_args(&fr, &a);
+    rdf_frames(rdf, &fr, checked);
+    return true;
+}
+
 bool steinhardt_ball_single(fg_steinhardt* st, fg_nq* nq, const fg_query_args* args)
 {
     if ((nq->kind != FG_NQ_RAWPOINTS && nq->kind != FG_NQ_AABB) ||

@@ -39,7 +39,7 @@ template<int LANES, int NL>
 __global__ void __launch_bounds__(128)
     k_qlm(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
           const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
-          const uint32_t* __restrict__ cnt, const float* __restrict__ bvec, StLs ls, int weighted,
+          const uint32_t* __restrict__ cnt, const float4* __restrict__ bvd, StLs ls, int weighted,
           float2* __restrict__ qlm_out, float* __restrict__ ql_out)
 {
     // recurrence coefficients staged once per block (lanes read different m)
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(128)
         const uint32_t b0 = seg[i];
         const uint32_t nbond = cnt[i];
         float pix = 0.f, piy = 0.f, piz = 0.f;
-        if (bvec == nullptr)
+        if (bvd == nullptr)
         {
             pix = pts[3 * (size_t) i];
             piy = pts[3 * (size_t) i + 1];
@@ -97,21 +97,23 @@ __global__ void __launch_bounds__(128)
             if (base + sub < nbond)
             {
                 const uint32_t e = b0 + base + sub;
-                float dx, dy, dz;
-                if (bvec != nullptr)
+                float dx, dy, dz, d;
+                if (bvd != nullptr)
                 {
-                    dx = bvec[3 * (size_t) e];
-                    dy = bvec[3 * (size_t) e + 1];
-                    dz = bvec[3 * (size_t) e + 2];
+                    const float4 v = bvd[e];
+                    dx = v.x;
+                    dy = v.y;
+                    dz = v.z;
+                    d = v.w;
                 }
                 else
                 {
                     const uint32_t j = ij[e].y;
                     box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pix), __fsub_rn(pts[3 * (size_t) j + 1], piy),
                              __fsub_rn(pts[3 * (size_t) j + 2], piz), dx, dy, dz);
+                    d = dist[e];
                 }
                 g_w = weighted ? weights[e] : 1.0f;
-                const float d = dist[e];
                 g_ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
                 g_st = sqrtf(fmaxf(0.0f, 1.0f - g_ct * g_ct));
                 const float rho = sqrtf(dx * dx + dy * dy);
@@ -129,41 +131,44 @@ __global__ void __launch_bounds__(128)
                 const float cp = __shfl_sync(gmask, g_cp, t, LANES);
                 const float sp = __shfl_sync(gmask, g_sp, t, LANES);
                 const float w = __shfl_sync(gmask, g_w, t, LANES);
-                // One loop of lmax steps for every lane: the first m steps build
-                // e^{i m phi} and sin^m(theta); the rest run the normalised Legendre
-                // recurrence in l divided by K_m sin^m(theta):
-                //   R_m = 1, R_{m+1} = sqrt(2m+3) x R_m, R_l = a_lm (x R_{l-1} - b_lm R_{l-2})
-                // so Q_l^m = K_m sin^m(theta) R_l and no lane waits on another.
-                float em_re = 1.0f, em_im = 0.0f, sm = 1.0f;
+                // e^{i m phi} and sin^m(theta) for every lane at once: an inclusive
+                // prefix product over the group's lanes of (1 at lane 0, z elsewhere)
+                // leaves z^m at lane m in log2(LANES) uniform steps.
+                float em_re = sub == 0 ? 1.0f : cp, em_im = sub == 0 ? 0.0f : sp, sm = sub == 0 ? 1.0f : st;
+#pragma unroll
+                for (int d = 1; d < LANES; d <<= 1)
+                {
+                    const float ore = __shfl_up_sync(gmask, em_re, d, LANES);
+                    const float oim = __shfl_up_sync(gmask, em_im, d, LANES);
+                    const float os = __shfl_up_sync(gmask, sm, d, LANES);
+                    if (sub >= d)
+                    {
+                        const float nr = em_re * ore - em_im * oim;
+                        em_im = em_re * oim + em_im * ore;
+                        em_re = nr;
+                        sm *= os;
+                    }
+                }
+                // normalised Legendre recurrence in l for this lane's m, divided by
+                // K_m sin^m(theta): R_m = 1, R_{m+1} = sqrt(2m+3) x R_m,
+                // R_l = a_lm (x R_{l-1} - b_lm R_{l-2}); Q_l^m = K_m sin^m(theta) R_l
                 float r_cur = 1.0f, r_prev = 0.0f;
                 float R[NL];
 #pragma unroll
                 for (int kk = 0; kk < NL; ++kk)
                     R[kk] = lt[kk] == m ? 1.0f : 0.0f;
-                int l = m;
-                for (int s = 0; s < lmax; ++s)
+                for (int l = m + 1; l <= lmax; ++l)
                 {
-                    if (s < m)
-                    {
-                        const float nr = em_re * cp - em_im * sp;
-                        em_im = em_re * sp + em_im * cp;
-                        em_re = nr;
-                        sm *= st;
-                    }
-                    else
-                    {
-                        ++l;
-                        const float r = l == m + 1
-                            ? c1 * ct * r_cur
-                            : s_a[l * (ST_MAX_L + 1) + m] * (ct * r_cur - s_b[l * (ST_MAX_L + 1) + m] * r_prev);
-                        r_prev = r_cur;
-                        r_cur = r;
+                    const float r = l == m + 1
+                        ? c1 * ct * r_cur
+                        : s_a[l * (ST_MAX_L + 1) + m] * (ct * r_cur - s_b[l * (ST_MAX_L + 1) + m] * r_prev);
+                    r_prev = r_cur;
+                    r_cur = r;
 #pragma unroll
-                        for (int kk = 0; kk < NL; ++kk)
-                        {
-                            if (lt[kk] == l)
-                                R[kk] = r;
-                        }
+                    for (int kk = 0; kk < NL; ++kk)
+                    {
+                        if (lt[kk] == l)
+                            R[kk] = r;
                     }
                 }
                 const float pf = w * km * sm;
@@ -227,8 +232,9 @@ __global__ void __launch_bounds__(128)
 // broadcast, so the row gathers do not wait on the index loads one by one.
 template<int LANES>
 __global__ void __launch_bounds__(128)
-    k_ave(uint32_t n, const uint2* __restrict__ ij, const uint32_t* __restrict__ seg, const uint32_t* __restrict__ cnt,
-          StLs ls, const float2* __restrict__ qlm, float2* __restrict__ ave, float* __restrict__ ql_ave)
+    k_ave(uint32_t n, const uint2* __restrict__ ij, const uint32_t* __restrict__ bj, const uint32_t* __restrict__ seg,
+          const uint32_t* __restrict__ cnt, StLs ls, const float2* __restrict__ qlm, float2* __restrict__ ave,
+          float* __restrict__ ql_ave)
 {
     const int lane = threadIdx.x & 31;
     const int sub = lane % LANES;
@@ -248,7 +254,7 @@ __global__ void __launch_bounds__(128)
             float pr = 0.f, pim = 0.f, nr = 0.f, nim = 0.f;
             for (uint32_t base = 0; base < nbond; base += LANES)
             {
-                const uint32_t jl = base + sub < nbond ? ij[b0 + base + sub].y : 0u;
+                const uint32_t jl = base + sub < nbond ? (bj != nullptr ? bj[b0 + base + sub] : ij[b0 + base + sub].y) : 0u;
                 const uint32_t nb_here = min(static_cast<uint32_t>(LANES), nbond - base);
                 for (uint32_t t = 0; t < nb_here; ++t)
                 {
@@ -415,7 +421,7 @@ static int lanes_for(int max_l)
 
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
-                float2* qlm, float* ql, cudaStream_t s, const float* bond_vec)
+                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd)
 {
     if (n == 0)
     {
@@ -429,7 +435,7 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
     const int nlt = ls.nl <= 1 ? 1 : (ls.nl <= 2 ? 2 : (ls.nl <= 5 ? 5 : ST_MAX_NL));
     auto go = [&](auto kernel, const char* name) {
         ProfScope prof_(name, s);
-        kernel<<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vec, ls, weighted, qlm, ql);
+        kernel<<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm, ql);
     };
     if (lanes == 8)
     {
@@ -467,7 +473,7 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
 }
 
 void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
-                const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s)
+                const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s, const uint32_t* bond_j)
 {
     if (n == 0)
     {
@@ -481,17 +487,17 @@ void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t
     if (lanes == 8)
         {
             ProfScope prof_("k_ave<8>", s);
-            k_ave<8><<<blocks, 128, 0, s>>>(n, ij, seg, cnt, ls, qlm, ave, ql_ave);
+            k_ave<8><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave);
         }
     else if (lanes == 16)
         {
             ProfScope prof_("k_ave<16>", s);
-            k_ave<16><<<blocks, 128, 0, s>>>(n, ij, seg, cnt, ls, qlm, ave, ql_ave);
+            k_ave<16><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave);
         }
     else
         {
             ProfScope prof_("k_ave<32>", s);
-            k_ave<32><<<blocks, 128, 0, s>>>(n, ij, seg, cnt, ls, qlm, ave, ql_ave);
+            k_ave<32><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave);
         }
 }
 
