@@ -57,7 +57,9 @@ struct Items
     uint32_t total;
 };
 
-struct ScanShared
+// Shared memory of the scan kernels; arrays one mode does not use shrink to one
+// element, so the count pass fits four blocks per SM.
+template<int MODE> struct ScanShared
 {
     union
     {
@@ -69,11 +71,11 @@ struct ScanShared
         unsigned int hist[HIST_BINS_SMEM]; // privatised RDF histogram (histogram pass)
     } u;
     float4 ps[CELL_CAP];              // prefilter position (wrap arithmetic)
-    float4 pos[CELL_CAP];             // candidate position (histogram pass)
+    float4 pos[MODE == SM_HIST ? CELL_CAP : 1];   // candidate position (histogram pass)
     uint32_t j[CELL_CAP];             // point index
     uint32_t slot[CELL_CAP];          // grid slot << 5 | cell wrap code
     unsigned char run[CELL_CAP];      // stencil item (sorted run) of each staged position
-    uint32_t mask[QB][CELL_CHUNKS];   // acceptance per (query, chunk) in sorted order (count pass)
+    uint32_t mask[MODE == SM_COUNT ? QB : 1][CELL_CHUNKS]; // acceptance per (query, chunk), count pass
     float4 q[QB];
     float4 qs[QB];
     uint32_t qi[QB];
@@ -214,13 +216,13 @@ __device__ __forceinline__ uint32_t rank_in(const unsigned long long* src, uint3
 }
 
 template<int MODE>
-__global__ void __launch_bounds__(STHREADS, 3)
+__global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
     k_cell_scan(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2,
                 uint32_t* __restrict__ counts, uint32_t* __restrict__ gmask, uint32_t* __restrict__ gsorted,
                 uint32_t* overflow, uint32_t* overflow_n, HistParams h, unsigned long long* __restrict__ hist)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ScanShared& S = *reinterpret_cast<ScanShared*>(smem_raw);
+    ScanShared<MODE>& S = *reinterpret_cast<ScanShared<MODE>*>(smem_raw);
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
@@ -659,7 +661,7 @@ struct EmitShared
     float img[27][3];
 };
 
-__global__ void __launch_bounds__(ETHREADS)
+__global__ void __launch_bounds__(ETHREADS, 5)
     k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
                 const uint32_t* __restrict__ gsorted, const uint64_t* __restrict__ offsets, uint2* __restrict__ ij,
                 float* __restrict__ dist, float* __restrict__ vec)
@@ -792,7 +794,7 @@ template<typename K> void configure(K kernel, size_t bytes, bool& done)
 
 size_t cell_smem_bytes()
 {
-    return sizeof(ScanShared);
+    return sizeof(ScanShared<SM_COUNT>);
 }
 
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
@@ -800,11 +802,11 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
                       uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
                       cudaStream_t s)
 {
-    const int want = 3 * sm_count_cell();
+    const int want = (hist_mode ? 3 : 4) * sm_count_cell();
     const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
-    const size_t smem = sizeof(ScanShared);
     if (!hist_mode)
     {
+        const size_t smem = sizeof(ScanShared<SM_COUNT>);
         static bool done = false;
         configure(k_cell_scan<SM_COUNT>, smem, done);
         ProfScope prof_("k_cell_scan<COUNT>", s);
@@ -813,6 +815,7 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
     }
     else
     {
+        const size_t smem = sizeof(ScanShared<SM_HIST>);
         static bool done = false;
         configure(k_cell_scan<SM_HIST>, smem, done);
         ProfScope prof_("k_cell_scan<HIST>", s);
@@ -825,7 +828,7 @@ void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, co
                       const uint32_t* gmask, const uint32_t* gsorted, const uint64_t* offsets, uint2* ij, float* dist,
                       float* vec, cudaStream_t s)
 {
-    const int want = 6 * sm_count_cell();
+    const int want = 5 * sm_count_cell();
     const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
     const size_t smem = sizeof(EmitShared);
     static bool done = false;
