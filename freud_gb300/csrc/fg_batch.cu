@@ -30,7 +30,7 @@ constexpr int BT_TILE = 1024;   // staged candidates per tile
 constexpr int BT_QB = 64;       // queries per shared-memory batch
 constexpr int BT_ITEMS = 96;    // stencil items: up to 32 rows x 3 x-segments
 constexpr int BT_HIST = 2048;   // shared histogram words (all copies)
-constexpr int BT_CHUNK = 4;     // cells per work-counter pop
+constexpr int BT_CHUNK_MAX = 4; // cells per work-counter pop (fewer for small grids)
 
 // Largest f with base[f] <= x (base[0] = 0 <= x < base[nframes]).
 __device__ __forceinline__ uint32_t frame_of(const uint32_t* __restrict__ base, uint32_t nframes, uint32_t x)
@@ -181,8 +181,8 @@ __device__ __forceinline__ int bitem_of(const BItems& it, uint32_t t)
 
 template<int WARPS, int COPIES>
 __global__ void __launch_bounds__(WARPS * 32)
-    k_frames_hist(BatchGrid g, BallParams p, HistParams h, uint32_t cell_limit, uint32_t* __restrict__ queue,
-                  unsigned long long* __restrict__ hist)
+    k_frames_hist(BatchGrid g, BallParams p, HistParams h, uint32_t cell_limit, uint32_t chunk,
+                  uint32_t* __restrict__ queue, unsigned long long* __restrict__ hist)
 {
     constexpr int THREADS = WARPS * 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -204,13 +204,13 @@ __global__ void __launch_bounds__(WARPS * 32)
     for (;;)
     {
         if (tid == 0)
-            S.work = atomicAdd(queue, static_cast<uint32_t>(BT_CHUNK));
+            S.work = atomicAdd(queue, chunk);
         __syncthreads();
         const uint32_t c0 = S.work;
         __syncthreads();
         if (c0 >= cell_limit)
             break;
-        const uint32_t c1 = min(c0 + static_cast<uint32_t>(BT_CHUNK), cell_limit);
+        const uint32_t c1 = min(c0 + chunk, cell_limit);
         for (uint32_t c = c0; c < c1; ++c)
         {
             const uint32_t q0 = g.start[c];
@@ -443,8 +443,8 @@ __global__ void __launch_bounds__(128)
 
 // Rows [r0, r1) of one frame split, warp per column: each lane keeps an FP64
 // running sum over every 32nd row (at most FRAME_SYS_ROWS / 32 values, so the
-// rounding is far below the float32 inputs' own), then a fixed shuffle tree;
-// lane 0 writes partial[f][split][col].
+// rounding is far below the float32 inputs' own and the dependent FP64 chain is
+// short), then a fixed shuffle tree; lane 0 writes partial[f][split][col].
 __global__ void __launch_bounds__(256)
     k_frames_sys(const uint32_t* __restrict__ pt_base, StLs ls, int stride, int splits,
                  const float2* __restrict__ src, double* __restrict__ partial)
@@ -560,10 +560,14 @@ void hist_launch(const BatchGrid& g, const BallParams& p, const HistParams& h, u
             per_sm = 1;
         attr = true;
     }
-    const uint32_t blocks = std::min<uint32_t>(static_cast<uint32_t>(sms() * per_sm),
-                                               std::max<uint32_t>(1u, (cell_limit + BT_CHUNK - 1) / BT_CHUNK));
+    // runs of up to 4 cells per pop, fewer when the grid is small: at least ~16
+    // pops per resident block keep every SM busy to the end
+    const uint32_t resident = static_cast<uint32_t>(sms() * per_sm);
+    const uint32_t chunk =
+        std::max<uint32_t>(1u, std::min<uint32_t>(BT_CHUNK_MAX, cell_limit / std::max<uint32_t>(1u, resident * 16)));
+    const uint32_t blocks = std::min<uint32_t>(resident, std::max<uint32_t>(1u, (cell_limit + chunk - 1) / chunk));
     ProfScope prof_("k_frames_hist", s);
-    k_frames_hist<WARPS, COPIES><<<blocks, WARPS * 32, smem, s>>>(g, p, h, cell_limit, queue, hist);
+    k_frames_hist<WARPS, COPIES><<<blocks, WARPS * 32, smem, s>>>(g, p, h, cell_limit, chunk, queue, hist);
 }
 
 } // namespace

@@ -2413,7 +2413,9 @@ BatchGridBufs& batch_grid(fg_frames* fr, float r_max, int shell)
 }
 
 // Enqueues the grid build (capturable: stream work on preallocated buffers only).
-void enqueue_grid_build(fg_frames* fr, BatchGridBufs& g, cudaStream_t s)
+// sorted: each cell's points in index order (fixed bond order for Steinhardt's
+// float sums); the histogram pass counts integers and needs no order.
+void enqueue_grid_build(fg_frames* fr, BatchGridBufs& g, cudaStream_t s, bool sorted)
 {
     const uint32_t F = static_cast<uint32_t>(fr->n.size());
     FG_CUDA(cudaMemsetAsync(g.counts.p, 0, sizeof(uint32_t) * (g.ncell + 1), s));
@@ -2421,6 +2423,12 @@ void enqueue_grid_build(fg_frames* fr, BatchGridBufs& g, cudaStream_t s)
                          g.cell_of.as<uint32_t>(), g.rank.as<uint32_t>(), g.pos4.as<float4>(), g.counts.as<uint32_t>(),
                          s);
     scan_u32_to_u32(g.counts.as<uint32_t>(), g.start.as<uint32_t>(), static_cast<size_t>(g.ncell) + 1, g.scan.p, s);
+    if (!sorted)
+    {
+        launch_frames_scatter(fr->total, g.cell_of.as<uint32_t>(), g.rank.as<uint32_t>(), g.pos4.as<float4>(),
+                              g.start.as<uint32_t>(), g.cpos.as<float4>(), g.cidx.as<uint32_t>(), s);
+        return;
+    }
     launch_frames_scatter(fr->total, g.cell_of.as<uint32_t>(), g.rank.as<uint32_t>(), g.pos4.as<float4>(),
                           g.start.as<uint32_t>(), g.cpos0.as<float4>(), g.cidx0.as<uint32_t>(), s);
     launch_sort_cells(g.start.as<uint32_t>(), static_cast<int>(g.ncell), g.cpos0.as<float4>(), g.cidx0.as<uint32_t>(),
@@ -2473,8 +2481,14 @@ std::string tune_key(const fg_frames* fr, float r_max, uint32_t bins)
     const double per_cell = vol > 0.0 ? fr->total / vol * std::pow(static_cast<double>(r_max), any2d ? 2.0 : 3.0)
                                       : 0.0;
     const int dens = per_cell > 0.0 ? static_cast<int>(std::lround(2.0 * std::log2(per_cell))) : -99;
+    // small frames behave differently (few cells to spread over the SMs): the
+    // key also holds the size of the first frame, in powers of 4
+    int size4 = 0;
+    for (uint32_t n0 = fr->n.empty() ? 0u : fr->n[0]; n0 >= 4; n0 /= 4)
+        ++size4;
     return std::string(any2d ? "2d" : "3d") + " pts_per_rmax_cell~2^" + std::to_string(dens / 2.0) +
-           " bins_le_" + std::to_string(bins <= 1024 ? 1024 : (bins <= 2048 ? 2048 : 1 << 30));
+           " first_frame~4^" + std::to_string(size4) + " bins_le_" +
+           std::to_string(bins <= 1024 ? 1024 : (bins <= 2048 ? 2048 : 1 << 30));
 }
 
 // Chooses the histogram kernel's launch shape for this batch (cached per key):
@@ -2510,7 +2524,7 @@ BatchHistConfig tuned_config(fg_frames* fr, const BallParams& p, const HistParam
     for (int shell = 1; shell <= 2; ++shell)
     {
         BatchGridBufs& g = batch_grid(fr, r_max, shell);
-        enqueue_grid_build(fr, g, s);
+        enqueue_grid_build(fr, g, s, false);
         uint32_t limit = g.cell_base_host[nf];
         if (nf == 1 && fr->n[0] > (1u << 20))
         {
@@ -2684,7 +2698,7 @@ static void rdf_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_args& a)
                                            fbits(a.r_max), fbits(a.r_min), static_cast<uint64_t>(a.exclude_ii),
                                            static_cast<uint64_t>(h.bins), fbits(h.h_min), fbits(h.h_max)};
         run_graph(fr->rdf_graph, fr->graphs, key, "graph:rdf_frames", [&] {
-            enqueue_grid_build(fr, g, s);
+            enqueue_grid_build(fr, g, s, false);
             FG_CUDA(cudaMemsetAsync(fr->queue.p, 0, sizeof(uint32_t), s));
             launch_frames_hist(cfg, v, p, h, g.ncell, fr->queue.as<uint32_t>(), rdf->hist.as<unsigned long long>(), s);
         });
@@ -2733,7 +2747,7 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
                                              reinterpret_cast<uint64_t>(fr->st_scan.p), fbits(a.r_max), fbits(a.r_min),
                                              static_cast<uint64_t>(a.exclude_ii)};
         run_graph(fr->st_graph_a, fr->graphs, key_a, "graph:steinhardt_frames_count", [&] {
-            enqueue_grid_build(fr, g, s);
+            enqueue_grid_build(fr, g, s, true);
             FG_CUDA(cudaMemsetAsync(fr->st_counts.p, 0, sizeof(uint32_t) * (P + 1), s));
             launch_frames_ball_count(v, p, P, fr->st_counts.as<uint32_t>(), s);
             scan_u32_to_u64(fr->st_counts.as<uint32_t>(), fr->st_offsets.as<uint64_t>(), static_cast<size_t>(P) + 1,
