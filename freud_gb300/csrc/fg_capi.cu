@@ -842,7 +842,10 @@ void knn_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a,
     const double vol = box_volume(nq->box);
     const double per = vol / std::max<uint32_t>(nq->n, 1) * std::max<uint32_t>(k, 1);
     double rk = nq->box.is2d ? std::sqrt(per / M_PI) : std::cbrt(3.0 * per / (4.0 * M_PI));
-    double width = 1.5 * rk;
+    // 1.3 x the mean k-th neighbour distance: queries whose k-th neighbour lies
+    // beyond the stencil (rare: a ~4 sigma density fluctuation for k = 12) are
+    // redone by the block brute force
+    double width = 1.3 * rk;
     if (std::isfinite(a.r_max) && a.r_max * (1.0 + 1e-5) < width)
     {
         width = a.r_max * (1.0 + 1e-5);

@@ -107,6 +107,12 @@ __device__ __forceinline__ void sort32(unsigned long long& key, uint32_t& pay, i
     }
 }
 
+// Stencil cells (dx + 1) + 3 (dy + 1) + 9 (dz + 1) ordered by distance class:
+// home, 6 faces, 12 edges, 8 corners (2D: home, 4 edges, 4 corners).
+__constant__ int c_order3d[27] = {13, 4,  10, 12, 14, 16, 22, 1,  3,  5,  7,  9,  11, 15,
+                                  17, 19, 21, 23, 25, 0,  2,  6,  8,  18, 20, 24, 26};
+__constant__ int c_order2d[9] = {4, 1, 3, 5, 7, 0, 2, 6, 8};
+
 __global__ void __launch_bounds__(KWARPS * 32)
     k_knn_warp(DevBox b, DevGrid g, const float4* __restrict__ qpos, const uint32_t* __restrict__ qidx, KnnParams p,
                float half_min_plane, uint32_t* __restrict__ tj, float* __restrict__ td, float* __restrict__ tv,
@@ -127,15 +133,18 @@ __global__ void __launch_bounds__(KWARPS * 32)
         const uint32_t qi = qidx[t];
         int cx, cy, cz, qimg;
         query_cell_k(b, g, q, cx, cy, cz, qimg);
-        // stencil (same rules as the ball kernels)
+        // stencil (same rules as the ball kernels), nearest cells first - home, faces,
+        // edges, corners - so the k-th key tightens early and later chunks that
+        // cannot improve it are skipped (the result does not depend on the order)
         uint32_t s_start = 0, s_count = 0;
         int s_wrap = 13;
         const int nst = b.is2d ? 9 : 27;
         if (lane < nst)
         {
-            const int dx = lane % 3 - 1;
-            const int dy = (lane / 3) % 3 - 1;
-            const int dz = b.is2d ? 0 : lane / 9 - 1;
+            const int code = b.is2d ? c_order2d[lane] : c_order3d[lane];
+            const int dx = code % 3 - 1;
+            const int dy = (code / 3) % 3 - 1;
+            const int dz = b.is2d ? 0 : code / 9 - 1;
             auto ok_axis = [&](int d, int dim) {
                 if (p.arith == ARITH_AABB || dim >= 3)
                     return true;
