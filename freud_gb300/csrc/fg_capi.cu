@@ -769,8 +769,10 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     const uint32_t* list = nullptr;
     if (cellwise)
     {
+        // ghost grids hold copies of point indices; any index fits the same bound
         launch_cell_scan(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, counts.as<uint32_t>(), gmask.as<uint32_t>(),
-                         gsorted.as<uint32_t>(), over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s);
+                         gsorted.as<uint32_t>(), over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s,
+                         nq->n);
         FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         sync();
         list = over.as<uint32_t>();

@@ -28,6 +28,8 @@
 // bonds in the reference's (i, j) order (NeighborBond.h:80-95); they are
 // compacted 32 at a time, their exact vectors recomputed and written to 32
 // consecutive slots at the query's offset.
+#include <algorithm>
+
 #include "fg_kernels.cuh"
 #include "fg_prof.cuh"
 
@@ -59,18 +61,18 @@ struct Items
 
 // Shared memory of the scan kernels; arrays one mode does not use shrink to one
 // element, so the count pass fits four blocks per SM.
-template<int MODE> struct ScanShared
+template<int MODE, typename K> struct ScanShared
 {
     union
     {
         struct
         {
-            unsigned long long a[CELL_CAP]; // merge ping-pong buffers: (j << 32) | staged index
-            unsigned long long b[CELL_CAP];
+            K a[CELL_CAP]; // merge ping-pong buffers (KeyTraits<K>)
+            K b[CELL_CAP];
         } keys;
-        unsigned int hist[HIST_BINS_SMEM]; // privatised RDF histogram (histogram pass)
+        unsigned int hist[MODE == SM_HIST ? HIST_BINS_SMEM : 1]; // privatised RDF histogram (histogram pass)
     } u;
-    float4 ps[CELL_CAP];              // prefilter position (wrap arithmetic)
+    float3 ps[CELL_CAP];              // prefilter position (wrap arithmetic)
     float4 pos[MODE == SM_HIST ? CELL_CAP : 1];   // candidate position (histogram pass)
     uint32_t j[CELL_CAP];             // point index
     uint32_t slot[CELL_CAP];          // grid slot << 5 | cell wrap code
@@ -199,9 +201,31 @@ __device__ __forceinline__ int item_of(const Items& it, uint32_t t)
     return s;
 }
 
+// Merge keys: (point index, staged position) packed so that key order is point
+// order with ties broken by position. 32-bit keys (index << 10 | position) when
+// every index is below 2^22, else 64-bit (index << 32 | position).
+template<typename K> struct KeyTraits;
+template<> struct KeyTraits<unsigned int>
+{
+    static constexpr int SHIFT = 10;
+    __device__ static unsigned int make(uint32_t j, uint32_t pos) { return (j << SHIFT) | pos; }
+    __device__ static uint32_t pos(unsigned int k) { return k & ((1u << SHIFT) - 1u); }
+    __device__ static uint32_t index(unsigned int k) { return k >> SHIFT; }
+};
+template<> struct KeyTraits<unsigned long long>
+{
+    static constexpr int SHIFT = 32;
+    __device__ static unsigned long long make(uint32_t j, uint32_t pos)
+    {
+        return (static_cast<unsigned long long>(j) << SHIFT) | pos;
+    }
+    __device__ static uint32_t pos(unsigned long long k) { return static_cast<uint32_t>(k & 0xffffffffull); }
+    __device__ static uint32_t index(unsigned long long k) { return static_cast<uint32_t>(k >> SHIFT); }
+};
+
 // Number of keys in src[lo, hi) smaller than key (keys are distinct).
-__device__ __forceinline__ uint32_t rank_in(const unsigned long long* src, uint32_t lo, uint32_t hi,
-                                            unsigned long long key)
+template<typename K>
+__device__ __forceinline__ uint32_t rank_in(const K* src, uint32_t lo, uint32_t hi, K key)
 {
     uint32_t a = lo, z = hi;
     while (a < z)
@@ -215,14 +239,15 @@ __device__ __forceinline__ uint32_t rank_in(const unsigned long long* src, uint3
     return a - lo;
 }
 
-template<int MODE>
-__global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
+template<int MODE, typename K>
+__global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
     k_cell_scan(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2,
                 uint32_t* __restrict__ counts, uint32_t* __restrict__ gmask, uint32_t* __restrict__ gsorted,
                 uint32_t* overflow, uint32_t* overflow_n, HistParams h, unsigned long long* __restrict__ hist)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ScanShared<MODE>& S = *reinterpret_cast<ScanShared<MODE>*>(smem_raw);
+    ScanShared<MODE, K>& S = *reinterpret_cast<ScanShared<MODE, K>*>(smem_raw);
+    using KT = KeyTraits<K>;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
@@ -281,18 +306,18 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
                     const int pim = __float_as_int(pp.w);
                     const float3 sp = shifted(b, pp, (wr % 3 - 1) - img_ax(pim, 0), ((wr / 3) % 3 - 1) - img_ax(pim, 1),
                                               (wr / 9 - 1) - img_ax(pim, 2));
-                    S.ps[tl] = make_float4(sp.x, sp.y, sp.z, 0.0f);
+                    S.ps[tl] = sp;
                 }
                 if (MODE == SM_COUNT)
-                    S.u.keys.a[tl] = (static_cast<unsigned long long>(jj) << 32) | tl;
+                    S.u.keys.a[tl] = KT::make(jj, tl);
             }
-            const unsigned long long* order = nullptr; // sorted keys (count pass)
+            const K* order = nullptr; // sorted keys (count pass)
             if (MODE == SM_COUNT)
             {
                 __syncthreads();
                 // merge the <= 32 sorted runs (one per stencil item) pairwise, 5 levels
-                unsigned long long* src = S.u.keys.a;
-                unsigned long long* dst = S.u.keys.b;
+                K* src = S.u.keys.a;
+                K* dst = S.u.keys.b;
                 for (int L = 0; L < 5; ++L)
                 {
                     for (uint32_t e = tid; e < T; e += STHREADS)
@@ -302,19 +327,19 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
                         const uint32_t lo_r = S.it.off[min(r << L, 32)];
                         const uint32_t lo_p = S.it.off[min(pr << L, 32)];
                         const uint32_t hi_p = S.it.off[min((pr + 1) << L, 32)];
-                        const unsigned long long key = src[e];
+                        const K key = src[e];
                         const uint32_t out = min(lo_r, lo_p) + (e - lo_r) + rank_in(src, lo_p, hi_p, key);
                         dst[out] = key;
                     }
                     __syncthreads();
-                    unsigned long long* tmp = src;
+                    K* tmp = src;
                     src = dst;
                     dst = tmp;
                 }
                 order = src;
                 // the sorted order (grid slot << 5 | wrap) is what the write pass replays
                 for (uint32_t e = tid; e < T; e += STHREADS)
-                    gsorted[static_cast<size_t>(c) * CELL_CAP + e] = S.slot[static_cast<uint32_t>(order[e] & 0xffffffffull)];
+                    gsorted[static_cast<size_t>(c) * CELL_CAP + e] = S.slot[KT::pos(order[e])];
             }
             __syncthreads();
             const uint32_t nchunks = (TT + 31) / 32;
@@ -345,7 +370,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
                         const uint32_t ent = queue[lane];
                         e = ent & 0x7ffu;
                         qq = ent >> 11;
-                        const uint32_t t = MODE == SM_COUNT ? static_cast<uint32_t>(order[e] & 0xffffffffull) : e;
+                        const uint32_t t = MODE == SM_COUNT ? KT::pos(order[e]) : e;
                         const float4 q = S.q[qq];
                         const uint32_t sl = S.slot[t];
                         const float4 pp = MODE == SM_HIST ? S.pos[t] : g.cpos[sl >> 5];
@@ -384,8 +409,8 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
                 {
                     const uint32_t e = ch * 32 + lane;
                     const bool live = e < TT;
-                    const uint32_t t = (MODE == SM_COUNT && live) ? static_cast<uint32_t>(order[e] & 0xffffffffull) : e;
-                    float4 ps = make_float4(3e30f, 3e30f, 3e30f, 0.f);
+                    const uint32_t t = (MODE == SM_COUNT && live) ? KT::pos(order[e]) : e;
+                    float3 ps = make_float3(3e30f, 3e30f, 3e30f);
                     uint32_t jj = 0xffffffffu;
                     if (live)
                     {
@@ -553,17 +578,16 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
                                 if (lane < 4)
                                     S.mask[qq + lane][ch] = lane == 0 ? im[0] : (lane == 1 ? im[1] : (lane == 2 ? im[2] : im[3]));
                             }
-                            unsigned nm[4];
-#pragma unroll
-                            for (int k = 0; k < 4; ++k)
-                                nm[k] = __ballot_sync(FULL, nd[k]);
-                            if ((nm[0] | nm[1] | nm[2] | nm[3]) != 0)
+                            // undecided pairs are rare (a shell of width 2 delta): one vote
+                            // for the four queries, ballots only when there are some
+                            if (__any_sync(FULL, nd[0] || nd[1] || nd[2] || nd[3]))
                             {
 #pragma unroll
                                 for (int k = 0; k < 4; ++k)
                                 {
-                                    if (nm[k] != 0)
-                                        append(nd[k], nm[k], qq + k);
+                                    const unsigned nm = __ballot_sync(FULL, nd[k]);
+                                    if (nm != 0)
+                                        append(nd[k], nm, qq + k);
                                 }
                             }
                         }
@@ -614,9 +638,9 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 4 : 3)
                         // (NeighborQuery exclude_ii); equal indices are adjacent in the sorted keys
                         for (uint32_t k = tid; k < nb; k += STHREADS)
                         {
-                            const unsigned long long lo_key = static_cast<unsigned long long>(S.qi[k]) << 32;
+                            const K lo_key = KT::make(S.qi[k], 0u);
                             uint32_t e = rank_in(order, 0, T, lo_key);
-                            while (e < T && (order[e] >> 32) == S.qi[k])
+                            while (e < T && KT::index(order[e]) == S.qi[k])
                             {
                                 atomicAnd(&S.mask[k][e >> 5], ~(1u << (e & 31u)));
                                 ++e;
@@ -794,33 +818,51 @@ template<typename K> void configure(K kernel, size_t bytes, bool& done)
 
 size_t cell_smem_bytes()
 {
-    return sizeof(ScanShared<SM_COUNT>);
+    return sizeof(ScanShared<SM_COUNT, unsigned long long>);
 }
 
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       float pre_out2, float pre_in2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
                       uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
-                      cudaStream_t s)
+                      cudaStream_t s, uint32_t n_points)
 {
-    const int want = (hist_mode ? 3 : 4) * sm_count_cell();
-    const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
-    if (!hist_mode)
+    // one wave of resident blocks walking the cells
+    auto grid = [&](auto kernel, size_t smem) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, STHREADS, smem);
+        const int want = std::max(per_sm, 1) * sm_count_cell();
+        return qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
+    };
+    if (!hist_mode && n_points <= (1u << 22))
     {
-        const size_t smem = sizeof(ScanShared<SM_COUNT>);
+        // 32-bit merge keys: point indices below 2^22
+        const size_t smem = sizeof(ScanShared<SM_COUNT, unsigned int>);
         static bool done = false;
-        configure(k_cell_scan<SM_COUNT>, smem, done);
+        configure(k_cell_scan<SM_COUNT, unsigned int>, smem, done);
+        const int blocks = grid(k_cell_scan<SM_COUNT, unsigned int>, smem);
         ProfScope prof_("k_cell_scan<COUNT>", s);
-        k_cell_scan<SM_COUNT><<<blocks, STHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, counts, gmask, gsorted,
-                                                             overflow, overflow_n, h, hist);
+        k_cell_scan<SM_COUNT, unsigned int><<<blocks, STHREADS, smem, s>>>(
+            box, g, qg, p, pre_out2, pre_in2, counts, gmask, gsorted, overflow, overflow_n, h, hist);
+    }
+    else if (!hist_mode)
+    {
+        const size_t smem = sizeof(ScanShared<SM_COUNT, unsigned long long>);
+        static bool done = false;
+        configure(k_cell_scan<SM_COUNT, unsigned long long>, smem, done);
+        const int blocks = grid(k_cell_scan<SM_COUNT, unsigned long long>, smem);
+        ProfScope prof_("k_cell_scan<COUNT>", s);
+        k_cell_scan<SM_COUNT, unsigned long long><<<blocks, STHREADS, smem, s>>>(
+            box, g, qg, p, pre_out2, pre_in2, counts, gmask, gsorted, overflow, overflow_n, h, hist);
     }
     else
     {
-        const size_t smem = sizeof(ScanShared<SM_HIST>);
+        const size_t smem = sizeof(ScanShared<SM_HIST, unsigned long long>);
         static bool done = false;
-        configure(k_cell_scan<SM_HIST>, smem, done);
+        configure(k_cell_scan<SM_HIST, unsigned long long>, smem, done);
+        const int blocks = grid(k_cell_scan<SM_HIST, unsigned long long>, smem);
         ProfScope prof_("k_cell_scan<HIST>", s);
-        k_cell_scan<SM_HIST><<<blocks, STHREADS, smem, s>>>(box, g, qg, p, pre_out2, 0.0f, counts, gmask, gsorted,
-                                                            overflow, overflow_n, h, hist);
+        k_cell_scan<SM_HIST, unsigned long long><<<blocks, STHREADS, smem, s>>>(
+            box, g, qg, p, pre_out2, 0.0f, counts, gmask, gsorted, overflow, overflow_n, h, hist);
     }
 }
 

@@ -123,10 +123,11 @@ void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, c
 constexpr int CELL_CAP = 1024;
 constexpr int CELL_CHUNKS = CELL_CAP / 32;
 size_t cell_smem_bytes();
+// n_points: number of points of g (point indices below 2^22 allow 32-bit merge keys).
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       float pre_out2, float pre_in2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
                       uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
-                      cudaStream_t s);
+                      cudaStream_t s, uint32_t n_points = 0xffffffffu);
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       const uint32_t* gmask, const uint32_t* gsorted, const uint64_t* offsets, uint2* ij, float* dist,
                       float* vec, cudaStream_t s);
