@@ -4,7 +4,7 @@ freud.density.RDF and freud.order.Steinhardt. Importing this package loads the
 CUDA library; there is no CPU fallback.
 """
 
-from . import box, data, density, locality, order, parallel
+from . import box, data, density, locality, order, parallel, replicas
 from .box import Box
 from .locality import AABBQuery, CellQuery, FrameBatch, LinkCell, NeighborList
 

@@ -85,6 +85,7 @@ SIGNATURES = {
     "fg_rdf_get_u64": [P, P, P, P],
     "fg_rdf_bin_edges": [P, P, P],
     "fg_rdf_state": [P, pbox, pu32, pu32, pu32],
+    "fg_rdf_set_state": [P, P, u32, pbox, u32, u32],
     "fg_steinhardt_create": [P, u32, i32, i32, i32, i32, PP],
     "fg_steinhardt_destroy": [P],
     "fg_steinhardt_compute": [P, P, P, pargs],

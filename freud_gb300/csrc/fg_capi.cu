@@ -1864,6 +1864,23 @@ fg_status fg_rdf_state(const fg_rdf* rdf, fg_box* box, uint32_t* n_frames, uint3
     });
 }
 
+fg_status fg_rdf_set_state(fg_rdf* rdf, const uint64_t* bin_counts, uint32_t n_frames, const fg_box* box,
+                           uint32_t n_points, uint32_t n_query)
+{
+    return guard([&] {
+        require(rdf, "rdf");
+        require(bin_counts, "bin_counts");
+        require(box, "box");
+        FG_CUDA(cudaMemcpyAsync(rdf->hist.p, bin_counts, sizeof(unsigned long long) * rdf->bins,
+                                cudaMemcpyHostToDevice, stream()));
+        rdf->frames = n_frames;
+        rdf->box = to_host_box(box);
+        rdf->n_points = n_points;
+        rdf->n_query = n_query;
+        sync();
+    });
+}
+
 // ---- Steinhardt ----------------------------------------------------------------------
 fg_status fg_steinhardt_create(const uint32_t* ls, uint32_t n_l, int average, int wl, int weighted, int wl_normalize,
                                fg_steinhardt** out)

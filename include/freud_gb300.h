@@ -170,6 +170,12 @@ fg_status fg_rdf_get_u64(fg_rdf* rdf, uint64_t* bin_counts, double* rdf_out, dou
 fg_status fg_rdf_bin_edges(const fg_rdf* rdf, float* edges, float* centers);
 /* getBox of the last accumulated frame; frame counter. */
 fg_status fg_rdf_state(const fg_rdf* rdf, fg_box* box, uint32_t* n_frames, uint32_t* n_points, uint32_t* n_query);
+/* No counterpart in the reference: replaces the accumulated state (uint64 bin
+ * counts, frame counter, last frame's box and N) - used to load the combination
+ * of RDFs accumulated over disjoint frame ranges by several processes (one GPU
+ * each), so rdf / n_r come out as if one process had accumulated every frame. */
+fg_status fg_rdf_set_state(fg_rdf* rdf, const uint64_t* bin_counts, uint32_t n_frames, const fg_box* box,
+                           uint32_t n_points, uint32_t n_query);
 
 /* ---- Steinhardt ----------------------------------------------------------------
  * freud::order::Steinhardt (freud/order/Steinhardt.h:59-223, Steinhardt.cc:85-359;

@@ -191,3 +191,22 @@ def test_steinhardt_frames_match_per_frame(freud):
         np.testing.assert_allclose(ql[off:off + len(pts)], s1.ql, rtol=2e-6, atol=1e-7)
         np.testing.assert_allclose(np.asarray(st.order)[f], s1.order, rtol=2e-6)
         off += len(pts)
+
+
+def test_rdf_states_of_frame_ranges_combine(freud):
+    """Two RDFs over disjoint frame ranges (as two processes would hold them),
+    combined on the host and loaded into a third: equal to one RDF over every frame."""
+    from freud_gb300 import replicas
+
+    frames = make_frames(freud, [900, 1400, 600, 1100, 750], 51)
+    whole = per_frame_rdf(freud, frames, 70, 2.0)
+    parts = []
+    for r in range(2):
+        lo, hi = replicas.frame_range(len(frames), r, 2)
+        rdf = freud.density.RDF(70, 2.0)
+        rdf.compute(freud.locality.FrameBatch(frames[lo:hi]), reset=False)
+        parts.append(replicas.rdf_state(rdf))
+    merged = replicas.load_rdf_state(freud.density.RDF(70, 2.0), replicas.combine_rdf_states(parts))
+    np.testing.assert_array_equal(merged.bin_counts_u64, whole.bin_counts_u64)
+    np.testing.assert_array_equal(merged.rdf, whole.rdf)
+    np.testing.assert_array_equal(merged.n_r, whole.n_r)
