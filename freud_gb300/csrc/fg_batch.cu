@@ -192,6 +192,14 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int warp = tid >> 5;
     const bool smem_hist = h.bins * COPIES <= static_cast<uint32_t>(BT_HIST);
     uint32_t* my_hist = S.hist + (warp % COPIES) * h.bins;
+    // exclude_ii without a per-pair index test: a query's own point is one of its
+    // candidates (home cell, image 0), so r = p - (p + 0) = 0 and the pair test
+    // accepts it exactly when r_min = 0; it then lands in bin 0 when the histogram
+    // starts at 0. Those self pairs - one per query - are taken back per cell.
+    // Bonds to other images of the query's own point are beyond r_max (2 r_max is
+    // below every nearest-plane distance), so no other pair carries j == i.
+    const bool self_in_bin0 = p.exclude_ii && p.r_min_sq <= 0.0f && h.h_min <= 0.0f && h.h_max > 0.0f;
+    const bool test_ii = p.exclude_ii && !self_in_bin0;
 
     if (smem_hist)
     {
@@ -299,7 +307,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                         {
                             const float4 q = S.q[qq];
                             const int qimg = __float_as_int(q.w);
-                            const bool ok = !(p.exclude_ii && jj == S.qi[qq]);
+                            const bool ok = !(test_ii && jj == S.qi[qq]);
                             bool acc = false;
                             float rsq = 0.f;
                             if (qimg == 0)
@@ -348,6 +356,14 @@ __global__ void __launch_bounds__(WARPS * 32)
                     }
                 }
                 __syncthreads();
+            }
+            if (self_in_bin0 && tid == 0)
+            {
+                // one self pair per query of the cell, counted into bin 0 above
+                if (smem_hist)
+                    S.hist[0] -= nqc;
+                else
+                    atomicAdd(&hist[0], ~static_cast<unsigned long long>(nqc) + 1ull);
             }
         }
     }

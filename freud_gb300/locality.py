@@ -13,6 +13,10 @@ from .box import Box
 from .util import _Compute, _convert_array, _convert_box
 
 ITERATOR_TERMINATOR = None
+
+_memcmp = _lib.ctypes.CDLL(None).memcmp
+_memcmp.restype = _lib.ctypes.c_int
+_memcmp.argtypes = [_lib.ctypes.c_void_p, _lib.ctypes.c_void_p, _lib.ctypes.c_size_t]
 NO_DEFAULT_QUERY_ARGS_MESSAGE = (
     "Query arguments must be provided for {} objects since there is no default set of arguments."
 )
@@ -141,7 +145,8 @@ class NeighborQueryResult:
 
     def __init__(self, nq, points, query_args):
         self._nq = nq
-        self._points = np.array(points, dtype=np.float32)
+        # query() has already converted the points; keep them without another copy
+        self._points = np.ascontiguousarray(points, dtype=np.float32)
         self._query_args = query_args
 
     def __iter__(self):
@@ -215,8 +220,16 @@ class NeighborQuery:
 
     # -- internals ------------------------------------------------------------------
     def _same_points(self, query_points):
-        return query_points is self._points or (
-            query_points.shape == self._points.shape and np.array_equal(query_points, self._points))
+        """Whether query_points hold exactly this object's points (then the query
+        reuses the object's own cell grid). Byte comparison with memcmp: no
+        temporaries for million-point arrays."""
+        p = self._points
+        if query_points is p:
+            return True
+        if query_points.shape != p.shape or query_points.dtype != p.dtype:
+            return False
+        q = np.ascontiguousarray(query_points)
+        return _memcmp(q.ctypes.data, p.ctypes.data, p.nbytes) == 0
 
     def _is_nearest(self, qargs):
         return qargs.mode == "nearest" or (qargs.mode is None and qargs.num_neighbors != _lib.DEFAULT_NUM_NEIGHBORS)
