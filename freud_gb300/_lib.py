@@ -59,6 +59,7 @@ SIGNATURES = {
     "fg_nq_destroy": [P],
     "fg_nq_cell_width": [P, pf32],
     "fg_nq_num_points": [P, pu32],
+    "fg_nq_get_points": [P, P],
     "fg_nq_query": [P, P, u32, pargs, i32, PP],
     "fg_nq_query_device": [P, P, u32, pargs, i32, PP],
     "fg_nlist_from_arrays": [u64, P, u32, P, u32, P, P, PP],

@@ -1144,6 +1144,17 @@ fg_status fg_nq_num_points(const fg_nq* nq, uint32_t* out)
     });
 }
 
+fg_status fg_nq_get_points(const fg_nq* nq, float* out)
+{
+    return guard([&] {
+        require(nq, "nq");
+        require(out, "out");
+        FG_CUDA(cudaMemcpyAsync(out, nq->dpts, sizeof(float) * 3 * static_cast<size_t>(nq->n), cudaMemcpyDeviceToHost,
+                                stream()));
+        sync();
+    });
+}
+
 fg_status fg_nq_query(fg_nq* nq, const float* query_points, uint32_t n_query, const fg_query_args* args,
                       int sort_by_distance, fg_nlist** out)
 {

@@ -173,12 +173,16 @@ class NeighborQuery:
     def _init(self, box, points, kind, cell_width=0.0):
         b = _convert_box(box)
         self._box = b
-        self._points = _convert_array(points, shape=(None, 3)).copy()
+        pts = _convert_array(points, shape=(None, 3))
         self._kind = kind
         h = _lib.ctypes.c_void_p()
-        _lib.check(_lib.lib.fg_nq_create(_lib.ctypes.byref(b._c_box()), _lib.ptr(self._points), len(self._points),
-                                         kind, float(cell_width), _lib.ctypes.byref(h)))
+        _lib.check(_lib.lib.fg_nq_create(_lib.ctypes.byref(b._c_box()), _lib.ptr(pts), len(pts), kind,
+                                         float(cell_width), _lib.ctypes.byref(h)))
         self._handle = _lib.Handle(h, _lib.lib.fg_nq_destroy)
+        # the library keeps its own copy of the points (on the device); the host
+        # copy behind .points is made from it on first use
+        self._n_points = len(pts)
+        self._points = None
 
     @property
     def _h(self):
@@ -211,7 +215,11 @@ class NeighborQuery:
 
     @property
     def points(self):
-        return np.asarray(self._points)
+        if self._points is None:
+            pts = np.empty((self._n_points, 3), np.float32)
+            _lib.check(_lib.lib.fg_nq_get_points(self._h, _lib.ptr(pts)))
+            self._points = pts
+        return self._points
 
     def query(self, query_points, query_args):
         query_points = _convert_array(np.atleast_2d(query_points), shape=(None, 3))
@@ -223,7 +231,7 @@ class NeighborQuery:
         """Whether query_points hold exactly this object's points (then the query
         reuses the object's own cell grid). Byte comparison with memcmp: no
         temporaries for million-point arrays."""
-        p = self._points
+        p = self.points
         if query_points is p:
             return True
         if query_points.shape != p.shape or query_points.dtype != p.dtype:

@@ -100,6 +100,9 @@ fg_status fg_nq_destroy(fg_nq* nq);
 /* LinkCell::getCellWidth (freud/locality/LinkCell.h:189-192). */
 fg_status fg_nq_cell_width(const fg_nq* nq, float* out);
 fg_status fg_nq_num_points(const fg_nq* nq, uint32_t* out);
+/* NeighborQuery::getPoints (NeighborQuery.h:145-153): the object's points (n x 3
+ * float32, as they were given) copied to out. */
+fg_status fg_nq_get_points(const fg_nq* nq, float* out);
 
 /* NeighborQuery::query(...) -> NeighborQueryIterator::toNeighborList(sort_by_distance)
  * (freud/locality/NeighborQuery.h:130-142, 434-481; export-NeighborQuery.cc:26-33,130-135).
