@@ -35,9 +35,279 @@ __constant__ float c_K[ST_MAX_L + 1];                    // Q_m^m prefactors
 __constant__ float c_a[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // a_lm at [l*(L+1)+m]
 __constant__ float c_b[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // b_lm
 
+// LANES threads per particle; thread a owns the orders ma = a and mb = l_max - a
+// (when mb > ma), so the two normalised Legendre recurrences of a thread take
+// l_max steps together and no thread of the group waits on another.
 template<int LANES, int NL>
 __global__ void __launch_bounds__(128)
     k_qlm(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
+          const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
+          const uint32_t* __restrict__ cnt, const float4* __restrict__ bvd, StLs ls, int weighted,
+          float2* __restrict__ qlm_out, float* __restrict__ ql_out)
+{
+    // recurrence coefficients staged once per block (threads read different m)
+    __shared__ float s_a[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
+    __shared__ float s_b[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
+    __shared__ float s_K[ST_MAX_L + 1];
+    for (int t = threadIdx.x; t <= ls.max_l * (ST_MAX_L + 1) + ST_MAX_L; t += blockDim.x)
+    {
+        s_a[t] = c_a[t];
+        s_b[t] = c_b[t];
+    }
+    for (int t = threadIdx.x; t <= ST_MAX_L; t += blockDim.x)
+        s_K[t] = c_K[t];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int sub = lane % LANES;
+    const int group = lane / LANES;             // particle slot within the warp
+    const int groups_per_block = blockDim.x / LANES;
+    const unsigned gmask = LANES == 32 ? FULL : (((1u << LANES) - 1u) << (group * LANES));
+    const int lmax = ls.max_l;
+    const int used = lmax / 2 + 1;              // threads with an order of their own
+    const bool has_a = sub < used;
+    const int ma = has_a ? sub : 0;             // idle threads shadow thread 0, with zero weight
+    const int mb = lmax - ma;
+    const bool has_b = has_a && mb > ma;
+    const int split = lmax - ma;                // steps of the ma recurrence; the mb one takes ma steps
+    const float ka = has_a ? s_K[ma] : 0.0f;
+    const float kb = has_b ? s_K[mb] : 0.0f;
+    const float c1a = sqrtf(2.0f * ma + 3.0f);
+    const float c1b = sqrtf(2.0f * mb + 3.0f);
+    const float sga = (ma & 1) ? -1.0f : 1.0f;
+    const float sgb = (mb & 1) ? -1.0f : 1.0f;
+    // slot kk holds the kk-th smallest requested l
+    int lt[NL];
+#pragma unroll
+    for (int kk = 0; kk < NL; ++kk)
+        lt[kk] = kk < ls.nl ? ls.l[ls.sorted_k[kk]] : -1;
+    for (uint32_t i = blockIdx.x * groups_per_block + threadIdx.x / LANES; i < n; i += gridDim.x * groups_per_block)
+    {
+        float accA_re[NL][2], accA_im[NL][2], accB_re[NL][2], accB_im[NL][2];
+#pragma unroll
+        for (int k = 0; k < NL; ++k)
+        {
+            accA_re[k][0] = accA_re[k][1] = accA_im[k][0] = accA_im[k][1] = 0.0f;
+            accB_re[k][0] = accB_re[k][1] = accB_im[k][0] = accB_im[k][1] = 0.0f;
+        }
+        float tw = 0.0f;
+        const uint32_t b0 = seg[i];
+        const uint32_t nbond = cnt[i];
+        float pix = 0.f, piy = 0.f, piz = 0.f;
+        if (bvd == nullptr)
+        {
+            pix = pts[3 * (size_t) i];
+            piy = pts[3 * (size_t) i + 1];
+            piz = pts[3 * (size_t) i + 2];
+        }
+        // bonds in batches of LANES: thread t computes the geometry of bond base + t
+        // (independent loads in flight), then the group walks the batch with shuffles
+        for (uint32_t base = 0; base < nbond; base += LANES)
+        {
+            float g_ct = 1.0f, g_st = 0.0f, g_cp = 1.0f, g_sp = 0.0f, g_w = 0.0f;
+            if (base + sub < nbond)
+            {
+                const uint32_t e = b0 + base + sub;
+                float dx, dy, dz, d;
+                if (bvd != nullptr)
+                {
+                    const float4 v = bvd[e];
+                    dx = v.x;
+                    dy = v.y;
+                    dz = v.z;
+                    d = v.w;
+                }
+                else
+                {
+                    const uint32_t j = ij[e].y;
+                    box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pix), __fsub_rn(pts[3 * (size_t) j + 1], piy),
+                             __fsub_rn(pts[3 * (size_t) j + 2], piz), dx, dy, dz);
+                    d = dist[e];
+                }
+                g_w = weighted ? weights[e] : 1.0f;
+                g_ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
+                g_st = sqrtf(fmaxf(0.0f, 1.0f - g_ct * g_ct));
+                const float rho = sqrtf(dx * dx + dy * dy);
+                if (rho > 0.0f)
+                {
+                    g_cp = dx / rho;
+                    g_sp = dy / rho;
+                }
+            }
+            const uint32_t nb_here = min(static_cast<uint32_t>(LANES), nbond - base);
+            for (uint32_t t = 0; t < nb_here; ++t)
+            {
+                const float ct = __shfl_sync(gmask, g_ct, t, LANES);
+                const float st = __shfl_sync(gmask, g_st, t, LANES);
+                const float cp = __shfl_sync(gmask, g_cp, t, LANES);
+                const float sp = __shfl_sync(gmask, g_sp, t, LANES);
+                const float w = __shfl_sync(gmask, g_w, t, LANES);
+                // z = e^{i phi}, s = sin(theta). Prefix products over the group's
+                // threads of (1 at thread 0, z elsewhere) give z^a at thread a;
+                // suffix products of (z below thread used - 1, 1 above) give
+                // z^(used - 1 - a), and z^mb = z^(lmax - used + 1) z^(used - 1 - a).
+                float pa_re = sub == 0 ? 1.0f : cp, pa_im = sub == 0 ? 0.0f : sp, pa_s = sub == 0 ? 1.0f : st;
+                float sf_re = sub < used - 1 ? cp : 1.0f, sf_im = sub < used - 1 ? sp : 0.0f,
+                      sf_s = sub < used - 1 ? st : 1.0f;
+#pragma unroll
+                for (int d = 1; d < LANES; d <<= 1)
+                {
+                    const float ore = __shfl_up_sync(gmask, pa_re, d, LANES);
+                    const float oim = __shfl_up_sync(gmask, pa_im, d, LANES);
+                    const float os = __shfl_up_sync(gmask, pa_s, d, LANES);
+                    const float dre = __shfl_down_sync(gmask, sf_re, d, LANES);
+                    const float dim = __shfl_down_sync(gmask, sf_im, d, LANES);
+                    const float ds = __shfl_down_sync(gmask, sf_s, d, LANES);
+                    if (sub >= d)
+                    {
+                        const float nr = pa_re * ore - pa_im * oim;
+                        pa_im = pa_re * oim + pa_im * ore;
+                        pa_re = nr;
+                        pa_s *= os;
+                    }
+                    if (sub + d < LANES)
+                    {
+                        const float nr = sf_re * dre - sf_im * dim;
+                        sf_im = sf_re * dim + sf_im * dre;
+                        sf_re = nr;
+                        sf_s *= ds;
+                    }
+                }
+                // z^(used - 1) and s^(used - 1) live at thread used - 1; lmax - used + 1
+                // is used - 1 (even lmax) or used (odd lmax)
+                float top_re = __shfl_sync(gmask, pa_re, used - 1, LANES);
+                float top_im = __shfl_sync(gmask, pa_im, used - 1, LANES);
+                float top_s = __shfl_sync(gmask, pa_s, used - 1, LANES);
+                if (lmax & 1)
+                {
+                    const float nr = top_re * cp - top_im * sp;
+                    top_im = top_re * sp + top_im * cp;
+                    top_re = nr;
+                    top_s *= st;
+                }
+                const float pb_re = top_re * sf_re - top_im * sf_im;
+                const float pb_im = top_re * sf_im + top_im * sf_re;
+                const float pb_s = top_s * sf_s;
+                // normalised Legendre recurrences in l divided by K_m sin^m(theta):
+                // R_m = 1, R_{m+1} = sqrt(2m+3) x R_m, R_l = a_lm (x R_{l-1} - b_lm R_{l-2});
+                // Q_l^m = K_m sin^m(theta) R_l. Steps 0 .. split-1 run m = ma,
+                // the remaining ma steps run m = mb.
+                float RA[NL], RB[NL];
+#pragma unroll
+                for (int kk = 0; kk < NL; ++kk)
+                {
+                    RA[kk] = lt[kk] == ma ? 1.0f : 0.0f;
+                    RB[kk] = lt[kk] == mb ? 1.0f : 0.0f;
+                }
+                float r_cur = 1.0f, r_prev = 0.0f;
+                int m = ma, l = ma;
+                float c1 = c1a;
+                for (int s = 0; s < lmax; ++s)
+                {
+                    if (s == split)
+                    {
+                        m = mb;
+                        l = mb;
+                        c1 = c1b;
+                        r_cur = 1.0f;
+                        r_prev = 0.0f;
+                    }
+                    ++l;
+                    const float r = l == m + 1
+                        ? c1 * ct * r_cur
+                        : s_a[l * (ST_MAX_L + 1) + m] * (ct * r_cur - s_b[l * (ST_MAX_L + 1) + m] * r_prev);
+                    r_prev = r_cur;
+                    r_cur = r;
+                    const bool in_a = s < split;
+#pragma unroll
+                    for (int kk = 0; kk < NL; ++kk)
+                    {
+                        if (lt[kk] == l)
+                        {
+                            if (in_a)
+                                RA[kk] = r;
+                            else
+                                RB[kk] = r;
+                        }
+                    }
+                }
+                const float pfa = w * ka * pa_s;
+                const float wa_re = pfa * pa_re, wa_im = pfa * pa_im;
+                const float pfb = w * kb * pb_s;
+                const float wb_re = pfb * pb_re, wb_im = pfb * pb_im;
+#pragma unroll
+                for (int kk = 0; kk < NL; ++kk)
+                {
+                    const float ar = RA[kk] * wa_re, ai = RA[kk] * wa_im;
+                    accA_re[kk][0] += ar;
+                    accA_im[kk][0] += ai;
+                    // Y_l^{-m} = (-1)^m conj(Y_l^m)
+                    accA_re[kk][1] += sga * ar;
+                    accA_im[kk][1] -= sga * ai;
+                    const float br = RB[kk] * wb_re, bi = RB[kk] * wb_im;
+                    accB_re[kk][0] += br;
+                    accB_im[kk][0] += bi;
+                    accB_re[kk][1] += sgb * br;
+                    accB_im[kk][1] -= sgb * bi;
+                }
+                tw += w;
+            }
+        }
+        // normalise, write, and reduce ql over the particle's threads (slot kk holds
+        // the kk-th smallest l, whose caller index is k)
+#pragma unroll
+        for (int kk = 0; kk < NL; ++kk)
+        {
+            if (kk >= ls.nl)
+            {
+                break;
+            }
+            const int k = ls.sorted_k[kk];
+            const int lk = lt[kk];
+            float part = 0.0f;
+            float2* row = qlm_out + ls.qlm_offset[k] + static_cast<size_t>(i) * (2 * lk + 1);
+            if (has_a && ma <= lk)
+            {
+                const float qr = accA_re[kk][0] / tw;
+                const float qi = accA_im[kk][0] / tw;
+                row[ma] = make_float2(qr, qi);
+                part += qr * qr + qi * qi;
+                if (ma > 0)
+                {
+                    const float nr = accA_re[kk][1] / tw;
+                    const float ni = accA_im[kk][1] / tw;
+                    row[lk + ma] = make_float2(nr, ni);
+                    part += nr * nr + ni * ni;
+                }
+            }
+            if (has_b && mb <= lk)
+            {
+                const float qr = accB_re[kk][0] / tw;
+                const float qi = accB_im[kk][0] / tw;
+                row[mb] = make_float2(qr, qi);
+                part += qr * qr + qi * qi;
+                const float nr = accB_re[kk][1] / tw;
+                const float ni = accB_im[kk][1] / tw;
+                row[lk + mb] = make_float2(nr, ni);
+                part += nr * nr + ni * ni;
+            }
+            for (int o = LANES / 2; o > 0; o >>= 1)
+            {
+                part += __shfl_xor_sync(gmask, part, o, LANES);
+            }
+            if (sub == 0)
+            {
+                ql_out[static_cast<size_t>(i) * ls.nl + k] = sqrtf(part * ls.norm[k]);
+            }
+        }
+    }
+}
+
+// One order m per thread (thread m of LANES >= l_max + 1): fewer registers than
+// the paired kernel, used when many l values are requested.
+template<int LANES, int NL>
+__global__ void __launch_bounds__(128)
+    k_qlm_m(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
           const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
           const uint32_t* __restrict__ cnt, const float4* __restrict__ bvd, StLs ls, int weighted,
           float2* __restrict__ qlm_out, float* __restrict__ ql_out)
@@ -419,6 +689,13 @@ static int lanes_for(int max_l)
     return max_l < 8 ? 8 : (max_l < 16 ? 16 : 32);
 }
 
+// Threads per particle of k_qlm: one per pair of orders (m, l_max - m).
+static int pair_lanes_for(int max_l)
+{
+    const int used = max_l / 2 + 1;
+    return used <= 4 ? 4 : (used <= 8 ? 8 : 16);
+}
+
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
                 float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd)
@@ -427,48 +704,48 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
     {
         return;
     }
-    const int lanes = lanes_for(ls.max_l);
+    const int nlt = ls.nl <= 1 ? 1 : (ls.nl <= 2 ? 2 : (ls.nl <= 5 ? 5 : ST_MAX_NL));
+    // paired orders for one or two l values; with more, the doubled accumulators
+    // cost more registers than the divergence they remove
+    const bool paired = nlt <= 2;
+    const int lanes = paired ? pair_lanes_for(ls.max_l) : lanes_for(ls.max_l);
     const uint32_t groups = 128 / lanes;
     uint32_t blocks = (n + groups - 1) / groups;
     const uint32_t cap = static_cast<uint32_t>(sm_count()) * 16;
     blocks = blocks < cap ? blocks : cap;
-    const int nlt = ls.nl <= 1 ? 1 : (ls.nl <= 2 ? 2 : (ls.nl <= 5 ? 5 : ST_MAX_NL));
     auto go = [&](auto kernel, const char* name) {
         ProfScope prof_(name, s);
         kernel<<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm, ql);
     };
-    if (lanes == 8)
+    if (!paired)
+    {
+        if (lanes == 8)
+            go(nlt == 5 ? k_qlm_m<8, 5> : k_qlm_m<8, ST_MAX_NL>, "k_qlm_m<8>");
+        else if (lanes == 16)
+            go(nlt == 5 ? k_qlm_m<16, 5> : k_qlm_m<16, ST_MAX_NL>, "k_qlm_m<16>");
+        else
+            go(nlt == 5 ? k_qlm_m<32, 5> : k_qlm_m<32, ST_MAX_NL>, "k_qlm_m<32>");
+    }
+    else if (lanes == 4)
+    {
+        if (nlt == 1)
+            go(k_qlm<4, 1>, "k_qlm<4>");
+        else
+            go(k_qlm<4, 2>, "k_qlm<4>");
+    }
+    else if (lanes == 8)
     {
         if (nlt == 1)
             go(k_qlm<8, 1>, "k_qlm<8>");
-        else if (nlt == 2)
+        else
             go(k_qlm<8, 2>, "k_qlm<8>");
-        else if (nlt == 5)
-            go(k_qlm<8, 5>, "k_qlm<8>");
-        else
-            go(k_qlm<8, ST_MAX_NL>, "k_qlm<8>");
-    }
-    else if (lanes == 16)
-    {
-        if (nlt == 1)
-            go(k_qlm<16, 1>, "k_qlm<16>");
-        else if (nlt == 2)
-            go(k_qlm<16, 2>, "k_qlm<16>");
-        else if (nlt == 5)
-            go(k_qlm<16, 5>, "k_qlm<16>");
-        else
-            go(k_qlm<16, ST_MAX_NL>, "k_qlm<16>");
     }
     else
     {
         if (nlt == 1)
-            go(k_qlm<32, 1>, "k_qlm<32>");
-        else if (nlt == 2)
-            go(k_qlm<32, 2>, "k_qlm<32>");
-        else if (nlt == 5)
-            go(k_qlm<32, 5>, "k_qlm<32>");
+            go(k_qlm<16, 1>, "k_qlm<16>");
         else
-            go(k_qlm<32, ST_MAX_NL>, "k_qlm<32>");
+            go(k_qlm<16, 2>, "k_qlm<16>");
     }
 }
 
