@@ -314,6 +314,7 @@ def measure_c4(freud, _lib, steps, warmup, nframes=64):
     ref = plain()
     got = batched()
     assert np.array_equal(ref, got), "batched RDF counts differ from the per-frame path"
+    small = measure_small_frames(freud, _lib, max(1, min(steps, 5)), max(1, warmup))
     pairs = int(got.sum())
     k = max(1, min(steps, 5))
     t_plain = _median_wall(plain, k, 1)
@@ -329,7 +330,41 @@ def measure_c4(freud, _lib, steps, warmup, nframes=64):
                         "particles_per_s": n_total / t_batch, "device_ms": dev_batch, "launches_per_step": l_batch,
                         "kernels_ms_per_step": top_batch},
             "speedup_e2e": t_plain / t_batch, "speedup_device": dev_plain / dev_batch if dev_batch else None,
+            "small_frames": small,
             "autotune": _lib.autotune_report().strip().splitlines()[-1:] }
+
+
+def measure_small_frames(freud, _lib, steps, warmup, nframes=1024, seed=44):
+    """Where batching pays most: 1,024 frames of 1,000-4,000 points (same density
+    and computes as the uneven trajectory), per frame vs one FrameBatch."""
+    rng = np.random.default_rng(seed)
+    frames = []
+    for n in rng.integers(1000, 4001, nframes):
+        L = float((n / 0.85) ** (1.0 / 3.0))
+        box = freud.box.Box.cube(L)
+        frames.append((box, box.make_absolute(rng.random((int(n), 3))).astype(np.float32)))
+    rdf = freud.density.RDF(200, 4.0)
+    st = freud.order.Steinhardt(6, average=True)
+
+    def plain():
+        for f, (box, p) in enumerate(frames):
+            rdf.compute((box, p), reset=(f == 0))
+            st.compute((box, p), neighbors={"r_max": 1.5})
+            st.ql
+        return rdf.bin_counts_u64
+
+    def batched():
+        batch = freud.locality.FrameBatch(frames)
+        rdf.compute(batch)
+        st.compute(batch, neighbors={"r_max": 1.5})
+        st.ql
+        return rdf.bin_counts_u64
+
+    assert np.array_equal(plain(), batched()), "batched RDF counts differ from the per-frame path"
+    t_plain = _median_wall(plain, steps, 1)
+    t_batch = _median_wall(batched, steps, warmup)
+    return {"workload": "1024_frames_1000-4000_points", "particles": int(sum(len(p) for _, p in frames)),
+            "plain_e2e_ms": t_plain * 1e3, "batched_e2e_ms": t_batch * 1e3, "speedup_e2e": t_plain / t_batch}
 
 
 def measure_c5(freud, _lib, steps, warmup, small=False):
