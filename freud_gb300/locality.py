@@ -140,6 +140,27 @@ class _QueryArgs:
         return repr(self)
 
 
+def _match_class_path(obj, *matches):
+    return any(c.__module__ + "." + c.__name__ in matches for c in inspect.getmro(type(obj)))
+
+
+def _as_box_points(system):
+    """(box, points) from a system-like object: a (box, points) sequence, a GSD
+    frame (gsd.hoomd.Frame / Snapshot, hoomd Snapshot, freud_gb300.gsd.Frame:
+    box from configuration.box, 2D frames with Lz, xz, yz zeroed, points from
+    particles.position; freud/locality.py:327-336) or an object with box and
+    points attributes."""
+    if _match_class_path(system, "gsd.hoomd.Frame", "gsd.hoomd.Snapshot", "hoomd.snapshot.Snapshot",
+                         "freud_gb300.gsd.Frame"):
+        box = np.array(system.configuration.box)
+        if system.configuration.dimensions == 2:
+            box[[2, 4, 5]] = 0
+        return box, system.particles.position
+    if hasattr(system, "box") and hasattr(system, "points"):
+        return system.box, system.points
+    return system
+
+
 class NeighborQueryResult:
     """Lazy result of NeighborQuery.query (freud/locality.py:178-229)."""
 
@@ -193,18 +214,9 @@ class NeighborQuery:
         """Create a NeighborQuery from a system-like object: a NeighborQuery, a
         (box, points) sequence, or an object with box and points attributes."""
 
-        def _match_class_path(obj, *matches):
-            return any(c.__module__ + "." + c.__name__ in matches for c in inspect.getmro(type(obj)))
-
         if isinstance(system, cls):
             return system
-        if _match_class_path(system, "gsd.hoomd.Frame", "gsd.hoomd.Snapshot", "hoomd.snapshot.Snapshot"):
-            box = np.array(system.configuration.box)
-            if system.configuration.dimensions == 2:
-                box[[2, 4, 5]] = 0
-            system = (box, system.particles.position)
-        elif hasattr(system, "box") and hasattr(system, "points"):
-            system = (system.box, system.points)
+        system = _as_box_points(system)
         if cls == NeighborQuery:
             return _RawPoints(*system)
         return cls(*system)
@@ -306,9 +318,7 @@ class FrameBatch:
     def __init__(self, frames):
         boxes, pts = [], []
         for system in frames:
-            if hasattr(system, "box") and hasattr(system, "points"):
-                system = (system.box, system.points)
-            box, points = system
+            box, points = _as_box_points(system)
             b = _convert_box(box)
             boxes.append(b._c_box())
             pts.append(_convert_array(points, shape=(None, 3)))
