@@ -650,17 +650,33 @@ void make_query_set(fg_nq* nq, const GridEntry& g, const float* dq, uint32_t nqp
 // >= 3 cells on every periodic axis, and r_max + delta below half the smallest
 // nearest-plane distance, so the cell-derived image is the minimum image. delta
 // bounds the difference between the cell-shifted float distance and the exact one.
+//
+// cull2 (count pass): candidates farther than sqrt(cull2) from the bounds of a
+// cell's queries, in the same cell-shifted coordinates, are dropped before the
+// merge. Valid for wrap arithmetic under the prefilter's conditions and for AABB
+// arithmetic always (there each stencil entry is one image, and the cell-shifted
+// vector approximates r = p_j - (q + image) within delta); not for ghost copies.
 struct Prefilter
 {
-    float out2 = 0.0f; // reject beyond
-    float in2 = 0.0f;  // accept inside without the exact test (count pass, r_min == 0)
+    float out2 = 0.0f;  // reject beyond
+    float in2 = 0.0f;   // accept inside without the exact test (count pass, r_min == 0)
+    float cull2 = 0.0f; // drop candidates beyond, per cell (count pass)
 };
 
 Prefilter prefilter(const fg_nq* nq, int arith, const int dim[3], float r_max, float r_min)
 {
     Prefilter pf;
-    if (arith != ARITH_WRAP)
+    if (arith != ARITH_WRAP && arith != ARITH_AABB)
         return pf;
+    const double lmax = std::max(std::max(nq->box.L[0], nq->box.L[1]), nq->box.L[2]) *
+        (1.0 + std::abs(nq->box.xy) + std::abs(nq->box.xz) + std::abs(nq->box.yz));
+    const double delta = 2e-5 * (lmax + r_max) + 1e-6;
+    const double ro = r_max + delta;
+    if (arith == ARITH_AABB)
+    {
+        pf.cull2 = static_cast<float>(ro * ro * (1.0 + 1e-5));
+        return pf;
+    }
     if (dim[0] < 3 || dim[1] < 3 || (!nq->box.is2d && dim[2] < 3))
         return pf;
     float pd[3];
@@ -668,13 +684,10 @@ Prefilter prefilter(const fg_nq* nq, int arith, const int dim[3], float r_max, f
     double minp = std::min(pd[0], pd[1]);
     if (!nq->box.is2d)
         minp = std::min(minp, static_cast<double>(pd[2]));
-    const double lmax = std::max(std::max(nq->box.L[0], nq->box.L[1]), nq->box.L[2]) *
-        (1.0 + std::abs(nq->box.xy) + std::abs(nq->box.xz) + std::abs(nq->box.yz));
-    const double delta = 2e-5 * (lmax + r_max) + 1e-6;
     if (!(r_max + delta < 0.5 * minp))
         return pf;
-    const double ro = r_max + delta;
     pf.out2 = static_cast<float>(ro * ro * (1.0 + 1e-6));
+    pf.cull2 = static_cast<float>(ro * ro * (1.0 + 1e-5));
     if (r_min == 0.0f && r_max > 2.0 * delta)
     {
         const double ri = r_max - delta;
@@ -750,7 +763,7 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     p.arith = arith;
     p.nq = nqp;
     const Prefilter pf = prefilter(nq, arith, dim, a.r_max, a.r_min);
-    DevBuf counts, offsets, scratch, heavy, heavy_n, over, over_n, gmask, gsorted;
+    DevBuf counts, offsets, scratch, heavy, heavy_n, over, over_n, gmask, gsorted, gtotal;
     counts.alloc(sizeof(uint32_t) * (nqp + 1));
     offsets.alloc(sizeof(uint64_t) * (nqp + 1));
     scratch.alloc(scan_scratch_bytes(nqp + 1));
@@ -761,6 +774,7 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     {
         gmask.alloc(sizeof(uint32_t) * static_cast<size_t>(nqp) * CELL_CHUNKS);
         gsorted.alloc(sizeof(uint32_t) * static_cast<size_t>(g.ncell) * CELL_CAP);
+        gtotal.alloc(sizeof(uint32_t) * static_cast<size_t>(std::max(g.ncell, 1)));
     }
     FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (nqp + 1), s));
     FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
@@ -770,9 +784,9 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     if (cellwise)
     {
         // ghost grids hold copies of point indices; any index fits the same bound
-        launch_cell_scan(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, counts.as<uint32_t>(), gmask.as<uint32_t>(),
-                         gsorted.as<uint32_t>(), over.as<uint32_t>(), over_n.as<uint32_t>(), HistParams {}, nullptr, s,
-                         nq->n);
+        launch_cell_scan(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, pf.cull2, counts.as<uint32_t>(),
+                         gmask.as<uint32_t>(), gsorted.as<uint32_t>(), gtotal.as<uint32_t>(), over.as<uint32_t>(),
+                         over_n.as<uint32_t>(), HistParams {}, nullptr, s, nq->n);
         FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         sync();
         list = over.as<uint32_t>();
@@ -803,7 +817,8 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     if (cellwise)
     {
         launch_cell_emit(nq->dbox, view(g), qs.qg, p, gmask.as<uint32_t>(), gsorted.as<uint32_t>(),
-                         offsets.as<uint64_t>(), out.ij.as<uint2>(), out.dist.as<float>(), out.vec.as<float>(), s);
+                         gtotal.as<uint32_t>(), offsets.as<uint64_t>(), out.ij.as<uint2>(), out.dist.as<float>(),
+                         out.vec.as<float>(), s);
     }
     if (n_over > 0)
     {
@@ -970,6 +985,26 @@ void upload_points(const float* host, uint32_t n, DevBuf& buf)
     if (n > 0)
         FG_CUDA(cudaMemcpyAsync(buf.p, host, sizeof(float) * 3 * static_cast<size_t>(n), cudaMemcpyHostToDevice,
                                 stream()));
+}
+
+// Whether n query points already on the device (dq) equal the object's points
+// bit for bit; such a query runs on the object's own grid, as one with
+// query_points == NULL does (equal words give identical pair arithmetic).
+bool same_as_points(const fg_nq* nq, const float* dq, uint32_t n)
+{
+    if (n != nq->n || n == 0 || dq == nullptr)
+        return false;
+    if (dq == nq->dpts)
+        return true;
+    DevBuf flag;
+    flag.alloc(sizeof(uint32_t));
+    FG_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(uint32_t), stream()));
+    launch_words_differ(reinterpret_cast<const uint32_t*>(dq), reinterpret_cast<const uint32_t*>(nq->dpts),
+                        3ull * n, flag.as<uint32_t>(), stream());
+    uint32_t differ = 1;
+    FG_CUDA(cudaMemcpyAsync(&differ, flag.p, sizeof(differ), cudaMemcpyDeviceToHost, stream()));
+    sync();
+    return differ == 0;
 }
 
 void nq_init(fg_nq* nq, const fg_box* box, uint32_t n, int kind, float cell_width, const float* host_pts_for_check)
@@ -1168,8 +1203,11 @@ fg_status fg_nq_query(fg_nq* nq, const float* query_points, uint32_t n_query, co
         if (query_points != nullptr)
         {
             upload_points(query_points, n_query, dq);
-            qp = dq.as<float>();
-            nqp = n_query;
+            if (!same_as_points(nq, dq.as<float>(), n_query))
+            {
+                qp = dq.as<float>();
+                nqp = n_query;
+            }
         }
         auto nl = std::make_unique<fg_nlist>();
         run_query(nq, qp, nqp, args, sort_by_distance, *nl);
@@ -1186,7 +1224,8 @@ fg_status fg_nq_query_device(fg_nq* nq, const float* device_query_points, uint32
         require(args, "args");
         require(out, "out");
         auto nl = std::make_unique<fg_nlist>();
-        run_query(nq, device_query_points, device_query_points ? n_query : nq->n, args, sort_by_distance, *nl);
+        const float* qp = (device_query_points == nq->dpts && n_query == nq->n) ? nullptr : device_query_points;
+        run_query(nq, qp, qp ? n_query : nq->n, args, sort_by_distance, *nl);
         sync();
         *out = nl.release();
     });
@@ -1693,7 +1732,7 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
             over_n.alloc(sizeof(uint32_t));
             FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
             const Prefilter pf = prefilter(nq, p.arith, dim, a.r_max, a.r_min);
-            launch_cell_scan(1, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, nullptr, nullptr, nullptr,
+            launch_cell_scan(1, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr,
                              over.as<uint32_t>(), over_n.as<uint32_t>(), h, rdf->hist.as<unsigned long long>(), s);
             uint32_t n_over = 0;
             FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -1738,8 +1777,11 @@ fg_status fg_rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* query_points, u
         if (query_points != nullptr)
         {
             upload_points(query_points, n_query, dq);
-            qp = dq.as<float>();
-            nqp = n_query;
+            if (!same_as_points(nq, dq.as<float>(), n_query))
+            {
+                qp = dq.as<float>();
+                nqp = n_query;
+            }
         }
         rdf_accumulate(rdf, nq, qp, nqp, nlist, args);
     });
@@ -1751,7 +1793,8 @@ fg_status fg_rdf_accumulate_device(fg_rdf* rdf, fg_nq* nq, const float* device_q
     return guard([&] {
         require(rdf, "rdf");
         require(nq, "nq");
-        rdf_accumulate(rdf, nq, device_query_points, device_query_points ? n_query : nq->n, nlist, args);
+        const float* qp = (device_query_points == nq->dpts && n_query == nq->n) ? nullptr : device_query_points;
+        rdf_accumulate(rdf, nq, qp, qp ? n_query : nq->n, nlist, args);
     });
 }
 
@@ -2238,7 +2281,8 @@ fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points
         fg_nq probe;
         probe.box = hb;
         const Prefilter pf = prefilter(&probe, arith, dim, r_max, 0.0f);
-        launch_cell_scan(1, db, g, g, p, pf.out2, 0.0f, nullptr, nullptr, nullptr, over, over + 1, h, device_counts, s);
+        launch_cell_scan(1, db, g, g, p, pf.out2, 0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, over, over + 1, h,
+                         device_counts, s);
         FG_CUDA(cudaGetLastError());
     });
 }

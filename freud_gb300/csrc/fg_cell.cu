@@ -77,6 +77,11 @@ template<int MODE, typename K> struct ScanShared
     uint32_t j[CELL_CAP];             // point index
     uint32_t slot[CELL_CAP];          // grid slot << 5 | cell wrap code
     unsigned char run[CELL_CAP];      // stencil item (sorted run) of each staged position
+    unsigned char runc[MODE == SM_COUNT ? CELL_CAP : 1]; // run of each kept candidate (count pass)
+    uint32_t keep[MODE == SM_COUNT ? CELL_CAP / 32 : 1];  // kept-candidate ballots per (round, warp)
+    uint32_t keep_pre[MODE == SM_COUNT ? CELL_CAP / 32 + 1 : 1];
+    float qbox[SWARPS][6];            // per-warp bounds of the cell's shifted queries (lo xyz, hi xyz)
+    float qfin[6];                    // their union
     uint32_t mask[MODE == SM_COUNT ? QB : 1][CELL_CHUNKS]; // acceptance per (query, chunk), count pass
     float4 q[QB];
     float4 qs[QB];
@@ -241,9 +246,10 @@ __device__ __forceinline__ uint32_t rank_in(const K* src, uint32_t lo, uint32_t 
 
 template<int MODE, typename K>
 __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
-    k_cell_scan(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2,
+    k_cell_scan(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2, float cull2,
                 uint32_t* __restrict__ counts, uint32_t* __restrict__ gmask, uint32_t* __restrict__ gsorted,
-                uint32_t* overflow, uint32_t* overflow_n, HistParams h, unsigned long long* __restrict__ hist)
+                uint32_t* __restrict__ gtotal, uint32_t* overflow, uint32_t* overflow_n, HistParams h,
+                unsigned long long* __restrict__ hist)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ScanShared<MODE, K>& S = *reinterpret_cast<ScanShared<MODE, K>*>(smem_raw);
@@ -253,6 +259,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
     const int warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1u;
     const bool use_pre = pre_out2 > 0.0f;
+    const bool cull = MODE == SM_COUNT && cull2 > 0.0f;
     const bool smem_hist = MODE == SM_HIST && h.bins <= HIST_BINS_SMEM;
     uint32_t* queue = S.queue[warp];
 
@@ -271,14 +278,51 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
         const uint32_t nqc = qg.start[c + 1] - q0;
         if (nqc == 0)
             continue;
+        if (cull)
+        {
+            // bounds of the cell's queries in cell-shifted coordinates (the prefilter's frame)
+            float lo[3] = {3e30f, 3e30f, 3e30f}, hi[3] = {-3e30f, -3e30f, -3e30f};
+            for (uint32_t k = tid; k < nqc; k += STHREADS)
+            {
+                const float4 q = qg.cpos[q0 + k];
+                const int qim = __float_as_int(q.w);
+                const float3 qs = shifted(b, q, -img_ax(qim, 0), -img_ax(qim, 1), -img_ax(qim, 2));
+                lo[0] = fminf(lo[0], qs.x);
+                lo[1] = fminf(lo[1], qs.y);
+                lo[2] = fminf(lo[2], qs.z);
+                hi[0] = fmaxf(hi[0], qs.x);
+                hi[1] = fmaxf(hi[1], qs.y);
+                hi[2] = fmaxf(hi[2], qs.z);
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    lo[a] = fminf(lo[a], __shfl_xor_sync(FULL, lo[a], o));
+                    hi[a] = fmaxf(hi[a], __shfl_xor_sync(FULL, hi[a], o));
+                }
+            }
+            if (lane == 0)
+            {
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                {
+                    S.qbox[warp][a] = lo[a];
+                    S.qbox[warp][3 + a] = hi[a];
+                }
+            }
+        }
         if (warp == 0)
             cell_items(b, g, p.arith, c, S.it, lane);
         __syncthreads();
-        const uint32_t T = S.it.total;
+        uint32_t T = S.it.total;
         if (MODE == SM_COUNT && T > CELL_CAP)
         {
             for (uint32_t k = tid; k < nqc; k += STHREADS)
                 overflow[atomicAdd(overflow_n, 1u)] = q0 + k;
+            if (tid == 0)
+                gtotal[c] = 0xffffffffu;
             __syncthreads();
             continue;
         }
@@ -288,32 +332,113 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
             const uint32_t t0 = tile * CELL_CAP;
             const uint32_t TT = min(static_cast<uint32_t>(CELL_CAP), T - t0);
             // ---- stage candidates [t0, t0 + TT) ----
-            for (uint32_t tl = tid; tl < TT; tl += STHREADS)
+            if (cull)
             {
-                const uint32_t t = t0 + tl;
-                const int s = item_of(S.it, t);
-                const uint32_t slot = S.it.start[s] + (t - S.it.off[s]);
-                const float4 pp = g.cpos[slot];
-                const int wr = S.it.wrap[s];
-                const uint32_t jj = g.cidx[slot];
-                S.j[tl] = jj;
-                S.slot[tl] = (slot << 5) | static_cast<uint32_t>(wr);
-                S.run[tl] = static_cast<unsigned char>(s);
-                if (MODE == SM_HIST)
-                    S.pos[tl] = pp;
-                if (use_pre)
+                if (tid < 6)
                 {
-                    const int pim = __float_as_int(pp.w);
-                    const float3 sp = shifted(b, pp, (wr % 3 - 1) - img_ax(pim, 0), ((wr / 3) % 3 - 1) - img_ax(pim, 1),
-                                              (wr / 9 - 1) - img_ax(pim, 2));
-                    S.ps[tl] = sp;
+                    float v = S.qbox[0][tid];
+                    for (int w = 1; w < SWARPS; ++w)
+                        v = tid < 3 ? fminf(v, S.qbox[w][tid]) : fmaxf(v, S.qbox[w][tid]);
+                    S.qfin[tid] = v;
+                }
+                __syncthreads();
+            }
+            for (uint32_t base = 0; base < TT; base += STHREADS)
+            {
+                const uint32_t tl = base + tid;
+                bool kept = false;
+                if (tl < TT)
+                {
+                    const uint32_t t = t0 + tl;
+                    const int s = item_of(S.it, t);
+                    const uint32_t slot = S.it.start[s] + (t - S.it.off[s]);
+                    const float4 pp = g.cpos[slot];
+                    const int wr = S.it.wrap[s];
+                    const uint32_t jj = g.cidx[slot];
+                    S.j[tl] = jj;
+                    S.slot[tl] = (slot << 5) | static_cast<uint32_t>(wr);
+                    S.run[tl] = static_cast<unsigned char>(s);
+                    if (MODE == SM_HIST)
+                        S.pos[tl] = pp;
+                    float3 sp = make_float3(0.f, 0.f, 0.f);
+                    if (use_pre || cull)
+                    {
+                        const int pim = __float_as_int(pp.w);
+                        sp = shifted(b, pp, (wr % 3 - 1) - img_ax(pim, 0), ((wr / 3) % 3 - 1) - img_ax(pim, 1),
+                                     (wr / 9 - 1) - img_ax(pim, 2));
+                    }
+                    if (use_pre)
+                        S.ps[tl] = sp;
+                    if (cull)
+                    {
+                        // farther than r_max (+ the prefilter's margin) from the box of
+                        // every query of the cell: no bond with any of them
+                        const float gx = fmaxf(fmaxf(S.qfin[0] - sp.x, sp.x - S.qfin[3]), 0.f);
+                        const float gy = fmaxf(fmaxf(S.qfin[1] - sp.y, sp.y - S.qfin[4]), 0.f);
+                        const float gz = fmaxf(fmaxf(S.qfin[2] - sp.z, sp.z - S.qfin[5]), 0.f);
+                        kept = gx * gx + gy * gy + gz * gz <= cull2;
+                    }
+                    else if (MODE == SM_COUNT)
+                    {
+                        kept = true;
+                    }
                 }
                 if (MODE == SM_COUNT)
-                    S.u.keys.a[tl] = KT::make(jj, tl);
+                {
+                    const unsigned kb = __ballot_sync(FULL, kept);
+                    if (lane == 0)
+                        S.keep[(base / STHREADS) * SWARPS + warp] = kb;
+                }
             }
             const K* order = nullptr; // sorted keys (count pass)
             if (MODE == SM_COUNT)
             {
+                __syncthreads();
+                // compact the kept candidates: keys (point index, staged position) and
+                // their runs in staged order, so every run stays sorted
+                const uint32_t nbal = (TT + 31) / 32;
+                if (warp == 0)
+                {
+                    const uint32_t v = lane < static_cast<int>(nbal) ? __popc(S.keep[lane]) : 0u;
+                    uint32_t incl = v;
+                    for (int o = 1; o < 32; o <<= 1)
+                    {
+                        const uint32_t u = __shfl_up_sync(FULL, incl, o);
+                        if (lane >= o)
+                            incl += u;
+                    }
+                    S.keep_pre[lane] = incl - v;
+                    if (lane == 31)
+                        S.keep_pre[32] = incl;
+                }
+                __syncthreads();
+                for (uint32_t tl = tid; tl < TT; tl += STHREADS)
+                {
+                    const uint32_t wi = tl >> 5;
+                    const uint32_t kb = S.keep[wi];
+                    if ((kb >> lane) & 1u)
+                    {
+                        const uint32_t pos = S.keep_pre[wi] + __popc(kb & lt);
+                        S.u.keys.a[pos] = KT::make(S.j[tl], tl);
+                        S.runc[pos] = S.run[tl];
+                    }
+                }
+                T = S.keep_pre[32];
+                __syncthreads();
+                // run offsets among the kept candidates (runc is ascending)
+                if (tid <= 32)
+                {
+                    uint32_t a = 0, z = T;
+                    while (a < z)
+                    {
+                        const uint32_t m = (a + z) >> 1;
+                        if (static_cast<int>(S.runc[m]) < tid)
+                            a = m + 1;
+                        else
+                            z = m;
+                    }
+                    S.it.off[tid] = a;
+                }
                 __syncthreads();
                 // merge the <= 32 sorted runs (one per stencil item) pairwise, 5 levels
                 K* src = S.u.keys.a;
@@ -322,7 +447,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                 {
                     for (uint32_t e = tid; e < T; e += STHREADS)
                     {
-                        const int r = static_cast<int>(S.run[e]) >> L;
+                        const int r = static_cast<int>(S.runc[e]) >> L;
                         const int pr = r ^ 1;
                         const uint32_t lo_r = S.it.off[min(r << L, 32)];
                         const uint32_t lo_p = S.it.off[min(pr << L, 32)];
@@ -340,9 +465,12 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                 // the sorted order (grid slot << 5 | wrap) is what the write pass replays
                 for (uint32_t e = tid; e < T; e += STHREADS)
                     gsorted[static_cast<size_t>(c) * CELL_CAP + e] = S.slot[KT::pos(order[e])];
+                if (tid == 0)
+                    gtotal[c] = T;
             }
             __syncthreads();
-            const uint32_t nchunks = (TT + 31) / 32;
+            const uint32_t TC = MODE == SM_COUNT ? T : TT; // candidates swept
+            const uint32_t nchunks = (TC + 31) / 32;
 
             for (uint32_t qb0 = 0; qb0 < nqc; qb0 += QB)
             {
@@ -408,7 +536,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                 for (uint32_t ch = warp; ch < nchunks; ch += SWARPS)
                 {
                     const uint32_t e = ch * 32 + lane;
-                    const bool live = e < TT;
+                    const bool live = e < TC;
                     const uint32_t t = (MODE == SM_COUNT && live) ? KT::pos(order[e]) : e;
                     float3 ps = make_float3(3e30f, 3e30f, 3e30f);
                     uint32_t jj = 0xffffffffu;
@@ -681,14 +809,14 @@ struct EmitShared
     uint32_t j[CELL_CAP];  // point index in sorted order
     unsigned char wrap[CELL_CAP];
     uint32_t queue[EWARPS][64];
-    Items it;
     float img[27][3];
 };
 
 __global__ void __launch_bounds__(ETHREADS, 5)
     k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
-                const uint32_t* __restrict__ gsorted, const uint64_t* __restrict__ offsets, uint2* __restrict__ ij,
-                float* __restrict__ dist, float* __restrict__ vec)
+                const uint32_t* __restrict__ gsorted, const uint32_t* __restrict__ gtotal,
+                const uint64_t* __restrict__ offsets, uint2* __restrict__ ij, float* __restrict__ dist,
+                float* __restrict__ vec)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     EmitShared& S = *reinterpret_cast<EmitShared*>(smem_raw);
@@ -706,15 +834,11 @@ __global__ void __launch_bounds__(ETHREADS, 5)
         const uint32_t nqc = qg.start[c + 1] - q0;
         if (nqc == 0)
             continue;
-        if (warp == 0)
-            cell_items(b, g, p.arith, c, S.it, lane);
-        __syncthreads();
-        const uint32_t T = S.it.total;
+        // candidates the scan pass kept for this cell (all-ones: the cell's queries
+        // went to the warp-per-query kernels)
+        const uint32_t T = gtotal[c];
         if (T > CELL_CAP)
-        {
-            __syncthreads();
-            continue; // written by the warp-per-query kernel
-        }
+            continue;
         for (uint32_t e = tid; e < T; e += ETHREADS)
         {
             const uint32_t ent = gsorted[static_cast<size_t>(c) * CELL_CAP + e];
@@ -822,9 +946,9 @@ size_t cell_smem_bytes()
 }
 
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
-                      float pre_out2, float pre_in2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
-                      uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
-                      cudaStream_t s, uint32_t n_points)
+                      float pre_out2, float pre_in2, float cull2, uint32_t* counts, uint32_t* gmask,
+                      uint32_t* gsorted, uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n,
+                      const HistParams& h, unsigned long long* hist, cudaStream_t s, uint32_t n_points)
 {
     // one wave of resident blocks walking the cells
     auto grid = [&](auto kernel, size_t smem) {
@@ -842,7 +966,7 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
         const int blocks = grid(k_cell_scan<SM_COUNT, unsigned int>, smem);
         ProfScope prof_("k_cell_scan<COUNT>", s);
         k_cell_scan<SM_COUNT, unsigned int><<<blocks, STHREADS, smem, s>>>(
-            box, g, qg, p, pre_out2, pre_in2, counts, gmask, gsorted, overflow, overflow_n, h, hist);
+            box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
     }
     else if (!hist_mode)
     {
@@ -852,7 +976,7 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
         const int blocks = grid(k_cell_scan<SM_COUNT, unsigned long long>, smem);
         ProfScope prof_("k_cell_scan<COUNT>", s);
         k_cell_scan<SM_COUNT, unsigned long long><<<blocks, STHREADS, smem, s>>>(
-            box, g, qg, p, pre_out2, pre_in2, counts, gmask, gsorted, overflow, overflow_n, h, hist);
+            box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
     }
     else
     {
@@ -862,13 +986,13 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
         const int blocks = grid(k_cell_scan<SM_HIST, unsigned long long>, smem);
         ProfScope prof_("k_cell_scan<HIST>", s);
         k_cell_scan<SM_HIST, unsigned long long><<<blocks, STHREADS, smem, s>>>(
-            box, g, qg, p, pre_out2, 0.0f, counts, gmask, gsorted, overflow, overflow_n, h, hist);
+            box, g, qg, p, pre_out2, 0.0f, 0.0f, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
     }
 }
 
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
-                      const uint32_t* gmask, const uint32_t* gsorted, const uint64_t* offsets, uint2* ij, float* dist,
-                      float* vec, cudaStream_t s)
+                      const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
+                      uint2* ij, float* dist, float* vec, cudaStream_t s)
 {
     const int want = 5 * sm_count_cell();
     const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
@@ -876,7 +1000,7 @@ void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, co
     static bool done = false;
     configure(k_cell_emit, smem, done);
     ProfScope prof_("k_cell_emit", s);
-    k_cell_emit<<<blocks, ETHREADS, smem, s>>>(box, g, qg, p, gmask, gsorted, offsets, ij, dist, vec);
+    k_cell_emit<<<blocks, ETHREADS, smem, s>>>(box, g, qg, p, gmask, gsorted, gtotal, offsets, ij, dist, vec);
 }
 
 } // namespace fg

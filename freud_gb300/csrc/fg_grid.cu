@@ -244,6 +244,35 @@ void launch_fill_f32(float* a, float v, uint64_t n, cudaStream_t s)
     }
 }
 
+// flag |= 1 when the n 32-bit words of a and b differ anywhere (bitwise: equal
+// words give identical pair arithmetic, so a query whose points equal the
+// object's points can run on the object's own grid).
+__global__ void k_words_differ(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t n,
+                               uint32_t* flag)
+{
+    bool d = false;
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+    {
+        d |= a[i] != b[i];
+    }
+    if (__syncthreads_or(d) && threadIdx.x == 0)
+    {
+        atomicOr(flag, 1u);
+    }
+}
+
+void launch_words_differ(const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* flag, cudaStream_t s)
+{
+    if (n == 0)
+    {
+        return;
+    }
+    {
+        ProfScope prof_("k_words_differ", s);
+        k_words_differ<<<grid_for(n, 256), 256, 0, s>>>(a, b, n, flag);
+    }
+}
+
 // segments[i] = first bond of query i, counts[i] = its bond count
 // (NeighborList::updateSegmentCounts, NeighborList.cc:199-232; queries with no
 // bonds keep segment 0 and count 0 as the reference leaves them).

@@ -124,13 +124,18 @@ constexpr int CELL_CAP = 1024;
 constexpr int CELL_CHUNKS = CELL_CAP / 32;
 size_t cell_smem_bytes();
 // n_points: number of points of g (point indices below 2^22 allow 32-bit merge keys).
+// cull2 > 0 (count pass): candidates farther than sqrt(cull2) from the bounds of
+// every query of the cell, in cell-shifted coordinates, are dropped before the
+// merge; gtotal[cell] = candidates kept (all-ones for cells handed to the
+// warp-per-query kernels), read by the emit pass.
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
-                      float pre_out2, float pre_in2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
-                      uint32_t* overflow, uint32_t* overflow_n, const HistParams& h, unsigned long long* hist,
-                      cudaStream_t s, uint32_t n_points = 0xffffffffu);
+                      float pre_out2, float pre_in2, float cull2, uint32_t* counts, uint32_t* gmask,
+                      uint32_t* gsorted, uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n,
+                      const HistParams& h, unsigned long long* hist, cudaStream_t s,
+                      uint32_t n_points = 0xffffffffu);
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
-                      const uint32_t* gmask, const uint32_t* gsorted, const uint64_t* offsets, uint2* ij, float* dist,
-                      float* vec, cudaStream_t s);
+                      const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
+                      uint2* ij, float* dist, float* vec, cudaStream_t s);
 
 // Histogram of a distance array (RDF over a NeighborList).
 void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,
@@ -169,6 +174,8 @@ void launch_knn_compact(const uint32_t* tj, const float* td, const float* tv, ui
 
 // ---- NeighborList helpers -------------------------------------------------------
 void launch_fill_f32(float* a, float v, uint64_t n, cudaStream_t s);
+// *flag |= 1 when a[0..n) and b[0..n) differ bitwise (flag zeroed by the caller).
+void launch_words_differ(const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* flag, cudaStream_t s);
 void launch_segments(const uint2* ij, uint64_t nb, uint32_t nq, uint32_t* segments, uint32_t* counts,
                      cudaStream_t s);
 // segments[i] = counts[i] ? offsets[i] : 0 (NeighborList.cc:199-232 for a list built in query order)

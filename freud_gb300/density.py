@@ -66,10 +66,9 @@ class RDF(_SpatialHistogram1D):
             return self
         nq, nlist, qargs, l_query_points, num_query_points = self._preprocess_arguments(
             system, query_points, neighbors)
-        qp = np.ascontiguousarray(l_query_points, dtype=np.float32)
-        qp_arg = None if nq._same_points(qp) else qp
+        qp_arg = nq._query_points_arg(l_query_points)
         _lib.check(_lib.lib.fg_rdf_accumulate(
-            self._h, nq._h, _lib.ptr(qp_arg), len(qp), None if nlist is None else nlist._h,
+            self._h, nq._h, _lib.ptr(qp_arg), num_query_points, None if nlist is None else nlist._h,
             ctypes.byref(qargs._c())))
         return self
 

@@ -14,9 +14,6 @@ from .util import _Compute, _convert_array, _convert_box
 
 ITERATOR_TERMINATOR = None
 
-_memcmp = _lib.ctypes.CDLL(None).memcmp
-_memcmp.restype = _lib.ctypes.c_int
-_memcmp.argtypes = [_lib.ctypes.c_void_p, _lib.ctypes.c_void_p, _lib.ctypes.c_size_t]
 NO_DEFAULT_QUERY_ARGS_MESSAGE = (
     "Query arguments must be provided for {} objects since there is no default set of arguments."
 )
@@ -239,24 +236,21 @@ class NeighborQuery:
         return NeighborQueryResult(self, query_points, args)
 
     # -- internals ------------------------------------------------------------------
-    def _same_points(self, query_points):
-        """Whether query_points hold exactly this object's points (then the query
-        reuses the object's own cell grid). Byte comparison with memcmp: no
-        temporaries for million-point arrays."""
-        p = self.points
-        if query_points is p:
-            return True
-        if query_points.shape != p.shape or query_points.dtype != p.dtype:
-            return False
-        q = np.ascontiguousarray(query_points)
-        return _memcmp(q.ctypes.data, p.ctypes.data, p.nbytes) == 0
+    def _query_points_arg(self, query_points):
+        """query_points as passed to the library: None for this object's own host
+        copy (already on the device); anything else is uploaded, and the library
+        compares it with the object's points on the device and reuses the
+        object's cell grid when they are equal."""
+        if query_points is None or query_points is self._points:
+            return None
+        return np.ascontiguousarray(query_points, dtype=np.float32)
 
     def _is_nearest(self, qargs):
         return qargs.mode == "nearest" or (qargs.mode is None and qargs.num_neighbors != _lib.DEFAULT_NUM_NEIGHBORS)
 
     def _query_nlist(self, query_points, qargs, sort_by_distance=False):
         query_points = np.ascontiguousarray(query_points, dtype=np.float32)
-        qp = None if self._same_points(query_points) else query_points
+        qp = self._query_points_arg(query_points)
         h = _lib.ctypes.c_void_p()
         _lib.check(_lib.lib.fg_nq_query(self._h, _lib.ptr(qp), len(query_points), _lib.ctypes.byref(qargs._c()),
                                         int(bool(sort_by_distance)), _lib.ctypes.byref(h)))
@@ -581,10 +575,11 @@ class _PairCompute(_Compute):
         nq = NeighborQuery.from_system(system)
         nlist, qargs = self._resolve_neighbors(neighbors, query_points)
         if query_points is None:
-            query_points = nq.points
+            # the system's own points, already on the device (no host copy)
+            num_query_points = nq._n_points
         else:
             query_points = _convert_array(query_points, shape=(None, 3))
-        num_query_points = query_points.shape[0]
+            num_query_points = query_points.shape[0]
         return (nq, nlist, qargs, query_points, num_query_points)
 
     def _resolve_neighbors(self, neighbors, query_points=None):
