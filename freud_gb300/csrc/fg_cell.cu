@@ -24,10 +24,12 @@
 //    candidates hand their queries to the warp-per-query kernels.
 //  - histogram (fused RDF): no ordering; the candidate set is processed in tiles
 //    of CELL_CAP, so dense cells stay on this path.
-// Write pass: warp per query; the set bits of its masks, in chunk order, are its
-// bonds in the reference's (i, j) order (NeighborBond.h:80-95); they are
-// compacted 32 at a time, their exact vectors recomputed and written to 32
-// consecutive slots at the query's offset.
+//    Before the merge, candidates farther than r_max (+ margin) from the bounds
+//    of every query of the cell are dropped.
+// Write pass: warp per cell, query by query; the set bits of a query's masks, in
+// chunk order, are its bonds in the reference's (i, j) order
+// (NeighborBond.h:80-95); each lane takes one bond of a round of 32, recomputes
+// its exact vector and writes it at the query's offset + the bond's rank.
 #include <algorithm>
 
 #include "fg_kernels.cuh"
@@ -803,120 +805,115 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
     }
 }
 
-struct EmitShared
+// Position of the k-th (from 0) set bit of w; k < popc(w).
+__device__ __forceinline__ uint32_t kth_set_bit(uint32_t w, uint32_t k)
 {
-    float4 pos[CELL_CAP];  // candidate positions in sorted order
-    uint32_t j[CELL_CAP];  // point index in sorted order
-    unsigned char wrap[CELL_CAP];
-    uint32_t queue[EWARPS][64];
-    float img[27][3];
-};
+    uint32_t pos = 0;
+#pragma unroll
+    for (int half = 16; half >= 1; half >>= 1)
+    {
+        const uint32_t c = __popc(w & ((1u << half) - 1u));
+        if (k >= c)
+        {
+            k -= c;
+            w >>= half;
+            pos += half;
+        }
+    }
+    return pos;
+}
 
+// Write pass, warp per cell: no shared staging and no block barriers. A warp
+// takes one cell and writes the bonds of each of its queries: lane l of a round
+// writes the query's bond number base + l, found from the prefix sums of the
+// per-chunk acceptance counts (one chunk per lane) and the set bits of that
+// chunk's mask. Candidates are read through the cell's sorted list (gsorted)
+// from L1/L2, where the cell's other queries keep them.
 __global__ void __launch_bounds__(ETHREADS, 5)
     k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
                 const uint32_t* __restrict__ gsorted, const uint32_t* __restrict__ gtotal,
                 const uint64_t* __restrict__ offsets, uint2* __restrict__ ij, float* __restrict__ dist,
                 float* __restrict__ vec)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    EmitShared& S = *reinterpret_cast<EmitShared*>(smem_raw);
+    __shared__ float img_s[27][3];
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
-    const unsigned lt = (1u << lane) - 1u;
-    uint32_t* queue = S.queue[warp];
     for (int t = tid; t < 81; t += ETHREADS)
-        S.img[t / 3][t % 3] = b.img[t / 3][t % 3];
+        img_s[t / 3][t % 3] = b.img[t / 3][t % 3];
     __syncthreads();
-    for (int c = blockIdx.x; c < qg.ncell; c += gridDim.x)
+    const int nwarps = gridDim.x * EWARPS;
+    for (int c = blockIdx.x * EWARPS + warp; c < qg.ncell; c += nwarps)
     {
         const uint32_t q0 = qg.start[c];
         const uint32_t nqc = qg.start[c + 1] - q0;
         if (nqc == 0)
             continue;
-        // candidates the scan pass kept for this cell (all-ones: the cell's queries
-        // went to the warp-per-query kernels)
         const uint32_t T = gtotal[c];
         if (T > CELL_CAP)
-            continue;
-        for (uint32_t e = tid; e < T; e += ETHREADS)
-        {
-            const uint32_t ent = gsorted[static_cast<size_t>(c) * CELL_CAP + e];
-            S.pos[e] = g.cpos[ent >> 5];
-            S.j[e] = g.cidx[ent >> 5];
-            S.wrap[e] = static_cast<unsigned char>(ent & 31u);
-        }
-        __syncthreads();
+            continue; // the cell's queries are written by the warp-per-query kernels
+        const uint32_t* srt = gsorted + static_cast<size_t>(c) * CELL_CAP;
         const uint32_t nchunks = (T + 31) / 32;
-        // one-ahead prefetch of each warp's next query (position, index, mask row)
-        float4 q_n = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint32_t qi_n = 0, mw_n = 0;
-        if (static_cast<uint32_t>(warp) < nqc)
-        {
-            q_n = qg.cpos[q0 + warp];
-            qi_n = qg.cidx[q0 + warp];
-            mw_n = lane < static_cast<int>(nchunks) ? gmask[static_cast<size_t>(q0 + warp) * CELL_CHUNKS + lane] : 0u;
-        }
-        for (uint32_t qq = warp; qq < nqc; qq += EWARPS)
+        float4 q_n = qg.cpos[q0];
+        uint32_t qi_n = qg.cidx[q0];
+        uint32_t mw_n = lane < static_cast<int>(nchunks) ? gmask[static_cast<size_t>(q0) * CELL_CHUNKS + lane] : 0u;
+        for (uint32_t qq = 0; qq < nqc; ++qq)
         {
             const float4 q = q_n;
             const uint32_t qi = qi_n;
             const uint32_t mword = mw_n;
             const int qimg = __float_as_int(q.w);
-            if (qq + EWARPS < nqc)
-            {
-                q_n = qg.cpos[q0 + qq + EWARPS];
-                qi_n = qg.cidx[q0 + qq + EWARPS];
-                mw_n = lane < static_cast<int>(nchunks)
-                    ? gmask[static_cast<size_t>(q0 + qq + EWARPS) * CELL_CHUNKS + lane] : 0u;
-            }
             const uint64_t out = offsets[qi];
-            uint32_t written = 0;
-            uint32_t qn = 0;
-            auto process = [&](uint32_t n) {
-                if (lane < static_cast<int>(n))
+            if (qq + 1 < nqc)
+            {
+                // one-ahead prefetch of the next query (position, index, mask row)
+                q_n = qg.cpos[q0 + qq + 1];
+                qi_n = qg.cidx[q0 + qq + 1];
+                mw_n = lane < static_cast<int>(nchunks)
+                    ? gmask[static_cast<size_t>(q0 + qq + 1) * CELL_CHUNKS + lane] : 0u;
+            }
+            const uint32_t cnt = __popc(mword);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o)
+                    incl += v;
+            }
+            const uint32_t excl = incl - cnt;
+            const uint32_t total = __shfl_sync(FULL, incl, 31);
+            for (uint32_t base = 0; base < total; base += 32)
+            {
+                const uint32_t bb = base + static_cast<uint32_t>(lane);
+                // chunk of bond bb: the last chunk whose exclusive prefix is <= bb
+                int ch = 0;
+#pragma unroll
+                for (int step = 16; step >= 1; step >>= 1)
                 {
-                    const uint32_t e = queue[lane];
+                    const uint32_t v = __shfl_sync(FULL, excl, ch + step);
+                    if (v <= bb)
+                        ch += step;
+                }
+                const uint32_t w = __shfl_sync(FULL, mword, ch);
+                const uint32_t k = bb - __shfl_sync(FULL, excl, ch);
+                if (bb < total)
+                {
+                    const uint32_t ent = srt[static_cast<uint32_t>(ch) * 32u + kth_set_bit(w, k)];
+                    const uint32_t slot = ent >> 5;
+                    const float4 pp = g.cpos[slot];
+                    const uint32_t jj = g.cidx[slot];
                     float rx, ry, rz;
-                    exact_vec(b, S.img, p.arith, q, qimg, S.pos[e], static_cast<int>(S.wrap[e]), rx, ry, rz);
-                    const uint64_t o = out + written + lane;
-                    ij[o] = make_uint2(qi, S.j[e]);
+                    exact_vec(b, img_s, p.arith, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
+                    const uint64_t o = out + bb;
+                    ij[o] = make_uint2(qi, jj);
                     dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
                     vec[3 * o] = rx;
                     vec[3 * o + 1] = ry;
                     vec[3 * o + 2] = rz;
                 }
-                written += n;
-            };
-            unsigned live_chunks = __ballot_sync(FULL, mword != 0);
-            while (live_chunks != 0)
-            {
-                const int ch = __ffs(live_chunks) - 1;
-                live_chunks &= live_chunks - 1;
-                const uint32_t m = __shfl_sync(FULL, mword, ch);
-                if ((m >> lane) & 1u)
-                    queue[qn + __popc(m & lt)] = static_cast<uint32_t>(ch) * 32u + lane;
-                qn += __popc(m);
-                __syncwarp();
-                if (qn >= 32)
-                {
-                    process(32);
-                    const uint32_t rest = qn - 32;
-                    uint32_t v = 0;
-                    if (lane < static_cast<int>(rest))
-                        v = queue[32 + lane];
-                    __syncwarp();
-                    if (lane < static_cast<int>(rest))
-                        queue[lane] = v;
-                    __syncwarp();
-                    qn = rest;
-                }
             }
-            if (qn > 0)
-                process(qn);
-            __syncwarp();
         }
-        __syncthreads();
     }
 }
 
@@ -994,13 +991,13 @@ void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, co
                       const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
                       uint2* ij, float* dist, float* vec, cudaStream_t s)
 {
-    const int want = 5 * sm_count_cell();
-    const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
-    const size_t smem = sizeof(EmitShared);
-    static bool done = false;
-    configure(k_cell_emit, smem, done);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_emit, ETHREADS, 0);
+    const int want = std::max(per_sm, 1) * sm_count_cell();
+    const int need = (qg.ncell + EWARPS - 1) / EWARPS;
+    const int blocks = need < want ? std::max(need, 1) : want;
     ProfScope prof_("k_cell_emit", s);
-    k_cell_emit<<<blocks, ETHREADS, smem, s>>>(box, g, qg, p, gmask, gsorted, gtotal, offsets, ij, dist, vec);
+    k_cell_emit<<<blocks, ETHREADS, 0, s>>>(box, g, qg, p, gmask, gsorted, gtotal, offsets, ij, dist, vec);
 }
 
 } // namespace fg
