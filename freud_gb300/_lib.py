@@ -76,6 +76,13 @@ SIGNATURES = {
     "fg_nlist_filter": [P, P],
     "fg_nlist_filter_r": [P, f32, f32],
     "fg_nlist_sort": [P, i32],
+    "fg_cf_create": [u32, f32, PP],
+    "fg_cf_destroy": [P],
+    "fg_cf_reset": [P],
+    "fg_cf_accumulate": [P, P, P, u32, P, u32, P, u32, P, pargs],
+    "fg_cf_get": [P, P, P],
+    "fg_cf_bin_edges": [P, P, P],
+    "fg_cf_state": [P, pbox, pu32],
     "fg_rdf_create": [u32, f32, f32, PP],
     "fg_rdf_destroy": [P],
     "fg_rdf_set_mode": [P, i32],

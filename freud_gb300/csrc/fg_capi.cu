@@ -338,6 +338,16 @@ struct fg_rdf
     uint32_t frames = 0, n_points = 0, n_query = 0;
 };
 
+struct fg_cf
+{
+    uint32_t bins;
+    float r_max;
+    DevBuf sums;   // double2 per bin: running sum of conj(values[j]) * query_values[i]
+    DevBuf counts; // uint64 per bin
+    HostBox box {};
+    uint32_t frames = 0;
+};
+
 struct fg_steinhardt
 {
     std::vector<uint32_t> ls;
@@ -1900,6 +1910,183 @@ fg_status fg_rdf_bin_edges(const fg_rdf* rdf, float* edges, float* centers)
         if (centers)
             for (uint32_t i = 0; i < rdf->bins; ++i)
                 centers[i] = fdiv(fadd(e[i], e[i + 1]), 2.0f);
+    });
+}
+
+// ---- CorrelationFunction ------------------------------------------------------------
+fg_status fg_cf_create(uint32_t bins, float r_max, fg_cf** out)
+{
+    return guard([&] {
+        require(out, "out");
+        // CorrelationFunction.cc:26-45
+        if (bins == 0)
+            value_error("CorrelationFunction  requires a nonzero number of bins.");
+        if (r_max <= 0.0f)
+            value_error("CorrelationFunction requires r_max to be positive.");
+        auto c = std::make_unique<fg_cf>();
+        c->bins = bins;
+        c->r_max = r_max;
+        c->sums.alloc(sizeof(double2) * bins);
+        c->counts.alloc(sizeof(unsigned long long) * bins);
+        FG_CUDA(cudaMemsetAsync(c->sums.p, 0, sizeof(double2) * bins, stream()));
+        FG_CUDA(cudaMemsetAsync(c->counts.p, 0, sizeof(unsigned long long) * bins, stream()));
+        sync();
+        *out = c.release();
+    });
+}
+
+fg_status fg_cf_destroy(fg_cf* cf)
+{
+    return guard([&] {
+        delete cf;
+        sync();
+    });
+}
+
+fg_status fg_cf_reset(fg_cf* cf)
+{
+    return guard([&] {
+        require(cf, "cf");
+        FG_CUDA(cudaMemsetAsync(cf->sums.p, 0, sizeof(double2) * cf->bins, stream()));
+        FG_CUDA(cudaMemsetAsync(cf->counts.p, 0, sizeof(unsigned long long) * cf->bins, stream()));
+        cf->frames = 0;
+        sync();
+    });
+}
+
+static HistParams cf_hist_params(const fg_cf* c)
+{
+    // RegularAxis(bins, 0, r_max), Histogram.h:123-138
+    HistParams h;
+    h.h_min = 0.0f;
+    h.h_max = c->r_max;
+    const float bw = fdiv(c->r_max, static_cast<float>(c->bins));
+    h.h_inv = fdiv(1.0f, bw);
+    h.bins = c->bins;
+    return h;
+}
+
+fg_status fg_cf_accumulate(fg_cf* cf, fg_nq* nq, const double* values, uint32_t n_values, const float* query_points,
+                           uint32_t n_query, const double* query_values, uint32_t n_query_values,
+                           const fg_nlist* nlist, const fg_query_args* args)
+{
+    return guard([&] {
+        require(cf, "cf");
+        require(nq, "nq");
+        require(values, "values");
+        if (n_values != nq->n)
+            value_error("values must hold one value per point.");
+        cudaStream_t s = stream();
+        DevBuf dq;
+        const float* qp = nullptr;
+        uint32_t nqp = nq->n;
+        if (query_points != nullptr)
+        {
+            upload_points(query_points, n_query, dq);
+            if (!same_as_points(nq, dq.as<float>(), n_query))
+            {
+                qp = dq.as<float>();
+                nqp = n_query;
+            }
+        }
+        if (query_values == nullptr)
+        {
+            query_values = values;
+            n_query_values = n_values;
+        }
+        if (n_query_values < nqp)
+            value_error("query_values must hold one value per query point.");
+        DevBuf dv, dqv;
+        dv.alloc(sizeof(double2) * std::max<uint32_t>(n_values, 1));
+        FG_CUDA(cudaMemcpyAsync(dv.p, values, sizeof(double2) * n_values, cudaMemcpyHostToDevice, s));
+        const double2* qv = dv.as<double2>();
+        if (query_values != values)
+        {
+            dqv.alloc(sizeof(double2) * std::max<uint32_t>(n_query_values, 1));
+            FG_CUDA(cudaMemcpyAsync(dqv.p, query_values, sizeof(double2) * n_query_values, cudaMemcpyHostToDevice,
+                                    s));
+            qv = dqv.as<double2>();
+        }
+        fg_nlist tmp;
+        const fg_nlist* bonds = nlist;
+        if (nlist == nullptr)
+        {
+            require(args, "args");
+            run_query(nq, qp, nqp, args, 0, tmp);
+            bonds = &tmp;
+        }
+        else if (nlist->np > n_values || nlist->nq > n_query_values)
+        {
+            // the reference indexes values with the list's indices unchecked
+            value_error("NeighborList found inconsistent array sizes.");
+        }
+        launch_cf_bonds(bonds->ij.as<uint2>(), bonds->dist.as<float>(), bonds->nb, dv.as<double2>(), qv,
+                        cf_hist_params(cf), cf->sums.as<double2>(), cf->counts.as<unsigned long long>(), s);
+        FG_CUDA(cudaGetLastError());
+        // BondHistogramCompute::accumulateGeneral (BondHistogramCompute.h:115-126)
+        cf->box = nq->box;
+        cf->frames += 1;
+        sync();
+    });
+}
+
+fg_status fg_cf_get(fg_cf* cf, uint32_t* bin_counts, double* correlation)
+{
+    return guard([&] {
+        require(cf, "cf");
+        std::vector<unsigned long long> c(cf->bins);
+        std::vector<double> sm(2 * static_cast<size_t>(cf->bins));
+        FG_CUDA(cudaMemcpyAsync(c.data(), cf->counts.p, sizeof(unsigned long long) * cf->bins, cudaMemcpyDeviceToHost,
+                                stream()));
+        FG_CUDA(cudaMemcpyAsync(sm.data(), cf->sums.p, sizeof(double2) * cf->bins, cudaMemcpyDeviceToHost, stream()));
+        sync();
+        for (uint32_t i = 0; i < cf->bins; ++i)
+        {
+            // CorrelationFunction::reduce (CorrelationFunction.cc:48-59): sum / count
+            // where the count is nonzero; the histogram holds unsigned int counts
+            const uint32_t n = static_cast<uint32_t>(c[i]);
+            if (bin_counts)
+                bin_counts[i] = n;
+            if (correlation)
+            {
+                double re = sm[2 * i], im = sm[2 * i + 1];
+                if (n != 0)
+                {
+                    re /= static_cast<double>(n);
+                    im /= static_cast<double>(n);
+                }
+                correlation[2 * i] = re;
+                correlation[2 * i + 1] = im;
+            }
+        }
+    });
+}
+
+fg_status fg_cf_bin_edges(const fg_cf* cf, float* edges, float* centers)
+{
+    return guard([&] {
+        require(cf, "cf");
+        // Histogram.h:126-138: edges[i] = min + float(i) * bin_width
+        const float bw = fdiv(cf->r_max, static_cast<float>(cf->bins));
+        std::vector<float> e(cf->bins + 1);
+        for (uint32_t i = 0; i <= cf->bins; ++i)
+            e[i] = fadd(0.0f, fmul(static_cast<float>(i), bw));
+        if (edges)
+            std::memcpy(edges, e.data(), sizeof(float) * (cf->bins + 1));
+        if (centers)
+            for (uint32_t i = 0; i < cf->bins; ++i)
+                centers[i] = fdiv(fadd(e[i], e[i + 1]), 2.0f);
+    });
+}
+
+fg_status fg_cf_state(const fg_cf* cf, fg_box* box, uint32_t* n_frames)
+{
+    return guard([&] {
+        require(cf, "cf");
+        if (box)
+            *box = to_c_box(cf->box);
+        if (n_frames)
+            *n_frames = cf->frames;
     });
 }
 

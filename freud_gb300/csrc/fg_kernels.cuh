@@ -141,6 +141,11 @@ void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, co
 void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,
                            cudaStream_t s);
 
+// CorrelationFunction over bonds (ij, distance): counts[bin] += 1 and
+// sums[bin] += conj(values[j]) * qvalues[i] (FP64 complex as double2).
+void launch_cf_bonds(const uint2* ij, const float* dist, uint64_t nb, const double2* values, const double2* qvalues,
+                     const HistParams& h, double2* sums, unsigned long long* counts, cudaStream_t s);
+
 // ---- k nearest neighbours ------------------------------------------------------
 struct KnnParams
 {

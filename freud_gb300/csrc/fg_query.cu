@@ -739,4 +739,93 @@ void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, 
     }
 }
 
+// CorrelationFunction::accumulate (CorrelationFunction.cc:79-96): for each bond
+// (query i, point j) whose distance falls in a bin, count[bin] += 1 and
+// sum[bin] += conj(values[j]) * query_values[i] in FP64, products rounded as
+// std::complex<double> forms them (re = vr*qr + vi*qi, im = vr*qi - vi*qr; no
+// contraction). Per-block shared sums (CF_SMEM_BINS bins or fewer) flushed with
+// global atomics; the FP64 summation order differs from the reference's
+// thread-local sums, as the reference's own order depends on its threads.
+constexpr int CF_SMEM_BINS = 1024;
+
+__global__ void k_cf_bonds(const uint2* __restrict__ ij, const float* __restrict__ dist, uint64_t nb,
+                           const double2* __restrict__ values, const double2* __restrict__ qvalues, HistParams h,
+                           double2* __restrict__ sums, unsigned long long* __restrict__ counts)
+{
+    __shared__ double s_re[CF_SMEM_BINS];
+    __shared__ double s_im[CF_SMEM_BINS];
+    __shared__ unsigned int s_cnt[CF_SMEM_BINS];
+    const bool smem = h.bins <= CF_SMEM_BINS;
+    if (smem)
+    {
+        for (uint32_t t = threadIdx.x; t < h.bins; t += blockDim.x)
+        {
+            s_re[t] = 0.0;
+            s_im[t] = 0.0;
+            s_cnt[t] = 0;
+        }
+    }
+    __syncthreads();
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < nb; e += stride)
+    {
+        const float d = dist[e];
+        if (d < h.h_min || d >= h.h_max)
+            continue;
+        uint32_t bin = static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
+        if (bin == h.bins)
+            bin = h.bins - 1;
+        const uint2 b = ij[e];
+        const double2 v = values[b.y];
+        const double2 q = qvalues[b.x];
+        const double re = __dadd_rn(__dmul_rn(v.x, q.x), __dmul_rn(v.y, q.y));
+        const double im = __dsub_rn(__dmul_rn(v.x, q.y), __dmul_rn(v.y, q.x));
+        if (smem)
+        {
+            atomicAdd(&s_re[bin], re);
+            atomicAdd(&s_im[bin], im);
+            atomicAdd(&s_cnt[bin], 1u);
+        }
+        else
+        {
+            atomicAdd(&sums[bin].x, re);
+            atomicAdd(&sums[bin].y, im);
+            atomicAdd(&counts[bin], 1ull);
+        }
+    }
+    if (smem)
+    {
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < h.bins; t += blockDim.x)
+        {
+            if (s_cnt[t] != 0)
+            {
+                atomicAdd(&sums[t].x, s_re[t]);
+                atomicAdd(&sums[t].y, s_im[t]);
+                atomicAdd(&counts[t], static_cast<unsigned long long>(s_cnt[t]));
+            }
+        }
+    }
+}
+
+void launch_cf_bonds(const uint2* ij, const float* dist, uint64_t nb, const double2* values, const double2* qvalues,
+                     const HistParams& h, double2* sums, unsigned long long* counts, cudaStream_t s)
+{
+    if (nb == 0)
+    {
+        return;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t want = (nb + 255) / 256;
+    const uint64_t cap = static_cast<uint64_t>(sms) * 4;
+    {
+        ProfScope prof_("k_cf_bonds", s);
+        k_cf_bonds<<<static_cast<unsigned>(want < cap ? want : cap), 256, 0, s>>>(ij, dist, nb, values, qvalues, h,
+                                                                                  sums, counts);
+    }
+}
+
 } // namespace fg

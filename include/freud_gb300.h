@@ -69,6 +69,7 @@ typedef struct fg_query_args
 typedef struct fg_nq fg_nq;
 typedef struct fg_nlist fg_nlist;
 typedef struct fg_rdf fg_rdf;
+typedef struct fg_cf fg_cf;
 typedef struct fg_steinhardt fg_steinhardt;
 typedef struct fg_frames fg_frames;
 
@@ -179,6 +180,29 @@ fg_status fg_rdf_state(const fg_rdf* rdf, fg_box* box, uint32_t* n_frames, uint3
  * each), so rdf / n_r come out as if one process had accumulated every frame. */
 fg_status fg_rdf_set_state(fg_rdf* rdf, const uint64_t* bin_counts, uint32_t n_frames, const fg_box* box,
                            uint32_t n_points, uint32_t n_query);
+
+/* ---- CorrelationFunction ----------------------------------------------------------
+ * freud::density::CorrelationFunction (freud/density/CorrelationFunction.cc:26-99;
+ * bindings export-CorrelationFunction.cc; Python freud/density.py:28-177). Values are
+ * complex double (re, im interleaved), as the reference converts them. */
+fg_status fg_cf_create(uint32_t bins, float r_max, fg_cf** out);
+fg_status fg_cf_destroy(fg_cf* cf);
+/* BondHistogramCompute::reset + the correlation sums (CorrelationFunction.cc:61-66). */
+fg_status fg_cf_reset(fg_cf* cf);
+/* CorrelationFunction::accumulate (CorrelationFunction.cc:79-96): for every bond
+ * (query i, point j), bin its distance and add conj(values[j]) * query_values[i].
+ * n_values must equal the number of points; query_values == NULL uses values;
+ * nlist == NULL queries nq with args. */
+fg_status fg_cf_accumulate(fg_cf* cf, fg_nq* nq, const double* values, uint32_t n_values,
+                           const float* query_points, uint32_t n_query, const double* query_values,
+                           uint32_t n_query_values, const fg_nlist* nlist, const fg_query_args* args);
+/* getBinCounts (uint32) and getCorrelation (sum / count per bin where the count is
+ * nonzero, CorrelationFunction.cc:48-59; complex double interleaved). Either may be NULL. */
+fg_status fg_cf_get(fg_cf* cf, uint32_t* bin_counts, double* correlation);
+/* getBinEdges / getBinCenters (Histogram.h:72-80, 126-138). */
+fg_status fg_cf_bin_edges(const fg_cf* cf, float* edges, float* centers);
+/* getBox of the last accumulated frame; frame counter. */
+fg_status fg_cf_state(const fg_cf* cf, fg_box* box, uint32_t* n_frames);
 
 /* ---- Steinhardt ----------------------------------------------------------------
  * freud::order::Steinhardt (freud/order/Steinhardt.h:59-223, Steinhardt.cc:85-359;

@@ -21,7 +21,8 @@ FLAGS=(-O3 -ffp-contract=off -std=c++17 -fPIC -shared -w
        -I"$HERE/ref_shim" -I"$SRC/box" -I"$SRC/util" -I"$SRC/locality" -I"$SRC/density" -I"$SRC/order")
 SOURCES=("$SRC/locality/LinkCell.cc" "$SRC/locality/AABBQuery.cc" "$SRC/locality/CellQuery.cc"
          "$SRC/locality/NeighborList.cc"
-         "$SRC/locality/NeighborComputeFunctional.cc" "$SRC/density/RDF.cc" "$SRC/order/Steinhardt.cc"
+         "$SRC/locality/NeighborComputeFunctional.cc" "$SRC/density/RDF.cc"
+         "$SRC/density/CorrelationFunction.cc" "$SRC/order/Steinhardt.cc"
          "$SRC/order/Wigner3j.cc" "$HERE/ref_harness.cpp")
 OBJS=()
 for s in "${SOURCES[@]}"; do

@@ -969,6 +969,19 @@ void ofg_hist(const float* distances, uint64_t nb, uint32_t bins, float r_min, f
     }
 }
 
+/* Bin index of each distance as Histogram::bin assigns it (Histogram.h:327-351),
+ * -1 for distances outside [r_min, r_max); used for the CorrelationFunction
+ * oracle (CorrelationFunction.cc:79-96), whose FP64 sums are formed in Python. */
+void ofg_bin_index(const float* distances, uint64_t nb, uint32_t bins, float r_min, float r_max, int64_t* out)
+{
+    const float bw = (r_max - r_min) / (float) bins;
+    const float inv = 1.0f / bw;
+    for (uint64_t b = 0; b < nb; ++b)
+    {
+        out[b] = hist_bin(distances[b], r_min, r_max, inv, bins);
+    }
+}
+
 /* Bin edges / centres (Histogram.h:126-138, :72-80). */
 void ofg_bin_edges(uint32_t bins, float r_min, float r_max, float* edges, float* centers)
 {

@@ -46,6 +46,7 @@ def _load():
     lib.ofg_rdf_query.restype = i32
     lib.ofg_rdf_query.argtypes = [P, P, u32, P, u32, f32, f32, i32, i32, u32, f32, f32, i32, P]
     lib.ofg_hist.argtypes = [P, u64, u32, f32, f32, P]
+    lib.ofg_bin_index.argtypes = [P, u64, u32, f32, f32, P]
     lib.ofg_bin_edges.argtypes = [u32, f32, f32, P, P]
     lib.ofg_rdf_reduce.argtypes = [P, u32, f32, f32, u32, u32, u32, f32, i32, i32, P, P]
     lib.ofg_ylm.argtypes = [i32, ctypes.c_double, ctypes.c_double, P]
@@ -121,6 +122,38 @@ def hist(distances, bins, r_max, r_min=0.0, counts=None):
         counts = np.zeros(bins, np.uint64)
     lib.ofg_hist(_p(d), len(d), int(bins), float(r_min), float(r_max), _p(counts))
     return counts
+
+
+def bin_index(distances, bins, r_max, r_min=0.0):
+    """Histogram bin of each distance (int64, -1 when outside [r_min, r_max))."""
+    lib = _load()
+    d = np.ascontiguousarray(distances, np.float32)
+    out = np.zeros(len(d), np.int64)
+    lib.ofg_bin_index(_p(d), len(d), int(bins), float(r_min), float(r_max), _p(out))
+    return out
+
+
+def correlation(ij, distances, values, query_values, bins, r_max, sums=None, counts=None):
+    """CorrelationFunction accumulate + reduce (CorrelationFunction.cc:48-59, 79-96)
+    over given bonds: per bin, the count and the FP64 sum of conj(values[j]) *
+    query_values[i]. Adds into (sums, counts) when given; returns
+    (correlation, counts, sums), correlation = sums / counts where counts != 0."""
+    ij = np.asarray(ij, np.int64).reshape(-1, 2)
+    k = bin_index(distances, bins, r_max)
+    keep = k >= 0
+    v = np.asarray(values, np.complex128)
+    q = np.asarray(query_values, np.complex128)
+    prod = np.conj(v[ij[keep, 1]]) * q[ij[keep, 0]]
+    if sums is None:
+        sums = np.zeros(bins, np.complex128)
+    if counts is None:
+        counts = np.zeros(bins, np.uint64)
+    np.add.at(sums, k[keep], prod)
+    np.add.at(counts, k[keep], 1)
+    corr = sums.copy()
+    nz = counts != 0
+    corr[nz] = sums[nz] / counts[nz].astype(np.float64)
+    return corr, counts, sums
 
 
 def bin_edges(bins, r_max, r_min=0.0):

@@ -51,6 +51,9 @@ def _load():
     lib.ref_rdf.restype = i32
     lib.ref_rdf.argtypes = [u32, f32, f32, i32, i32, P, P, P, P, i32, f32, i32, u32, f32,
                             f32, i32, P, P, P, P, P, P, P, ctypes.c_char_p, i32]
+    lib.ref_cf.restype = i32
+    lib.ref_cf.argtypes = [u32, f32, i32, P, P, P, P, P, P, P, P, i32, f32, i32, u32, f32, f32, i32, P, P,
+                           ctypes.c_char_p, i32]
     lib.ref_steinhardt.restype = i32
     lib.ref_steinhardt.argtypes = [P, u32, i32, i32, i32, i32, P, i32, P, u32, i32, f32,
                                    i32, u32, f32, f32, i32, i32, u32, P, P, P, P, P, P,
@@ -122,6 +125,35 @@ def rdf(bins, r_max, frames, r_min=0.0, finite_size=False, kind=KIND_RAW, cell_w
     if st != 0:
         raise RefError(st, err.value.decode())
     return counts, g, nr
+
+
+def cf(bins, r_max, frames, values, query_frames=None, query_values=None, kind=KIND_RAW, cell_width=0.0,
+       mode=MODE_BALL, num_neighbors=DEFAULT_NUM_NEIGHBORS, q_r_max=None, q_r_min=0.0, exclude_ii=True):
+    """CorrelationFunction over frames (list of (box, points)) with per-frame values
+    (list of complex arrays); query_frames: per-frame query points (None: the
+    points). Returns (counts uint32, correlation complex128)."""
+    lib = _load()
+    boxes = np.concatenate([_box6(b)[0] for b, _ in frames]).astype(np.float32)
+    is2d = np.array([int(b[6]) for b, _ in frames], np.int32)
+    offsets = np.concatenate([[0], np.cumsum([len(p) for _, p in frames])]).astype(np.uint32)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float32) for _, p in frames]))
+    vals = np.ascontiguousarray(np.concatenate([np.asarray(v, np.complex128) for v in values]))
+    qoff = qpts = qvals = None
+    if query_frames is not None:
+        qoff = np.concatenate([[0], np.cumsum([len(q) for q in query_frames])]).astype(np.uint32)
+        qpts = np.ascontiguousarray(np.concatenate([np.asarray(q, np.float32) for q in query_frames]))
+        if query_values is not None:
+            qvals = np.ascontiguousarray(np.concatenate([np.asarray(v, np.complex128) for v in query_values]))
+    counts = np.zeros(bins, np.uint32)
+    corr = np.zeros(bins, np.complex128)
+    err = ctypes.create_string_buffer(512)
+    st = lib.ref_cf(bins, r_max, len(frames), _ptr(boxes), _ptr(is2d), _ptr(offsets), _ptr(pts), _ptr(vals),
+                    _ptr(qoff), _ptr(qpts), _ptr(qvals), kind, cell_width, mode, num_neighbors,
+                    r_max if q_r_max is None else q_r_max, q_r_min, int(exclude_ii), _ptr(counts), _ptr(corr),
+                    err, 512)
+    if st != 0:
+        raise RefError(st, err.value.decode())
+    return counts, corr
 
 
 def steinhardt(ls, box, points, average=False, wl=False, weighted=False, wl_normalize=False,

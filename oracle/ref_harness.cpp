@@ -13,6 +13,7 @@
 //   freud/locality/CellQuery.cc:17-137        CellQuery (ghost-particle grid, ball queries)
 //   freud/locality/NeighborList.cc:51-82      NeighborList from arrays
 //   freud/density/RDF.cc:25-110               RDF ctor / accumulate / reduce
+//   freud/density/CorrelationFunction.cc:26-96 CorrelationFunction ctor / accumulate / reduce
 //   freud/order/Steinhardt.cc:85-118          Steinhardt::compute
 #include <complex>
 #include <cstring>
@@ -24,6 +25,7 @@
 #include "AABBQuery.h"
 #include "CellQuery.h"
 #include "Box.h"
+#include "CorrelationFunction.h"
 #include "LinkCell.h"
 #include "NeighborList.h"
 #include "NeighborQuery.h"
@@ -212,6 +214,60 @@ int ref_rdf(unsigned bins, float r_max, float r_min, int finite_size, int nframe
             counts[i] = (*c)[i];
             rdf[i] = (*g)[i];
             nr[i] = (*nn)[i];
+        }
+        return REF_OK;
+    }
+    catch (const std::invalid_argument& e)
+    {
+        return report(e, REF_VALUE_ERROR, err, errlen);
+    }
+    catch (const std::exception& e)
+    {
+        return report(e, REF_RUNTIME_ERROR, err, errlen);
+    }
+}
+
+// CorrelationFunction accumulated over nframes (reset=False after the first frame)
+// with a live query per frame. values / qvalues: complex double interleaved, per
+// point of each frame. qpts == NULL queries each frame's own points (and qvalues
+// == NULL uses values). corr: bins complex values interleaved.
+int ref_cf(unsigned bins, float r_max, int nframes, const float* boxes6, const int* is2d, const unsigned* offsets,
+           const float* pts, const double* values, const unsigned* qoffsets, const float* qpts,
+           const double* qvalues, int kind, float cell_width, int mode, unsigned num_neighbors, float q_r_max,
+           float q_r_min, int exclude_ii, unsigned* counts, double* corr, char* err, int errlen)
+{
+    try
+    {
+        freud::density::CorrelationFunction cf(bins, r_max);
+        for (int f = 0; f < nframes; ++f)
+        {
+            const Box box = make_box(boxes6 + 6 * f, is2d[f]);
+            const unsigned n = offsets[f + 1] - offsets[f];
+            const float* p = pts + 3 * static_cast<size_t>(offsets[f]);
+            const auto* v = reinterpret_cast<const std::complex<double>*>(values) + offsets[f];
+            auto nqo = make_nq(kind, box, p, n, cell_width);
+            const float* qp = p;
+            unsigned nqp = n;
+            const std::complex<double>* qv = v;
+            if (qpts != nullptr)
+            {
+                qp = qpts + 3 * static_cast<size_t>(qoffsets[f]);
+                nqp = qoffsets[f + 1] - qoffsets[f];
+                if (qvalues != nullptr)
+                {
+                    qv = reinterpret_cast<const std::complex<double>*>(qvalues) + qoffsets[f];
+                }
+            }
+            cf.accumulate(nqo, v, reinterpret_cast<const vec3<float>*>(qp), qv, nqp, nullptr,
+                          make_qargs(mode, num_neighbors, q_r_max, q_r_min, -1.0F, -1.0F, exclude_ii));
+        }
+        auto c = cf.getBinCounts();
+        auto g = cf.getCorrelation();
+        for (unsigned i = 0; i < bins; ++i)
+        {
+            counts[i] = (*c)[i];
+            corr[2 * i] = (*g)[i].real();
+            corr[2 * i + 1] = (*g)[i].imag();
         }
         return REF_OK;
     }
