@@ -249,6 +249,43 @@ def measure_c1(freud, _lib, steps, warmup, cpu=True):
     return out
 
 
+def measure_cf(freud, _lib, steps, warmup, cpu=True):
+    """CorrelationFunction(200, 4.0).compute((box, points), values) on the plain RDF
+    system (10,000 uniform points) with complex values e^{i theta}: bonds found on
+    the GPU, conj(values[j]) * values[i] summed per bin in FP64."""
+    L, pts = c1_system()
+    box = freud.box.Box.cube(L)
+    rs = np.random.RandomState(5)
+    vals = np.exp(1j * rs.random_sample(len(pts)) * 2.0 * np.pi)
+    cf = freud.density.CorrelationFunction(200, 4.0)
+
+    def step():
+        cf.compute((box, pts), vals)
+        return cf.bin_counts
+
+    pairs = int(step().astype(np.int64).sum())
+    t = _median_wall(step, steps, warmup)
+    dev_ms, launches, top = _device_ms(_lib, step, steps)
+    out = {"workload": "correlation_function_n10000_L21.544_rmax4_bins200_complex", "pairs": pairs,
+           "e2e_ms": t * 1e3, "e2e": pairs / t, "device_ms": dev_ms, "device": pairs / (dev_ms / 1e3),
+           "unit": "pair evals/s", "launches_per_step": launches, "kernels_ms_per_step": top}
+    if cpu:
+        from oracle import oracle as O
+
+        bx = (L, L, L, 0.0, 0.0, 0.0, 0.0)
+        threads = os.cpu_count() or 1
+        ts = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            ij, d, _ = O.query(bx, pts, r_max=4.0, exclude_ii=True, threads=threads)
+            O.correlation(ij, d, vals, vals, 200, 4.0)
+            ts.append(time.perf_counter() - t0)
+        out["cpu_baseline"] = {"value": pairs / statistics.median(ts), "unit": "pair evals/s", "cores": threads,
+                               "kind": "port", "sample": "whole workload (oracle query on all threads, numpy "
+                                                         "FP64 sums), median of 5"}
+    return out
+
+
 def measure_c3(freud, _lib, steps, warmup, cpu=True):
     """Steinhardt([4, 6, 8, 10, 12], average, wl, wl_normalize) with 12 nearest
     neighbours on a 256,000-point noisy FCC crystal."""
@@ -461,6 +498,7 @@ def run_only(args):
     torch.cuda.set_stream(stream)
     fns = {"plain_rdf": lambda: measure_c1(freud, _lib, args.steps, args.warmup, cpu=False),
            "steinhardt": lambda: measure_c3(freud, _lib, args.steps, args.warmup, cpu=False),
+           "correlation_function": lambda: measure_cf(freud, _lib, args.steps, args.warmup, cpu=False),
            "batched_frames": lambda: measure_c4(freud, _lib, args.steps, args.warmup, 8 if args.small else 64),
            "precision_stress": lambda: measure_c5(freud, _lib, args.steps, args.warmup, args.small)}
     print(json.dumps({"only": args.only, "result": fns[args.only]()}), flush=True)
@@ -478,7 +516,8 @@ def main():
                     help="skip the plain-RDF, Steinhardt, batched-frames and stress workloads")
     ap.add_argument("--n-side", type=int, default=102,
                     help="lattice points per side; 102 is the benchmark workload, smaller sizes are for profiling")
-    ap.add_argument("--only", default=None, choices=["plain_rdf", "steinhardt", "batched_frames", "precision_stress"],
+    ap.add_argument("--only", default=None, choices=["plain_rdf", "steinhardt", "correlation_function",
+                                                     "batched_frames", "precision_stress"],
                     help="run one of the other workloads alone and print its result (profiling)")
     ap.add_argument("--small", action="store_true",
                     help="with --only: the profiling-size case (8 frames; 512 blobs in L = 128)")
@@ -627,6 +666,8 @@ def main():
                                                             cpu=not args.no_cpu_baseline)),
                          ("steinhardt", lambda: measure_c3(freud, _lib, args.steps, args.warmup,
                                                             cpu=not args.no_cpu_baseline)),
+                         ("correlation_function", lambda: measure_cf(freud, _lib, args.steps, args.warmup,
+                                                                     cpu=not args.no_cpu_baseline)),
                          ("batched_frames", lambda: measure_c4(freud, _lib, args.steps, args.warmup)),
                          ("precision_stress", lambda: measure_c5(freud, _lib, args.steps, args.warmup))):
             try:

@@ -780,10 +780,13 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     over.alloc(sizeof(uint32_t) * (nqp + 1));
     over_n.alloc(sizeof(uint32_t));
     const bool cellwise = !by_distance;
+    // candidate capacity per cell: 4096 for dense point sets, whose 27-cell stencils
+    // would overflow 1024 and fall back to the warp-per-query kernels
+    const int cap = cell_cap_for(view(g), nq->n, nq->box.is2d && arith != ARITH_GHOST);
     if (cellwise)
     {
-        gmask.alloc(sizeof(uint32_t) * static_cast<size_t>(nqp) * CELL_CHUNKS);
-        gsorted.alloc(sizeof(uint32_t) * static_cast<size_t>(g.ncell) * CELL_CAP);
+        gmask.alloc(sizeof(uint32_t) * static_cast<size_t>(nqp) * (cap / 32));
+        gsorted.alloc(sizeof(uint32_t) * static_cast<size_t>(g.ncell) * cap);
         gtotal.alloc(sizeof(uint32_t) * static_cast<size_t>(std::max(g.ncell, 1)));
     }
     FG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (nqp + 1), s));
@@ -796,7 +799,7 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
         // ghost grids hold copies of point indices; any index fits the same bound
         launch_cell_scan(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, pf.cull2, counts.as<uint32_t>(),
                          gmask.as<uint32_t>(), gsorted.as<uint32_t>(), gtotal.as<uint32_t>(), over.as<uint32_t>(),
-                         over_n.as<uint32_t>(), HistParams {}, nullptr, s, nq->n);
+                         over_n.as<uint32_t>(), HistParams {}, nullptr, s, nq->n, cap);
         FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         sync();
         list = over.as<uint32_t>();
@@ -828,7 +831,7 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     {
         launch_cell_emit(nq->dbox, view(g), qs.qg, p, gmask.as<uint32_t>(), gsorted.as<uint32_t>(),
                          gtotal.as<uint32_t>(), offsets.as<uint64_t>(), out.ij.as<uint2>(), out.dist.as<float>(),
-                         out.vec.as<float>(), s);
+                         out.vec.as<float>(), s, cap);
     }
     if (n_over > 0)
     {

@@ -44,7 +44,14 @@ constexpr int SWARPS = 8;
 constexpr int STHREADS = SWARPS * 32;
 constexpr int EWARPS = 8;
 constexpr int ETHREADS = EWARPS * 32;
-constexpr int QB = 64; // queries per shared-memory batch in the scan pass
+// Candidate capacity of a cell's stencil (CAP) and queries per shared-memory
+// batch of the scan pass: 1024 / 64 for the common case (five blocks per SM),
+// 4096 / 32 for dense point sets (one block per SM).
+template<int CAP> struct CellCfg
+{
+    static constexpr int QB = CAP <= 1024 ? 64 : 32;
+    static constexpr int POS_BITS = CAP <= 1024 ? 10 : 12; // staged-position bits of a 32-bit merge key
+};
 constexpr int HIST_BINS_SMEM = 4096;
 
 enum ScanMode
@@ -62,33 +69,34 @@ struct Items
 };
 
 // Shared memory of the scan kernels; arrays one mode does not use shrink to one
-// element, so the count pass fits four blocks per SM.
-template<int MODE, typename K> struct ScanShared
+// element, so the count pass with CAP 1024 fits five blocks per SM.
+template<int MODE, typename K, int CAP> struct ScanShared
 {
+    static constexpr int QB = CellCfg<CAP>::QB;
     union
     {
         struct
         {
-            K a[CELL_CAP]; // merge ping-pong buffers (KeyTraits<K>)
-            K b[CELL_CAP];
+            K a[CAP]; // merge ping-pong buffers (KeyTraits<K>)
+            K b[CAP];
         } keys;
         unsigned int hist[MODE == SM_HIST ? HIST_BINS_SMEM : 1]; // privatised RDF histogram (histogram pass)
     } u;
-    float3 ps[CELL_CAP];              // prefilter position (wrap arithmetic)
-    float4 pos[MODE == SM_HIST ? CELL_CAP : 1];   // candidate position (histogram pass)
-    uint32_t j[CELL_CAP];             // point index
-    uint32_t slot[CELL_CAP];          // grid slot << 5 | cell wrap code
-    unsigned char run[CELL_CAP];      // stencil item (sorted run) of each staged position
-    unsigned char runc[MODE == SM_COUNT ? CELL_CAP : 1]; // run of each kept candidate (count pass)
-    uint32_t keep[MODE == SM_COUNT ? CELL_CAP / 32 : 1];  // kept-candidate ballots per (round, warp)
-    uint32_t keep_pre[MODE == SM_COUNT ? CELL_CAP / 32 + 1 : 1];
+    float3 ps[CAP];                   // prefilter position (wrap arithmetic)
+    float4 pos[MODE == SM_HIST ? CAP : 1];   // candidate position (histogram pass)
+    uint32_t j[CAP];                  // point index
+    uint32_t slot[CAP];               // grid slot << 5 | cell wrap code
+    unsigned char run[CAP];           // stencil item (sorted run) of each staged position
+    unsigned char runc[MODE == SM_COUNT ? CAP : 1]; // run of each kept candidate (count pass)
+    uint32_t keep[MODE == SM_COUNT ? CAP / 32 : 1];  // kept-candidate ballots per (round, warp)
+    uint32_t keep_pre[MODE == SM_COUNT ? CAP / 32 + 1 : 1];
     float qbox[SWARPS][6];            // per-warp bounds of the cell's shifted queries (lo xyz, hi xyz)
     float qfin[6];                    // their union
-    uint32_t mask[MODE == SM_COUNT ? QB : 1][CELL_CHUNKS]; // acceptance per (query, chunk), count pass
+    uint32_t mask[MODE == SM_COUNT ? QB : 1][CAP / 32]; // acceptance per (query, chunk), count pass
     float4 q[QB];
     float4 qs[QB];
     uint32_t qi[QB];
-    uint32_t queue[SWARPS][64];       // undecided pairs: sorted index | query << 11
+    uint32_t queue[SWARPS][64];       // undecided pairs: sorted index | query << 16
     Items it;
     float img[27][3];
 };
@@ -209,17 +217,18 @@ __device__ __forceinline__ int item_of(const Items& it, uint32_t t)
 }
 
 // Merge keys: (point index, staged position) packed so that key order is point
-// order with ties broken by position. 32-bit keys (index << 10 | position) when
-// every index is below 2^22, else 64-bit (index << 32 | position).
-template<typename K> struct KeyTraits;
-template<> struct KeyTraits<unsigned int>
+// order with ties broken by position. 32-bit keys (index << PB | position, PB =
+// 10 for CAP 1024, 12 for CAP 4096) when every index is below 2^(32 - PB), else
+// 64-bit (index << 32 | position).
+template<typename K, int PB> struct KeyTraits;
+template<int PB> struct KeyTraits<unsigned int, PB>
 {
-    static constexpr int SHIFT = 10;
+    static constexpr int SHIFT = PB;
     __device__ static unsigned int make(uint32_t j, uint32_t pos) { return (j << SHIFT) | pos; }
     __device__ static uint32_t pos(unsigned int k) { return k & ((1u << SHIFT) - 1u); }
     __device__ static uint32_t index(unsigned int k) { return k >> SHIFT; }
 };
-template<> struct KeyTraits<unsigned long long>
+template<int PB> struct KeyTraits<unsigned long long, PB>
 {
     static constexpr int SHIFT = 32;
     __device__ static unsigned long long make(uint32_t j, uint32_t pos)
@@ -246,16 +255,19 @@ __device__ __forceinline__ uint32_t rank_in(const K* src, uint32_t lo, uint32_t 
     return a - lo;
 }
 
-template<int MODE, typename K>
-__global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
+template<int MODE, typename K, int CAP>
+__global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? (CAP <= 1024 ? 5 : 1) : 3)
     k_cell_scan(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2, float cull2,
                 uint32_t* __restrict__ counts, uint32_t* __restrict__ gmask, uint32_t* __restrict__ gsorted,
                 uint32_t* __restrict__ gtotal, uint32_t* overflow, uint32_t* overflow_n, HistParams h,
                 unsigned long long* __restrict__ hist)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ScanShared<MODE, K>& S = *reinterpret_cast<ScanShared<MODE, K>*>(smem_raw);
-    using KT = KeyTraits<K>;
+    using SS = ScanShared<MODE, K, CAP>;
+    SS& S = *reinterpret_cast<SS*>(smem_raw);
+    using KT = KeyTraits<K, CellCfg<CAP>::POS_BITS>;
+    constexpr int QB = SS::QB;
+    constexpr int CHUNKS = CAP / 32;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
@@ -319,7 +331,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
             cell_items(b, g, p.arith, c, S.it, lane);
         __syncthreads();
         uint32_t T = S.it.total;
-        if (MODE == SM_COUNT && T > CELL_CAP)
+        if (MODE == SM_COUNT && T > CAP)
         {
             for (uint32_t k = tid; k < nqc; k += STHREADS)
                 overflow[atomicAdd(overflow_n, 1u)] = q0 + k;
@@ -328,11 +340,11 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
             __syncthreads();
             continue;
         }
-        const uint32_t ntiles = MODE == SM_COUNT ? 1u : (T + CELL_CAP - 1) / CELL_CAP;
+        const uint32_t ntiles = MODE == SM_COUNT ? 1u : (T + CAP - 1) / CAP;
         for (uint32_t tile = 0; tile < ntiles; ++tile)
         {
-            const uint32_t t0 = tile * CELL_CAP;
-            const uint32_t TT = min(static_cast<uint32_t>(CELL_CAP), T - t0);
+            const uint32_t t0 = tile * CAP;
+            const uint32_t TT = min(static_cast<uint32_t>(CAP), T - t0);
             // ---- stage candidates [t0, t0 + TT) ----
             if (cull)
             {
@@ -401,17 +413,22 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                 const uint32_t nbal = (TT + 31) / 32;
                 if (warp == 0)
                 {
-                    const uint32_t v = lane < static_cast<int>(nbal) ? __popc(S.keep[lane]) : 0u;
-                    uint32_t incl = v;
-                    for (int o = 1; o < 32; o <<= 1)
+                    uint32_t carry = 0;
+                    for (int w0 = 0; w0 < CHUNKS; w0 += 32)
                     {
-                        const uint32_t u = __shfl_up_sync(FULL, incl, o);
-                        if (lane >= o)
-                            incl += u;
+                        const uint32_t v = w0 + lane < static_cast<int>(nbal) ? __popc(S.keep[w0 + lane]) : 0u;
+                        uint32_t incl = v;
+                        for (int o = 1; o < 32; o <<= 1)
+                        {
+                            const uint32_t u = __shfl_up_sync(FULL, incl, o);
+                            if (lane >= o)
+                                incl += u;
+                        }
+                        S.keep_pre[w0 + lane] = carry + incl - v;
+                        carry += __shfl_sync(FULL, incl, 31);
                     }
-                    S.keep_pre[lane] = incl - v;
-                    if (lane == 31)
-                        S.keep_pre[32] = incl;
+                    if (lane == 0)
+                        S.keep_pre[CHUNKS] = carry;
                 }
                 __syncthreads();
                 for (uint32_t tl = tid; tl < TT; tl += STHREADS)
@@ -425,7 +442,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                         S.runc[pos] = S.run[tl];
                     }
                 }
-                T = S.keep_pre[32];
+                T = S.keep_pre[CHUNKS];
                 __syncthreads();
                 // run offsets among the kept candidates (runc is ascending)
                 if (tid <= 32)
@@ -466,7 +483,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                 order = src;
                 // the sorted order (grid slot << 5 | wrap) is what the write pass replays
                 for (uint32_t e = tid; e < T; e += STHREADS)
-                    gsorted[static_cast<size_t>(c) * CELL_CAP + e] = S.slot[KT::pos(order[e])];
+                    gsorted[static_cast<size_t>(c) * CAP + e] = S.slot[KT::pos(order[e])];
                 if (tid == 0)
                     gtotal[c] = T;
             }
@@ -498,8 +515,8 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                     if (lane < static_cast<int>(n))
                     {
                         const uint32_t ent = queue[lane];
-                        e = ent & 0x7ffu;
-                        qq = ent >> 11;
+                        e = ent & 0xffffu;
+                        qq = ent >> 16;
                         const uint32_t t = MODE == SM_COUNT ? KT::pos(order[e]) : e;
                         const float4 q = S.q[qq];
                         const uint32_t sl = S.slot[t];
@@ -551,7 +568,7 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                     // queue the undecided pairs of one query (warp-uniform nm != 0)
                     auto append = [&](bool need, unsigned nm, uint32_t qq) {
                         if (need)
-                            queue[qn + __popc(nm & lt)] = e | (qq << 11);
+                            queue[qn + __popc(nm & lt)] = e | (qq << 16);
                         qn += __popc(nm);
                         __syncwarp();
                         if (qn >= 32)
@@ -778,12 +795,16 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? 5 : 3)
                         }
                         __syncthreads();
                     }
-                    // masks and counts of this query batch: warp per query, lane per chunk
+                    // masks and counts of this query batch: warp per query, lanes over chunks
                     for (uint32_t k = warp; k < nb; k += SWARPS)
                     {
-                        const uint32_t m = lane < static_cast<int>(nchunks) ? S.mask[k][lane] : 0u;
-                        gmask[static_cast<size_t>(q0 + qb0 + k) * CELL_CHUNKS + lane] = m;
-                        uint32_t cnt = __popc(m);
+                        uint32_t cnt = 0;
+                        for (int ch = lane; ch < CHUNKS; ch += 32)
+                        {
+                            const uint32_t m = ch < static_cast<int>(nchunks) ? S.mask[k][ch] : 0u;
+                            gmask[static_cast<size_t>(q0 + qb0 + k) * CHUNKS + ch] = m;
+                            cnt += __popc(m);
+                        }
                         for (int o = 16; o > 0; o >>= 1)
                             cnt += __shfl_xor_sync(FULL, cnt, o);
                         if (lane == 0)
@@ -829,12 +850,16 @@ __device__ __forceinline__ uint32_t kth_set_bit(uint32_t w, uint32_t k)
 // per-chunk acceptance counts (one chunk per lane) and the set bits of that
 // chunk's mask. Candidates are read through the cell's sorted list (gsorted)
 // from L1/L2, where the cell's other queries keep them.
+template<int CAP>
 __global__ void __launch_bounds__(ETHREADS, 5)
     k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
                 const uint32_t* __restrict__ gsorted, const uint32_t* __restrict__ gtotal,
                 const uint64_t* __restrict__ offsets, uint2* __restrict__ ij, float* __restrict__ dist,
-                float* __restrict__ vec)
+                float* __restrict__ vec, uint32_t nq_total, uint32_t per_item)
 {
+    // WPL mask words per lane: lane l holds chunks l*WPL .. l*WPL + WPL - 1
+    constexpr int CHUNKS = CAP / 32;
+    constexpr int WPL = CHUNKS / 32;
     __shared__ float img_s[27][3];
     const int tid = threadIdx.x;
     const int lane = tid & 31;
@@ -842,75 +867,142 @@ __global__ void __launch_bounds__(ETHREADS, 5)
     for (int t = tid; t < 81; t += ETHREADS)
         img_s[t / 3][t % 3] = b.img[t / 3][t % 3];
     __syncthreads();
-    const int nwarps = gridDim.x * EWARPS;
-    for (int c = blockIdx.x * EWARPS + warp; c < qg.ncell; c += nwarps)
+    // work items: one cell's queries (per_item == 0, many cells), or runs of
+    // per_item consecutive cell-sorted queries (few, dense cells)
+    const uint32_t nwarps = gridDim.x * EWARPS;
+    const uint32_t n_items = per_item == 0 ? static_cast<uint32_t>(qg.ncell) : (nq_total + per_item - 1) / per_item;
+    for (uint32_t item = blockIdx.x * EWARPS + warp; item < n_items; item += nwarps)
     {
-        const uint32_t q0 = qg.start[c];
-        const uint32_t nqc = qg.start[c + 1] - q0;
-        if (nqc == 0)
-            continue;
-        const uint32_t T = gtotal[c];
-        if (T > CELL_CAP)
-            continue; // the cell's queries are written by the warp-per-query kernels
-        const uint32_t* srt = gsorted + static_cast<size_t>(c) * CELL_CAP;
-        const uint32_t nchunks = (T + 31) / 32;
-        float4 q_n = qg.cpos[q0];
-        uint32_t qi_n = qg.cidx[q0];
-        uint32_t mw_n = lane < static_cast<int>(nchunks) ? gmask[static_cast<size_t>(q0) * CELL_CHUNKS + lane] : 0u;
-        for (uint32_t qq = 0; qq < nqc; ++qq)
+        uint32_t k0, k1;
+        int c = 0;
+        if (per_item == 0)
         {
-            const float4 q = q_n;
-            const uint32_t qi = qi_n;
-            const uint32_t mword = mw_n;
-            const int qimg = __float_as_int(q.w);
-            const uint64_t out = offsets[qi];
-            if (qq + 1 < nqc)
+            c = static_cast<int>(item);
+            k0 = qg.start[c];
+            k1 = qg.start[c + 1];
+        }
+        else
+        {
+            k0 = item * per_item;
+            k1 = min(k0 + per_item, nq_total);
+            // cell of query k0: the last cell whose start is <= k0
+            int hi = qg.ncell;
+            while (hi - c > 1)
             {
-                // one-ahead prefetch of the next query (position, index, mask row)
-                q_n = qg.cpos[q0 + qq + 1];
-                qi_n = qg.cidx[q0 + qq + 1];
-                mw_n = lane < static_cast<int>(nchunks)
-                    ? gmask[static_cast<size_t>(q0 + qq + 1) * CELL_CHUNKS + lane] : 0u;
+                const int mid = (c + hi) >> 1;
+                if (qg.start[mid] <= k0)
+                    c = mid;
+                else
+                    hi = mid;
             }
-            const uint32_t cnt = __popc(mword);
-            uint32_t incl = cnt;
+        }
+        for (uint32_t q0 = k0; q0 < k1 && c < qg.ncell; ++c)
+        {
+            // queries [q0, q0 + nqc) of cell c within this item
+            const uint32_t cend = qg.start[c + 1];
+            if (cend <= q0)
+                continue;
+            const uint32_t nqc = min(cend, k1) - q0;
+            const uint32_t qbeg = q0;
+            q0 += nqc;
+            const uint32_t T = gtotal[c];
+            if (T > CAP)
+                continue; // the cell's queries are written by the warp-per-query kernels
+            const uint32_t* srt = gsorted + static_cast<size_t>(c) * CAP;
+            const uint32_t nchunks = (T + 31) / 32;
+            auto load_row = [&](uint32_t row, uint32_t (&w)[WPL]) {
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
-            {
-                const uint32_t v = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o)
-                    incl += v;
-            }
-            const uint32_t excl = incl - cnt;
-            const uint32_t total = __shfl_sync(FULL, incl, 31);
-            for (uint32_t base = 0; base < total; base += 32)
-            {
-                const uint32_t bb = base + static_cast<uint32_t>(lane);
-                // chunk of bond bb: the last chunk whose exclusive prefix is <= bb
-                int ch = 0;
-#pragma unroll
-                for (int step = 16; step >= 1; step >>= 1)
+                for (int k = 0; k < WPL; ++k)
                 {
-                    const uint32_t v = __shfl_sync(FULL, excl, ch + step);
-                    if (v <= bb)
-                        ch += step;
+                    const uint32_t ch = static_cast<uint32_t>(lane * WPL + k);
+                    w[k] = ch < nchunks ? gmask[static_cast<size_t>(row) * CHUNKS + ch] : 0u;
                 }
-                const uint32_t w = __shfl_sync(FULL, mword, ch);
-                const uint32_t k = bb - __shfl_sync(FULL, excl, ch);
-                if (bb < total)
+            };
+            float4 q_n = qg.cpos[qbeg];
+            uint32_t qi_n = qg.cidx[qbeg];
+            uint32_t mw_n[WPL];
+            load_row(qbeg, mw_n);
+            for (uint32_t qq = 0; qq < nqc; ++qq)
+            {
+                const float4 q = q_n;
+                const uint32_t qi = qi_n;
+                uint32_t mword[WPL];
+#pragma unroll
+                for (int k = 0; k < WPL; ++k)
+                    mword[k] = mw_n[k];
+                const int qimg = __float_as_int(q.w);
+                const uint64_t out = offsets[qi];
+                if (qq + 1 < nqc)
                 {
-                    const uint32_t ent = srt[static_cast<uint32_t>(ch) * 32u + kth_set_bit(w, k)];
-                    const uint32_t slot = ent >> 5;
-                    const float4 pp = g.cpos[slot];
-                    const uint32_t jj = g.cidx[slot];
-                    float rx, ry, rz;
-                    exact_vec(b, img_s, p.arith, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
-                    const uint64_t o = out + bb;
-                    ij[o] = make_uint2(qi, jj);
-                    dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
-                    vec[3 * o] = rx;
-                    vec[3 * o + 1] = ry;
-                    vec[3 * o + 2] = rz;
+                    // one-ahead prefetch of the next query (position, index, mask row)
+                    q_n = qg.cpos[qbeg + qq + 1];
+                    qi_n = qg.cidx[qbeg + qq + 1];
+                    load_row(qbeg + qq + 1, mw_n);
+                }
+                uint32_t cnt = 0;
+#pragma unroll
+                for (int k = 0; k < WPL; ++k)
+                    cnt += __popc(mword[k]);
+                uint32_t incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1)
+                {
+                    const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o)
+                        incl += v;
+                }
+                const uint32_t excl = incl - cnt;
+                const uint32_t total = __shfl_sync(FULL, incl, 31);
+                for (uint32_t base = 0; base < total; base += 32)
+                {
+                    const uint32_t bb = base + static_cast<uint32_t>(lane);
+                    // lane holding bond bb: the last lane whose exclusive prefix is <= bb
+                    int ln = 0;
+#pragma unroll
+                    for (int step = 16; step >= 1; step >>= 1)
+                    {
+                        const uint32_t v = __shfl_sync(FULL, excl, ln + step);
+                        if (v <= bb)
+                            ln += step;
+                    }
+                    uint32_t k = bb - __shfl_sync(FULL, excl, ln);
+                    // then the word of that lane, in chunk order
+                    uint32_t w = 0, ch = 0;
+                    bool found = false;
+#pragma unroll
+                    for (int kw = 0; kw < WPL; ++kw)
+                    {
+                        const uint32_t wk = __shfl_sync(FULL, mword[kw], ln);
+                        const uint32_t ck = __popc(wk);
+                        if (!found)
+                        {
+                            if (k < ck)
+                            {
+                                w = wk;
+                                ch = static_cast<uint32_t>(ln * WPL + kw);
+                                found = true;
+                            }
+                            else
+                            {
+                                k -= ck;
+                            }
+                        }
+                    }
+                    if (bb < total)
+                    {
+                        const uint32_t ent = srt[ch * 32u + kth_set_bit(w, k)];
+                        const uint32_t slot = ent >> 5;
+                        const float4 pp = g.cpos[slot];
+                        const uint32_t jj = g.cidx[slot];
+                        float rx, ry, rz;
+                        exact_vec(b, img_s, p.arith, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
+                        const uint64_t o = out + bb;
+                        ij[o] = make_uint2(qi, jj);
+                        dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
+                        vec[3 * o] = rx;
+                        vec[3 * o + 1] = ry;
+                        vec[3 * o + 2] = rz;
+                    }
                 }
             }
         }
@@ -939,65 +1031,105 @@ template<typename K> void configure(K kernel, size_t bytes, bool& done)
 
 size_t cell_smem_bytes()
 {
-    return sizeof(ScanShared<SM_COUNT, unsigned long long>);
+    return sizeof(ScanShared<SM_COUNT, unsigned long long, 1024>);
 }
+
+int cell_cap_for(const DevGrid& g, uint32_t n_points, bool is2d)
+{
+    // mean candidates of a 27-cell (9 in 2D) stencil: below ~850 the largest of
+    // ~10^5 uniformly filled stencils (mean + 4.5 sigma, Poisson) stays under 1024
+    const double mean = static_cast<double>(n_points) / std::max(g.ncell, 1) * (is2d ? 9.0 : 27.0);
+    return mean > 850.0 ? 4096 : 1024;
+}
+
+namespace {
+template<int CAP>
+void scan_count(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_out2,
+                float pre_in2, float cull2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted, uint32_t* gtotal,
+                uint32_t* overflow, uint32_t* overflow_n, cudaStream_t s, uint32_t n_points)
+{
+    auto go = [&](auto kernel, size_t smem, bool& done) {
+        configure(kernel, smem, done);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, STHREADS, smem);
+        const int want = std::max(per_sm, 1) * sm_count_cell();
+        const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
+        ProfScope prof_("k_cell_scan<COUNT>", s);
+        kernel<<<blocks, STHREADS, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal,
+                                              overflow, overflow_n, HistParams {}, nullptr);
+    };
+    // 32-bit merge keys while every point index fits beside the staged position
+    if (n_points <= (1u << (32 - CellCfg<CAP>::POS_BITS)))
+    {
+        static bool done = false;
+        go(k_cell_scan<SM_COUNT, unsigned int, CAP>, sizeof(ScanShared<SM_COUNT, unsigned int, CAP>), done);
+    }
+    else
+    {
+        static bool done = false;
+        go(k_cell_scan<SM_COUNT, unsigned long long, CAP>, sizeof(ScanShared<SM_COUNT, unsigned long long, CAP>),
+           done);
+    }
+}
+} // namespace
 
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       float pre_out2, float pre_in2, float cull2, uint32_t* counts, uint32_t* gmask,
                       uint32_t* gsorted, uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n,
-                      const HistParams& h, unsigned long long* hist, cudaStream_t s, uint32_t n_points)
+                      const HistParams& h, unsigned long long* hist, cudaStream_t s, uint32_t n_points, int cap)
 {
+    if (!hist_mode)
+    {
+        if (cap > 1024)
+            scan_count<4096>(box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal, overflow,
+                             overflow_n, s, n_points);
+        else
+            scan_count<1024>(box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal, overflow,
+                             overflow_n, s, n_points);
+        return;
+    }
     // one wave of resident blocks walking the cells
-    auto grid = [&](auto kernel, size_t smem) {
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, STHREADS, smem);
-        const int want = std::max(per_sm, 1) * sm_count_cell();
-        return qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
-    };
-    if (!hist_mode && n_points <= (1u << 22))
-    {
-        // 32-bit merge keys: point indices below 2^22
-        const size_t smem = sizeof(ScanShared<SM_COUNT, unsigned int>);
-        static bool done = false;
-        configure(k_cell_scan<SM_COUNT, unsigned int>, smem, done);
-        const int blocks = grid(k_cell_scan<SM_COUNT, unsigned int>, smem);
-        ProfScope prof_("k_cell_scan<COUNT>", s);
-        k_cell_scan<SM_COUNT, unsigned int><<<blocks, STHREADS, smem, s>>>(
-            box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
-    }
-    else if (!hist_mode)
-    {
-        const size_t smem = sizeof(ScanShared<SM_COUNT, unsigned long long>);
-        static bool done = false;
-        configure(k_cell_scan<SM_COUNT, unsigned long long>, smem, done);
-        const int blocks = grid(k_cell_scan<SM_COUNT, unsigned long long>, smem);
-        ProfScope prof_("k_cell_scan<COUNT>", s);
-        k_cell_scan<SM_COUNT, unsigned long long><<<blocks, STHREADS, smem, s>>>(
-            box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
-    }
-    else
-    {
-        const size_t smem = sizeof(ScanShared<SM_HIST, unsigned long long>);
-        static bool done = false;
-        configure(k_cell_scan<SM_HIST, unsigned long long>, smem, done);
-        const int blocks = grid(k_cell_scan<SM_HIST, unsigned long long>, smem);
-        ProfScope prof_("k_cell_scan<HIST>", s);
-        k_cell_scan<SM_HIST, unsigned long long><<<blocks, STHREADS, smem, s>>>(
-            box, g, qg, p, pre_out2, 0.0f, 0.0f, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
-    }
+    const size_t smem = sizeof(ScanShared<SM_HIST, unsigned long long, 1024>);
+    static bool done = false;
+    configure(k_cell_scan<SM_HIST, unsigned long long, 1024>, smem, done);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_scan<SM_HIST, unsigned long long, 1024>, STHREADS,
+                                                  smem);
+    const int want = std::max(per_sm, 1) * sm_count_cell();
+    const int blocks = qg.ncell < want ? (qg.ncell < 1 ? 1 : qg.ncell) : want;
+    ProfScope prof_("k_cell_scan<HIST>", s);
+    k_cell_scan<SM_HIST, unsigned long long, 1024><<<blocks, STHREADS, smem, s>>>(
+        box, g, qg, p, pre_out2, 0.0f, 0.0f, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
 }
 
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
-                      uint2* ij, float* dist, float* vec, cudaStream_t s)
+                      uint2* ij, float* dist, float* vec, cudaStream_t s, int cap)
 {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cell_emit, ETHREADS, 0);
-    const int want = std::max(per_sm, 1) * sm_count_cell();
-    const int need = (qg.ncell + EWARPS - 1) / EWARPS;
-    const int blocks = need < want ? std::max(need, 1) : want;
-    ProfScope prof_("k_cell_emit", s);
-    k_cell_emit<<<blocks, ETHREADS, 0, s>>>(box, g, qg, p, gmask, gsorted, gtotal, offsets, ij, dist, vec);
+    auto go = [&](auto kernel) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ETHREADS, 0);
+        const int want = std::max(per_sm, 1) * sm_count_cell();
+        // a cell per work item when there are at least two cells per resident warp;
+        // else runs of queries, about four per resident warp
+        const uint64_t warps = static_cast<uint64_t>(want) * EWARPS;
+        uint32_t per_item = 0;
+        uint64_t items = static_cast<uint64_t>(std::max(qg.ncell, 1));
+        if (items < 2 * warps)
+        {
+            per_item = std::max<uint32_t>(1, static_cast<uint32_t>(p.nq / (4 * warps)));
+            items = (p.nq + per_item - 1) / per_item;
+        }
+        const uint64_t need = (items + EWARPS - 1) / EWARPS;
+        const int blocks = need < static_cast<uint64_t>(want) ? static_cast<int>(std::max<uint64_t>(need, 1)) : want;
+        ProfScope prof_("k_cell_emit", s);
+        kernel<<<blocks, ETHREADS, 0, s>>>(box, g, qg, p, gmask, gsorted, gtotal, offsets, ij, dist, vec, p.nq,
+                                           per_item);
+    };
+    if (cap > 1024)
+        go(k_cell_emit<4096>);
+    else
+        go(k_cell_emit<1024>);
 }
 
 } // namespace fg

@@ -128,14 +128,18 @@ size_t cell_smem_bytes();
 // every query of the cell, in cell-shifted coordinates, are dropped before the
 // merge; gtotal[cell] = candidates kept (all-ones for cells handed to the
 // warp-per-query kernels), read by the emit pass.
+// cap: candidate capacity of a cell in the count and emit passes, 1024 or 4096
+// (dense point sets; cell_cap_for picks it); gsorted is [ncell][cap] and gmask
+// [nq][cap / 32]. The histogram pass uses tiles of CELL_CAP.
+int cell_cap_for(const DevGrid& g, uint32_t n_points, bool is2d);
 void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       float pre_out2, float pre_in2, float cull2, uint32_t* counts, uint32_t* gmask,
                       uint32_t* gsorted, uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n,
                       const HistParams& h, unsigned long long* hist, cudaStream_t s,
-                      uint32_t n_points = 0xffffffffu);
+                      uint32_t n_points = 0xffffffffu, int cap = CELL_CAP);
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
-                      uint2* ij, float* dist, float* vec, cudaStream_t s);
+                      uint2* ij, float* dist, float* vec, cudaStream_t s, int cap = CELL_CAP);
 
 // Histogram of a distance array (RDF over a NeighborList).
 void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,

@@ -176,6 +176,48 @@ def test_heavy_queries(freud):
         assert_nlist_equal(nl, ij, d, v)
 
 
+@pytest.mark.parametrize("kind", [0, 2, 3])
+@pytest.mark.parametrize("tilt", [(0, 0, 0), (0.2, 0.1, 0.0)])
+def test_dense_ball_nlist(freud, kind, tilt):
+    """Density 1 with r_max 4 (~2,000 candidates per 27-cell stencil): the
+    block-per-cell kernels with a 4,096-candidate capacity."""
+    box, pts = random_box_points(freud, 21.544, 10000, 12, tilt)
+    nq = make_nq(freud, kind, box, pts, 4.0)
+    nl = nq.query(pts, dict(r_max=4.0, exclude_ii=True)).toNeighborList()
+    ij, d, v = O.query(box, pts, r_max=4.0, exclude_ii=True, arith=ARITH[kind])
+    assert_nlist_equal(nl, ij, d, v)
+    _, qpts = random_box_points(freud, 21.544, 3000, 13, tilt)
+    nl = nq.query(qpts, dict(r_max=4.0, r_min=0.7)).toNeighborList()
+    ij, d, v = O.query(box, pts, query_points=qpts, r_max=4.0, r_min=0.7, arith=ARITH[kind])
+    assert_nlist_equal(nl, ij, d, v)
+
+
+def test_dense_ball_nlist_2d(freud):
+    box, pts = random_box_points(freud, 60.0, 20000, 14, (0.1, 0, 0), is2d=True)
+    for kind in (0, 2):
+        nq = make_nq(freud, kind, box, pts, 5.0)
+        nl = nq.query(pts, dict(r_max=5.0, exclude_ii=True)).toNeighborList()
+        ij, d, v = O.query(box, pts, r_max=5.0, exclude_ii=True, arith=ARITH[kind])
+        assert_nlist_equal(nl, ij, d, v)
+
+
+def test_dense_ball_nlist_wide_keys(freud):
+    """More than 2^20 points with dense stencils: 64-bit merge keys at the
+    4,096-candidate capacity. The first 2,000 queries' rows against the oracle."""
+    box, pts = random_box_points(freud, 103.0, 1100000, 15)
+    nq = freud.locality.LinkCell(box, pts, 4.0)
+    nl = nq.query(pts, dict(r_max=4.0, exclude_ii=True)).toNeighborList()
+    m = 2000
+    ij, d, v = O.query(box, pts, query_points=pts[:m], r_max=4.0, exclude_ii=True, arith=O.ARITH_WRAP)
+    nb = len(ij)
+    np.testing.assert_array_equal(nl[:nb], ij)
+    np.testing.assert_array_equal(nl.distances[:nb], d)
+    np.testing.assert_array_equal(nl.vectors[:nb], v)
+    assert nl[nb, 0] == m
+    counts = nl.neighbor_counts
+    assert counts.sum() == len(nl) and counts.min() > 150
+
+
 def test_points_outside_box(freud):
     box, pts = random_box_points(freud, 10.0, 800, 4)
     shifted = pts.copy()
