@@ -76,6 +76,13 @@ SIGNATURES = {
     "fg_nlist_filter": [P, P],
     "fg_nlist_filter_r": [P, f32, f32],
     "fg_nlist_sort": [P, i32],
+    "fg_pmft_create": [i32, P, P, PP],
+    "fg_pmft_destroy": [P],
+    "fg_pmft_reset": [P],
+    "fg_pmft_accumulate": [P, P, P, u32, P, u32, P, u32, P, u32, P, pargs],
+    "fg_pmft_get": [P, P, P],
+    "fg_pmft_axis": [P, i32, P, P, P, pu32],
+    "fg_pmft_state": [P, pbox, pu32],
     "fg_cf_create": [u32, f32, PP],
     "fg_cf_destroy": [P],
     "fg_cf_reset": [P],

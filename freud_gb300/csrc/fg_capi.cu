@@ -57,6 +57,10 @@ static void runtime_error(const std::string& m)
 {
     throw Error(FG_ERR_RUNTIME, m);
 }
+static void index_error(const std::string& m)
+{
+    throw Error(FG_ERR_INDEX, m);
+}
 
 // ---------------------------------------------------------------------------
 // Stream and device memory
@@ -346,6 +350,20 @@ struct fg_cf
     DevBuf counts; // uint64 per bin
     HostBox box {};
     uint32_t frames = 0;
+};
+
+struct fg_pmft
+{
+    int kind;
+    int naxes;
+    PmftParams pp {};
+    uint64_t nbins = 0;
+    float jacobian = 1.0f;          // XY, XYT, XYZ: product of the bin widths
+    std::vector<float> inv_jac;     // R12: 1 / (r_center * dr * dt1 * dt2) per r bin
+    DevBuf hist;                    // uint64 per bin
+    HostBox box {};
+    uint32_t frames = 0, n_points = 0, n_query = 0;
+    uint32_t n_equiv = 0xffffffffu; // XYZ: fixed by the first accumulate after a reset
 };
 
 struct fg_steinhardt
@@ -2090,6 +2108,299 @@ fg_status fg_cf_state(const fg_cf* cf, fg_box* box, uint32_t* n_frames)
             *box = to_c_box(cf->box);
         if (n_frames)
             *n_frames = cf->frames;
+    });
+}
+
+// ---- PMFT ------------------------------------------------------------------------------
+namespace {
+constexpr float PMFT_TWO_PI = 6.2831854820251465f; // float(2 pi) (Box.h:24)
+
+PmftAxis pmft_axis(uint32_t n, float lo, float hi)
+{
+    // RegularAxis (Histogram.h:126-131)
+    PmftAxis a;
+    a.min = lo;
+    a.max = hi;
+    a.n = n;
+    a.inv = fdiv(1.0f, fdiv(fsub(hi, lo), static_cast<float>(n)));
+    return a;
+}
+
+float host_volume(const HostBox& b)
+{
+    // Box::getVolume (Box.h:196-205)
+    return b.is2d ? fmul(b.L[0], b.L[1]) : fmul(fmul(b.L[0], b.L[1]), b.L[2]);
+}
+} // namespace
+
+fg_status fg_pmft_create(int kind, const float* maxes, const uint32_t* bins, fg_pmft** out)
+{
+    return guard([&] {
+        require(out, "out");
+        require(maxes, "maxes");
+        require(bins, "bins");
+        auto pm = std::make_unique<fg_pmft>();
+        pm->kind = kind;
+        const char* name[4] = {"PMFTR12", "PMFTXYT", "PMFTXY", "PMFTXYZ"};
+        if (kind < FG_PMFT_R12 || kind > FG_PMFT_XYZ)
+            value_error("unknown PMFT kind");
+        // constructors: PMFTR12.cc:28-80, PMFTXYT.cc:29-69, PMFTXY.cc:25-62, PMFTXYZ.cc:26-90
+        const char* axis_names[4][3] = {{"R", "T1", "T2"}, {"X", "Y", "T"}, {"X", "Y", ""}, {"X", "Y", "Z"}};
+        pm->naxes = kind == FG_PMFT_XY ? 2 : 3;
+        for (int a = 0; a < pm->naxes; ++a)
+            if (bins[a] < 1)
+                value_error(std::string(name[kind]) + " requires at least 1 bin in " + axis_names[kind][a] + ".");
+        if (kind == FG_PMFT_R12)
+        {
+            if (maxes[0] < 0.0f)
+                value_error("PMFTR12 requires that r_max must be positive.");
+            pm->pp.ax[0] = pmft_axis(bins[0], 0.0f, maxes[0]);
+            pm->pp.ax[1] = pmft_axis(bins[1], 0.0f, PMFT_TWO_PI);
+            pm->pp.ax[2] = pmft_axis(bins[2], 0.0f, PMFT_TWO_PI);
+            const float dr = fdiv(maxes[0], static_cast<float>(bins[0]));
+            const float dt1 = fdiv(PMFT_TWO_PI, static_cast<float>(bins[1]));
+            const float dt2 = fdiv(1.0f, static_cast<float>(bins[2]));
+            const float product = fmul(fmul(dr, dt1), dt2);
+            const float bw = fdiv(maxes[0], static_cast<float>(bins[0]));
+            pm->inv_jac.resize(bins[0]);
+            for (uint32_t i = 0; i < bins[0]; ++i)
+            {
+                // bin centre (Histogram.h:87-95)
+                const float e0 = fmul(static_cast<float>(i), bw);
+                const float e1 = fmul(static_cast<float>(i + 1), bw);
+                const float r = fdiv(fadd(e0, e1), 2.0f);
+                pm->inv_jac[i] = fdiv(1.0f, fmul(r, product));
+            }
+        }
+        else
+        {
+            const char* ax[3] = {"x_max", "y_max", "z_max"};
+            const int nm = kind == FG_PMFT_XYZ ? 3 : 2;
+            for (int a = 0; a < nm; ++a)
+                if (maxes[a] < 0.0f)
+                    value_error(std::string(name[kind]) + " requires that " + ax[a] + " must be positive.");
+            float jac = 1.0f;
+            for (int a = 0; a < nm; ++a)
+            {
+                pm->pp.ax[a] = pmft_axis(bins[a], -maxes[a], maxes[a]);
+                const float d = fdiv(fmul(2.0f, maxes[a]), static_cast<float>(bins[a]));
+                jac = a == 0 ? d : fmul(jac, d);
+            }
+            if (kind == FG_PMFT_XYT)
+            {
+                pm->pp.ax[2] = pmft_axis(bins[2], 0.0f, PMFT_TWO_PI);
+                jac = fmul(jac, fdiv(1.0f, static_cast<float>(bins[2])));
+            }
+            pm->jacobian = jac;
+        }
+        if (pm->naxes == 2)
+            pm->pp.ax[2] = pmft_axis(1, 0.0f, 1.0f);
+        pm->nbins = static_cast<uint64_t>(pm->pp.ax[0].n) * pm->pp.ax[1].n * pm->pp.ax[2].n;
+        pm->hist.alloc(sizeof(unsigned long long) * pm->nbins);
+        FG_CUDA(cudaMemsetAsync(pm->hist.p, 0, sizeof(unsigned long long) * pm->nbins, stream()));
+        sync();
+        *out = pm.release();
+    });
+}
+
+fg_status fg_pmft_destroy(fg_pmft* pm)
+{
+    return guard([&] {
+        delete pm;
+        sync();
+    });
+}
+
+fg_status fg_pmft_reset(fg_pmft* pm)
+{
+    return guard([&] {
+        require(pm, "pmft");
+        FG_CUDA(cudaMemsetAsync(pm->hist.p, 0, sizeof(unsigned long long) * pm->nbins, stream()));
+        pm->frames = 0;
+        pm->n_equiv = 0xffffffffu;
+        sync();
+    });
+}
+
+fg_status fg_pmft_accumulate(fg_pmft* pm, fg_nq* nq, const float* orientations, uint32_t n_orient,
+                             const float* query_points, uint32_t n_query, const float* query_orientations,
+                             uint32_t n_query_orient, const float* equiv_orientations, uint32_t n_equiv,
+                             const fg_nlist* nlist, const fg_query_args* args)
+{
+    return guard([&] {
+        require(pm, "pmft");
+        require(nq, "nq");
+        cudaStream_t s = stream();
+        // Box::enforce2D / enforce3D (Box.h:571-585)
+        if (pm->kind == FG_PMFT_XYZ && nq->box.is2d)
+            value_error("A 2D box was provided to a class that only supports 3D systems.");
+        if (pm->kind != FG_PMFT_XYZ && !nq->box.is2d)
+            value_error("A 3D box was provided to a class that only supports 2D systems.");
+        DevBuf dq;
+        const float* qp = nullptr;
+        uint32_t nqp = nq->n;
+        if (query_points != nullptr)
+        {
+            upload_points(query_points, n_query, dq);
+            if (!same_as_points(nq, dq.as<float>(), n_query))
+            {
+                qp = dq.as<float>();
+                nqp = n_query;
+            }
+        }
+        const bool point_angles = pm->kind == FG_PMFT_R12 || pm->kind == FG_PMFT_XYT;
+        if (point_angles)
+        {
+            require(orientations, "orientations");
+            if (n_orient != nq->n)
+                value_error("orientations must hold one angle per point.");
+            if (query_orientations == nullptr)
+            {
+                query_orientations = orientations;
+                n_query_orient = n_orient;
+            }
+        }
+        require(query_orientations, "query_orientations");
+        if (n_query_orient < nqp)
+            value_error("query_orientations must hold one orientation per query point.");
+        if (pm->kind == FG_PMFT_XYZ)
+        {
+            require(equiv_orientations, "equiv_orientations");
+            // PMFTXYZ.cc:100-111
+            if (pm->n_equiv == 0xffffffffu)
+                pm->n_equiv = n_equiv;
+            else if (pm->n_equiv != n_equiv)
+                runtime_error("The number of equivalent orientations must be constant while accumulating data into "
+                              "PMFTXYZ.");
+        }
+        DevBuf d_pa, d_qa, d_cs, d_quat, d_eq;
+        if (point_angles)
+        {
+            d_pa.alloc(sizeof(float) * std::max<uint32_t>(n_orient, 1));
+            FG_CUDA(cudaMemcpyAsync(d_pa.p, orientations, sizeof(float) * n_orient, cudaMemcpyHostToDevice, s));
+            d_qa.alloc(sizeof(float) * std::max<uint32_t>(n_query_orient, 1));
+            FG_CUDA(cudaMemcpyAsync(d_qa.p, query_orientations, sizeof(float) * n_query_orient,
+                                    cudaMemcpyHostToDevice, s));
+        }
+        std::vector<float> cs;
+        if (pm->kind == FG_PMFT_XYT || pm->kind == FG_PMFT_XY)
+        {
+            // rotmat2::fromAngle(-theta) (VectorMath.h:912-921): cos and sin from the C
+            // library, once per query point
+            cs.resize(2 * static_cast<size_t>(n_query_orient));
+            for (uint32_t i = 0; i < n_query_orient; ++i)
+            {
+                const float th = -query_orientations[i];
+                cs[2 * i] = std::cos(th);
+                cs[2 * i + 1] = std::sin(th);
+            }
+            d_cs.alloc(sizeof(float2) * std::max<uint32_t>(n_query_orient, 1));
+            FG_CUDA(cudaMemcpyAsync(d_cs.p, cs.data(), sizeof(float2) * n_query_orient, cudaMemcpyHostToDevice, s));
+        }
+        if (pm->kind == FG_PMFT_XYZ)
+        {
+            d_quat.alloc(sizeof(float4) * std::max<uint32_t>(n_query_orient, 1));
+            FG_CUDA(cudaMemcpyAsync(d_quat.p, query_orientations, sizeof(float4) * n_query_orient,
+                                    cudaMemcpyHostToDevice, s));
+            d_eq.alloc(sizeof(float4) * std::max<uint32_t>(n_equiv, 1));
+            if (n_equiv > 0)
+                FG_CUDA(cudaMemcpyAsync(d_eq.p, equiv_orientations, sizeof(float4) * n_equiv, cudaMemcpyHostToDevice,
+                                        s));
+        }
+        fg_nlist tmp;
+        const fg_nlist* bonds = nlist;
+        if (nlist == nullptr)
+        {
+            require(args, "args");
+            run_query(nq, qp, nqp, args, 0, tmp);
+            bonds = &tmp;
+        }
+        else if ((point_angles && nlist->np > n_orient) || nlist->nq > n_query_orient)
+        {
+            // the reference indexes the orientations with the list's indices unchecked
+            value_error("NeighborList found inconsistent array sizes.");
+        }
+        PmftParams pp = pm->pp;
+        pp.n_equiv = pm->kind == FG_PMFT_XYZ ? n_equiv : 0;
+        launch_pmft_bonds(pm->kind, bonds->ij.as<uint2>(), bonds->dist.as<float>(), bonds->vec.as<float>(), bonds->nb,
+                          d_pa.as<float>(), d_qa.as<float>(), d_cs.as<float2>(), d_quat.as<float4>(), d_eq.as<float4>(),
+                          pp, pm->hist.as<unsigned long long>(), s);
+        FG_CUDA(cudaGetLastError());
+        // BondHistogramCompute::accumulateGeneral (BondHistogramCompute.h:115-126)
+        pm->box = nq->box;
+        pm->frames += 1;
+        pm->n_points = nq->n;
+        pm->n_query = nqp;
+        sync();
+    });
+}
+
+fg_status fg_pmft_get(fg_pmft* pm, uint32_t* bin_counts, float* pcf)
+{
+    return guard([&] {
+        require(pm, "pmft");
+        std::vector<unsigned long long> h(pm->nbins);
+        FG_CUDA(cudaMemcpyAsync(h.data(), pm->hist.p, sizeof(unsigned long long) * pm->nbins, cudaMemcpyDeviceToHost,
+                                stream()));
+        sync();
+        // PMFT::reduce (PMFT.h:70-82), PMFTXYZ::reduce (PMFTXYZ.cc:92-104): float32
+        const float inv_num_dens = fdiv(host_volume(pm->box), static_cast<float>(pm->n_query));
+        float denom = fmul(static_cast<float>(pm->frames), static_cast<float>(pm->n_points));
+        if (pm->kind == FG_PMFT_XYZ)
+            denom = fmul(denom, static_cast<float>(pm->n_equiv));
+        const float norm_factor = fdiv(1.0f, denom);
+        const float prefactor = fmul(inv_num_dens, norm_factor);
+        const float jf = fdiv(1.0f, pm->jacobian);
+        const uint64_t per_r = static_cast<uint64_t>(pm->pp.ax[1].n) * pm->pp.ax[2].n;
+        for (uint64_t i = 0; i < pm->nbins; ++i)
+        {
+            const uint32_t c = static_cast<uint32_t>(h[i]);
+            if (bin_counts)
+                bin_counts[i] = c;
+            if (pcf)
+            {
+                const float f = pm->kind == FG_PMFT_R12 ? pm->inv_jac[i / per_r] : jf;
+                pcf[i] = fmul(fmul(static_cast<float>(c), prefactor), f);
+            }
+        }
+    });
+}
+
+fg_status fg_pmft_axis(const fg_pmft* pm, int axis, float* edges, float* centers, float* bounds, uint32_t* n)
+{
+    return guard([&] {
+        require(pm, "pmft");
+        if (axis < 0 || axis >= pm->naxes)
+            index_error("PMFT axis out of range");
+        const PmftAxis& a = pm->pp.ax[axis];
+        // RegularAxis edges / centres (Histogram.h:126-138, 87-95)
+        const float bw = fdiv(fsub(a.max, a.min), static_cast<float>(a.n));
+        std::vector<float> e(a.n + 1);
+        for (uint32_t i = 0; i <= a.n; ++i)
+            e[i] = fadd(a.min, fmul(static_cast<float>(i), bw));
+        if (edges)
+            std::memcpy(edges, e.data(), sizeof(float) * (a.n + 1));
+        if (centers)
+            for (uint32_t i = 0; i < a.n; ++i)
+                centers[i] = fdiv(fadd(e[i], e[i + 1]), 2.0f);
+        if (bounds)
+        {
+            bounds[0] = a.min;
+            bounds[1] = a.max;
+        }
+        if (n)
+            *n = a.n;
+    });
+}
+
+fg_status fg_pmft_state(const fg_pmft* pm, fg_box* box, uint32_t* n_frames)
+{
+    return guard([&] {
+        require(pm, "pmft");
+        if (box)
+            *box = to_c_box(pm->box);
+        if (n_frames)
+            *n_frames = pm->frames;
     });
 }
 

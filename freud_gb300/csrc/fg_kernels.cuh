@@ -150,6 +150,32 @@ void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, 
 void launch_cf_bonds(const uint2* ij, const float* dist, uint64_t nb, const double2* values, const double2* qvalues,
                      const HistParams& h, double2* sums, unsigned long long* counts, cudaStream_t s);
 
+// ---- PMFT ------------------------------------------------------------------------
+enum PmftKind
+{
+    PMFT_R12 = 0,
+    PMFT_XYT = 1,
+    PMFT_XY = 2,
+    PMFT_XYZ = 3,
+};
+// RegularAxis(n, min, max): inv = 1 / ((max - min) / n) in float (Histogram.h:126-131)
+struct PmftAxis
+{
+    float min, max, inv;
+    uint32_t n;
+};
+struct PmftParams
+{
+    PmftAxis ax[3];   // XY uses two
+    uint32_t n_equiv; // XYZ equivalent orientations
+};
+// Bins every bond of a list: p_angle / q_angle per point / query (R12, XYT),
+// q_cs = (cos, sin) of minus the query angle (XYT, XY), q_quat the query
+// quaternions (s, x, y, z) and equiv the equivalent orientations (XYZ).
+void launch_pmft_bonds(int kind, const uint2* ij, const float* dist, const float* vec, uint64_t nb,
+                       const float* p_angle, const float* q_angle, const float2* q_cs, const float4* q_quat,
+                       const float4* equiv, const PmftParams& pp, unsigned long long* hist, cudaStream_t s);
+
 // ---- k nearest neighbours ------------------------------------------------------
 struct KnnParams
 {

@@ -70,6 +70,7 @@ typedef struct fg_nq fg_nq;
 typedef struct fg_nlist fg_nlist;
 typedef struct fg_rdf fg_rdf;
 typedef struct fg_cf fg_cf;
+typedef struct fg_pmft fg_pmft;
 typedef struct fg_steinhardt fg_steinhardt;
 typedef struct fg_frames fg_frames;
 
@@ -203,6 +204,32 @@ fg_status fg_cf_get(fg_cf* cf, uint32_t* bin_counts, double* correlation);
 fg_status fg_cf_bin_edges(const fg_cf* cf, float* edges, float* centers);
 /* getBox of the last accumulated frame; frame counter. */
 fg_status fg_cf_state(const fg_cf* cf, fg_box* box, uint32_t* n_frames);
+
+/* ---- PMFT -------------------------------------------------------------------------
+ * freud::pmft::PMFTR12 / PMFTXYT / PMFTXY / PMFTXYZ (freud/pmft/PMFTR12.cc, PMFTXYT.cc,
+ * PMFTXY.cc, PMFTXYZ.cc, PMFT.h:29-88;
+ * bindings freud/pmft/export-PMFT*; Python freud/pmft.py). */
+#define FG_PMFT_R12 0 /* maxes = {r_max}, bins = {n_r, n_t1, n_t2} */
+#define FG_PMFT_XYT 1 /* maxes = {x_max, y_max}, bins = {n_x, n_y, n_t} */
+#define FG_PMFT_XY 2  /* maxes = {x_max, y_max}, bins = {n_x, n_y} */
+#define FG_PMFT_XYZ 3 /* maxes = {x_max, y_max, z_max}, bins = {n_x, n_y, n_z} */
+fg_status fg_pmft_create(int kind, const float* maxes, const uint32_t* bins, fg_pmft** out);
+fg_status fg_pmft_destroy(fg_pmft* pm);
+fg_status fg_pmft_reset(fg_pmft* pm);
+/* PMFT*::accumulate: orientations are per-point angles (R12, XYT; NULL otherwise),
+ * query_orientations per-query angles (R12, XYT, XY; NULL: orientations for R12 /
+ * XYT) or quaternions (s, x, y, z) (XYZ); equiv_orientations quaternions (XYZ).
+ * nlist == NULL queries nq with args. */
+fg_status fg_pmft_accumulate(fg_pmft* pm, fg_nq* nq, const float* orientations, uint32_t n_orient,
+                             const float* query_points, uint32_t n_query, const float* query_orientations,
+                             uint32_t n_query_orient, const float* equiv_orientations, uint32_t n_equiv,
+                             const fg_nlist* nlist, const fg_query_args* args);
+/* getBinCounts (uint32, row-major over the axes) and getPCF (PMFT.h:70-82). */
+fg_status fg_pmft_get(fg_pmft* pm, uint32_t* bin_counts, float* pcf);
+/* One axis: bin edges (n + 1), centres (n), bounds (min, max), bin count. */
+fg_status fg_pmft_axis(const fg_pmft* pm, int axis, float* edges, float* centers, float* bounds, uint32_t* n);
+/* getBox of the last accumulated frame; frame counter. */
+fg_status fg_pmft_state(const fg_pmft* pm, fg_box* box, uint32_t* n_frames);
 
 /* ---- Steinhardt ----------------------------------------------------------------
  * freud::order::Steinhardt (freud/order/Steinhardt.h:59-223, Steinhardt.cc:85-359;

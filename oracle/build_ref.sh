@@ -18,11 +18,12 @@ OUT="$HERE/_ref"
 mkdir -p "$OUT"
 CXX="${CXX:-g++}"
 FLAGS=(-O3 -ffp-contract=off -std=c++17 -fPIC -shared -w
-       -I"$HERE/ref_shim" -I"$SRC/box" -I"$SRC/util" -I"$SRC/locality" -I"$SRC/density" -I"$SRC/order")
+       -I"$HERE/ref_shim" -I"$SRC/box" -I"$SRC/util" -I"$SRC/locality" -I"$SRC/density" -I"$SRC/pmft" -I"$SRC/order")
 SOURCES=("$SRC/locality/LinkCell.cc" "$SRC/locality/AABBQuery.cc" "$SRC/locality/CellQuery.cc"
          "$SRC/locality/NeighborList.cc"
          "$SRC/locality/NeighborComputeFunctional.cc" "$SRC/density/RDF.cc"
-         "$SRC/density/CorrelationFunction.cc" "$SRC/order/Steinhardt.cc"
+         "$SRC/density/CorrelationFunction.cc" "$SRC/pmft/PMFTR12.cc" "$SRC/pmft/PMFTXYT.cc"
+         "$SRC/pmft/PMFTXY.cc" "$SRC/pmft/PMFTXYZ.cc" "$SRC/order/Steinhardt.cc"
          "$SRC/order/Wigner3j.cc" "$HERE/ref_harness.cpp")
 OBJS=()
 for s in "${SOURCES[@]}"; do

@@ -982,6 +982,95 @@ void ofg_bin_index(const float* distances, uint64_t nb, uint32_t bins, float r_m
     }
 }
 
+/* PMFT binning of a list's bonds (PMFTR12.cc:92-110, PMFTXYT.cc:79-100,
+ * PMFTXY.cc:71-88, PMFTXYZ.cc:116-145), in the reference's float arithmetic with
+ * the C library's cosf / sinf / atan2f / fmodf. kind 0 R12, 1 XYT, 2 XY, 3 XYZ.
+ * axes: (min, max, n) per axis (n = 1 for the unused third axis of XY). Adds into
+ * row-major uint64 counts. */
+static float o_modpos(float a, float b)
+{
+    return fmodf(fmodf(a, b) + b, b);
+}
+
+static void o_qrotate(const float* q, const float* b, float* o)
+{
+    /* rotate(quat, vec3) (VectorMath.h:810-823) */
+    const float vv = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    const float t1 = q[0] * q[0] - vv;
+    const float s2 = 2.0f * q[0];
+    const float cx = q[2] * b[2] - q[3] * b[1];
+    const float cy = q[3] * b[0] - q[1] * b[2];
+    const float cz = q[1] * b[1] - q[2] * b[0];
+    const float d2 = 2.0f * (q[1] * b[0] + q[2] * b[1] + q[3] * b[2]);
+    o[0] = t1 * b[0] + s2 * cx + d2 * q[1];
+    o[1] = t1 * b[1] + s2 * cy + d2 * q[2];
+    o[2] = t1 * b[2] + s2 * cz + d2 * q[3];
+}
+
+void ofg_pmft(int kind, uint64_t nb, const uint32_t* ij, const float* dist, const float* vec, const float* p_angle,
+              const float* q_angle, const float* q_quat, const float* equiv, uint32_t n_equiv, const float* axes,
+              uint64_t* counts)
+{
+    const float two_pi = (float) (2.0 * M_PI);
+    float inv[3];
+    for (int a = 0; a < 3; ++a)
+    {
+        inv[a] = 1.0f / ((axes[3 * a + 1] - axes[3 * a]) / (float) (uint32_t) axes[3 * a + 2]);
+    }
+    const uint32_t n1 = (uint32_t) axes[5], n2 = (uint32_t) axes[8];
+    for (uint64_t e = 0; e < nb; ++e)
+    {
+        const uint32_t i = ij[2 * e], j = ij[2 * e + 1];
+        const float dx = vec[3 * e], dy = vec[3 * e + 1], dz = vec[3 * e + 2];
+        float c[3];
+        int ncoord = 1;
+        float vals[64][3];
+        if (kind == 0)
+        {
+            const float t1 = o_modpos(p_angle[j] - atan2f(dy, dx), two_pi);
+            const float t2 = o_modpos(q_angle[i] - atan2f(-dy, -dx), two_pi);
+            vals[0][0] = dist[e];
+            vals[0][1] = t1;
+            vals[0][2] = t2;
+        }
+        else if (kind == 1 || kind == 2)
+        {
+            const float th = -q_angle[i];
+            const float cs = cosf(th), sn = sinf(th);
+            vals[0][0] = cs * dx + (-sn) * dy;
+            vals[0][1] = sn * dx + cs * dy;
+            vals[0][2] = kind == 1 ? o_modpos(p_angle[j] - atan2f(-dy, -dx), two_pi) : 0.0f;
+        }
+        else
+        {
+            const float cq[4] = {q_quat[4 * i], -q_quat[4 * i + 1], -q_quat[4 * i + 2], -q_quat[4 * i + 3]};
+            const float d[3] = {dx, dy, dz};
+            float u[3];
+            o_qrotate(cq, d, u);
+            ncoord = (int) n_equiv;
+            for (int k = 0; k < ncoord && k < 64; ++k)
+            {
+                o_qrotate(equiv + 4 * k, u, vals[k]);
+            }
+        }
+        for (int k = 0; k < ncoord && k < 64; ++k)
+        {
+            int64_t b[3];
+            int ok = 1;
+            for (int a = 0; a < 3; ++a)
+            {
+                c[a] = vals[k][a];
+                b[a] = hist_bin(c[a], axes[3 * a], axes[3 * a + 1], inv[a], (uint32_t) axes[3 * a + 2]);
+                ok &= b[a] >= 0;
+            }
+            if (ok)
+            {
+                counts[((uint64_t) b[0] * n1 + (uint64_t) b[1]) * n2 + (uint64_t) b[2]]++;
+            }
+        }
+    }
+}
+
 /* Bin edges / centres (Histogram.h:126-138, :72-80). */
 void ofg_bin_edges(uint32_t bins, float r_min, float r_max, float* edges, float* centers)
 {

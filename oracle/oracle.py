@@ -47,6 +47,7 @@ def _load():
     lib.ofg_rdf_query.argtypes = [P, P, u32, P, u32, f32, f32, i32, i32, u32, f32, f32, i32, P]
     lib.ofg_hist.argtypes = [P, u64, u32, f32, f32, P]
     lib.ofg_bin_index.argtypes = [P, u64, u32, f32, f32, P]
+    lib.ofg_pmft.argtypes = [ctypes.c_int, u64, P, P, P, P, P, P, P, u32, P, P]
     lib.ofg_bin_edges.argtypes = [u32, f32, f32, P, P]
     lib.ofg_rdf_reduce.argtypes = [P, u32, f32, f32, u32, u32, u32, f32, i32, i32, P, P]
     lib.ofg_ylm.argtypes = [i32, ctypes.c_double, ctypes.c_double, P]
@@ -154,6 +155,37 @@ def correlation(ij, distances, values, query_values, bins, r_max, sums=None, cou
     nz = counts != 0
     corr[nz] = sums[nz] / counts[nz].astype(np.float64)
     return corr, counts, sums
+
+
+PMFT_AXES = {
+    0: lambda m, b: [(0.0, m[0], b[0]), (0.0, 2 * np.pi, b[1]), (0.0, 2 * np.pi, b[2])],
+    1: lambda m, b: [(-m[0], m[0], b[0]), (-m[1], m[1], b[1]), (0.0, 2 * np.pi, b[2])],
+    2: lambda m, b: [(-m[0], m[0], b[0]), (-m[1], m[1], b[1]), (0.0, 1.0, 1)],
+    3: lambda m, b: [(-m[0], m[0], b[0]), (-m[1], m[1], b[1]), (-m[2], m[2], b[2])],
+}
+
+
+def pmft_counts(kind, maxes, bins, ij, distances, vectors, p_angle=None, q_angle=None, q_quat=None, equiv=None,
+                counts=None):
+    """PMFT bin counts (kind 0 R12, 1 XYT, 2 XY, 3 XYZ) of a list's bonds, in the
+    reference's float arithmetic (PMFT*.cc accumulate). Adds into and returns
+    uint64 counts shaped by bins (XY: (n_x, n_y))."""
+    lib = _load()
+    axes = np.array([[np.float32(a), np.float32(b), np.float32(n)] for a, b, n in
+                     PMFT_AXES[kind](list(maxes), list(bins))], np.float32).reshape(-1)
+    shape = tuple(int(x) for x in bins)
+    n = int(np.prod(shape))
+    if counts is None:
+        counts = np.zeros(n, np.uint64)
+    c = np.ascontiguousarray(counts.reshape(-1))
+    ijc = np.ascontiguousarray(ij, np.uint32).reshape(-1, 2)
+    d = np.ascontiguousarray(distances, np.float32)
+    v = np.ascontiguousarray(vectors, np.float32).reshape(-1, 3)
+    conv = (lambda a: None if a is None else np.ascontiguousarray(a, np.float32))
+    eq = conv(equiv)
+    lib.ofg_pmft(int(kind), len(d), _p(ijc), _p(d), _p(v), _p(conv(p_angle)), _p(conv(q_angle)), _p(conv(q_quat)),
+                 _p(eq), 0 if eq is None else len(eq), _p(axes), _p(c))
+    return c.reshape(shape)
 
 
 def bin_edges(bins, r_max, r_min=0.0):

@@ -51,6 +51,9 @@ def _load():
     lib.ref_rdf.restype = i32
     lib.ref_rdf.argtypes = [u32, f32, f32, i32, i32, P, P, P, P, i32, f32, i32, u32, f32,
                             f32, i32, P, P, P, P, P, P, P, ctypes.c_char_p, i32]
+    lib.ref_pmft.restype = i32
+    lib.ref_pmft.argtypes = [i32, P, P, i32, P, P, P, P, P, P, P, P, P, u32, i32, i32, u32, f32, f32, i32, P, P,
+                             ctypes.c_char_p, i32]
     lib.ref_cf.restype = i32
     lib.ref_cf.argtypes = [u32, f32, i32, P, P, P, P, P, P, P, P, i32, f32, i32, u32, f32, f32, i32, P, P,
                            ctypes.c_char_p, i32]
@@ -154,6 +157,41 @@ def cf(bins, r_max, frames, values, query_frames=None, query_values=None, kind=K
     if st != 0:
         raise RefError(st, err.value.decode())
     return counts, corr
+
+
+def pmft(kind, maxes, bins, frames, orientations=None, query_frames=None, query_orientations=None,
+         equiv=None, nq_kind=KIND_RAW, mode=MODE_BALL, num_neighbors=DEFAULT_NUM_NEIGHBORS, r_max=-1.0,
+         r_min=0.0, exclude_ii=True):
+    """PMFT (kind 0 R12, 1 XYT, 2 XY, 3 XYZ) over frames (list of (box, points)).
+    orientations / query_orientations: per-frame lists (angles, or (n, 4)
+    quaternions for XYZ). Returns (counts uint32, pcf float32) shaped by bins."""
+    lib = _load()
+    boxes = np.concatenate([_box6(b)[0] for b, _ in frames]).astype(np.float32)
+    is2d = np.array([int(b[6]) for b, _ in frames], np.int32)
+    offsets = np.concatenate([[0], np.cumsum([len(p) for _, p in frames])]).astype(np.uint32)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float32) for _, p in frames]))
+    cat = (lambda xs: None if xs is None else np.ascontiguousarray(np.concatenate(
+        [np.asarray(x, np.float32).reshape(len(x), -1) for x in xs]), np.float32))
+    orient = cat(orientations)
+    qoff = qpts = None
+    if query_frames is not None:
+        qoff = np.concatenate([[0], np.cumsum([len(q) for q in query_frames])]).astype(np.uint32)
+        qpts = np.ascontiguousarray(np.concatenate([np.asarray(q, np.float32) for q in query_frames]))
+    qorient = cat(query_orientations)
+    eq = None if equiv is None else np.ascontiguousarray(equiv, np.float32)
+    m = np.asarray(maxes, np.float32)
+    b = np.asarray(bins, np.uint32)
+    n = int(np.prod(b))
+    counts = np.zeros(n, np.uint32)
+    pcf = np.zeros(n, np.float32)
+    err = ctypes.create_string_buffer(512)
+    st = lib.ref_pmft(int(kind), _ptr(m), _ptr(b), len(frames), _ptr(boxes), _ptr(is2d), _ptr(offsets), _ptr(pts),
+                      _ptr(orient), _ptr(qoff), _ptr(qpts), _ptr(qorient), _ptr(eq), 0 if eq is None else len(eq),
+                      nq_kind, mode, num_neighbors, r_max, r_min, int(exclude_ii), _ptr(counts), _ptr(pcf), err,
+                      512)
+    if st != 0:
+        raise RefError(st, err.value.decode())
+    return counts.reshape(tuple(int(x) for x in b)), pcf.reshape(tuple(int(x) for x in b))
 
 
 def steinhardt(ls, box, points, average=False, wl=False, weighted=False, wl_normalize=False,

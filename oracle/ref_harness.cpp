@@ -14,6 +14,7 @@
 //   freud/locality/NeighborList.cc:51-82      NeighborList from arrays
 //   freud/density/RDF.cc:25-110               RDF ctor / accumulate / reduce
 //   freud/density/CorrelationFunction.cc:26-96 CorrelationFunction ctor / accumulate / reduce
+//   freud/pmft/PMFTR12.cc, PMFTXYT.cc, PMFTXY.cc, PMFTXYZ.cc   PMFT ctors / accumulate / reduce
 //   freud/order/Steinhardt.cc:85-118          Steinhardt::compute
 #include <complex>
 #include <cstring>
@@ -26,6 +27,10 @@
 #include "CellQuery.h"
 #include "Box.h"
 #include "CorrelationFunction.h"
+#include "PMFTR12.h"
+#include "PMFTXY.h"
+#include "PMFTXYT.h"
+#include "PMFTXYZ.h"
 #include "LinkCell.h"
 #include "NeighborList.h"
 #include "NeighborQuery.h"
@@ -268,6 +273,86 @@ int ref_cf(unsigned bins, float r_max, int nframes, const float* boxes6, const i
             counts[i] = (*c)[i];
             corr[2 * i] = (*g)[i].real();
             corr[2 * i + 1] = (*g)[i].imag();
+        }
+        return REF_OK;
+    }
+    catch (const std::invalid_argument& e)
+    {
+        return report(e, REF_VALUE_ERROR, err, errlen);
+    }
+    catch (const std::exception& e)
+    {
+        return report(e, REF_RUNTIME_ERROR, err, errlen);
+    }
+}
+
+// PMFT accumulated over nframes with a live query per frame. kind 0 R12, 1 XYT,
+// 2 XY, 3 XYZ. orient: per-point angles (R12, XYT); qorient: per-query angles
+// (R12, XYT, XY; NULL: orient) or quaternions (XYZ); qpts == NULL queries the
+// frame's points. counts / pcf: row-major over the axes.
+int ref_pmft(int kind, const float* maxes, const unsigned* bins, int nframes, const float* boxes6, const int* is2d,
+             const unsigned* offsets, const float* pts, const float* orient, const unsigned* qoffsets,
+             const float* qpts, const float* qorient, const float* equiv, unsigned n_equiv, int nq_kind, int mode,
+             unsigned num_neighbors, float q_r_max, float q_r_min, int exclude_ii, unsigned* counts, float* pcf,
+             char* err, int errlen)
+{
+    try
+    {
+        std::unique_ptr<freud::pmft::PMFT> pm;
+        freud::pmft::PMFTR12* r12 = nullptr;
+        freud::pmft::PMFTXYT* xyt = nullptr;
+        freud::pmft::PMFTXY* xy = nullptr;
+        freud::pmft::PMFTXYZ* xyz = nullptr;
+        if (kind == 0)
+            pm.reset(r12 = new freud::pmft::PMFTR12(maxes[0], bins[0], bins[1], bins[2]));
+        else if (kind == 1)
+            pm.reset(xyt = new freud::pmft::PMFTXYT(maxes[0], maxes[1], bins[0], bins[1], bins[2]));
+        else if (kind == 2)
+            pm.reset(xy = new freud::pmft::PMFTXY(maxes[0], maxes[1], bins[0], bins[1]));
+        else
+            pm.reset(xyz = new freud::pmft::PMFTXYZ(maxes[0], maxes[1], maxes[2], bins[0], bins[1], bins[2]));
+        for (int f = 0; f < nframes; ++f)
+        {
+            const Box box = make_box(boxes6 + 6 * f, is2d[f]);
+            const unsigned n = offsets[f + 1] - offsets[f];
+            const float* p = pts + 3 * static_cast<size_t>(offsets[f]);
+            auto nqo = make_nq(nq_kind, box, p, n, 0.0F);
+            const float* qp = p;
+            unsigned nqp = n;
+            size_t qbase = offsets[f];
+            if (qpts != nullptr)
+            {
+                qp = qpts + 3 * static_cast<size_t>(qoffsets[f]);
+                nqp = qoffsets[f + 1] - qoffsets[f];
+                qbase = qoffsets[f];
+            }
+            const auto qargs = make_qargs(mode, num_neighbors, q_r_max, q_r_min, -1.0F, -1.0F, exclude_ii);
+            const auto* qv = reinterpret_cast<const vec3<float>*>(qp);
+            if (r12 != nullptr || xyt != nullptr)
+            {
+                const float* o = orient + offsets[f];
+                const float* qo = qorient != nullptr ? qorient + qbase : o;
+                if (r12 != nullptr)
+                    r12->accumulate(nqo, o, qv, qo, nqp, nullptr, qargs);
+                else
+                    xyt->accumulate(nqo, o, qv, qo, nqp, nullptr, qargs);
+            }
+            else if (xy != nullptr)
+            {
+                xy->accumulate(nqo, qorient + qbase, qv, nqp, nullptr, qargs);
+            }
+            else
+            {
+                xyz->accumulate(nqo, reinterpret_cast<const quat<float>*>(qorient) + qbase, qv, nqp,
+                                reinterpret_cast<const quat<float>*>(equiv), n_equiv, nullptr, qargs);
+            }
+        }
+        auto c = pm->getBinCounts();
+        auto g = pm->getPCF();
+        for (size_t i = 0; i < c->size(); ++i)
+        {
+            counts[i] = (*c)[i];
+            pcf[i] = (*g)[i];
         }
         return REF_OK;
     }
