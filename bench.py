@@ -286,6 +286,44 @@ def measure_cf(freud, _lib, steps, warmup, cpu=True):
     return out
 
 
+def measure_pmft(freud, _lib, steps, warmup, cpu=True):
+    """PMFTXYZ(1.5, 1.5, 1.5, 40) on the 256,000-particle FCC system with random
+    unit-quaternion orientations (ball neighbours within sqrt(3) * 1.5)."""
+    L, pts = c3_system()
+    box = freud.box.Box.cube(float(L))
+    rs = np.random.RandomState(6)
+    q = rs.standard_normal((len(pts), 4))
+    q = (q / np.linalg.norm(q, axis=1, keepdims=True)).astype(np.float32)
+    pm = freud.pmft.PMFTXYZ(1.5, 1.5, 1.5, 40)
+
+    def step():
+        pm.compute((box, pts), q)
+        return pm.bin_counts
+
+    bonds = int(step().astype(np.int64).sum())
+    t = _median_wall(step, steps, warmup)
+    dev_ms, launches, top = _device_ms(_lib, step, steps)
+    out = {"workload": "pmftxyz_fcc_256000_xyz1.5_bins40", "binned_bonds": bonds, "e2e_ms": t * 1e3,
+           "e2e": bonds / t, "device_ms": dev_ms, "device": bonds / (dev_ms / 1e3), "unit": "pair evals/s",
+           "launches_per_step": launches, "kernels_ms_per_step": top}
+    if cpu:
+        from oracle import oracle as O
+
+        bx = (float(L),) * 3 + (0.0, 0.0, 0.0, 0.0)
+        rm = float(np.float32(np.sqrt(3 * 1.5 ** 2)))
+        t0 = time.perf_counter()
+        ij, d, v = O.query(bx, pts, r_max=rm, exclude_ii=True)
+        tq = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.pmft_counts(3, [1.5, 1.5, 1.5], [40, 40, 40], ij, d, v, q_quat=q,
+                      equiv=np.array([[1, 0, 0, 0]], np.float32))
+        tb = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": bonds / (tq + tb), "unit": "pair evals/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": "whole workload: oracle ball query (all threads) + PMFT "
+                                                         "binning (1 thread)"}
+    return out
+
+
 def measure_c3(freud, _lib, steps, warmup, cpu=True):
     """Steinhardt([4, 6, 8, 10, 12], average, wl, wl_normalize) with 12 nearest
     neighbours on a 256,000-point noisy FCC crystal."""
@@ -499,6 +537,7 @@ def run_only(args):
     fns = {"plain_rdf": lambda: measure_c1(freud, _lib, args.steps, args.warmup, cpu=False),
            "steinhardt": lambda: measure_c3(freud, _lib, args.steps, args.warmup, cpu=False),
            "correlation_function": lambda: measure_cf(freud, _lib, args.steps, args.warmup, cpu=False),
+           "pmft": lambda: measure_pmft(freud, _lib, args.steps, args.warmup, cpu=False),
            "batched_frames": lambda: measure_c4(freud, _lib, args.steps, args.warmup, 8 if args.small else 64),
            "precision_stress": lambda: measure_c5(freud, _lib, args.steps, args.warmup, args.small)}
     print(json.dumps({"only": args.only, "result": fns[args.only]()}), flush=True)
@@ -516,7 +555,7 @@ def main():
                     help="skip the plain-RDF, Steinhardt, batched-frames and stress workloads")
     ap.add_argument("--n-side", type=int, default=102,
                     help="lattice points per side; 102 is the benchmark workload, smaller sizes are for profiling")
-    ap.add_argument("--only", default=None, choices=["plain_rdf", "steinhardt", "correlation_function",
+    ap.add_argument("--only", default=None, choices=["plain_rdf", "steinhardt", "correlation_function", "pmft",
                                                      "batched_frames", "precision_stress"],
                     help="run one of the other workloads alone and print its result (profiling)")
     ap.add_argument("--small", action="store_true",
@@ -668,6 +707,8 @@ def main():
                                                             cpu=not args.no_cpu_baseline)),
                          ("correlation_function", lambda: measure_cf(freud, _lib, args.steps, args.warmup,
                                                                      cpu=not args.no_cpu_baseline)),
+                         ("pmft", lambda: measure_pmft(freud, _lib, args.steps, args.warmup,
+                                                       cpu=not args.no_cpu_baseline)),
                          ("batched_frames", lambda: measure_c4(freud, _lib, args.steps, args.warmup)),
                          ("precision_stress", lambda: measure_c5(freud, _lib, args.steps, args.warmup))):
             try:

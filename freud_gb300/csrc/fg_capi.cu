@@ -2563,7 +2563,8 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
         const bool use_w = st->weighted && !nl->unit_weights;
         launch_qlm(nq->dbox, nq->dpts, n, nl->ij.as<uint2>(), nl->dist.as<float>(),
                    use_w ? nl->weights.as<float>() : nullptr, nl->seg.as<uint32_t>(), nl->cnt.as<uint32_t>(), st->st,
-                   use_w ? 1 : 0, st->qlm.as<float2>(), st->ql.as<float>(), s);
+                   use_w ? 1 : 0, st->qlm.as<float2>(), st->ql.as<float>(), s, nullptr,
+                   static_cast<double>(nl->nb) / std::max<uint32_t>(n, 1));
         const float2* src = st->qlm.as<float2>();
         const float* qn = st->ql.as<float>();
         if (st->average)
@@ -3381,7 +3382,7 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
                                          fr->st_seg.as<uint32_t>(), s);
             launch_qlm(g.fd_host[0].b, fr->dpts, P, nullptr, nullptr, nullptr, fr->st_seg.as<uint32_t>(),
                        fr->st_counts.as<uint32_t>(), st->st, 0, st->qlm.as<float2>(), st->ql.as<float>(), s,
-                       fr->st_vd.as<float4>());
+                       fr->st_vd.as<float4>(), static_cast<double>(nb) / std::max<uint32_t>(P, 1));
             const float2* src = st->qlm.as<float2>();
             const float* qn = st->ql.as<float>();
             if (st->average)

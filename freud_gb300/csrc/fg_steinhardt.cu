@@ -18,6 +18,7 @@
 // k_wl: thread per (particle, l), Wigner-3j triple sum with compensated float sum.
 // The FP64 system sums (qlm or averaged qlm over the particles, divided by N)
 // are taken by the per-frame column-sum kernels of fg_batch.cu.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -300,6 +301,182 @@ __global__ void __launch_bounds__(128)
                 ql_out[static_cast<size_t>(i) * ls.nl + k] = sqrtf(part * ls.norm[k]);
             }
         }
+    }
+}
+
+// One l value, bonds spread flat over the lanes: a warp takes per_warp consecutive
+// particles (a few bonds each), lane t of a round computes every order m of
+// Y_l^m for bond round*32 + t of the warp's particles (one geometry and l(l+1)/2
+// recurrence steps per bond, all lanes busy), and a segmented shuffle scan keyed
+// by particle adds each particle's part of the round into its shared-memory row.
+// Summation order is fixed (tree within a round, rounds in sequence).
+template<int L>
+__global__ void __launch_bounds__(128)
+    k_qlm_flat(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
+               const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
+               const uint32_t* __restrict__ cnt, const float4* __restrict__ bvd, StLs ls, int weighted,
+               uint32_t per_warp, float2* __restrict__ qlm_out, float* __restrict__ ql_out)
+{
+    constexpr int NV = 2 * (L + 1) + 1; // re, im for m = 0..L, then the weight (odd: no bank conflicts)
+    __shared__ float acc_s[4][32][NV];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    float (*acc)[NV] = acc_s[warp];
+    const uint32_t nwarps = gridDim.x * 4;
+    for (uint32_t p0 = (blockIdx.x * 4 + warp) * per_warp; p0 < n; p0 += nwarps * per_warp)
+    {
+        const uint32_t np = min(per_warp, n - p0);
+        uint32_t c = 0, sg = 0;
+        if (static_cast<uint32_t>(lane) < np)
+        {
+            c = cnt[p0 + lane];
+            sg = seg[p0 + lane];
+        }
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o)
+                incl += v;
+        }
+        const uint32_t excl = incl - c;
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        // the warp's bonds are contiguous from the first particle that has any
+        const unsigned nz = __ballot_sync(FULL, c > 0);
+        const uint32_t base = nz ? __shfl_sync(FULL, sg, __ffs(nz) - 1) : 0u;
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+            acc[lane][v] = 0.0f;
+        __syncwarp();
+        for (uint32_t r0 = 0; r0 < total; r0 += 32)
+        {
+            const uint32_t bb = r0 + static_cast<uint32_t>(lane);
+            const bool live = bb < total;
+            // particle slot of bond bb: the last slot whose exclusive prefix is <= bb
+            int k = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1)
+            {
+                const uint32_t v = __shfl_sync(FULL, excl, k + step);
+                if (v <= bb)
+                    k += step;
+            }
+            float vals[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v)
+                vals[v] = 0.0f;
+            if (live)
+            {
+                const uint32_t e = base + bb;
+                float dx, dy, dz, d;
+                if (bvd != nullptr)
+                {
+                    const float4 v4 = bvd[e];
+                    dx = v4.x;
+                    dy = v4.y;
+                    dz = v4.z;
+                    d = v4.w;
+                }
+                else
+                {
+                    const uint32_t i = p0 + static_cast<uint32_t>(k);
+                    const uint32_t j = ij[e].y;
+                    box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pts[3 * (size_t) i]),
+                             __fsub_rn(pts[3 * (size_t) j + 1], pts[3 * (size_t) i + 1]),
+                             __fsub_rn(pts[3 * (size_t) j + 2], pts[3 * (size_t) i + 2]), dx, dy, dz);
+                    d = dist[e];
+                }
+                const float w = weighted ? weights[e] : 1.0f;
+                const float ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
+                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                const float rho = sqrtf(dx * dx + dy * dy);
+                float cp = 1.0f, sp = 0.0f;
+                if (rho > 0.0f)
+                {
+                    cp = dx / rho;
+                    sp = dy / rho;
+                }
+                // z^m = e^{i m phi} and s^m by repeated products; Q_L^m = K_m s^m R_L^m
+                float zr = 1.0f, zi = 0.0f, sm = 1.0f;
+#pragma unroll
+                for (int m = 0; m <= L; ++m)
+                {
+                    if (m > 0)
+                    {
+                        const float nr = zr * cp - zi * sp;
+                        zi = zr * sp + zi * cp;
+                        zr = nr;
+                        sm *= st;
+                    }
+                    float r_prev = 0.0f, r_cur = 1.0f;
+                    if (L > m)
+                    {
+                        r_prev = r_cur;
+                        r_cur = sqrtf(2.0f * m + 3.0f) * ct * r_prev;
+                    }
+#pragma unroll
+                    for (int l = m + 2; l <= L; ++l)
+                    {
+                        const float r = c_a[l * (ST_MAX_L + 1) + m] * (ct * r_cur - c_b[l * (ST_MAX_L + 1) + m] * r_prev);
+                        r_prev = r_cur;
+                        r_cur = r;
+                    }
+                    const float pf = w * c_K[m] * sm;
+                    vals[2 * m] = r_cur * (pf * zr);
+                    vals[2 * m + 1] = r_cur * (pf * zi);
+                }
+                vals[NV - 1] = w;
+            }
+            // segmented inclusive scan keyed by particle slot (dead lanes get unique keys)
+            const int key = live ? k : 32 + lane;
+#pragma unroll
+            for (int dlt = 1; dlt < 32; dlt <<= 1)
+            {
+                const int kup = __shfl_up_sync(FULL, key, dlt);
+                const bool take = lane >= dlt && kup == key;
+#pragma unroll
+                for (int v = 0; v < NV; ++v)
+                {
+                    const float up = __shfl_up_sync(FULL, vals[v], dlt);
+                    if (take)
+                        vals[v] += up;
+                }
+            }
+            const int knext = __shfl_down_sync(FULL, key, 1);
+            if (live && (lane == 31 || knext != key))
+            {
+#pragma unroll
+                for (int v = 0; v < NV; ++v)
+                    acc[k][v] += vals[v];
+            }
+            __syncwarp();
+        }
+        if (static_cast<uint32_t>(lane) < np)
+        {
+            const uint32_t i = p0 + lane;
+            const float tw = acc[lane][NV - 1];
+            float2* row = qlm_out + ls.qlm_offset[0] + static_cast<size_t>(i) * (2 * L + 1);
+            float part = 0.0f;
+#pragma unroll
+            for (int m = 0; m <= L; ++m)
+            {
+                const float qr = acc[lane][2 * m] / tw;
+                const float qi = acc[lane][2 * m + 1] / tw;
+                row[m] = make_float2(qr, qi);
+                part += qr * qr + qi * qi;
+                if (m > 0)
+                {
+                    // Y_l^{-m} = (-1)^m conj(Y_l^m)
+                    const float sgn = (m & 1) ? -1.0f : 1.0f;
+                    const float nr = sgn * qr, ni = -sgn * qi;
+                    row[L + m] = make_float2(nr, ni);
+                    part += nr * nr + ni * ni;
+                }
+            }
+            ql_out[static_cast<size_t>(i) * ls.nl] = sqrtf(part * ls.norm[0]);
+        }
+        __syncwarp();
     }
 }
 
@@ -696,13 +873,51 @@ static int pair_lanes_for(int max_l)
     return used <= 4 ? 4 : (used <= 8 ? 8 : 16);
 }
 
+namespace {
+template<int L>
+void qlm_flat(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist, const float* weights,
+              const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted, float2* qlm, float* ql,
+              cudaStream_t s, const float4* bond_vd, uint32_t per_warp)
+{
+    const uint32_t per_block = 4 * per_warp;
+    uint32_t blocks = (n + per_block - 1) / per_block;
+    const uint32_t cap = static_cast<uint32_t>(sm_count()) * 16;
+    blocks = blocks < cap ? blocks : cap;
+    ProfScope prof_("k_qlm_flat", s);
+    k_qlm_flat<L><<<blocks, 128, 0, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, per_warp,
+                                         qlm, ql);
+}
+} // namespace
+
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
-                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd)
+                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd, double mean_bonds)
 {
     if (n == 0)
     {
         return;
+    }
+    if (ls.nl == 1 && ls.max_l <= 12)
+    {
+        // one l: bonds flat over the lanes, about three rounds of 32 per warp
+        const double mb = mean_bonds > 0.0 ? mean_bonds : 24.0;
+        const uint32_t per_warp = static_cast<uint32_t>(std::min(32.0, std::max(1.0, std::floor(96.0 / mb))));
+        switch (ls.max_l)
+        {
+        case 0: qlm_flat<0>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 1: qlm_flat<1>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 2: qlm_flat<2>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 3: qlm_flat<3>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 4: qlm_flat<4>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 5: qlm_flat<5>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 6: qlm_flat<6>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 7: qlm_flat<7>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 8: qlm_flat<8>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 9: qlm_flat<9>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 10: qlm_flat<10>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        case 11: qlm_flat<11>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        default: qlm_flat<12>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
+        }
     }
     const int nlt = ls.nl <= 1 ? 1 : (ls.nl <= 2 ? 2 : (ls.nl <= 5 ? 5 : ST_MAX_NL));
     // paired orders for one or two l values; with more, the doubled accumulators

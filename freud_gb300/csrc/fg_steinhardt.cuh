@@ -28,9 +28,10 @@ void st_upload_tables(cudaStream_t s);
 // bond_vd (optional, one float4 per bond): the bond vector box.wrap(p_j - p_i)
 // and the bond distance, precomputed per bond (batched frames, where the box
 // differs per particle); without it they come from pts, box and dist.
+// mean_bonds (optional): bonds per particle, sizes the single-l kernel's work per warp.
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
-                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd = nullptr);
+                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd = nullptr, double mean_bonds = 0.0);
 // bond_j (optional): the neighbour index of each bond, used instead of ij[e].y.
 void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
                 const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s, const uint32_t* bond_j = nullptr);
