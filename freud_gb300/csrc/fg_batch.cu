@@ -280,12 +280,57 @@ __global__ void __launch_bounds__(WARPS * 32)
                 {
                     const uint32_t nb = min(static_cast<uint32_t>(BT_QB), nqc - qb0);
                     __syncthreads();
+                    bool out_of_box = false;
                     for (uint32_t k = tid; k < nb; k += THREADS)
                     {
-                        S.q[k] = g.cpos[q0 + qb0 + k];
+                        const float4 qv = g.cpos[q0 + qb0 + k];
+                        S.q[k] = qv;
                         S.qi[k] = g.cidx[q0 + qb0 + k];
+                        out_of_box |= __float_as_int(qv.w) != 0;
                     }
-                    __syncthreads();
+                    // queries inside the box take a branch-free pair loop: invalid
+                    // candidates (image beyond +-1) are moved out of range instead
+                    const bool general = __syncthreads_or(out_of_box) != 0 || test_ii;
+                    if (!general)
+                    {
+                        for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
+                        {
+                            const uint32_t e = ch * 32 + lane;
+                            float4 pp = make_float4(3e30f, 3e30f, 3e30f, 0.f);
+                            float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (e < TT)
+                            {
+                                iv = S.iv[e];
+                                if (iv.w != 0.0f)
+                                    pp = S.pos[e];
+                            }
+#pragma unroll 4
+                            for (uint32_t qq = 0; qq < nb; ++qq)
+                            {
+                                const float4 q = S.q[qq];
+                                const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, iv.x));
+                                const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iv.y));
+                                const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iv.z));
+                                const float rsq = dot3(rx, ry, rz);
+                                if (rsq < p.r_max_sq && rsq >= p.r_min_sq)
+                                {
+                                    const float d = __fsqrt_rn(rsq);
+                                    if (!(d < h.h_min || d >= h.h_max))
+                                    {
+                                        uint32_t bin =
+                                            static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
+                                        if (bin == h.bins)
+                                            bin = h.bins - 1;
+                                        if (smem_hist)
+                                            atomicAdd(&my_hist[bin], 1u);
+                                        else
+                                            atomicAdd(&hist[bin], 1ull);
+                                    }
+                                }
+                            }
+                        }
+                        continue;
+                    }
                     for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
                     {
                         const uint32_t e = ch * 32 + lane;
