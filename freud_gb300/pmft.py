@@ -253,9 +253,12 @@ class PMFTXYZ(_PMFT):
         if reset:
             self._reset()
         nq, nlist, qargs, query_points, num_query_points = self._preprocess_arguments(system, query_points, neighbors)
-        if query_points is None:
-            query_points = nq.points
-        query_points = np.ascontiguousarray(query_points - self.shiftvec.reshape(1, 3), dtype=np.float32)
+        if query_points is not None or np.any(self.shiftvec != 0):
+            # query_points - shiftvec (freud/pmft.py:553); a zero shift of the
+            # system's own points leaves them as they are on the device
+            if query_points is None:
+                query_points = nq.points
+            query_points = np.ascontiguousarray(query_points - self.shiftvec.reshape(1, 3), dtype=np.float32)
         query_orientations = _convert_array(np.atleast_1d(query_orientations), shape=(num_query_points, 4))
         if equiv_orientations is None:
             equiv_orientations = np.array([[1, 0, 0, 0]], dtype=np.float32)
