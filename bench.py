@@ -534,6 +534,8 @@ def run_only(args):
     stream = torch.cuda.Stream()
     _lib.set_stream(stream.cuda_stream)
     torch.cuda.set_stream(stream)
+    if args.batch_config:
+        _lib.set_batch_config(*[int(x) for x in args.batch_config.split(",")])
     fns = {"plain_rdf": lambda: measure_c1(freud, _lib, args.steps, args.warmup, cpu=False),
            "steinhardt": lambda: measure_c3(freud, _lib, args.steps, args.warmup, cpu=False),
            "correlation_function": lambda: measure_cf(freud, _lib, args.steps, args.warmup, cpu=False),
@@ -560,6 +562,9 @@ def main():
                     help="run one of the other workloads alone and print its result (profiling)")
     ap.add_argument("--small", action="store_true",
                     help="with --only: the profiling-size case (8 frames; 512 blobs in L = 128)")
+    ap.add_argument("--batch-config", default=None,
+                    help="SHELL,WARPS,COPIES: fix the batched histogram's launch shape instead of autotuning "
+                         "(profiling: no trial launches)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
