@@ -502,14 +502,19 @@ __global__ void __launch_bounds__(128)
 // Per-frame system sums
 // ---------------------------------------------------------------------------
 
-// Rows [r0, r1) of one frame split, warp per column: each lane keeps an FP64
-// running sum over every 32nd row (at most FRAME_SYS_ROWS / 32 values, so the
-// rounding is far below the float32 inputs' own and the dependent FP64 chain is
-// short), then a fixed shuffle tree; lane 0 writes partial[f][split][col].
+// Rows [r0, r1) of one frame split. For each l, the (row, m) block of qlm is read
+// with consecutive threads on consecutive values (thread t: column t mod (2l+1),
+// row offset t div (2l+1), rows advancing by 256 div (2l+1)): coalesced loads. Each
+// thread keeps FP64 running sums (at most FRAME_SYS_ROWS / (256 div (2l+1)) values,
+// so the rounding is far below the float32 inputs' own); the threads of a column
+// are then added in a fixed order through shared memory and partial[f][split][col]
+// is written (the same order every run).
 __global__ void __launch_bounds__(256)
     k_frames_sys(const uint32_t* __restrict__ pt_base, StLs ls, int stride, int splits,
                  const float2* __restrict__ src, double* __restrict__ partial)
 {
+    __shared__ double s_re[256];
+    __shared__ double s_im[256];
     const uint32_t f = blockIdx.x;
     const uint32_t split = blockIdx.y;
     const uint32_t r_lo = pt_base[f];
@@ -517,37 +522,42 @@ __global__ void __launch_bounds__(256)
     const uint32_t per = (nf + splits - 1) / splits;
     const uint32_t r0 = r_lo + min(nf, split * per);
     const uint32_t r1 = r_lo + min(nf, (split + 1) * per);
-    const int lane = threadIdx.x & 31;
-    const int warps = blockDim.x >> 5;
-    for (int col = threadIdx.x >> 5; col < stride; col += warps)
+    const int t = threadIdx.x;
+    int col0 = 0;
+    for (int k = 0; k < ls.nl; ++k)
     {
-        // column -> (l index, m slot)
-        int k = 0, m = col;
-        while (k < ls.nl - 1 && m >= 2 * ls.l[k] + 1)
-        {
-            m -= 2 * ls.l[k] + 1;
-            ++k;
-        }
         const int nm = 2 * ls.l[k] + 1;
-        const float2* base = src + ls.qlm_offset[k] + m;
+        const int rows_per_pass = blockDim.x / nm;
+        const int m = t % nm;
+        const int rr = t / nm;
         double sr = 0.0, si = 0.0;
-        for (uint32_t r = r0 + lane; r < r1; r += 32)
+        if (rr < rows_per_pass)
         {
-            const float2 v = base[static_cast<size_t>(r) * nm];
-            sr += static_cast<double>(v.x);
-            si += static_cast<double>(v.y);
+            const float2* base = src + ls.qlm_offset[k];
+            for (uint32_t r = r0 + rr; r < r1; r += rows_per_pass)
+            {
+                const float2 v = base[static_cast<size_t>(r) * nm + m];
+                sr += static_cast<double>(v.x);
+                si += static_cast<double>(v.y);
+            }
         }
-        for (int o = 16; o > 0; o >>= 1)
+        s_re[t] = sr;
+        s_im[t] = si;
+        __syncthreads();
+        if (t < nm)
         {
-            sr += __shfl_xor_sync(0xffffffffu, sr, o);
-            si += __shfl_xor_sync(0xffffffffu, si, o);
+            double ar = 0.0, ai = 0.0;
+            for (int q = 0; q < rows_per_pass; ++q)
+            {
+                ar += s_re[q * nm + t];
+                ai += s_im[q * nm + t];
+            }
+            double* out = partial + ((static_cast<size_t>(f) * splits + split) * stride + col0 + t) * 2;
+            out[0] = ar;
+            out[1] = ai;
         }
-        if (lane == 0)
-        {
-            double* out = partial + ((static_cast<size_t>(f) * splits + split) * stride + col) * 2;
-            out[0] = sr;
-            out[1] = si;
-        }
+        __syncthreads();
+        col0 += nm;
     }
 }
 
