@@ -464,10 +464,11 @@ __global__ void __launch_bounds__(128)
             const uint32_t a = g.start[cell], b = g.start[cell + 1];
             for (uint32_t u = a; u < b; ++u)
             {
+                // both loads issued before the self-pair test
+                const float4 pp = g.cpos[u];
                 const uint32_t j = g.cidx[u];
                 if (p.exclude_ii && j == i)
                     continue;
-                const float4 pp = g.cpos[u];
                 const int pim = __float_as_int(pp.w);
                 const int kx = img_ax(pim, 0) - img_ax(qimg, 0) - wx;
                 const int ky = img_ax(pim, 1) - img_ax(qimg, 1) - wy;

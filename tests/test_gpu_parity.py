@@ -218,6 +218,21 @@ def test_dense_ball_nlist_wide_keys(freud):
     assert counts.sum() == len(nl) and counts.min() > 150
 
 
+def test_ball_nlist_wide_keys_sparse(freud):
+    """More than 2^22 points at low density: 64-bit merge keys at the 1,024-candidate
+    capacity. The first 3,000 queries' rows against the oracle."""
+    box, pts = random_box_points(freud, 172.0, 4400000, 16, (0.1, 0.0, 0.0))
+    nq = freud.locality.AABBQuery(box, pts)
+    nl = nq.query(pts, dict(r_max=1.3, exclude_ii=True)).toNeighborList()
+    m = 3000
+    ij, d, v = O.query(box, pts, query_points=pts[:m], r_max=1.3, exclude_ii=True)
+    nb = len(ij)
+    np.testing.assert_array_equal(nl[:nb], ij)
+    np.testing.assert_array_equal(nl.distances[:nb], d)
+    np.testing.assert_array_equal(nl.vectors[:nb], v)
+    assert nl[nb, 0] == m
+
+
 def test_points_outside_box(freud):
     box, pts = random_box_points(freud, 10.0, 800, 4)
     shifted = pts.copy()
