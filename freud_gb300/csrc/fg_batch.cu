@@ -105,6 +105,10 @@ struct HistShared
     int shell;
     uint32_t cell_base;
     uint32_t work;
+    uint32_t nkeep;             // candidates kept in the current tile
+    float qbox[8][6];           // per-warp bounds of the cell's queries (lo xyz, hi xyz)
+    float qfin[6];              // their union
+    int qout;                   // some query of the cell lies outside the box
     uint32_t hist[BT_HIST];
 };
 
@@ -207,6 +211,7 @@ __global__ void __launch_bounds__(WARPS * 32)
             S.hist[t] = 0;
     }
     int cur_frame = -1;
+    float cull2 = 0.0f;
     __syncthreads();
 
     for (;;)
@@ -244,37 +249,129 @@ __global__ void __launch_bounds__(WARPS * 32)
                     S.shell = F.shell;
                     S.cell_base = F.cell_base;
                 }
+                // candidate cull radius of this frame: r_max plus a margin bounding the
+                // difference between the shifted float distance and the exact one
+                const float lmax = fmaxf(fmaxf(F.b.L[0], F.b.L[1]), F.b.L[2]) *
+                    (1.0f + fabsf(F.b.xy) + fabsf(F.b.xz) + fabsf(F.b.yz));
+                const float rmax = sqrtf(p.r_max_sq);
+                const float ro = rmax + 2e-5f * (lmax + rmax) + 1e-6f;
+                cull2 = ro * ro * (1.0f + 1e-5f);
                 __syncthreads();
             }
             if (warp == 0)
                 frame_items(S, g.start, static_cast<int>(c - S.cell_base), S.it, lane);
-            __syncthreads();
+            {
+                // bounds of the cell's queries, for the candidate cull
+                float lo[3] = {3e30f, 3e30f, 3e30f}, hi[3] = {-3e30f, -3e30f, -3e30f};
+                bool out = false;
+                for (uint32_t k = tid; k < nqc; k += THREADS)
+                {
+                    const float4 qv = g.cpos[q0 + k];
+                    out |= __float_as_int(qv.w) != 0;
+                    lo[0] = fminf(lo[0], qv.x);
+                    lo[1] = fminf(lo[1], qv.y);
+                    lo[2] = fminf(lo[2], qv.z);
+                    hi[0] = fmaxf(hi[0], qv.x);
+                    hi[1] = fmaxf(hi[1], qv.y);
+                    hi[2] = fmaxf(hi[2], qv.z);
+                }
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                {
+                    for (int o = 16; o > 0; o >>= 1)
+                    {
+                        lo[a] = fminf(lo[a], __shfl_xor_sync(FULL, lo[a], o));
+                        hi[a] = fmaxf(hi[a], __shfl_xor_sync(FULL, hi[a], o));
+                    }
+                }
+                const bool wout = __any_sync(FULL, out);
+                if (lane == 0)
+                {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+                    {
+                        S.qbox[warp][a] = lo[a];
+                        S.qbox[warp][3 + a] = hi[a];
+                    }
+                }
+                if (__syncthreads_or(wout && lane == 0) != 0)
+                {
+                    if (tid == 0)
+                        S.qout = 1;
+                }
+                else if (tid == 0)
+                {
+                    S.qout = 0;
+                }
+                if (tid < 6)
+                {
+                    float v = S.qbox[0][tid];
+                    for (int w = 1; w < WARPS; ++w)
+                        v = tid < 3 ? fminf(v, S.qbox[w][tid]) : fmaxf(v, S.qbox[w][tid]);
+                    S.qfin[tid] = v;
+                }
+                __syncthreads();
+            }
+            // the cull needs every query in the box (image 0); otherwise all candidates stay
+            const bool cull = S.qout == 0 && !test_ii;
             const uint32_t T = S.it.off[BT_ITEMS];
             for (uint32_t t0 = 0; t0 < T; t0 += BT_TILE)
             {
-                const uint32_t TT = min(static_cast<uint32_t>(BT_TILE), T - t0);
-                for (uint32_t tl = tid; tl < TT; tl += THREADS)
+                const uint32_t TT0 = min(static_cast<uint32_t>(BT_TILE), T - t0);
+                if (tid == 0)
+                    S.nkeep = 0;
+                __syncthreads();
+                for (uint32_t base = 0; base < TT0; base += THREADS)
                 {
-                    const uint32_t t = t0 + tl;
-                    const int s = bitem_of(S.it, t);
-                    const uint32_t slot = S.it.start[s] + (t - S.it.off[s]);
-                    const float4 pp = g.cpos[slot];
-                    const int wr = S.it.wrap[s];
-                    const int pim = __float_as_int(pp.w);
-                    const int kx = img_ax(pim, 0) - (wr % 3 - 1);
-                    const int ky = img_ax(pim, 1) - ((wr / 3) % 3 - 1);
-                    const int kz = img_ax(pim, 2) - (wr / 9 - 1);
-                    float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1)
+                    const uint32_t tl = base + tid;
+                    bool keep = false;
+                    float4 pp = make_float4(0.f, 0.f, 0.f, 0.f), iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                    uint32_t slot = 0;
+                    int wr = 13;
+                    if (tl < TT0)
                     {
-                        const float* v = S.box.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
-                        iv = make_float4(v[0], v[1], v[2], 1.0f);
+                        const uint32_t t = t0 + tl;
+                        const int s = bitem_of(S.it, t);
+                        slot = S.it.start[s] + (t - S.it.off[s]);
+                        pp = g.cpos[slot];
+                        wr = S.it.wrap[s];
+                        const int pim = __float_as_int(pp.w);
+                        const int kx = img_ax(pim, 0) - (wr % 3 - 1);
+                        const int ky = img_ax(pim, 1) - ((wr / 3) % 3 - 1);
+                        const int kz = img_ax(pim, 2) - (wr / 9 - 1);
+                        if (kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1)
+                        {
+                            const float* v = S.box.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
+                            iv = make_float4(v[0], v[1], v[2], 1.0f);
+                        }
+                        keep = true;
+                        if (cull)
+                        {
+                            // farther than r_max (+ margin) from every query of the cell:
+                            // no pair with any of them (invalid images are dropped too)
+                            const float sx = pp.x - iv.x, sy = pp.y - iv.y, sz = pp.z - iv.z;
+                            const float gx = fmaxf(fmaxf(S.qfin[0] - sx, sx - S.qfin[3]), 0.f);
+                            const float gy = fmaxf(fmaxf(S.qfin[1] - sy, sy - S.qfin[4]), 0.f);
+                            const float gz = fmaxf(fmaxf(S.qfin[2] - sz, sz - S.qfin[5]), 0.f);
+                            keep = iv.w != 0.0f && gx * gx + gy * gy + gz * gz <= cull2;
+                        }
                     }
-                    S.pos[tl] = pp;
-                    S.iv[tl] = iv;
-                    S.j[tl] = g.cidx[slot];
-                    S.wr[tl] = static_cast<unsigned char>(wr);
+                    const unsigned km = __ballot_sync(FULL, keep);
+                    uint32_t wbase = 0;
+                    if (lane == 0 && km != 0)
+                        wbase = atomicAdd(&S.nkeep, static_cast<uint32_t>(__popc(km)));
+                    wbase = __shfl_sync(FULL, wbase, 0);
+                    if (keep)
+                    {
+                        const uint32_t idx = wbase + __popc(km & ((1u << lane) - 1u));
+                        S.pos[idx] = pp;
+                        S.iv[idx] = iv;
+                        S.j[idx] = g.cidx[slot];
+                        S.wr[idx] = static_cast<unsigned char>(wr);
+                    }
                 }
+                __syncthreads();
+                const uint32_t TT = S.nkeep;
                 const uint32_t nchunks = (TT + 31) / 32;
                 for (uint32_t qb0 = 0; qb0 < nqc; qb0 += BT_QB)
                 {
