@@ -110,6 +110,7 @@ SIGNATURES = {
     "fg_frames_create": [P, P, P, u32, PP],
     "fg_frames_create_device": [P, P, P, u32, PP],
     "fg_frames_set_points": [P, P],
+    "fg_frames_create_list": [P, P, P, u32, PP],
     "fg_frames_destroy": [P],
     "fg_frames_info": [P, pu32, pu64],
     "fg_rdf_accumulate_frames": [P, P, pargs],

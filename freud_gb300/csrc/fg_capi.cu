@@ -3210,6 +3210,30 @@ fg_status fg_frames_create(const fg_box* boxes, const float* points, const uint6
     });
 }
 
+fg_status fg_frames_create_list(const fg_box* boxes, const float* const* frame_points, const uint64_t* frame_offsets,
+                                uint32_t n_frames, fg_frames** out)
+{
+    return guard([&] {
+        require(out, "out");
+        require(frame_points, "frame_points");
+        std::unique_ptr<fg_frames> fr(new_frames(boxes, frame_offsets, n_frames));
+        fr->own.alloc(sizeof(float) * 3 * std::max<size_t>(fr->total, 1));
+        // one copy per frame straight into its slice: no host-side concatenation
+        for (uint32_t f = 0; f < n_frames; ++f)
+        {
+            const uint64_t nf = frame_offsets[f + 1] - frame_offsets[f];
+            if (nf == 0)
+                continue;
+            require(frame_points[f], "frame_points[f]");
+            FG_CUDA(cudaMemcpyAsync(fr->own.as<float>() + 3 * frame_offsets[f], frame_points[f],
+                                    sizeof(float) * 3 * nf, cudaMemcpyHostToDevice, stream()));
+        }
+        fr->dpts = fr->own.as<float>();
+        sync();
+        *out = fr.release();
+    });
+}
+
 fg_status fg_frames_create_device(const fg_box* boxes, const float* device_points, const uint64_t* frame_offsets,
                                   uint32_t n_frames, fg_frames** out)
 {

@@ -324,10 +324,13 @@ class FrameBatch:
         self._offsets = np.zeros(len(boxes) + 1, dtype=np.uint64)
         self._offsets[1:] = np.cumsum([len(p) for p in pts])
         self._boxes = (_lib.fg_box * len(boxes))(*boxes)
-        self._points = np.ascontiguousarray(np.concatenate(pts, axis=0), dtype=np.float32)
+        # each frame's float32 array goes to its slice of the device buffer (no
+        # host-side concatenation)
+        self._host_total = int(self._offsets[-1])
+        ptrs = (_lib.ctypes.c_void_p * len(pts))(*[p.ctypes.data for p in pts])
         h = _lib.ctypes.c_void_p()
-        _lib.check(_lib.lib.fg_frames_create(self._boxes, _lib.ptr(self._points), _lib.ptr(self._offsets),
-                                             len(boxes), _lib.ctypes.byref(h)))
+        _lib.check(_lib.lib.fg_frames_create_list(self._boxes, ptrs, _lib.ptr(self._offsets), len(boxes),
+                                                  _lib.ctypes.byref(h)))
         self._handle = _lib.Handle(h, _lib.lib.fg_frames_destroy)
 
     @classmethod
@@ -345,7 +348,7 @@ class FrameBatch:
             raise ValueError("a FrameBatch needs at least one frame")
         self._offsets = np.ascontiguousarray(offs)
         self._boxes = (_lib.fg_box * len(c_boxes))(*c_boxes)
-        self._points = None
+        self._host_total = None
         self._keepalive = keepalive
         h = _lib.ctypes.c_void_p()
         _lib.check(_lib.lib.fg_frames_create_device(self._boxes, _lib.ctypes.c_void_p(device_points_ptr),
@@ -375,11 +378,11 @@ class FrameBatch:
         return Box(b.Lx, b.Ly, b.Lz, b.xy, b.xz, b.yz, bool(b.is2D))
 
     def set_points(self, points):
-        """New positions (same frames and N) for a batch built from host points."""
+        """New positions (same frames and N, all frames concatenated) for a batch
+        built from host points."""
         pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
-        if self._points is None or pts.shape != self._points.shape:
+        if self._host_total is None or len(pts) != self._host_total:
             raise ValueError("set_points needs the same total number of points as the batch")
-        self._points = pts
         _lib.check(_lib.lib.fg_frames_set_points(self._h, _lib.ptr(pts)))
 
 

@@ -277,6 +277,10 @@ fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points
  * (AABBQuery.cc:93,125), as for a (box, points) system. */
 fg_status fg_frames_create(const fg_box* boxes, const float* points, const uint64_t* frame_offsets, uint32_t n_frames,
                            fg_frames** out);
+/* As fg_frames_create with one host array per frame (frame_points[f]: n_f x 3
+ * float32), copied straight into the batch's device buffer. */
+fg_status fg_frames_create_list(const fg_box* boxes, const float* const* frame_points, const uint64_t* frame_offsets,
+                                uint32_t n_frames, fg_frames** out);
 /* As fg_frames_create with the caller's device points (borrowed, not copied). */
 fg_status fg_frames_create_device(const fg_box* boxes, const float* device_points, const uint64_t* frame_offsets,
                                   uint32_t n_frames, fg_frames** out);
