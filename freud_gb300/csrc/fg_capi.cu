@@ -886,6 +886,8 @@ void knn_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a,
             runtime_error("The scale query argument must be greater than 1.");
     }
     const uint32_t k = a.num_neighbors;
+    if (k > knn_block_capacity() / 2)
+        runtime_error("num_neighbors above " + std::to_string(knn_block_capacity() / 2) + " is not supported");
     // cell width ~1.5x the expected k-th neighbour distance (or r_max when smaller)
     const double vol = box_volume(nq->box);
     const double per = vol / std::max<uint32_t>(nq->n, 1) * std::max<uint32_t>(k, 1);

@@ -66,6 +66,7 @@ struct Items
     uint32_t off[33];
     int wrap[32];
     uint32_t total;
+    uint32_t maxrun; // most points in one item's cell
 };
 
 // Shared memory of the scan kernels; arrays one mode does not use shrink to one
@@ -194,6 +195,7 @@ __device__ void cell_items(const DevBox& b, const DevGrid& g, int arith, int c, 
         if (lane >= o)
             incl += v;
     }
+    const uint32_t mx = __reduce_max_sync(FULL, cnt);
     it.start[lane] = st;
     it.off[lane] = incl - cnt;
     it.wrap[lane] = wr;
@@ -201,6 +203,7 @@ __device__ void cell_items(const DevBox& b, const DevGrid& g, int arith, int c, 
     {
         it.off[32] = incl;
         it.total = incl;
+        it.maxrun = mx;
     }
 }
 
@@ -331,7 +334,9 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? (CAP <= 1024 ? 5 
             cell_items(b, g, p.arith, c, S.it, lane);
         __syncthreads();
         uint32_t T = S.it.total;
-        if (MODE == SM_COUNT && T > CAP)
+        // the merge needs every run sorted by point index: cells above
+        // SORT_CELL_MAX points are not, so their stencils overflow too
+        if (MODE == SM_COUNT && (T > CAP || S.it.maxrun > static_cast<uint32_t>(SORT_CELL_MAX)))
         {
             for (uint32_t k = tid; k < nqc; k += STHREADS)
                 overflow[atomicAdd(overflow_n, 1u)] = q0 + k;

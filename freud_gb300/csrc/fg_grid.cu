@@ -337,7 +337,6 @@ void launch_segments_from_offsets(const uint32_t* counts, const uint64_t* offset
 // merge, whose candidate capacity they exceed). A home cell's candidate set is
 // then a union of runs already sorted by index.
 // ---------------------------------------------------------------------------
-constexpr int SORT_CELL_MAX = 1024;
 constexpr int SORT_WARPS = 4;
 
 // Reads the scatter-ordered (cpos_in, cidx_in) and writes every cell's points

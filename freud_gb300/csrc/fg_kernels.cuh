@@ -64,7 +64,9 @@ void launch_assign(const DevBox& box, const float* pts, uint32_t n, const int di
                    uint32_t* rank, uint32_t* cell_count, cudaStream_t s);
 void launch_scatter(const DevBox& box, const float* pts, uint32_t n, const uint32_t* cell_of,
                     const uint32_t* rank, const uint32_t* start, float4* cpos, uint32_t* cidx, cudaStream_t s);
-// Every cell's points sorted by point index (cells of up to 1024 points).
+// Every cell's points sorted by point index (cells of up to SORT_CELL_MAX points;
+// larger cells stay in scatter order).
+constexpr int SORT_CELL_MAX = 1024;
 void launch_sort_cells(const uint32_t* start, int ncell, const float4* cpos_in, const uint32_t* cidx_in,
                        float4* cpos_out, uint32_t* cidx_out, cudaStream_t s);
 
@@ -196,8 +198,8 @@ void launch_knn_warp(const DevBox& box, const DevGrid& g, const float4* qpos, co
                      uint32_t* fail_list, uint32_t* fail_count, cudaStream_t s);
 // Block-per-query brute force over every point (minimum over the 27 images in AABB
 // arithmetic), used for k > 32 and for queries the warp kernel could not prove.
-// list holds positions in the sorted query array. Needs the number of accepted
-// points per query <= knn_block_capacity() (else err = DEV_CAPACITY).
+// list holds positions in the sorted query array. Any number of points; needs
+// k <= knn_block_capacity() / 2 (else err = DEV_CAPACITY).
 void launch_knn_block(const DevBox& box, const float4* cpos, const uint32_t* cidx, uint32_t n, const float4* qpos,
                       const uint32_t* qidx, const KnnParams& p, const uint32_t* list, uint32_t nlist, uint32_t* tj,
                       float* td, float* tv, uint32_t* counts, int* err, cudaStream_t s);

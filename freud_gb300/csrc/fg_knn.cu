@@ -274,82 +274,10 @@ __global__ void __launch_bounds__(KWARPS * 32)
     }
 }
 
-// Brute force over all points for the listed queries (t indexes the sorted query array).
-__global__ void __launch_bounds__(256)
-    k_knn_block(DevBox b, const float4* __restrict__ cpos, const uint32_t* __restrict__ cidx, uint32_t n,
-                const float4* __restrict__ qpos, const uint32_t* __restrict__ qidx, KnnParams p,
-                const uint32_t* __restrict__ list, uint32_t* __restrict__ tj, float* __restrict__ td,
-                float* __restrict__ tv, uint32_t* __restrict__ counts, int* err)
+// Block-wide bitonic sort of key[0, m) with its payload (padded to a power of two
+// with the largest key).
+__device__ void block_sort_keys(unsigned long long* key, uint32_t* pay, uint32_t m)
 {
-    extern __shared__ unsigned char smem[];
-    unsigned long long* key = reinterpret_cast<unsigned long long*>(smem);
-    uint32_t* pay = reinterpret_cast<uint32_t*>(key + KB_CAP);
-    __shared__ float s_img[27][3];
-    __shared__ uint32_t s_n;
-    const int nimg = b.is2d ? 9 : 27;
-    for (int t = threadIdx.x; t < 81; t += blockDim.x)
-    {
-        s_img[t / 3][t % 3] = b.img[t / 3][t % 3];
-    }
-    if (threadIdx.x == 0)
-        s_n = 0;
-    __syncthreads();
-    const uint32_t t = list[blockIdx.x];
-    const float4 q = qpos[t];
-    const uint32_t qi = qidx[t];
-    for (uint32_t s = threadIdx.x; s < n; s += blockDim.x)
-    {
-        const uint32_t j = cidx[s];
-        if (p.exclude_ii && j == qi)
-            continue;
-        const float4 pj = cpos[s];
-        float best = __int_as_float(0x7f800000);
-        int bi = 0;
-        if (p.arith == ARITH_WRAP)
-        {
-            float rx, ry, rz;
-            box_wrap(b, __fsub_rn(pj.x, q.x), __fsub_rn(pj.y, q.y), __fsub_rn(pj.z, q.z), rx, ry, rz);
-            best = dot3(rx, ry, rz);
-        }
-        else
-        {
-            // reference image order: image 0 first, then (i, j, k) lexicographic
-            for (int m = 0; m < 27; ++m)
-            {
-                const int code = m == 0 ? 13 : (m <= 13 ? m - 1 : m);
-                const int kz = code % 3 - 1;
-                if (b.is2d && kz != 0)
-                    continue;
-                const float* iv = s_img[code];
-                const float rx = __fsub_rn(pj.x, __fadd_rn(q.x, iv[0]));
-                const float ry = __fsub_rn(pj.y, __fadd_rn(q.y, iv[1]));
-                const float rz = __fsub_rn(pj.z, __fadd_rn(q.z, iv[2]));
-                const float rs = dot3(rx, ry, rz);
-                if (rs < best)
-                {
-                    best = rs;
-                    bi = code;
-                }
-            }
-        }
-        (void) nimg;
-        if (!knn_accept(p, best))
-            continue;
-        const uint32_t e = atomicAdd(&s_n, 1u);
-        if (e < KB_CAP)
-        {
-            key[e] = (static_cast<unsigned long long>(__float_as_uint(best)) << 32) | j;
-            pay[e] = (s << 5) | static_cast<uint32_t>(bi);
-        }
-    }
-    __syncthreads();
-    const uint32_t m = s_n;
-    if (m > KB_CAP)
-    {
-        if (threadIdx.x == 0)
-            atomicExch(err, DEV_CAPACITY);
-        return;
-    }
     uint32_t np = 1;
     while (np < m)
         np <<= 1;
@@ -383,6 +311,110 @@ __global__ void __launch_bounds__(256)
             __syncthreads();
         }
     }
+}
+
+// Brute force over all points for the listed queries (t indexes the sorted query
+// array). Accepted points stream into a shared buffer of KB_CAP keys (distance,
+// index); when a round of blockDim points could overflow it, the buffer is sorted
+// and cut to the k best, whose k-th key then filters the rest: the exact k nearest
+// for any number of points (k <= KB_CAP / 2).
+__global__ void __launch_bounds__(256)
+    k_knn_block(DevBox b, const float4* __restrict__ cpos, const uint32_t* __restrict__ cidx, uint32_t n,
+                const float4* __restrict__ qpos, const uint32_t* __restrict__ qidx, KnnParams p,
+                const uint32_t* __restrict__ list, uint32_t* __restrict__ tj, float* __restrict__ td,
+                float* __restrict__ tv, uint32_t* __restrict__ counts, int* err)
+{
+    extern __shared__ unsigned char smem[];
+    unsigned long long* key = reinterpret_cast<unsigned long long*>(smem);
+    uint32_t* pay = reinterpret_cast<uint32_t*>(key + KB_CAP);
+    __shared__ float s_img[27][3];
+    __shared__ uint32_t s_n;
+    __shared__ unsigned long long s_thr;
+    for (int t = threadIdx.x; t < 81; t += blockDim.x)
+    {
+        s_img[t / 3][t % 3] = b.img[t / 3][t % 3];
+    }
+    if (threadIdx.x == 0)
+    {
+        s_n = 0;
+        s_thr = ~0ull;
+    }
+    __syncthreads();
+    if (p.k > static_cast<uint32_t>(KB_CAP / 2))
+    {
+        if (threadIdx.x == 0)
+            atomicExch(err, DEV_CAPACITY);
+        return;
+    }
+    const uint32_t t = list[blockIdx.x];
+    const float4 q = qpos[t];
+    const uint32_t qi = qidx[t];
+    for (uint32_t r0 = 0; r0 < n; r0 += blockDim.x)
+    {
+        __syncthreads(); // every thread has read the previous round's count
+        const uint32_t s = r0 + threadIdx.x;
+        const unsigned long long thr = s_thr;
+        if (s < n)
+        {
+            const uint32_t j = cidx[s];
+            if (!(p.exclude_ii && j == qi))
+            {
+                const float4 pj = cpos[s];
+                float best = __int_as_float(0x7f800000);
+                int bi = 0;
+                if (p.arith == ARITH_WRAP)
+                {
+                    float rx, ry, rz;
+                    box_wrap(b, __fsub_rn(pj.x, q.x), __fsub_rn(pj.y, q.y), __fsub_rn(pj.z, q.z), rx, ry, rz);
+                    best = dot3(rx, ry, rz);
+                }
+                else
+                {
+                    // reference image order: image 0 first, then (i, j, k) lexicographic
+                    for (int m = 0; m < 27; ++m)
+                    {
+                        const int code = m == 0 ? 13 : (m <= 13 ? m - 1 : m);
+                        const int kz = code % 3 - 1;
+                        if (b.is2d && kz != 0)
+                            continue;
+                        const float* iv = s_img[code];
+                        const float rx = __fsub_rn(pj.x, __fadd_rn(q.x, iv[0]));
+                        const float ry = __fsub_rn(pj.y, __fadd_rn(q.y, iv[1]));
+                        const float rz = __fsub_rn(pj.z, __fadd_rn(q.z, iv[2]));
+                        const float rs = dot3(rx, ry, rz);
+                        if (rs < best)
+                        {
+                            best = rs;
+                            bi = code;
+                        }
+                    }
+                }
+                const unsigned long long kk = (static_cast<unsigned long long>(__float_as_uint(best)) << 32) | j;
+                if (knn_accept(p, best) && kk < thr)
+                {
+                    const uint32_t e = atomicAdd(&s_n, 1u);
+                    key[e] = kk;
+                    pay[e] = (s << 5) | static_cast<uint32_t>(bi);
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t m = s_n;
+        if (m > static_cast<uint32_t>(KB_CAP) - blockDim.x)
+        {
+            block_sort_keys(key, pay, m);
+            if (threadIdx.x == 0)
+            {
+                const uint32_t kept = m < p.k ? m : p.k;
+                s_n = kept;
+                if (kept == p.k && kept > 0)
+                    s_thr = key[kept - 1];
+            }
+            __syncthreads();
+        }
+    }
+    const uint32_t m = s_n;
+    block_sort_keys(key, pay, m);
     const uint32_t found = m < p.k ? m : p.k;
     for (uint32_t e = threadIdx.x; e < found; e += blockDim.x)
     {

@@ -438,7 +438,63 @@ __global__ void __launch_bounds__(QWARPS * 32)
     }
 }
 
-// Block-per-query emit for queries with more than EMIT_CAP bonds (up to HEAVY_CAP).
+// Block-wide sort of one query's bonds in place in the output arrays by their
+// order key: a bitonic network in its all-ascending form (each merge opens by
+// comparing element e with its mirror in the block), which sorts any n when the
+// missing elements past n are taken as +infinity and their comparisons skipped.
+__device__ void block_sort_bonds(uint2* ij, float* dist, float* vec, uint32_t n, int by_distance)
+{
+    uint32_t np = 1;
+    while (np < n)
+    {
+        np <<= 1;
+    }
+    auto cswap = [&](uint32_t e, uint32_t pe) {
+        const uint2 a = ij[e], c = ij[pe];
+        const float da = dist[e], dc = dist[pe];
+        if (order_key(by_distance, a.y, da) > order_key(by_distance, c.y, dc))
+        {
+            ij[e] = c;
+            ij[pe] = a;
+            dist[e] = dc;
+            dist[pe] = da;
+            for (int x = 0; x < 3; ++x)
+            {
+                const float t = vec[3 * static_cast<size_t>(e) + x];
+                vec[3 * static_cast<size_t>(e) + x] = vec[3 * static_cast<size_t>(pe) + x];
+                vec[3 * static_cast<size_t>(pe) + x] = t;
+            }
+        }
+    };
+    for (uint32_t k = 2; k <= np; k <<= 1)
+    {
+        for (uint32_t e = threadIdx.x; e < n; e += blockDim.x)
+        {
+            const uint32_t pe = e ^ (k - 1);
+            if ((e & (k >> 1)) == 0 && pe < n)
+            {
+                cswap(e, pe);
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = k >> 2; j > 0; j >>= 1)
+        {
+            for (uint32_t e = threadIdx.x; e < n; e += blockDim.x)
+            {
+                const uint32_t pe = e ^ j;
+                if (pe > e && pe < n)
+                {
+                    cswap(e, pe);
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Block-per-query emit for queries with more than EMIT_CAP bonds: up to HEAVY_CAP
+// are staged and sorted in shared memory; a query with more writes its bonds
+// unsorted into its output rows and sorts them there.
 __global__ void __launch_bounds__(256)
     k_ball_emit_heavy(DevBox b, DevGrid g, const float4* __restrict__ qpos, const uint32_t* __restrict__ qidx,
                       BallParams p, const uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets,
@@ -464,14 +520,8 @@ __global__ void __launch_bounds__(256)
         s_found = 0;
     }
     __syncthreads();
-    if (n > HEAVY_CAP)
-    {
-        if (threadIdx.x == 0)
-        {
-            atomicExch(err, DEV_CAPACITY);
-        }
-        return;
-    }
+    const bool huge = n > HEAVY_CAP;
+    const uint64_t off = offsets[qi];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
@@ -495,9 +545,20 @@ __global__ void __launch_bounds__(256)
                 if (rsq < p.r_max_sq && rsq >= p.r_min_sq)
                 {
                     const uint32_t e = atomicAdd(&s_found, 1u);
-                    if (e < HEAVY_CAP)
+                    const float d = __fsqrt_rn(rsq);
+                    if (huge)
                     {
-                        const float d = __fsqrt_rn(rsq);
+                        if (e < n)
+                        {
+                            ij[off + e] = make_uint2(qi, j);
+                            dist[off + e] = d;
+                            vec[3 * (off + e)] = rx;
+                            vec[3 * (off + e) + 1] = ry;
+                            vec[3 * (off + e) + 2] = rz;
+                        }
+                    }
+                    else if (e < HEAVY_CAP)
+                    {
                         key[e] = order_key(by_distance, j, d);
                         val[e] = make_float4(rx, ry, rz, d);
                         slot[e] = static_cast<unsigned short>(e);
@@ -513,6 +574,11 @@ __global__ void __launch_bounds__(256)
         {
             atomicExch(err, DEV_CAPACITY);
         }
+        return;
+    }
+    if (huge)
+    {
+        block_sort_bonds(ij + off, dist + off, vec + 3 * off, n, by_distance);
         return;
     }
     int np = 1;
@@ -551,7 +617,6 @@ __global__ void __launch_bounds__(256)
             __syncthreads();
         }
     }
-    const uint64_t off = offsets[qi];
     for (int e = threadIdx.x; e < static_cast<int>(n); e += blockDim.x)
     {
         const unsigned long long k = key[e];

@@ -146,6 +146,22 @@ def test_knn_large_k_small_system(freud):
     assert_nlist_equal(nl, ij, d, v)
 
 
+@pytest.mark.parametrize("kind", [1, 2])
+def test_knn_large_k_many_points(freud, kind):
+    """k > 32 on 12,000 points: the block brute force streams more accepted points
+    than its 8,192-key buffer holds, cutting it to the k best as it fills."""
+    box, pts = random_box_points(freud, 24.0, 12000, 21, (0.1, 0.0, 0.05))
+    nq = make_nq(freud, kind, box, pts, 2.0)
+    for k, r_max in ((40, None), (300, None), (64, 5.0)):
+        args = dict(num_neighbors=k, exclude_ii=True)
+        oargs = dict(num_neighbors=k, exclude_ii=True, arith=ARITH[kind])
+        if r_max is not None:
+            args["r_max"] = oargs["r_max"] = r_max
+        nl = nq.query(pts, args).toNeighborList()
+        ij, d, v = O.query(box, pts, **oargs)
+        assert_nlist_equal(nl, ij, d, v)
+
+
 def test_rdf_fused_vs_oracle_medium(freud):
     box, pts = random_box_points(freud, 21.544, 10000, 5)
     rdf = freud.density.RDF(200, 4.0)
@@ -189,6 +205,38 @@ def test_dense_ball_nlist(freud, kind, tilt):
     _, qpts = random_box_points(freud, 21.544, 3000, 13, tilt)
     nl = nq.query(qpts, dict(r_max=4.0, r_min=0.7)).toNeighborList()
     ij, d, v = O.query(box, pts, query_points=qpts, r_max=4.0, r_min=0.7, arith=ARITH[kind])
+    assert_nlist_equal(nl, ij, d, v)
+
+
+def test_dense_ball_nlist_with_overflow_cluster(freud):
+    """Dense uniform points (4,096-candidate capacity) plus a tight cluster whose
+    stencils exceed even that: those cells go to the warp-per-query kernels."""
+    box, pts = random_box_points(freud, 21.544, 12000, 17)
+    rs = np.random.RandomState(18)
+    cluster = (rs.normal(0, 0.8, (3500, 3)) + np.array([2.0, -3.0, 1.0])).astype(np.float32)
+    pts = np.concatenate([pts, cluster]).astype(np.float32)
+    for kind in (0, 2):
+        nq = make_nq(freud, kind, box, pts, 4.0)
+        nl = nq.query(pts, dict(r_max=4.0, exclude_ii=True)).toNeighborList()
+        ij, d, v = O.query(box, pts, r_max=4.0, exclude_ii=True, arith=ARITH[kind])
+        assert nl.neighbor_counts.max() > 3000
+        assert_nlist_equal(nl, ij, d, v)
+
+
+@pytest.mark.parametrize("kind", [0, 2, 3])
+def test_ball_queries_beyond_shared_capacity(freud, kind):
+    """Query points inside a 12,000-point cluster: each has more bonds than the
+    8,192-bond shared-memory staging of the heavy-query kernel, so its bonds are
+    sorted in place in the output."""
+    box, pts = random_box_points(freud, 20.0, 3000, 31)
+    rs = np.random.RandomState(32)
+    cluster = (rs.normal(0, 0.5, (12000, 3)) + np.array([1.0, 2.0, -1.5])).astype(np.float32)
+    pts = np.concatenate([pts, cluster]).astype(np.float32)
+    qpts = np.concatenate([cluster[:6], pts[:4]]).astype(np.float32)
+    nq = make_nq(freud, kind, box, pts, 2.5)
+    nl = nq.query(qpts, dict(r_max=2.5)).toNeighborList()
+    ij, d, v = O.query(box, pts, query_points=qpts, r_max=2.5, arith=ARITH[kind])
+    assert nl.neighbor_counts.max() > 9000
     assert_nlist_equal(nl, ij, d, v)
 
 
