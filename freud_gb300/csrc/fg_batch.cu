@@ -600,13 +600,24 @@ __global__ void __launch_bounds__(128)
 // Per-frame system sums
 // ---------------------------------------------------------------------------
 
+// hi + lo += v with the rounding error of hi + v kept exactly (TwoSum).
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v)
+{
+    const float s = __fadd_rn(hi, v);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(v, bp));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
 // Rows [r0, r1) of one frame split. For each l, the (row, m) block of qlm is read
 // with consecutive threads on consecutive values (thread t: column t mod (2l+1),
 // row offset t div (2l+1), rows advancing by 256 div (2l+1)): coalesced loads. Each
-// thread keeps FP64 running sums (at most FRAME_SYS_ROWS / (256 div (2l+1)) values,
-// so the rounding is far below the float32 inputs' own); the threads of a column
-// are then added in a fixed order through shared memory and partial[f][split][col]
-// is written (the same order every run).
+// thread keeps float-float running sums (hi + lo, every addition an exact two-sum,
+// Knuth's TwoSum: about 48 significant bits, far below the float32 inputs' own
+// rounding, on the FP32 pipe instead of GB300's slow FP64 one); the threads of a
+// column are then added in FP64 in a fixed order through shared memory and
+// partial[f][split][col] is written (the same order every run).
 __global__ void __launch_bounds__(256)
     k_frames_sys(const uint32_t* __restrict__ pt_base, StLs ls, int stride, int splits,
                  const float2* __restrict__ src, double* __restrict__ partial)
@@ -628,19 +639,19 @@ __global__ void __launch_bounds__(256)
         const int rows_per_pass = blockDim.x / nm;
         const int m = t % nm;
         const int rr = t / nm;
-        double sr = 0.0, si = 0.0;
+        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
         if (rr < rows_per_pass)
         {
             const float2* base = src + ls.qlm_offset[k];
             for (uint32_t r = r0 + rr; r < r1; r += rows_per_pass)
             {
                 const float2 v = base[static_cast<size_t>(r) * nm + m];
-                sr += static_cast<double>(v.x);
-                si += static_cast<double>(v.y);
+                two_sum_acc(hr, lr, v.x);
+                two_sum_acc(hi, li, v.y);
             }
         }
-        s_re[t] = sr;
-        s_im[t] = si;
+        s_re[t] = static_cast<double>(hr) + static_cast<double>(lr);
+        s_im[t] = static_cast<double>(hi) + static_cast<double>(li);
         __syncthreads();
         if (t < nm)
         {
@@ -659,8 +670,9 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Block per frame, warp per column: the split sums reduced by lanes (every 32nd
-// split) and a fixed shuffle tree (the same order every run), divided by n_f.
+// Blocks of 8 columns per frame, warp per column: the split sums reduced by lanes
+// (every 32nd split) and a fixed shuffle tree (the same order every run), divided
+// by n_f.
 __global__ void __launch_bounds__(256)
     k_frames_sys_final(const uint32_t* __restrict__ pt_base, int stride, int splits,
                        const double* __restrict__ partial, double* __restrict__ sys)
@@ -669,7 +681,7 @@ __global__ void __launch_bounds__(256)
     const int lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;
     const double nf = static_cast<double>(pt_base[f + 1] - pt_base[f]);
-    for (int col = threadIdx.x >> 5; col < stride; col += warps)
+    for (int col = blockIdx.y * warps + (threadIdx.x >> 5); col < stride; col += warps * gridDim.y)
     {
         double sr = 0.0, si = 0.0;
         for (int k = lane; k < splits; k += 32)
@@ -820,7 +832,7 @@ void launch_frames_sys(const uint32_t* pt_base, uint32_t nframes, uint32_t max_r
     }
     {
         ProfScope prof_("k_frames_sys_final", s);
-        k_frames_sys_final<<<nframes, 256, 0, s>>>(pt_base, stride, splits, partial, sys);
+        k_frames_sys_final<<<dim3(nframes, (stride + 7) / 8), 256, 0, s>>>(pt_base, stride, splits, partial, sys);
     }
 }
 

@@ -75,9 +75,9 @@ void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n
 
 // Per-frame FP64 system sums of the per-l (n, 2l + 1) qlm layout: sys[f][col]
 // (complex, col running over every l's m) = (FP64 sum over the frame's rows) /
-// n_f: FP64 running sums over runs of at most FRAME_SYS_ROWS rows (a warp per
-// column, fixed shuffle trees), then a fixed tree over the runs, so results do
-// not depend on scheduling. max_rows is the
+// n_f: float-float (exact TwoSum) running sums over runs of at most FRAME_SYS_ROWS
+// rows, FP64 from there on (fixed shuffle trees, then a fixed tree over the runs),
+// so results do not depend on scheduling. max_rows is the
 // largest frame; partial holds nframes * frames_sys_splits(max_rows) * stride * 2
 // doubles.
 constexpr uint32_t FRAME_SYS_ROWS = 512;
