@@ -21,6 +21,11 @@
 #include "fg_batch.cuh"
 #include "fg_prof.cuh"
 
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
 namespace fg {
 
 namespace {
@@ -30,6 +35,7 @@ constexpr int BT_TILE = 1024;   // staged candidates per tile
 constexpr int BT_QB = 64;       // queries per shared-memory batch
 constexpr int BT_ITEMS = 96;    // stencil items: up to 32 rows x 3 x-segments
 constexpr int BT_HIST = 2048;   // shared histogram words (all copies)
+constexpr int BT_RB_WORDS = 1792; // exact r^2 -> bin table (thresholds + keys)
 constexpr int BT_CHUNK_MAX = 4; // cells per work-counter pop (fewer for small grids)
 
 // Largest f with base[f] <= x (base[0] = 0 <= x < base[nframes]).
@@ -110,6 +116,7 @@ struct HistShared
     float qfin[6];              // their union
     int qout;                   // some query of the cell lies outside the box
     uint32_t hist[BT_HIST];
+    uint32_t rb[BT_RB_WORDS];   // HistParams::rb, when given
 };
 
 // Stencil items of local cell c (run by one warp): lane = one (dy, dz) row of
@@ -210,6 +217,16 @@ __global__ void __launch_bounds__(WARPS * 32)
         for (uint32_t t = tid; t < h.bins * COPIES; t += THREADS)
             S.hist[t] = 0;
     }
+    // exact r^2 -> bin table: bin = key's first bin + (r^2 >= the next two
+    // thresholds); no square root or float-to-int conversion per pair
+    const bool rbins = h.rb != nullptr;
+    if (rbins)
+    {
+        for (uint32_t t = tid; t < h.rb_words; t += THREADS)
+            S.rb[t] = h.rb[t];
+    }
+    const float* rb_thr = reinterpret_cast<const float*>(S.rb);
+    const unsigned short* rb_key = reinterpret_cast<const unsigned short*>(S.rb + h.bins + 2);
     int cur_frame = -1;
     float cull2 = 0.0f;
     __syncthreads();
@@ -388,6 +405,44 @@ __global__ void __launch_bounds__(WARPS * 32)
                     // queries inside the box take a branch-free pair loop: invalid
                     // candidates (image beyond +-1) are moved out of range instead
                     const bool general = __syncthreads_or(out_of_box) != 0 || test_ii;
+                    if (!general && rbins)
+                    {
+                        for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
+                        {
+                            const uint32_t e = ch * 32 + lane;
+                            float4 pp = make_float4(3e30f, 3e30f, 3e30f, 0.f);
+                            float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (e < TT)
+                            {
+                                iv = S.iv[e];
+                                if (iv.w != 0.0f)
+                                    pp = S.pos[e];
+                            }
+#pragma unroll 4
+                            for (uint32_t qq = 0; qq < nb; ++qq)
+                            {
+                                const float4 q = S.q[qq];
+                                const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, iv.x));
+                                const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iv.y));
+                                const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iv.z));
+                                const float rsq = dot3(rx, ry, rz);
+                                const bool ok = rsq >= h.rb_a && rsq < h.rb_b;
+                                const uint32_t u = __float_as_uint(rsq);
+                                const uint32_t key = (ok && u >= h.rb_ut) ? ((u - h.rb_ut) >> h.rb_s) + 1u : 0u;
+                                const uint32_t b0 = rb_key[key];
+                                const uint32_t bin = b0 + (rsq >= rb_thr[b0 + 1] ? 1u : 0u) +
+                                    (rsq >= rb_thr[b0 + 2] ? 1u : 0u);
+                                if (ok)
+                                {
+                                    if (smem_hist)
+                                        atomicAdd(&my_hist[bin], 1u);
+                                    else
+                                        atomicAdd(&hist[bin], 1ull);
+                                }
+                            }
+                        }
+                        continue;
+                    }
                     if (!general)
                     {
                         for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
@@ -834,6 +889,196 @@ void launch_frames_sys(const uint32_t* pt_base, uint32_t nframes, uint32_t max_r
         ProfScope prof_("k_frames_sys_final", s);
         k_frames_sys_final<<<dim3(nframes, (stride + 7) / 8), 256, 0, s>>>(pt_base, stride, splits, partial, sys);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Exact r^2 -> bin tables
+//
+// A pair is counted into bin F(r^2): the pair test r_min^2 <= r^2 < r_max^2, then
+// d = sqrt(r^2) (correctly rounded) and the regular-axis bin of d
+// (Histogram.h:327-351). Every step is monotone in r^2, and so in the bits u of
+// the non-negative float r^2: the counted pairs are an interval [uA, uB) of bit
+// patterns, on which F is non-decreasing. So F is fixed by its thresholds
+// T[b] = min{u : F(u) >= b}, found here by bisection over float bit patterns with
+// the same float operations the kernels use. The kernel finds F(u) from a key
+// table: key 0 covers [uA, T[b0 + 1]) (b0 = F(uA)); key k > 0 covers a run of
+// 2^s bit patterns from there, stores F at the run's start, and each run holds at
+// most two thresholds (checked here for every run), so F(u) = key value + [u >=
+// T[v + 1]] + [u >= T[v + 2]].
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t INF_BITS = 0x7f800000u;
+
+int host_pair_bin(uint32_t u, const HistParams& h, float r_min_sq, float r_max_sq)
+{
+    float rsq;
+    std::memcpy(&rsq, &u, sizeof(float));
+    if (!(rsq < r_max_sq && rsq >= r_min_sq))
+        return -1;
+    const float d = std::sqrt(rsq);
+    if (d < h.h_min || d >= h.h_max)
+        return -1;
+    uint32_t bin = static_cast<uint32_t>(fmul(fsub(d, h.h_min), h.h_inv));
+    if (bin == h.bins)
+        bin = h.bins - 1;
+    return static_cast<int>(bin);
+}
+
+// smallest u in [lo, hi) with pred(u), else hi; pred is false then true
+template<typename P> uint32_t first_true(uint32_t lo, uint32_t hi, P pred)
+{
+    while (lo < hi)
+    {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (pred(mid))
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+struct RbEntry
+{
+    uint32_t id[6];
+    HistParams h;
+};
+
+std::mutex g_rb_mutex;
+std::vector<RbEntry> g_rb_cache;
+constexpr size_t RB_CACHE_MAX = 256;
+
+float bits_float(uint32_t u)
+{
+    float f;
+    std::memcpy(&f, &u, sizeof(float));
+    return f;
+}
+
+uint32_t float_bits(float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, sizeof(float));
+    return u;
+}
+
+// false when the table does not fit BT_RB_WORDS
+bool build_rsq_bins(const HistParams& h, float r_min_sq, float r_max_sq, std::vector<uint32_t>& words,
+                    HistParams& out)
+{
+    const uint32_t bins = h.bins;
+    if (bins == 0 || bins + 3 > static_cast<uint32_t>(BT_RB_WORDS))
+        return false;
+    auto F = [&](uint32_t u) { return host_pair_bin(u, h, r_min_sq, r_max_sq); };
+    const uint32_t ua = first_true(0u, INF_BITS + 1, [&](uint32_t u) {
+        const float r = bits_float(u);
+        return r >= r_min_sq && std::sqrt(r) >= h.h_min;
+    });
+    const uint32_t ub = first_true(0u, INF_BITS + 1, [&](uint32_t u) {
+        const float r = bits_float(u);
+        return r >= r_max_sq || std::sqrt(r) >= h.h_max;
+    });
+    std::vector<uint32_t> thr(bins + 2, INF_BITS);
+    std::vector<uint16_t> keys(1, 0);
+    uint32_t ut = ub, shift = 31;
+    if (ua >= ub)
+    {
+        // nothing is counted: r^2 >= 0 and r^2 < 0 never both hold
+        out.rb_a = 0.0f;
+        out.rb_b = 0.0f;
+    }
+    else
+    {
+        if (bins > 65535)
+            return false;
+        thr[0] = ua;
+        for (uint32_t b = 1; b < bins; ++b)
+            thr[b] = first_true(ua, ub, [&](uint32_t u) { return F(u) >= static_cast<int>(b); });
+        const int b0 = F(ua);
+        keys[0] = static_cast<uint16_t>(b0);
+        ut = static_cast<uint32_t>(b0) + 1 < bins ? thr[b0 + 1] : ub;
+        if (ut < ub)
+        {
+            bool done = false;
+            for (int s = 31; s >= 0 && !done; --s)
+            {
+                const uint64_t nkeys = (static_cast<uint64_t>(ub - 1 - ut) >> s) + 2;
+                if (bins + 2 + (nkeys + 1) / 2 > static_cast<uint64_t>(BT_RB_WORDS))
+                    return false;
+                keys.assign(nkeys, 0);
+                keys[0] = static_cast<uint16_t>(b0);
+                bool ok = true;
+                for (uint64_t k = 1; k < nkeys && ok; ++k)
+                {
+                    const uint64_t start = ut + ((k - 1) << s);
+                    const uint64_t end = std::min<uint64_t>(ut + (k << s), ub) - 1;
+                    const int fs = F(static_cast<uint32_t>(start));
+                    const int fe = F(static_cast<uint32_t>(end));
+                    ok = fs >= 0 && fe >= fs && fe <= fs + 2;
+                    keys[k] = static_cast<uint16_t>(fs);
+                }
+                if (ok)
+                {
+                    shift = static_cast<uint32_t>(s);
+                    done = true;
+                }
+            }
+            if (!done)
+                return false;
+        }
+        out.rb_a = bits_float(ua);
+        out.rb_b = bits_float(ub);
+    }
+    words.assign(bins + 2 + (keys.size() + 1) / 2, 0u);
+    std::memcpy(words.data(), thr.data(), sizeof(uint32_t) * thr.size());
+    std::memcpy(words.data() + bins + 2, keys.data(), sizeof(uint16_t) * keys.size());
+    out.rb_ut = ut;
+    out.rb_s = shift;
+    out.rb_words = static_cast<uint32_t>(words.size());
+    return true;
+}
+
+} // namespace
+
+HistParams with_rsq_bins(const HistParams& h, float r_min_sq, float r_max_sq)
+{
+    const uint32_t id[6] = {float_bits(h.h_min), float_bits(h.h_max), float_bits(h.h_inv), h.bins,
+                            float_bits(r_min_sq), float_bits(r_max_sq)};
+    std::lock_guard<std::mutex> lock(g_rb_mutex);
+    for (const RbEntry& e : g_rb_cache)
+    {
+        if (std::memcmp(e.id, id, sizeof(id)) == 0)
+            return e.h;
+    }
+    HistParams out = h;
+    out.rb = nullptr;
+    if (g_rb_cache.size() >= RB_CACHE_MAX)
+        return out;
+    std::vector<uint32_t> words;
+    HistParams t = h;
+    if (build_rsq_bins(h, r_min_sq, r_max_sq, words, t))
+    {
+        void* d = nullptr;
+        if (cudaMalloc(&d, sizeof(uint32_t) * words.size()) == cudaSuccess &&
+            cudaMemcpy(d, words.data(), sizeof(uint32_t) * words.size(), cudaMemcpyHostToDevice) == cudaSuccess)
+        {
+            t.rb = static_cast<const uint32_t*>(d);
+            out = t;
+        }
+        else
+        {
+            if (d != nullptr)
+                cudaFree(d);
+            cudaGetLastError();
+            return out; // not cached: tried again next call
+        }
+    }
+    RbEntry e;
+    std::memcpy(e.id, id, sizeof(id));
+    e.h = out;
+    g_rb_cache.push_back(e);
+    return out;
 }
 
 } // namespace fg

@@ -62,6 +62,12 @@ void launch_frames_scatter(uint32_t n, const uint32_t* cell_of, const uint32_t* 
 // blocks pull runs of cells from a device work counter (*queue, zeroed before
 // the launch) until cell_limit. hist is uint64[h.bins].
 size_t frames_hist_smem_bytes();
+
+// h with its exact r^2 -> bin table filled in (the pair test r_min_sq <= r^2 <
+// r_max_sq folded in), or h unchanged when the table does not fit the kernel's
+// shared memory. Tables are built once per parameter set and kept for the life of
+// the process, so graphs may hold their pointers; call outside stream capture.
+HistParams with_rsq_bins(const HistParams& h, float r_min_sq, float r_max_sq);
 void launch_frames_hist(const BatchHistConfig& cfg, const BatchGrid& g, const BallParams& p, const HistParams& h,
                         uint32_t cell_limit, uint32_t* queue, unsigned long long* hist, cudaStream_t s);
 

@@ -3285,13 +3285,13 @@ static void rdf_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_args& a)
 {
     {
         cudaStream_t s = stream();
-        const HistParams h = hist_params(rdf);
         BallParams p;
         p.r_max_sq = fmul(a.r_max, a.r_max);
         p.r_min_sq = fmul(a.r_min, a.r_min);
         p.exclude_ii = a.exclude_ii;
         p.arith = ARITH_AABB;
         p.nq = fr->total;
+        const HistParams h = with_rsq_bins(hist_params(rdf), p.r_min_sq, p.r_max_sq);
         if (fr->queue.bytes < sizeof(uint32_t))
             fr->queue.alloc(sizeof(uint32_t));
         const BatchHistConfig cfg = tuned_config(fr, p, h, a.r_max);

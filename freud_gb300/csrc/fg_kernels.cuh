@@ -107,6 +107,13 @@ struct HistParams
 {
     float h_min, h_max, h_inv;
     uint32_t bins;
+    // optional exact r^2 -> bin table (frames histogram kernel): device words
+    // [thresholds: bins + 2 floats][keys: u16], pairs counted iff rb_a <= r^2 < rb_b
+    const uint32_t* rb = nullptr;
+    uint32_t rb_words = 0;
+    uint32_t rb_ut = 0; // bits of the first threshold above the first bin
+    uint32_t rb_s = 0;  // key shift
+    float rb_a = 0.0f, rb_b = 0.0f;
 };
 void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, const uint32_t* qidx,
                       const BallParams& p, const HistParams& h, unsigned long long* hist, cudaStream_t s,

@@ -330,6 +330,24 @@ def test_dense_blob_histogram(freud):
     np.testing.assert_array_equal(rdf2.bin_counts_u64, O.hist(d, 120, 3.0))
 
 
+@pytest.mark.parametrize("bins,r_max,r_min", [(200, 4.0, 0.0), (16, 4.0, 0.0), (500, 5.0, 0.0), (75, 3.75, 1.0),
+                                              (1, 4.0, 0.0), (1000, 2.0, 0.5), (1500, 4.0, 0.0)])
+def test_rdf_lattice_distances_on_bin_edges(freud, bins, r_max, r_min):
+    """Simple-cubic lattice of spacing 0.5: every pair distance is the root of an
+    integer multiple of 1/4, so many land exactly on bin edges (and on r_max): the
+    r^2 -> bin tables must bin them as sqrt then truncation does. 1,500 bins
+    exceed the table's capacity (square-root path)."""
+    n = 22
+    g = (np.arange(n, dtype=np.float32) - n / 2) * np.float32(0.5)
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    box = freud.box.Box.cube(n * 0.5)
+    rdf = freud.density.RDF(bins, r_max, r_min).compute((box, pts), neighbors={"r_max": r_max, "r_min": r_min,
+                                                                               "exclude_ii": True})
+    c = O.rdf_counts_query(box, pts, bins, r_max, r_min)
+    np.testing.assert_array_equal(rdf.bin_counts_u64, c)
+    assert c.sum() > 0
+
+
 def test_empty_result(freud):
     box, pts = random_box_points(freud, 10.0, 100, 1)
     nq = freud.locality.AABBQuery(box, pts)
