@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 namespace fg {
@@ -418,28 +419,37 @@ __global__ void __launch_bounds__(WARPS * 32)
                                 if (iv.w != 0.0f)
                                     pp = S.pos[e];
                             }
+                            // image 0 for the whole chunk: q + 0 is q (up to the sign of a
+                            // zero, which r^2 does not see), so the three additions go
+                            auto sweep = [&](auto zero_image) {
+                                constexpr bool Z = decltype(zero_image)::value;
 #pragma unroll 4
-                            for (uint32_t qq = 0; qq < nb; ++qq)
-                            {
-                                const float4 q = S.q[qq];
-                                const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, iv.x));
-                                const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iv.y));
-                                const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iv.z));
-                                const float rsq = dot3(rx, ry, rz);
-                                const bool ok = rsq >= h.rb_a && rsq < h.rb_b;
-                                const uint32_t u = __float_as_uint(rsq);
-                                const uint32_t key = (ok && u >= h.rb_ut) ? ((u - h.rb_ut) >> h.rb_s) + 1u : 0u;
-                                const uint32_t b0 = rb_key[key];
-                                const uint32_t bin = b0 + (rsq >= rb_thr[b0 + 1] ? 1u : 0u) +
-                                    (rsq >= rb_thr[b0 + 2] ? 1u : 0u);
-                                if (ok)
+                                for (uint32_t qq = 0; qq < nb; ++qq)
                                 {
-                                    if (smem_hist)
-                                        atomicAdd(&my_hist[bin], 1u);
-                                    else
-                                        atomicAdd(&hist[bin], 1ull);
+                                    const float4 q = S.q[qq];
+                                    const float rx = __fsub_rn(pp.x, Z ? q.x : __fadd_rn(q.x, iv.x));
+                                    const float ry = __fsub_rn(pp.y, Z ? q.y : __fadd_rn(q.y, iv.y));
+                                    const float rz = __fsub_rn(pp.z, Z ? q.z : __fadd_rn(q.z, iv.z));
+                                    const float rsq = dot3(rx, ry, rz);
+                                    const bool ok = rsq >= h.rb_a && rsq < h.rb_b;
+                                    const uint32_t u = __float_as_uint(rsq);
+                                    const uint32_t key = (ok && u >= h.rb_ut) ? ((u - h.rb_ut) >> h.rb_s) + 1u : 0u;
+                                    const uint32_t b0 = rb_key[key];
+                                    const uint32_t bin = b0 + (rsq >= rb_thr[b0 + 1] ? 1u : 0u) +
+                                        (rsq >= rb_thr[b0 + 2] ? 1u : 0u);
+                                    if (ok)
+                                    {
+                                        if (smem_hist)
+                                            atomicAdd(&my_hist[bin], 1u);
+                                        else
+                                            atomicAdd(&hist[bin], 1ull);
+                                    }
                                 }
-                            }
+                            };
+                            if (__all_sync(FULL, iv.x == 0.0f && iv.y == 0.0f && iv.z == 0.0f))
+                                sweep(std::true_type {});
+                            else
+                                sweep(std::false_type {});
                         }
                         continue;
                     }
