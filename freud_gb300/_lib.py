@@ -119,6 +119,7 @@ SIGNATURES = {
     "fg_batch_set_config": [i32, i32, i32],
     "fg_autotune_report": [ctypes.c_char_p, ctypes.c_size_t],
     "fg_set_graphs": [i32],
+    "fg_check_division": [u64, u64, pu64, P],
 }
 _RESTYPES = {"fg_last_error": ctypes.c_char_p, "fg_version": ctypes.c_int}
 

@@ -15,12 +15,14 @@
 // (AABBQuery.cc:93,125) and binning (Histogram.h:327-351) into privatised
 // shared histograms, flushed once per block with 64-bit atomics.
 //
-// Steinhardt neighbours: thread per query over the 27-cell stencil, count then
-// fill; the bonds of a frame batch feed the existing qlm / average / wl kernels
-// over the concatenated rows, and the system sums are taken per frame.
+// Steinhardt neighbours: warp per cell over the 27-cell stencil (staged in
+// shared memory, lanes over candidates), count then fill; the bonds of a frame
+// batch feed the existing qlm / average / wl kernels over the concatenated
+// rows, and the system sums are taken per frame.
 #include "fg_batch.cuh"
 #include "fg_prof.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -590,75 +592,285 @@ __global__ void __launch_bounds__(WARPS * 32)
 }
 
 // ---------------------------------------------------------------------------
-// Steinhardt neighbours (thread per query, 27-cell stencil of r_max cells)
+// Steinhardt neighbours (warp per cell, 27-cell stencil of r_max cells)
 // ---------------------------------------------------------------------------
+//
+// A warp takes one home cell at a time (cells strided over the resident warps,
+// ascending, so a warp meets each frame once). Its queries are the cell's own
+// points, handled in groups of at most 32; for each group the stencil's
+// candidates - item s in 0..26 (x fastest), slots in cell order: the fixed
+// order in which each query's bonds are written and later summed - are staged in
+// shared memory FB_TILE at a time, with the image vector that a query inside the
+// box needs already resolved. For each query of the group the lanes test 32
+// candidates per round (AABBQuery.cc:93,125 arithmetic); bonds keep candidate
+// order. The count pass adds ballots; the fill pass appends each accepted bond
+// (output row, p_j - q, r^2, j) to a per-warp queue that is drained 32 entries at
+// a time, so the exact box.wrap of Steinhardt.cc:155 (three IEEE divisions) runs
+// on full warps.
+
+constexpr int FB_WARPS = 4;
+constexpr int FB_THREADS = FB_WARPS * 32;
+constexpr int FB_TILE = 128;  // staged candidates per warp
+constexpr int FB_QUEUE = 64;  // bond queue entries per warp (drained at 32)
+constexpr int FB_K0_OK = 1 << 24; // staged image resolved (query in the box)
+
+struct FBWarp
+{
+    float4 pos[FB_TILE];      // x, y, z, point index (bits)
+    float4 img[FB_TILE];      // image vector for a query in the box; w = packed n_j - wrap | FB_K0_OK
+    float4 q[32];             // the group's queries (w = packed box image)
+    uint32_t qi[32];
+    unsigned long long qe[FB_QUEUE];  // fill: output row of a queued bond
+    float4 qv[FB_QUEUE];              // fill: p_j - q (x, y, z), r^2
+    uint32_t qj[FB_QUEUE];            // fill: neighbour index
+    uint32_t it_off[28];      // stencil item offsets (prefix of counts)
+    uint32_t it_start[27];    // first slot of the item's cell
+    int it_wrap[27];          // (wx + 1) + 3 (wy + 1) + 9 (wz + 1)
+};
 
 template<bool FILL>
-__global__ void __launch_bounds__(128)
-    k_frames_ball(BatchGrid g, BallParams p, uint32_t n, uint32_t* __restrict__ counts,
-                  const uint64_t* __restrict__ offsets, uint32_t* __restrict__ bj, float4* __restrict__ bvd)
+__global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 8)
+    k_frames_ball(BatchGrid g, BallParams p, uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets,
+                  uint32_t* __restrict__ bj, float4* __restrict__ bvd)
 {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    __shared__ FBWarp sw[FB_WARPS];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    FBWarp& W = sw[warp];
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t nwarps = gridDim.x * FB_WARPS;
+    uint32_t c = blockIdx.x * FB_WARPS + warp;
+    if (c >= g.ncell)
+        return;
+    uint32_t f = frame_of(g.cell_base, g.nframes, c);
+    uint32_t qn = 0; // queued bonds (fill)
+
+    // drain the first n queued bonds: exact box.wrap of p_j - q in frame f
+    auto drain = [&](uint32_t n) {
+        if (lane < static_cast<int>(n))
+        {
+            const DevBox& B = g.fd[f].b;
+            const unsigned long long e = W.qe[lane];
+            const float4 v = W.qv[lane];
+            float wx, wy, wz;
+            box_wrap(B, v.x, v.y, v.z, wx, wy, wz);
+            bj[e] = W.qj[lane];
+            bvd[e] = make_float4(wx, wy, wz, __fsqrt_rn(v.w));
+        }
+        __syncwarp();
+    };
+
+    for (; c < g.ncell; c += nwarps)
     {
-        const float4 q = g.cpos[t];
-        const uint32_t i = g.cidx[t];
-        const uint32_t c = g.cell_of[i];
-        const FrameDesc& F = g.fd[frame_of(g.cell_base, g.nframes, c)];
+        const uint32_t q0 = g.start[c];
+        const uint32_t nqc = g.start[c + 1] - q0;
+        if (nqc == 0)
+            continue;
+        if (c >= g.cell_base[f + 1])
+        {
+            if (FILL && qn > 0)
+            {
+                drain(qn);
+                qn = 0;
+            }
+            while (c >= g.cell_base[f + 1])
+                ++f;
+        }
+        const FrameDesc& F = g.fd[f];
         const int d0 = F.dim[0], d1 = F.dim[1], d2 = F.dim[2];
         const int lc = static_cast<int>(c - F.cell_base);
         const int cz = lc / (d0 * d1);
         const int cy = (lc / d0) % d1;
         const int cx = lc % d0;
-        const int qimg = __float_as_int(q.w);
         const int nst = F.b.is2d ? 9 : 27;
-        uint32_t cnt = 0;
-        const uint64_t o = FILL ? offsets[i] : 0;
-        for (int s = 0; s < nst; ++s)
+        // stencil items (lane s < nst), same enumeration as the reference order restated above
         {
-            const int ux = cx + s % 3 - 1;
-            const int uy = cy + (s / 3) % 3 - 1;
-            const int uz = cz + (F.b.is2d ? 0 : s / 9 - 1);
-            const int wx = ux < 0 ? -1 : (ux >= d0 ? 1 : 0);
-            const int wy = uy < 0 ? -1 : (uy >= d1 ? 1 : 0);
-            const int wz = uz < 0 ? -1 : (uz >= d2 ? 1 : 0);
-            const uint32_t cell =
-                F.cell_base + static_cast<uint32_t>((ux - wx * d0) + d0 * ((uy - wy * d1) + d1 * (uz - wz * d2)));
-            const uint32_t a = g.start[cell], b = g.start[cell + 1];
-            for (uint32_t u = a; u < b; ++u)
+            uint32_t cnt = 0, st = 0;
+            int wr = 13;
+            if (lane < nst)
             {
-                // both loads issued before the self-pair test
-                const float4 pp = g.cpos[u];
-                const uint32_t j = g.cidx[u];
-                if (p.exclude_ii && j == i)
-                    continue;
-                const int pim = __float_as_int(pp.w);
-                const int kx = img_ax(pim, 0) - img_ax(qimg, 0) - wx;
-                const int ky = img_ax(pim, 1) - img_ax(qimg, 1) - wy;
-                const int kz = img_ax(pim, 2) - img_ax(qimg, 2) - wz;
-                if (kx < -1 || kx > 1 || ky < -1 || ky > 1 || kz < -1 || kz > 1)
-                    continue;
-                const float* v = F.b.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
-                const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, v[0]));
-                const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, v[1]));
-                const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, v[2]));
-                const float rsq = dot3(rx, ry, rz);
-                if (rsq < p.r_max_sq && rsq >= p.r_min_sq)
+                const int ux = cx + lane % 3 - 1;
+                const int uy = cy + (lane / 3) % 3 - 1;
+                const int uz = cz + (F.b.is2d ? 0 : lane / 9 - 1);
+                const int wx = ux < 0 ? -1 : (ux >= d0 ? 1 : 0);
+                const int wy = uy < 0 ? -1 : (uy >= d1 ? 1 : 0);
+                const int wz = uz < 0 ? -1 : (uz >= d2 ? 1 : 0);
+                const uint32_t cell = F.cell_base +
+                                      static_cast<uint32_t>((ux - wx * d0) + d0 * ((uy - wy * d1) + d1 * (uz - wz * d2)));
+                st = g.start[cell];
+                cnt = g.start[cell + 1] - st;
+                wr = (wx + 1) + 3 * (wy + 1) + 9 * (wz + 1);
+            }
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o)
+                    incl += v;
+            }
+            if (lane < 27)
+            {
+                W.it_off[lane] = incl - cnt;
+                W.it_start[lane] = st;
+                W.it_wrap[lane] = wr;
+            }
+            if (lane == 26)
+                W.it_off[27] = incl;
+        }
+        __syncwarp();
+        const uint32_t T = W.it_off[27];
+        const uint32_t ntile = (T + FB_TILE - 1) / FB_TILE;
+
+        for (uint32_t g0 = 0; g0 < nqc; g0 += 32)
+        {
+            const uint32_t ng = min(32u, nqc - g0);
+            uint32_t my_cnt = 0;          // bonds so far of query g0 + lane
+            uint64_t my_off = 0;
+            if (lane < static_cast<int>(ng))
+            {
+                const uint32_t i = g.cidx[q0 + g0 + lane];
+                W.q[lane] = g.cpos[q0 + g0 + lane];
+                W.qi[lane] = i;
+                if (FILL)
+                    my_off = offsets[i];
+            }
+            for (uint32_t tile = 0; tile < ntile; ++tile)
+            {
+                const uint32_t t0 = tile * FB_TILE;
+                const uint32_t TT = min(static_cast<uint32_t>(FB_TILE), T - t0);
+                // stage candidates [t0, t0 + TT) unless this tile is already staged
+                if (ntile > 1 || g0 == 0)
                 {
-                    if (FILL)
+                    __syncwarp();
+                    for (uint32_t tl = lane; tl < TT; tl += 32)
                     {
-                        const uint64_t e = o + cnt;
-                        float dx, dy, dz;
-                        box_wrap(F.b, __fsub_rn(pp.x, q.x), __fsub_rn(pp.y, q.y), __fsub_rn(pp.z, q.z), dx, dy, dz);
-                        bj[e] = j;
-                        bvd[e] = make_float4(dx, dy, dz, __fsqrt_rn(rsq));
+                        const uint32_t t = t0 + tl;
+                        int s = 0;
+#pragma unroll
+                        for (int step = 16; step >= 1; step >>= 1)
+                        {
+                            if (s + step < 27 && W.it_off[s + step] <= t)
+                                s += step;
+                        }
+                        const uint32_t slot = W.it_start[s] + (t - W.it_off[s]);
+                        const float4 pp = g.cpos[slot];
+                        const uint32_t j = g.cidx[slot];
+                        const int wr = W.it_wrap[s];
+                        const int pim = __float_as_int(pp.w);
+                        const int kx = img_ax(pim, 0) - (wr % 3 - 1);
+                        const int ky = img_ax(pim, 1) - ((wr / 3) % 3 - 1);
+                        const int kz = img_ax(pim, 2) - (wr / 9 - 1);
+                        int k0 = pack_image(kx, ky, kz);
+                        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1)
+                        {
+                            const float* iv = F.b.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
+                            v.x = iv[0];
+                            v.y = iv[1];
+                            v.z = iv[2];
+                            k0 |= FB_K0_OK;
+                        }
+                        v.w = __int_as_float(k0);
+                        W.pos[tl] = make_float4(pp.x, pp.y, pp.z, __uint_as_float(j));
+                        W.img[tl] = v;
                     }
-                    ++cnt;
+                    __syncwarp();
+                }
+                for (uint32_t k = 0; k < ng; ++k)
+                {
+                    const float4 q = W.q[k];
+                    const uint32_t qi = W.qi[k];
+                    const int qimg = __float_as_int(q.w);
+                    uint32_t base = __shfl_sync(FULL, my_cnt, k);
+                    const uint64_t off = FILL ? __shfl_sync(FULL, my_off, k) : 0;
+                    for (uint32_t r0 = 0; r0 < TT; r0 += 32)
+                    {
+                        const uint32_t tl = r0 + lane;
+                        bool acc = false;
+                        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+                        float rsq = 0.f;
+                        if (tl < TT)
+                        {
+                            a = W.pos[tl];
+                            const float4 v = W.img[tl];
+                            const int k0 = __float_as_int(v.w);
+                            float ix = v.x, iy = v.y, iz = v.z;
+                            bool ok = (k0 & FB_K0_OK) != 0;
+                            if (qimg != 0)
+                            {
+                                // query outside the box: image k = n_j - n_q - wrap
+                                const int kx = img_ax(k0, 0) - img_ax(qimg, 0);
+                                const int ky = img_ax(k0, 1) - img_ax(qimg, 1);
+                                const int kz = img_ax(k0, 2) - img_ax(qimg, 2);
+                                ok = kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1;
+                                if (ok)
+                                {
+                                    const float* iv = F.b.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
+                                    ix = iv[0];
+                                    iy = iv[1];
+                                    iz = iv[2];
+                                }
+                            }
+                            if (ok && !(p.exclude_ii && __float_as_uint(a.w) == qi))
+                            {
+                                const float rx = __fsub_rn(a.x, __fadd_rn(q.x, ix));
+                                const float ry = __fsub_rn(a.y, __fadd_rn(q.y, iy));
+                                const float rz = __fsub_rn(a.z, __fadd_rn(q.z, iz));
+                                rsq = dot3(rx, ry, rz);
+                                acc = rsq < p.r_max_sq && rsq >= p.r_min_sq;
+                            }
+                        }
+                        const unsigned bal = __ballot_sync(FULL, acc);
+                        if (FILL && bal != 0)
+                        {
+                            if (acc)
+                            {
+                                const uint32_t slot = qn + __popc(bal & lt);
+                                W.qe[slot] = off + base + __popc(bal & lt);
+                                W.qv[slot] = make_float4(__fsub_rn(a.x, q.x), __fsub_rn(a.y, q.y),
+                                                         __fsub_rn(a.z, q.z), rsq);
+                                W.qj[slot] = __float_as_uint(a.w);
+                            }
+                            qn += __popc(bal);
+                            __syncwarp();
+                            if (qn >= 32)
+                            {
+                                drain(32);
+                                const uint32_t rest = qn - 32;
+                                unsigned long long e = 0;
+                                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                                uint32_t j = 0;
+                                if (lane < static_cast<int>(rest))
+                                {
+                                    e = W.qe[32 + lane];
+                                    v = W.qv[32 + lane];
+                                    j = W.qj[32 + lane];
+                                }
+                                __syncwarp();
+                                if (lane < static_cast<int>(rest))
+                                {
+                                    W.qe[lane] = e;
+                                    W.qv[lane] = v;
+                                    W.qj[lane] = j;
+                                }
+                                __syncwarp();
+                                qn = rest;
+                            }
+                        }
+                        base += __popc(bal);
+                    }
+                    if (lane == static_cast<int>(k))
+                        my_cnt = base;
                 }
             }
+            if (!FILL && lane < static_cast<int>(ng))
+                counts[W.qi[lane]] = my_cnt;
+            __syncwarp();
         }
-        if (!FILL)
-            counts[i] = cnt;
     }
+    if (FILL && qn > 0)
+        drain(qn);
 }
 
 // ---------------------------------------------------------------------------
@@ -862,21 +1074,34 @@ void launch_frames_hist(const BatchHistConfig& cfg, const BatchGrid& g, const Ba
     }
 }
 
+namespace {
+// one wave of resident blocks, or fewer when the grid has few cells
+template<typename K> uint32_t frames_ball_blocks(K kernel, uint32_t ncell)
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, FB_THREADS, 0);
+    const uint32_t want = static_cast<uint32_t>(sms()) * static_cast<uint32_t>(std::max(per_sm, 1));
+    return std::max(1u, std::min<uint32_t>(want, (ncell + FB_WARPS - 1) / FB_WARPS));
+}
+} // namespace
+
 void launch_frames_ball_count(const BatchGrid& g, const BallParams& p, uint32_t n, uint32_t* counts, cudaStream_t s)
 {
-    if (n == 0)
+    if (n == 0 || g.ncell == 0)
         return;
+    const uint32_t blocks = frames_ball_blocks(k_frames_ball<false>, g.ncell);
     ProfScope prof_("k_frames_ball<COUNT>", s);
-    k_frames_ball<false><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, counts, nullptr, nullptr, nullptr);
+    k_frames_ball<false><<<blocks, FB_THREADS, 0, s>>>(g, p, counts, nullptr, nullptr, nullptr);
 }
 
 void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n, const uint64_t* offsets,
                              uint32_t* bond_j, float4* bond_vd, cudaStream_t s)
 {
-    if (n == 0)
+    if (n == 0 || g.ncell == 0)
         return;
+    const uint32_t blocks = frames_ball_blocks(k_frames_ball<true>, g.ncell);
     ProfScope prof_("k_frames_ball<FILL>", s);
-    k_frames_ball<true><<<grid_blocks(n, 128), 128, 0, s>>>(g, p, n, nullptr, offsets, bond_j, bond_vd);
+    k_frames_ball<true><<<blocks, FB_THREADS, 0, s>>>(g, p, nullptr, offsets, bond_j, bond_vd);
 }
 
 int frames_sys_splits(uint32_t max_rows)

@@ -71,7 +71,7 @@ HistParams with_rsq_bins(const HistParams& h, float r_min_sq, float r_max_sq);
 void launch_frames_hist(const BatchHistConfig& cfg, const BatchGrid& g, const BallParams& p, const HistParams& h,
                         uint32_t cell_limit, uint32_t* queue, unsigned long long* hist, cudaStream_t s);
 
-// Ball query over every frame (grid of r_max cells, shell 1), thread per query.
+// Ball query over every frame (grid of r_max cells, shell 1), warp per cell.
 // Count pass: counts[i] = bonds of point i. Fill pass: bonds of point i at
 // offsets[i] in candidate order: the neighbour index j and one float4 holding the
 // Steinhardt bond vector box.wrap(p_j - p_i) (Steinhardt.cc:155) and the distance.

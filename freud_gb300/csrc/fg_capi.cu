@@ -264,6 +264,9 @@ static DevBox make_devbox(const HostBox& h)
     d.xz = h.xz;
     d.yz = h.yz;
     d.is2d = h.is2d ? 1 : 0;
+    for (int a = 0; a < 3; ++a)
+        d.rcp[a] = h.L[a] != 0.0f ? fdiv(1.0f, h.L[a]) : 0.0f;
+    d.tilted = (h.xy != 0.0f || h.xz != 0.0f || h.yz != 0.0f) ? 1 : 0;
     const float a1[3] = {h.L[0], 0.0f, 0.0f};
     const float a2[3] = {fmul(h.L[1], h.xy), h.L[1], 0.0f};
     float a3[3] = {0.0f, 0.0f, 0.0f};
@@ -3471,6 +3474,82 @@ fg_status fg_batch_set_config(int shell, int warps_per_block, int hist_copies)
             (hist_copies != 1 && hist_copies != 2))
             value_error("batch config: shell 1 or 2, 4 or 8 warps per block, 1 or 2 histogram copies");
         g_forced = BatchHistConfig {shell, warps_per_block, hist_copies};
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Self-check of the box arithmetic's division (div_rn_recip) against IEEE division
+// ---------------------------------------------------------------------------
+namespace {
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+// Sample t: a divisor b (every other sample one of a few box lengths, else a
+// random float in [2^-3, 2^13)) and a dividend a of either sign (random
+// significand, exponent in [-10, 14)); counts quotients that differ in any bit
+// from __fdiv_rn and keeps one offending pair.
+__global__ void k_check_div(uint64_t n, uint64_t seed, unsigned long long* mism, float* example)
+{
+    const float lens[8] = {102.0f, 21.544f, 63.496f, 12.0f, 256.0f, 1.5874f, 3.0f, 7.0f};
+    for (uint64_t t = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; t < n;
+         t += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const uint64_t h = mix64(seed + t * 0x9e3779b97f4a7c15ull);
+        float b;
+        if (t & 1)
+            b = lens[(h >> 40) & 7];
+        else
+            b = __uint_as_float(static_cast<uint32_t>(((124 + ((h >> 50) % 16)) << 23) | ((h >> 24) & 0x7fffff)));
+        const uint32_t ea = 117 + static_cast<uint32_t>((h >> 10) % 24);
+        const uint32_t sa = static_cast<uint32_t>(h & 1) << 31;
+        const float a = __uint_as_float(sa | (ea << 23) | static_cast<uint32_t>((h >> 33) & 0x7fffff));
+        const float q = div_rn_recip(a, b, __frcp_rn(b));
+        const float r = __fdiv_rn(a, b);
+        if (__float_as_uint(q) != __float_as_uint(r))
+        {
+            if (atomicAdd(mism, 1ull) == 0ull)
+            {
+                example[0] = a;
+                example[1] = b;
+            }
+        }
+    }
+}
+} // namespace
+
+fg_status fg_check_division(uint64_t samples, uint64_t seed, uint64_t* mismatches, float* example)
+{
+    return guard([&] {
+        require(mismatches, "mismatches");
+        DevBuf buf;
+        buf.alloc(sizeof(unsigned long long) + 2 * sizeof(float));
+        cudaStream_t s = stream();
+        FG_CUDA(cudaMemsetAsync(buf.p, 0, buf.bytes, s));
+        auto* m = buf.as<unsigned long long>();
+        auto* ex = reinterpret_cast<float*>(m + 1);
+        if (samples > 0)
+        {
+            int dev = 0, sms = 152;
+            FG_CUDA(cudaGetDevice(&dev));
+            FG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            k_check_div<<<sms * 8, 256, 0, s>>>(samples, seed, m, ex);
+            FG_CUDA(cudaGetLastError());
+        }
+        unsigned long long hm = 0;
+        float hex[2] = {0.0f, 0.0f};
+        FG_CUDA(cudaMemcpyAsync(&hm, m, sizeof(hm), cudaMemcpyDeviceToHost, s));
+        FG_CUDA(cudaMemcpyAsync(hex, ex, sizeof(hex), cudaMemcpyDeviceToHost, s));
+        sync();
+        *mismatches = hm;
+        if (example != nullptr)
+        {
+            example[0] = hex[0];
+            example[1] = hex[1];
+        }
     });
 }
 

@@ -23,6 +23,8 @@ struct DevBox
     float xy, xz, yz;
     int is2d;
     float img[27][3]; // reference image vectors, index (kx+1)*9 + (ky+1)*3 + (kz+1)
+    float rcp[3];     // RN(1 / L) per axis (0 where L = 0), for div_rn_recip
+    int tilted;       // nonzero when any of xy, xz, yz is nonzero
 };
 
 __host__ __device__ inline float fadd(float a, float b)
@@ -75,36 +77,63 @@ __device__ __forceinline__ float fmod1(float a)
     return __fsub_rn(a, truncf(a));
 }
 
+// a / b rounded to nearest even, given y = RN(1 / b), for a / b normal or zero
+// (the box arithmetic divides coordinates by box lengths: no overflow or
+// underflow). q0 = RN(a y) is within 1.5 ulp of a / b; one correction
+// q1 = RN(q0 + (a - b q0) y) (fused, so the residual enters unrounded) brings it
+// within one ulp; from a q1 within one ulp and y = RN(1 / b), Markstein's theorem
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of
+// Floating-Point Arithmetic, the theorem on correcting a quotient with the exact
+// FMA remainder) makes q1 + (a - b q1) y, rounded once, the correctly rounded
+// quotient. a = +-0 returns q0, which carries the sign of the exact quotient.
+__device__ __forceinline__ float div_rn_recip(float a, float b, float y)
+{
+    const float q0 = __fmul_rn(a, y);
+    const float q1 = __fmaf_rn(__fmaf_rn(-q0, b, a), y, q0);
+    const float q2 = __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
+    return a == 0.0f ? q0 : q2;
+}
+
 // util::modulusPositive(a, 1.0f) = fmod(fmod(a, 1) + 1, 1), utils.h:29-32
 __device__ __forceinline__ float mod_pos1(float a)
 {
     return fmod1(__fadd_rn(fmod1(a), 1.0f));
 }
 
-// Box::makeFractional, Box.h:243-255
+// Box::makeFractional, Box.h:243-255. In a box without tilt the tilt terms are
+// +-0 and subtracting them changes nothing (for finite v): dx = v - lo is never
+// -0 because lo != 0, so they are skipped there. Divisions by the box lengths are
+// correctly rounded (div_rn_recip), so the quotients equal IEEE division's.
 __device__ __forceinline__ void make_fractional(const DevBox& b, float vx, float vy, float vz, float& fx,
                                                 float& fy, float& fz)
 {
     float dx = __fsub_rn(vx, b.lo[0]);
     float dy = __fsub_rn(vy, b.lo[1]);
     float dz = __fsub_rn(vz, b.lo[2]);
-    const float t2 = __fsub_rn(b.xz, __fmul_rn(b.yz, b.xy));
-    dx = __fsub_rn(dx, __fadd_rn(__fmul_rn(t2, vz), __fmul_rn(b.xy, vy)));
-    dy = __fsub_rn(dy, __fmul_rn(b.yz, vz));
-    fx = __fdiv_rn(dx, b.L[0]);
-    fy = __fdiv_rn(dy, b.L[1]);
-    fz = b.is2d ? 0.0f : __fdiv_rn(dz, b.L[2]);
+    if (b.tilted)
+    {
+        const float t2 = __fsub_rn(b.xz, __fmul_rn(b.yz, b.xy));
+        dx = __fsub_rn(dx, __fadd_rn(__fmul_rn(t2, vz), __fmul_rn(b.xy, vy)));
+        dy = __fsub_rn(dy, __fmul_rn(b.yz, vz));
+    }
+    fx = div_rn_recip(dx, b.L[0], b.rcp[0]);
+    fy = div_rn_recip(dy, b.L[1], b.rcp[1]);
+    fz = b.is2d ? 0.0f : div_rn_recip(dz, b.L[2], b.rcp[2]);
 }
 
-// Box::makeAbsolute, Box.h:212-222
+// Box::makeAbsolute, Box.h:212-222 (tilt terms skipped in a box without tilt:
+// x + (+-0) = x for finite x, and x = lo + f L is never -0)
 __device__ __forceinline__ void make_absolute(const DevBox& b, float fx, float fy, float fz, float& x, float& y,
                                               float& z)
 {
     x = __fadd_rn(b.lo[0], __fmul_rn(fx, b.L[0]));
     y = __fadd_rn(b.lo[1], __fmul_rn(fy, b.L[1]));
     z = __fadd_rn(b.lo[2], __fmul_rn(fz, b.L[2]));
-    x = __fadd_rn(x, __fadd_rn(__fmul_rn(b.xy, y), __fmul_rn(b.xz, z)));
-    y = __fadd_rn(y, __fmul_rn(b.yz, z));
+    if (b.tilted)
+    {
+        x = __fadd_rn(x, __fadd_rn(__fmul_rn(b.xy, y), __fmul_rn(b.xz, z)));
+        y = __fadd_rn(y, __fmul_rn(b.yz, z));
+    }
     if (b.is2d)
     {
         z = 0.0f;

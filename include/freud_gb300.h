@@ -309,6 +309,15 @@ fg_status fg_autotune_report(char* buf, size_t len);
  * default) or launch it directly (0). */
 fg_status fg_set_graphs(int enable);
 
+/* Self-check of the device division that the box arithmetic uses (no counterpart
+ * in the reference, whose Box::makeFractional, Box.h:243-255, divides with the
+ * host's IEEE division): the quotients of `samples` seeded (a, b) pairs (box
+ * lengths and random divisors, dividends of either sign) computed from a
+ * precomputed reciprocal are compared bit for bit with CUDA's IEEE division;
+ * *mismatches receives the number that differ and example (optional, 2 floats)
+ * one differing (a, b). Synchronous. */
+fg_status fg_check_division(uint64_t samples, uint64_t seed, uint64_t* mismatches, float* example);
+
 #ifdef __cplusplus
 }
 #endif

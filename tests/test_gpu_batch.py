@@ -210,3 +210,39 @@ def test_rdf_states_of_frame_ranges_combine(freud):
     np.testing.assert_array_equal(merged.bin_counts_u64, whole.bin_counts_u64)
     np.testing.assert_array_equal(merged.rdf, whole.rdf)
     np.testing.assert_array_equal(merged.n_r, whole.n_r)
+
+
+def _clustered_frame(freud, seed, L=12.0, blobs=3, per_blob=300, sigma=0.35, background=500):
+    """Dense Gaussian clusters (cells of well over 32 points, stencils of several
+    hundred candidates) over a uniform background; 60 points moved up to 0.5
+    outside the box (queries and candidates with a nonzero box image)."""
+    rs = np.random.RandomState(seed)
+    box = freud.box.Box.cube(L)
+    centres = rs.uniform(-L / 2 + 1.5, L / 2 - 1.5, (blobs, 3))
+    pts = np.concatenate([c + rs.normal(0, sigma, (per_blob, 3)) for c in centres]
+                         + [rs.uniform(-L / 2, L / 2, (background, 3))])
+    pts[-30:, 0] = rs.uniform(L / 2, L / 2 + 0.5, 30)
+    pts[-60:-30, 1] = rs.uniform(-L / 2 - 0.5, -L / 2, 30)
+    return box, pts.astype(np.float32)
+
+
+@pytest.mark.parametrize("average", [False, True])
+def test_steinhardt_ball_dense_cells_points_outside(freud, average):
+    """Steinhardt l = 4, 6 on AABB ball neighbours (r_max 1.2) of clustered points,
+    some outside the box, as one (box, points) call and inside a FrameBatch with a
+    uniform frame: Ql within 1e-5 relative of the FP64 oracle per frame."""
+    dense = _clustered_frame(freud, 71)
+    uni = make_frames(freud, [1500], 72, tilt_every=1, unwrapped=True)[0]
+    ls = [4, 6]
+    one = freud.order.Steinhardt(ls, average=average).compute(dense, neighbors={"r_max": 1.2})
+    st = freud.order.Steinhardt(ls, average=average)
+    st.compute(freud.locality.FrameBatch([uni, dense]), neighbors={"r_max": 1.2})
+    ql_b = np.asarray(st.ql).reshape(-1, 2)
+    for ql, (box, pts) in ((np.asarray(one.ql).reshape(-1, 2), dense), (ql_b[:len(uni[1])], uni),
+                           (ql_b[len(uni[1]):], dense)):
+        ij, d, v = O.query(box, pts, r_max=1.2, exclude_ii=True, arith=O.ARITH_AABB)
+        o = O.steinhardt(ls, box, pts, ij, d, average=average)
+        qref = o["ql_ave"] if average else o["ql"]
+        ok = np.isfinite(qref)
+        assert np.array_equal(ok, np.isfinite(ql))
+        np.testing.assert_allclose(ql[ok], qref[ok], rtol=1e-5, atol=1e-7)

@@ -438,3 +438,18 @@ def test_cellquery_errors(freud):
         nq.query(pts, dict(r_max=5.5)).toNeighborList()
     with pytest.raises(ValueError, match="r_max must be greater than r_min"):
         nq.query(pts, dict(r_max=1.0, r_min=2.0)).toNeighborList()
+
+
+def test_box_division_matches_ieee(freud):
+    """The box arithmetic divides by box lengths through a precomputed reciprocal
+    with a Markstein correction; 2^30 seeded quotients (box lengths and random
+    divisors, dividends of either sign over 24 binades) equal CUDA's IEEE division
+    bit for bit."""
+    import ctypes
+
+    from freud_gb300 import _lib
+
+    mism = ctypes.c_uint64()
+    ex = (ctypes.c_float * 2)()
+    _lib.check(_lib.lib.fg_check_division(1 << 30, 12345, ctypes.byref(mism), ex))
+    assert mism.value == 0, "first differing (a, b) = (%r, %r)" % (ex[0], ex[1])
