@@ -44,6 +44,7 @@ constexpr int SWARPS = 8;
 constexpr int STHREADS = SWARPS * 32;
 constexpr int EWARPS = 8;
 constexpr int ETHREADS = EWARPS * 32;
+constexpr int EMIT_LIST = 512; // write pass: bonds per query listed in shared memory (more: per-round search)
 // Candidate capacity of a cell's stencil (CAP) and queries per shared-memory
 // batch of the scan pass: 1024 / 64 for the common case (five blocks per SM),
 // 4096 / 32 for dense point sets (one block per SM).
@@ -849,12 +850,15 @@ __device__ __forceinline__ uint32_t kth_set_bit(uint32_t w, uint32_t k)
     return pos;
 }
 
-// Write pass, warp per cell: no shared staging and no block barriers. A warp
-// takes one cell and writes the bonds of each of its queries: lane l of a round
-// writes the query's bond number base + l, found from the prefix sums of the
-// per-chunk acceptance counts (one chunk per lane) and the set bits of that
-// chunk's mask. Candidates are read through the cell's sorted list (gsorted)
-// from L1/L2, where the cell's other queries keep them.
+// Write pass, warp per cell: no block barriers. A warp takes one cell and writes
+// the bonds of each of its queries: each lane lists the set bits of its chunks'
+// masks (one chunk per lane with CAP 1024) as candidate positions in a per-warp
+// shared list at the exclusive prefix of the per-lane bond counts, so the list
+// holds the query's bonds in order; lane l then writes bonds l, l + 32, ... of
+// the list. A query with more than EMIT_LIST bonds instead finds bond base + l of
+// each round from the prefix sums and the k-th set bit of the chunk's mask.
+// Candidates are read through the cell's sorted list (gsorted) from L1/L2, where
+// the cell's other queries keep them.
 template<int CAP>
 __global__ void __launch_bounds__(ETHREADS, 5)
     k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
@@ -866,6 +870,7 @@ __global__ void __launch_bounds__(ETHREADS, 5)
     constexpr int CHUNKS = CAP / 32;
     constexpr int WPL = CHUNKS / 32;
     __shared__ float img_s[27][3];
+    __shared__ uint16_t blist[EWARPS][EMIT_LIST]; // a query's bonds as candidate positions
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
@@ -958,6 +963,44 @@ __global__ void __launch_bounds__(ETHREADS, 5)
                 }
                 const uint32_t excl = incl - cnt;
                 const uint32_t total = __shfl_sync(FULL, incl, 31);
+                // bond bb of the query: candidate position e (chunk * 32 + bit) in the cell's sorted list
+                auto write_bond = [&](uint32_t bb, uint32_t e) {
+                    const uint32_t ent = srt[e];
+                    const uint32_t slot = ent >> 5;
+                    const float4 pp = g.cpos[slot];
+                    const uint32_t jj = g.cidx[slot];
+                    float rx, ry, rz;
+                    exact_vec(b, img_s, p.arith, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
+                    const uint64_t o = out + bb;
+                    ij[o] = make_uint2(qi, jj);
+                    dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
+                    vec[3 * o] = rx;
+                    vec[3 * o + 1] = ry;
+                    vec[3 * o + 2] = rz;
+                };
+                if (total <= static_cast<uint32_t>(EMIT_LIST))
+                {
+                    // each lane lists the set bits of its mask words at its prefix, so
+                    // the list holds the bonds in chunk order, bits ascending
+                    uint16_t* lst = blist[warp];
+                    uint32_t k = excl;
+#pragma unroll
+                    for (int kw = 0; kw < WPL; ++kw)
+                    {
+                        uint32_t w = mword[kw];
+                        const uint32_t chb = static_cast<uint32_t>(lane * WPL + kw) * 32u;
+                        while (w != 0)
+                        {
+                            lst[k++] = static_cast<uint16_t>(chb + static_cast<uint32_t>(__ffs(w) - 1));
+                            w &= w - 1u;
+                        }
+                    }
+                    __syncwarp();
+                    for (uint32_t bb = lane; bb < total; bb += 32)
+                        write_bond(bb, lst[bb]);
+                    __syncwarp();
+                    continue;
+                }
                 for (uint32_t base = 0; base < total; base += 32)
                 {
                     const uint32_t bb = base + static_cast<uint32_t>(lane);
@@ -994,20 +1037,7 @@ __global__ void __launch_bounds__(ETHREADS, 5)
                         }
                     }
                     if (bb < total)
-                    {
-                        const uint32_t ent = srt[ch * 32u + kth_set_bit(w, k)];
-                        const uint32_t slot = ent >> 5;
-                        const float4 pp = g.cpos[slot];
-                        const uint32_t jj = g.cidx[slot];
-                        float rx, ry, rz;
-                        exact_vec(b, img_s, p.arith, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
-                        const uint64_t o = out + bb;
-                        ij[o] = make_uint2(qi, jj);
-                        dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
-                        vec[3 * o] = rx;
-                        vec[3 * o + 1] = ry;
-                        vec[3 * o + 2] = rz;
-                    }
+                        write_bond(bb, ch * 32u + kth_set_bit(w, k));
                 }
             }
         }
