@@ -860,7 +860,7 @@ __device__ __forceinline__ uint32_t kth_set_bit(uint32_t w, uint32_t k)
 // Candidates are read through the cell's sorted list (gsorted) from L1/L2, where
 // the cell's other queries keep them.
 template<int CAP>
-__global__ void __launch_bounds__(ETHREADS, 5)
+__global__ void __launch_bounds__(ETHREADS, 4)
     k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
                 const uint32_t* __restrict__ gsorted, const uint32_t* __restrict__ gtotal,
                 const uint64_t* __restrict__ offsets, uint2* __restrict__ ij, float* __restrict__ dist,
@@ -964,11 +964,8 @@ __global__ void __launch_bounds__(ETHREADS, 5)
                 const uint32_t excl = incl - cnt;
                 const uint32_t total = __shfl_sync(FULL, incl, 31);
                 // bond bb of the query: candidate position e (chunk * 32 + bit) in the cell's sorted list
-                auto write_bond = [&](uint32_t bb, uint32_t e) {
-                    const uint32_t ent = srt[e];
-                    const uint32_t slot = ent >> 5;
-                    const float4 pp = g.cpos[slot];
-                    const uint32_t jj = g.cidx[slot];
+                // store bond bb from its candidate (entry ent of the sorted list, position pp, index jj)
+                auto store_bond = [&](uint32_t bb, uint32_t ent, float4 pp, uint32_t jj) {
                     float rx, ry, rz;
                     exact_vec(b, img_s, p.arith, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
                     const uint64_t o = out + bb;
@@ -977,6 +974,10 @@ __global__ void __launch_bounds__(ETHREADS, 5)
                     vec[3 * o] = rx;
                     vec[3 * o + 1] = ry;
                     vec[3 * o + 2] = rz;
+                };
+                auto write_bond = [&](uint32_t bb, uint32_t e) {
+                    const uint32_t ent = srt[e];
+                    store_bond(bb, ent, g.cpos[ent >> 5], g.cidx[ent >> 5]);
                 };
                 if (total <= static_cast<uint32_t>(EMIT_LIST))
                 {
@@ -996,8 +997,35 @@ __global__ void __launch_bounds__(ETHREADS, 5)
                         }
                     }
                     __syncwarp();
-                    for (uint32_t bb = lane; bb < total; bb += 32)
-                        write_bond(bb, lst[bb]);
+                    // one bond ahead: the next bond's candidate loads are issued before
+                    // this bond's stores (the grid arrays may alias the outputs as far as
+                    // the compiler knows, so it would not hoist them itself)
+                    uint32_t bb = lane;
+                    uint32_t ent = 0, jj = 0;
+                    float4 pp = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (bb < total)
+                    {
+                        ent = srt[lst[bb]];
+                        pp = g.cpos[ent >> 5];
+                        jj = g.cidx[ent >> 5];
+                    }
+                    while (bb < total)
+                    {
+                        const uint32_t bn = bb + 32u;
+                        uint32_t ent_n = 0, jj_n = 0;
+                        float4 pp_n = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (bn < total)
+                        {
+                            ent_n = srt[lst[bn]];
+                            pp_n = g.cpos[ent_n >> 5];
+                            jj_n = g.cidx[ent_n >> 5];
+                        }
+                        store_bond(bb, ent, pp, jj);
+                        bb = bn;
+                        ent = ent_n;
+                        pp = pp_n;
+                        jj = jj_n;
+                    }
                     __syncwarp();
                     continue;
                 }
