@@ -736,7 +736,13 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
-                         "algorithmic_bytes": alg_desc, "launch_ms": per_launch_ms},
+                         "algorithmic_bytes": alg_desc, "launch_ms": per_launch_ms,
+                         "note": ("the scan pass reads positions and writes counts only (its masks and "
+                                  "sorted candidate lists stay in L2): HBM is not what bounds it; ncu shows "
+                                  "it instruction-bound (66% issue-active, "
+                                  "profiles/k_cell_scan_k_cell_emit_k_hist_distances_262k.md); "
+                                  "roofline_build gives the whole NeighborList build against its output bytes")
+                         if dom_name is not None and "COUNT" in dom_name else None},
             "roofline_build": {"bound": "hbm", "what": "NeighborList build: grid + scan + write passes",
                                "achieved": build_gbs, "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
                                "algorithmic_bytes": "12*N + 24*B", "ms_per_step": build_ms},
