@@ -340,8 +340,11 @@ void launch_segments_from_offsets(const uint32_t* counts, const uint64_t* offset
 constexpr int SORT_WARPS = 4;
 
 // Reads the scatter-ordered (cpos_in, cidx_in) and writes every cell's points
-// sorted by point index to (cpos_out, cidx_out). Cells larger than SORT_CELL_MAX
-// are copied in scatter order.
+// sorted by (point index, scatter slot) to (cpos_out, cidx_out). Cells larger than
+// SORT_CELL_MAX are copied in scatter order. A warp takes 4 consecutive cells at
+// a time: each 8-lane group ranks the points of a cell of at most 8 (the common
+// case for grids of r_max cells at liquid densities) by counting the smaller keys
+// of its group; larger cells are then sorted by the whole warp, one at a time.
 __global__ void __launch_bounds__(SORT_WARPS * 32)
     k_sort_cells(const uint32_t* __restrict__ start, int ncell, const float4* __restrict__ cpos_in,
                  const uint32_t* __restrict__ cidx_in, float4* __restrict__ cpos_out, uint32_t* __restrict__ cidx_out)
@@ -350,12 +353,8 @@ __global__ void __launch_bounds__(SORT_WARPS * 32)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     unsigned long long* key = s_key[warp];
-    for (int c = blockIdx.x * SORT_WARPS + warp; c < ncell; c += gridDim.x * SORT_WARPS)
-    {
-        const uint32_t b0 = start[c];
-        const uint32_t n = start[c + 1] - b0;
-        if (n == 0)
-            continue;
+    // one cell of more than 8 points, by the whole warp
+    auto sort_one = [&](uint32_t b0, uint32_t n) {
         if (n > static_cast<uint32_t>(SORT_CELL_MAX))
         {
             for (uint32_t e = lane; e < n; e += 32)
@@ -363,7 +362,7 @@ __global__ void __launch_bounds__(SORT_WARPS * 32)
                 cpos_out[b0 + e] = cpos_in[b0 + e];
                 cidx_out[b0 + e] = cidx_in[b0 + e];
             }
-            continue;
+            return;
         }
         if (n <= 32)
         {
@@ -388,7 +387,7 @@ __global__ void __launch_bounds__(SORT_WARPS * 32)
                 cpos_out[b0 + lane] = cpos_in[b0 + static_cast<uint32_t>(k & 0xffffffffull)];
                 cidx_out[b0 + lane] = static_cast<uint32_t>(k >> 32);
             }
-            continue;
+            return;
         }
         uint32_t np2 = 64;
         while (np2 < n)
@@ -421,6 +420,39 @@ __global__ void __launch_bounds__(SORT_WARPS * 32)
             cidx_out[b0 + e] = static_cast<uint32_t>(key[e] >> 32);
         }
         __syncwarp();
+    };
+    const int grp = lane >> 3;
+    const int e = lane & 7;
+    for (int c4 = (blockIdx.x * SORT_WARPS + warp) * 4; c4 < ncell; c4 += gridDim.x * SORT_WARPS * 4)
+    {
+        const int c = c4 + grp;
+        uint32_t b0 = 0, n = 0;
+        if (c < ncell)
+        {
+            b0 = start[c];
+            n = start[c + 1] - b0;
+        }
+        const bool small = n <= 8;
+        const uint32_t my = (small && e < static_cast<int>(n)) ? cidx_in[b0 + e] : 0xffffffffu;
+        uint32_t rank = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            const uint32_t o = __shfl_sync(0xffffffffu, my, k, 8);
+            rank += (o < my || (o == my && k < e)) ? 1u : 0u;
+        }
+        if (small && e < static_cast<int>(n))
+        {
+            cpos_out[b0 + rank] = cpos_in[b0 + e];
+            cidx_out[b0 + rank] = my;
+        }
+        unsigned big = __ballot_sync(0xffffffffu, e == 0 && !small);
+        while (big != 0)
+        {
+            const int src = __ffs(big) - 1;
+            big &= big - 1u;
+            sort_one(__shfl_sync(0xffffffffu, b0, src), __shfl_sync(0xffffffffu, n, src));
+        }
     }
 }
 
@@ -431,7 +463,7 @@ void launch_sort_cells(const uint32_t* start, int ncell, const float4* cpos_in, 
     {
         return;
     }
-    const int blocks = grid_for(static_cast<size_t>(ncell) * 32, SORT_WARPS * 32);
+    const int blocks = grid_for(static_cast<size_t>(ncell) * 8, SORT_WARPS * 32);
     {
         ProfScope prof_("k_sort_cells", s);
         k_sort_cells<<<blocks, SORT_WARPS * 32, 0, s>>>(start, ncell, cpos_in, cidx_in, cpos_out, cidx_out);
