@@ -3418,7 +3418,7 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
             {
                 launch_ave(P, nullptr, fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st,
                            st->qlm.as<float2>(), st->qlm_ave.as<float2>(), st->ql_ave.as<float>(), s,
-                           fr->st_j.as<uint32_t>());
+                           fr->st_j.as<uint32_t>(), v.cidx);
                 src = st->qlm_ave.as<float2>();
                 qn = st->ql_ave.as<float>();
             }

@@ -681,7 +681,7 @@ template<int LANES>
 __global__ void __launch_bounds__(128)
     k_ave(uint32_t n, const uint2* __restrict__ ij, const uint32_t* __restrict__ bj, const uint32_t* __restrict__ seg,
           const uint32_t* __restrict__ cnt, StLs ls, const float2* __restrict__ qlm, float2* __restrict__ ave,
-          float* __restrict__ ql_ave)
+          float* __restrict__ ql_ave, const uint32_t* __restrict__ order)
 {
     const int lane = threadIdx.x & 31;
     const int sub = lane % LANES;
@@ -689,8 +689,10 @@ __global__ void __launch_bounds__(128)
     const int groups_per_block = blockDim.x / LANES;
     const unsigned gmask = LANES == 32 ? FULL : (((1u << LANES) - 1u) << (group * LANES));
     const int m = sub;
-    for (uint32_t i = blockIdx.x * groups_per_block + threadIdx.x / LANES; i < n; i += gridDim.x * groups_per_block)
+    for (uint32_t t = blockIdx.x * groups_per_block + threadIdx.x / LANES; t < n; t += gridDim.x * groups_per_block)
     {
+        // particles in the given order (cell order: neighbours share qlm rows in L2), else by index
+        const uint32_t i = order != nullptr ? order[t] : t;
         const uint32_t b0 = seg[i];
         const uint32_t nbond = cnt[i];
         const float cntf = static_cast<float>(1u + nbond);
@@ -965,7 +967,8 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
 }
 
 void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
-                const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s, const uint32_t* bond_j)
+                const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s, const uint32_t* bond_j,
+                const uint32_t* order)
 {
     if (n == 0)
     {
@@ -979,17 +982,17 @@ void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t
     if (lanes == 8)
         {
             ProfScope prof_("k_ave<8>", s);
-            k_ave<8><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave);
+            k_ave<8><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave, order);
         }
     else if (lanes == 16)
         {
             ProfScope prof_("k_ave<16>", s);
-            k_ave<16><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave);
+            k_ave<16><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave, order);
         }
     else
         {
             ProfScope prof_("k_ave<32>", s);
-            k_ave<32><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave);
+            k_ave<32><<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, qlm, ave, ql_ave, order);
         }
 }
 

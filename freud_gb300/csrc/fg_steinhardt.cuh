@@ -33,8 +33,12 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
                 float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd = nullptr, double mean_bonds = 0.0);
 // bond_j (optional): the neighbour index of each bond, used instead of ij[e].y.
+// order (optional): a permutation of the n particles to process them in (e.g. a
+// cell grid's slot order, so neighbours' qlm rows are reused from L2); results do
+// not depend on it.
 void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
-                const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s, const uint32_t* bond_j = nullptr);
+                const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s, const uint32_t* bond_j = nullptr,
+                const uint32_t* order = nullptr);
 void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float* w3j_dev, const float* qnorm,
                int normalize, float* wl, cudaStream_t s);
 
