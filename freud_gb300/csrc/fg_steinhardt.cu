@@ -764,12 +764,17 @@ __global__ void __launch_bounds__(128)
     extern __shared__ float2 rows[];
     const int nm = 2 * l + 1;
     const uint32_t i0 = blockIdx.x * blockDim.x;
-    // stage the block's rows (coalesced)
+    // the block's rows (coalesced), then the l's Wigner-3j coefficients (every
+    // thread reads coefficient c at the same time: a shared-memory broadcast)
+    float* w3s = reinterpret_cast<float*>(rows + blockDim.x * static_cast<uint32_t>(nm));
     for (uint32_t e = threadIdx.x; e < blockDim.x * static_cast<uint32_t>(nm); e += blockDim.x)
     {
         const uint32_t gi = i0 + e / nm;
         rows[e] = gi < n ? src[qlm_offset + static_cast<size_t>(i0) * nm + e] : make_float2(0.f, 0.f);
     }
+    const int nterms = 3 * l * l + 3 * l + 1;
+    for (int e = threadIdx.x; e < nterms; e += blockDim.x)
+        w3s[e] = w3j[e];
     __syncthreads();
     const uint32_t i = i0 + threadIdx.x;
     if (i >= n)
@@ -791,7 +796,7 @@ __global__ void __launch_bounds__(128)
             const float2 cq = q[m3 < 0 ? l - m3 : m3];
             const float abr = a.x * bq.x - a.y * bq.y;
             const float abi = a.x * bq.y + a.y * bq.x;
-            const float term = w3j[c] * (abr * cq.x - abi * cq.y);
+            const float term = w3s[c] * (abr * cq.x - abi * cq.y);
             // compensated (Kahan) summation
             const float y = term - comp;
             const float t = sum + y;
@@ -1004,12 +1009,14 @@ void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float
         return;
     }
     const int l = ls.l[k];
-    const size_t smem = 128 * static_cast<size_t>(2 * l + 1) * sizeof(float2);
+    const size_t smem = 128 * static_cast<size_t>(2 * l + 1) * sizeof(float2) +
+                        static_cast<size_t>(3 * l * l + 3 * l + 1) * sizeof(float);
     static bool configured = false;
     if (!configured)
     {
         cudaFuncSetAttribute(k_wl, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(128 * (2 * ST_MAX_L + 1) * sizeof(float2)));
+                             static_cast<int>(128 * (2 * ST_MAX_L + 1) * sizeof(float2) +
+                                              (3 * ST_MAX_L * ST_MAX_L + 3 * ST_MAX_L + 1) * sizeof(float)));
         configured = true;
     }
     {
