@@ -614,29 +614,29 @@ constexpr int FB_TILE = 128;  // staged candidates per warp
 constexpr int FB_QUEUE = 64;  // bond queue entries per warp (drained at 32)
 constexpr int FB_K0_OK = 1 << 24; // staged image resolved (query in the box)
 
-struct FBWarp
+template<bool FILL> struct FBWarp
 {
     float4 pos[FB_TILE];      // x, y, z, point index (bits)
     float4 img[FB_TILE];      // image vector for a query in the box; w = packed n_j - wrap | FB_K0_OK
     float4 q[32];             // the group's queries (w = packed box image)
     uint32_t qi[32];
-    unsigned long long qe[FB_QUEUE];  // fill: output row of a queued bond
-    float4 qv[FB_QUEUE];              // fill: p_j - q (x, y, z), r^2
-    uint32_t qj[FB_QUEUE];            // fill: neighbour index
+    unsigned long long qe[FILL ? FB_QUEUE : 1]; // fill: output row of a queued bond
+    float4 qv[FILL ? FB_QUEUE : 1];             // fill: p_j - q (x, y, z), r^2
+    uint32_t qj[FILL ? FB_QUEUE : 1];           // fill: neighbour index
     uint32_t it_off[28];      // stencil item offsets (prefix of counts)
     uint32_t it_start[27];    // first slot of the item's cell
     int it_wrap[27];          // (wx + 1) + 3 (wy + 1) + 9 (wz + 1)
 };
 
 template<bool FILL>
-__global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 8)
+__global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
     k_frames_ball(BatchGrid g, BallParams p, uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets,
                   uint32_t* __restrict__ bj, float4* __restrict__ bvd)
 {
-    __shared__ FBWarp sw[FB_WARPS];
+    __shared__ FBWarp<FILL> sw[FB_WARPS];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    FBWarp& W = sw[warp];
+    FBWarp<FILL>& W = sw[warp];
     const unsigned lt = (1u << lane) - 1u;
     const uint32_t nwarps = gridDim.x * FB_WARPS;
     uint32_t c = blockIdx.x * FB_WARPS + warp;
