@@ -633,17 +633,19 @@ __global__ void __launch_bounds__(256)
 __global__ void k_hist_distances(const float* __restrict__ dist, uint64_t nb, HistParams h,
                                  unsigned long long* __restrict__ hist)
 {
-    __shared__ unsigned int s_hist[HIST_COPIES * HIST_SMEM_BINS];
+    // HIST_COPIES privatised copies of h.bins counters (dynamic shared memory sized
+    // by the launch, so a few hundred bins leave room for a full wave of blocks)
+    extern __shared__ unsigned int s_hist[];
     const bool smem_hist = h.bins <= HIST_SMEM_BINS;
     if (smem_hist)
     {
         for (int t = threadIdx.x; t < HIST_COPIES * static_cast<int>(h.bins); t += blockDim.x)
         {
-            s_hist[(t / h.bins) * HIST_SMEM_BINS + t % h.bins] = 0;
+            s_hist[t] = 0;
         }
     }
     __syncthreads();
-    unsigned int* my = s_hist + ((threadIdx.x >> 5) % HIST_COPIES) * HIST_SMEM_BINS;
+    unsigned int* my = s_hist + ((threadIdx.x >> 5) % HIST_COPIES) * h.bins;
     auto add = [&](float d) {
         if (d < h.h_min || d >= h.h_max)
             return;
@@ -691,7 +693,7 @@ __global__ void k_hist_distances(const float* __restrict__ dist, uint64_t nb, Hi
             unsigned long long s = 0;
             for (int c = 0; c < HIST_COPIES; ++c)
             {
-                s += s_hist[c * HIST_SMEM_BINS + bin];
+                s += s_hist[c * h.bins + bin];
             }
             if (s != 0)
             {
@@ -796,11 +798,15 @@ void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, 
     cudaGetDevice(&dev);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // one wave of resident blocks (a partial second wave would run alone at the end)
+    const size_t smem = h.bins <= static_cast<uint32_t>(HIST_SMEM_BINS) ? sizeof(unsigned int) * HIST_COPIES * h.bins : 0;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hist_distances, 256, smem);
     uint64_t want = (nb + 255) / 256;
-    const uint64_t cap = static_cast<uint64_t>(sms) * 8;
+    const uint64_t cap = static_cast<uint64_t>(sms) * static_cast<uint64_t>(per_sm > 0 ? per_sm : 1);
     {
         ProfScope prof_("k_hist_distances", s);
-        k_hist_distances<<<static_cast<unsigned>(want < cap ? want : cap), 256, 0, s>>>(dist, nb, h, hist);
+        k_hist_distances<<<static_cast<unsigned>(want < cap ? want : cap), 256, smem, s>>>(dist, nb, h, hist);
     }
 }
 
