@@ -1234,12 +1234,37 @@ static int lm_index(int l, int m)
     return m < 0 ? l - m : m; /* Wigner3j.cc:17-20 */
 }
 
-/* Wigner3j.cc:22-57 in double; *mag (optional) receives the sum of |terms|, the
- * scale against which the cancellation in the sum is judged. */
-static double reduce_w3j_mag(const double* q /* 2*(2l+1) */, int l, double* mag)
+/* Wigner-3j coefficients of one l in the iteration order of reduce_w3j_tab
+ * (m1 ascending, then m2 ascending): computed once per l, not per particle. */
+static double* w3j_table(int l)
+{
+    size_t n = 0;
+    for (int m1 = -l; m1 <= l; ++m1)
+    {
+        const int lo = (-l - m1) > -l ? (-l - m1) : -l;
+        const int hi = (l - m1) < l ? (l - m1) : l;
+        n += (size_t) (hi - lo + 1);
+    }
+    double* t = (double*) malloc(sizeof(double) * (n ? n : 1));
+    size_t k = 0;
+    for (int m1 = -l; m1 <= l; ++m1)
+    {
+        const int lo = (-l - m1) > -l ? (-l - m1) : -l;
+        const int hi = (l - m1) < l ? (l - m1) : l;
+        for (int m2 = lo; m2 <= hi; ++m2)
+            t[k++] = ofg_wigner3j(l, m1, m2, -m1 - m2);
+    }
+    return t;
+}
+
+/* Wigner3j.cc:22-57 in double, with the coefficients from w3j_table(l); *mag
+ * (optional) receives the sum of |terms|, the scale against which the
+ * cancellation in the sum is judged. */
+static double reduce_w3j_tab(const double* q, int l, const double* w3j, double* mag)
 {
     double res = 0.0;
     double m_abs = 0.0;
+    size_t k = 0;
     for (int m1 = -l; m1 <= l; ++m1)
     {
         const int lo = (-l - m1) > -l ? (-l - m1) : -l;
@@ -1247,7 +1272,7 @@ static double reduce_w3j_mag(const double* q /* 2*(2l+1) */, int l, double* mag)
         for (int m2 = lo; m2 <= hi; ++m2)
         {
             const int m3 = -m1 - m2;
-            const double w = ofg_wigner3j(l, m1, m2, m3);
+            const double w = w3j[k++];
             const double* a = q + 2 * lm_index(l, m1);
             const double* b = q + 2 * lm_index(l, m2);
             const double* c = q + 2 * lm_index(l, m3);
@@ -1263,14 +1288,193 @@ static double reduce_w3j_mag(const double* q /* 2*(2l+1) */, int l, double* mag)
     return res;
 }
 
-static double reduce_w3j(const double* q, int l)
+/* Shared state of the threaded Steinhardt phases; each phase is a loop over
+ * particles split into contiguous ranges, one per thread. Every particle's
+ * result depends only on its own bonds (and, for the average, on the finished
+ * plain qlm), so the output does not depend on the thread count. */
+typedef struct
 {
-    return reduce_w3j_mag(q, l, NULL);
+    const uint32_t* ls;
+    uint32_t nl, maxl;
+    int weighted, wl_normalize, average;
+    obox box;
+    const float* pts;
+    uint32_t n;
+    const uint32_t* ij;
+    const float* bond_dist;
+    const float* bond_w;
+    const uint64_t* first;
+    size_t stride;
+    double* ql;
+    double* ql_ave;
+    double* wl_out;
+    double* wl_mag;
+    double* qlm;
+    double* qave;
+    double** w3j; /* per l index */
+    int phase;    /* 0 plain qlm, 1 average, 2 wl */
+    int nthreads;
+} stctx;
+
+typedef struct
+{
+    stctx* c;
+    int tid;
+} starg;
+
+/* Steinhardt.cc:120-222 for particle i in FP64 (pair vector wrap(p_j - p_i) in float32) */
+static void st_plain(stctx* c, uint32_t i, double* ylm)
+{
+    double tw = 0.0;
+    const float* pi = c->pts + 3 * (size_t) i;
+    double* row = c->qlm + 2 * (size_t) i * c->stride;
+    for (uint64_t t = c->first[i]; t < c->first[i + 1]; ++t)
+    {
+        const uint32_t j = c->ij[2 * t + 1];
+        const float* pj = c->pts + 3 * (size_t) j;
+        float dv[3] = {pj[0] - pi[0], pj[1] - pi[1], pj[2] - pi[2]};
+        float dl[3];
+        box_wrap(&c->box, dv, dl);
+        const double w = c->weighted ? (double) c->bond_w[t] : 1.0;
+        const double phi = atan2((double) dl[1], (double) dl[0]);
+        const double dist = (double) c->bond_dist[t];
+        double ct = (double) dl[2] / dist;
+        if (ct < -1.0)
+            ct = -1.0;
+        if (ct > 1.0)
+            ct = 1.0;
+        double theta = acos(ct);
+        if (c->bond_dist[t] == 0.0f)
+            theta = 0.0;
+        size_t off = 0;
+        for (uint32_t k = 0; k < c->nl; ++k)
+        {
+            const int l = (int) c->ls[k];
+            ofg_ylm(l, theta, phi, ylm);
+            for (int m = 0; m < 2 * l + 1; ++m)
+            {
+                row[2 * (off + m)] += w * ylm[2 * m];
+                row[2 * (off + m) + 1] += w * ylm[2 * m + 1];
+            }
+            off += 2 * l + 1;
+        }
+        tw += w;
+    }
+    size_t off = 0;
+    for (uint32_t k = 0; k < c->nl; ++k)
+    {
+        const int l = (int) c->ls[k];
+        double s = 0.0;
+        for (int m = 0; m < 2 * l + 1; ++m)
+        {
+            double* v = &row[2 * (off + m)];
+            v[0] /= tw;
+            v[1] /= tw;
+            s += v[0] * v[0] + v[1] * v[1];
+        }
+        c->ql[(size_t) i * c->nl + k] = sqrt(s * (4.0 * M_PI / (2 * l + 1)));
+        off += 2 * l + 1;
+    }
+}
+
+/* Steinhardt.cc:224-289 for particle i in FP64 */
+static void st_average(stctx* c, uint32_t i)
+{
+    const size_t s2 = 2 * c->stride;
+    double* dst = &c->qave[(size_t) i * s2];
+    for (size_t m = 0; m < s2; ++m)
+        dst[m] = c->qlm[(size_t) i * s2 + m];
+    uint64_t cnt = 1;
+    for (uint64_t t = c->first[i]; t < c->first[i + 1]; ++t)
+    {
+        const uint32_t j = c->ij[2 * t + 1];
+        for (size_t m = 0; m < s2; ++m)
+            dst[m] += c->qlm[(size_t) j * s2 + m];
+        cnt++;
+    }
+    for (size_t m = 0; m < s2; ++m)
+        dst[m] /= (double) cnt;
+    size_t off = 0;
+    for (uint32_t k = 0; k < c->nl; ++k)
+    {
+        const int l = (int) c->ls[k];
+        double s = 0.0;
+        for (int m = 0; m < 2 * l + 1; ++m)
+        {
+            const double* v = &dst[2 * (off + m)];
+            s += v[0] * v[0] + v[1] * v[1];
+        }
+        c->ql_ave[(size_t) i * c->nl + k] = sqrt(s * (4.0 * M_PI / (2 * l + 1)));
+        off += 2 * l + 1;
+    }
+}
+
+/* Steinhardt.cc:329-359 (wl of the plain or averaged qlm) for particle i in FP64 */
+static void st_wl(stctx* c, uint32_t i)
+{
+    const double* src = c->average ? c->qave : c->qlm;
+    const double* nsrc = c->average ? c->ql_ave : c->ql;
+    size_t off = 0;
+    for (uint32_t k = 0; k < c->nl; ++k)
+    {
+        const int l = (int) c->ls[k];
+        double mag = 0.0;
+        double v = reduce_w3j_tab(&src[2 * ((size_t) i * c->stride + off)], l, c->w3j[k], &mag);
+        if (c->wl_normalize)
+        {
+            const double nf = sqrt(4.0 * M_PI / (2 * l + 1)) / nsrc[(size_t) i * c->nl + k];
+            v *= nf * nf * nf;
+            mag *= nf * nf * nf;
+        }
+        c->wl_out[(size_t) i * c->nl + k] = v;
+        if (c->wl_mag)
+            c->wl_mag[(size_t) i * c->nl + k] = mag;
+        off += 2 * l + 1;
+    }
+}
+
+static void* st_worker(void* varg)
+{
+    starg* a = (starg*) varg;
+    stctx* c = a->c;
+    const uint32_t per = (c->n + (uint32_t) c->nthreads - 1) / (uint32_t) c->nthreads;
+    const uint32_t i0 = per * (uint32_t) a->tid;
+    const uint32_t i1 = i0 + per < c->n ? i0 + per : c->n;
+    double* ylm = (double*) malloc(sizeof(double) * 2 * (2 * c->maxl + 1));
+    for (uint32_t i = i0; i < i1; ++i)
+    {
+        if (c->phase == 0)
+            st_plain(c, i, ylm);
+        else if (c->phase == 1)
+            st_average(c, i);
+        else
+            st_wl(c, i);
+    }
+    free(ylm);
+    return NULL;
+}
+
+static void st_run(stctx* c, int phase)
+{
+    c->phase = phase;
+    pthread_t* th = (pthread_t*) malloc(sizeof(pthread_t) * (size_t) c->nthreads);
+    starg* args = (starg*) malloc(sizeof(starg) * (size_t) c->nthreads);
+    for (int t = 0; t < c->nthreads; ++t)
+    {
+        args[t].c = c;
+        args[t].tid = t;
+        pthread_create(&th[t], NULL, st_worker, &args[t]);
+    }
+    for (int t = 0; t < c->nthreads; ++t)
+        pthread_join(th[t], NULL);
+    free(th);
+    free(args);
 }
 
 /* Steinhardt over a NeighborList sorted by query index (Steinhardt.cc:120-359).
  * Pair vectors are recomputed as wrap(p_j - p_i) in float32 (Steinhardt.cc:155),
- * the rest is FP64. Outputs (row-major, n rows):
+ * the rest is FP64. Per-particle phases run on nthreads threads (the results do
+ * not depend on the thread count). Outputs (row-major, n rows):
  *   ql      (n, nl)        plain ql
  *   ql_ave  (n, nl)        averaged ql (only when average)
  *   wl      (n, nl)        wl of (averaged if average) qlm (only when wl)
@@ -1279,20 +1483,35 @@ static double reduce_w3j(const double* q, int l)
 int ofg_steinhardt(const uint32_t* ls, uint32_t nl, int average, int wl, int weighted, int wl_normalize,
                    const float* box7, const float* pts, uint32_t n, uint64_t nbonds, const uint32_t* ij,
                    const float* bond_dist, const float* bond_w, double* ql, double* ql_ave, double* wl_out,
-                   double* qlm, double* order, double* wl_mag)
+                   double* qlm, double* order, double* wl_mag, int nthreads)
 {
-    obox box;
-    box_init(&box, box7);
-    size_t stride = 0;
-    uint32_t maxl = 0;
+    stctx c;
+    memset(&c, 0, sizeof(c));
+    box_init(&c.box, box7);
+    c.ls = ls;
+    c.nl = nl;
+    c.weighted = weighted;
+    c.wl_normalize = wl_normalize;
+    c.average = average;
+    c.pts = pts;
+    c.n = n;
+    c.ij = ij;
+    c.bond_dist = bond_dist;
+    c.bond_w = bond_w;
+    c.ql = ql;
+    c.ql_ave = ql_ave;
+    c.wl_out = wl_out;
+    c.wl_mag = wl_mag;
+    c.qlm = qlm;
+    c.nthreads = nthreads < 1 ? 1 : nthreads;
     for (uint32_t k = 0; k < nl; ++k)
     {
-        stride += 2 * ls[k] + 1;
-        if (ls[k] > maxl)
-            maxl = ls[k];
+        c.stride += 2 * ls[k] + 1;
+        if (ls[k] > c.maxl)
+            c.maxl = ls[k];
     }
-    double* ylm = (double*) malloc(sizeof(double) * 2 * (2 * maxl + 1));
-    double* qave = (double*) calloc((size_t) n * stride * 2, sizeof(double));
+    const size_t stride = c.stride;
+    c.qave = (double*) calloc((size_t) n * stride * 2 + 1, sizeof(double));
     double* sys = (double*) calloc(stride * 2, sizeof(double));
     uint64_t* first = (uint64_t*) malloc(sizeof(uint64_t) * ((size_t) n + 1));
     /* segments (NeighborList.cc:199-232) */
@@ -1303,94 +1522,17 @@ int ofg_steinhardt(const uint32_t* ls, uint32_t nl, int average, int wl, int wei
             ++b;
         first[i] = b;
     }
+    c.first = first;
     memset(qlm, 0, sizeof(double) * (size_t) n * stride * 2);
-    for (uint32_t i = 0; i < n; ++i)
-    {
-        double tw = 0.0;
-        const float* pi = pts + 3 * (size_t) i;
-        for (uint64_t t = first[i]; t < first[i + 1]; ++t)
-        {
-            const uint32_t j = ij[2 * t + 1];
-            const float* pj = pts + 3 * (size_t) j;
-            float dv[3] = {pj[0] - pi[0], pj[1] - pi[1], pj[2] - pi[2]};
-            float dl[3];
-            box_wrap(&box, dv, dl);
-            const double w = weighted ? (double) bond_w[t] : 1.0;
-            const double phi = atan2((double) dl[1], (double) dl[0]);
-            const double dist = (double) bond_dist[t];
-            double ct = (double) dl[2] / dist;
-            if (ct < -1.0)
-                ct = -1.0;
-            if (ct > 1.0)
-                ct = 1.0;
-            double theta = acos(ct);
-            if (bond_dist[t] == 0.0f)
-                theta = 0.0;
-            size_t off = 0;
-            for (uint32_t k = 0; k < nl; ++k)
-            {
-                const int l = (int) ls[k];
-                ofg_ylm(l, theta, phi, ylm);
-                for (int m = 0; m < 2 * l + 1; ++m)
-                {
-                    qlm[2 * ((size_t) i * stride + off + m)] += w * ylm[2 * m];
-                    qlm[2 * ((size_t) i * stride + off + m) + 1] += w * ylm[2 * m + 1];
-                }
-                off += 2 * l + 1;
-            }
-            tw += w;
-        }
-        size_t off = 0;
-        for (uint32_t k = 0; k < nl; ++k)
-        {
-            const int l = (int) ls[k];
-            double s = 0.0;
-            for (int m = 0; m < 2 * l + 1; ++m)
-            {
-                double* v = &qlm[2 * ((size_t) i * stride + off + m)];
-                v[0] /= tw;
-                v[1] /= tw;
-                s += v[0] * v[0] + v[1] * v[1];
-            }
-            ql[(size_t) i * nl + k] = sqrt(s * (4.0 * M_PI / (2 * l + 1)));
-            off += 2 * l + 1;
-        }
-    }
+    st_run(&c, 0);
     const double* src = qlm;
     if (average)
     {
-        for (uint32_t i = 0; i < n; ++i)
-        {
-            double* dst = &qave[2 * (size_t) i * stride];
-            for (size_t m = 0; m < 2 * stride; ++m)
-                dst[m] = qlm[2 * (size_t) i * stride + m];
-            uint64_t cnt = 1;
-            for (uint64_t t = first[i]; t < first[i + 1]; ++t)
-            {
-                const uint32_t j = ij[2 * t + 1];
-                for (size_t m = 0; m < 2 * stride; ++m)
-                    dst[m] += qlm[2 * (size_t) j * stride + m];
-                cnt++;
-            }
-            for (size_t m = 0; m < 2 * stride; ++m)
-                dst[m] /= (double) cnt;
-            size_t off = 0;
-            for (uint32_t k = 0; k < nl; ++k)
-            {
-                const int l = (int) ls[k];
-                double s = 0.0;
-                for (int m = 0; m < 2 * l + 1; ++m)
-                {
-                    const double* v = &dst[2 * (off + m)];
-                    s += v[0] * v[0] + v[1] * v[1];
-                }
-                ql_ave[(size_t) i * nl + k] = sqrt(s * (4.0 * M_PI / (2 * l + 1)));
-                off += 2 * l + 1;
-            }
-        }
-        src = qave;
+        st_run(&c, 1);
+        src = c.qave;
     }
-    /* system qlm: mean over particles of qlmi (or qlmiAve), Steinhardt.cc:203-207, 265-266 */
+    /* system qlm: mean over particles of qlmi (or qlmiAve), Steinhardt.cc:203-207,
+     * 265-266, summed in particle order */
     for (uint32_t i = 0; i < n; ++i)
     {
         for (size_t m = 0; m < 2 * stride; ++m)
@@ -1398,27 +1540,10 @@ int ofg_steinhardt(const uint32_t* ls, uint32_t nl, int average, int wl, int wei
     }
     if (wl)
     {
-        const double* nsrc = average ? ql_ave : ql;
-        for (uint32_t i = 0; i < n; ++i)
-        {
-            size_t off = 0;
-            for (uint32_t k = 0; k < nl; ++k)
-            {
-                const int l = (int) ls[k];
-                double mag = 0.0;
-                double v = reduce_w3j_mag(&src[2 * ((size_t) i * stride + off)], l, &mag);
-                if (wl_normalize)
-                {
-                    const double nf = sqrt(4.0 * M_PI / (2 * l + 1)) / nsrc[(size_t) i * nl + k];
-                    v *= nf * nf * nf;
-                    mag *= nf * nf * nf;
-                }
-                wl_out[(size_t) i * nl + k] = v;
-                if (wl_mag)
-                    wl_mag[(size_t) i * nl + k] = mag;
-                off += 2 * l + 1;
-            }
-        }
+        c.w3j = (double**) malloc(sizeof(double*) * (nl ? nl : 1));
+        for (uint32_t k = 0; k < nl; ++k)
+            c.w3j[k] = w3j_table((int) ls[k]);
+        st_run(&c, 2);
     }
     /* Steinhardt.cc:291-327 */
     size_t off = 0;
@@ -1432,7 +1557,7 @@ int ofg_steinhardt(const uint32_t* ls, uint32_t nl, int average, int wl, int wei
         const double qsys = sqrt(s * nf);
         if (wl)
         {
-            double v = reduce_w3j(&sys[2 * off], l);
+            double v = reduce_w3j_tab(&sys[2 * off], l, c.w3j[k], NULL);
             if (wl_normalize)
             {
                 const double w = sqrt(nf) / qsys;
@@ -1446,8 +1571,13 @@ int ofg_steinhardt(const uint32_t* ls, uint32_t nl, int average, int wl, int wei
         }
         off += 2 * l + 1;
     }
-    free(ylm);
-    free(qave);
+    if (c.w3j)
+    {
+        for (uint32_t k = 0; k < nl; ++k)
+            free(c.w3j[k]);
+        free(c.w3j);
+    }
+    free(c.qave);
     free(sys);
     free(first);
     return 0;

@@ -54,7 +54,7 @@ def _load():
     lib.ofg_wigner3j.restype = ctypes.c_double
     lib.ofg_wigner3j.argtypes = [i32, i32, i32, i32]
     lib.ofg_steinhardt.restype = i32
-    lib.ofg_steinhardt.argtypes = [P, u32, i32, i32, i32, i32, P, P, u32, u64, P, P, P, P, P, P, P, P, P]
+    lib.ofg_steinhardt.argtypes = [P, u32, i32, i32, i32, i32, P, P, u32, u64, P, P, P, P, P, P, P, P, P, i32]
     lib.ofg_box_wrap.argtypes = [P, P, u64, P]
     lib.ofg_box_fractional.argtypes = [P, P, u64, P]
     _lib = lib
@@ -222,7 +222,7 @@ def wigner3j(l, m1, m2, m3):
 
 
 def steinhardt(ls, box, points, ij, distances, weights=None, average=False, wl=False, weighted=False,
-               wl_normalize=False):
+               wl_normalize=False, threads=None):
     """FP64 Steinhardt over a NeighborList sorted by query index. Returns a dict with
     ql, ql_ave, wl (N, nl) float64, wl_mag (N, nl) = sum of |Wigner-3j terms| (the
     scale of the cancellation in w_l), qlm list of (N, 2l+1) complex128, order (nl,)."""
@@ -243,7 +243,8 @@ def steinhardt(ls, box, points, ij, distances, weights=None, average=False, wl=F
     order = np.zeros(nl)
     wmag = np.zeros((n, nl))
     lib.ofg_steinhardt(_p(ls), nl, int(average), int(wl), int(weighted), int(wl_normalize), _p(b), _p(pts), n,
-                       len(d), _p(ij), _p(d), _p(w), _p(ql), _p(qla), _p(wlo), _p(qlm), _p(order), _p(wmag))
+                       len(d), _p(ij), _p(d), _p(w), _p(ql), _p(qla), _p(wlo), _p(qlm), _p(order), _p(wmag),
+                       int(threads or default_threads()))
     qc = qlm[..., 0] + 1j * qlm[..., 1]
     out, off = [], 0
     for l in ls:
