@@ -12,10 +12,15 @@ A pair evaluation is one accepted ordered bond.
 value      device-resident points, C-ABI calls, CUDA events around each step
 e2e        the public Python API with host (pinned) points: H2D, build, query,
            RDF, D2H of the RDF; host wall clock around each synchronous step
-roofline   the dominant kernel's algorithmic bytes / its event-timed duration
+e2e_nlist_readback  the same plus nlist[:], distances and vectors read to host
+roofline   the NeighborList build (every kernel of the step except the RDF over
+           the finished list): 12 N + 24 B bytes over the kernels' event time
 cpu_baseline  the CPU oracle (restatement of the reference, all host threads)
-              on a bounded sample of the same workload (a prefix of the query points)
---impl reference  times that CPU path alone with the same metric.
+              over the whole workload; its list is also the parity reference
+parity     per workload: the GPU results against the oracle (bit-exact lists and
+           counts; Steinhardt within the stated FP64 tolerances); a mismatch
+           makes the run exit with status 1 after printing the line
+--impl reference  times the CPU path alone with the same metric (a bounded sample).
 Multi-GPU: independent replicas (the path has no exchange step); value sums ranks.
 """
 
@@ -37,6 +42,8 @@ sys.path.insert(0, ROOT)
 METRIC = "pair evals/s (RDF) & particles/s (Steinhardt l=6), batched vs plain, 1 GB300"
 WORKLOAD = "large_n_nlist_rdf"
 L2_BYTES = 129 * 1024 * 1024
+PARITY_OK = ("bit-exact", "within tolerance")
+WL_FLOOR = 1e-7  # absolute floor of the Wl tolerance (normalised Wl is O(0.01-0.1))
 
 
 def c2_system(seed=2024, n1=102):
@@ -168,28 +175,38 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(L, pts, r_max=3.0, bins=300, target_s=12.0, threads=None):
-    """CPU oracle (restatement of the reference path, all host threads) on a bounded
-    sample: the first M query points against all points, M scaled so the measured
-    run takes about target_s seconds. Returns (bonds/s, sample description, cores)."""
+def cpu_baseline(L, pts, r_max=3.0, bins=300, target_s=12.0, threads=None, sample=None):
+    """CPU oracle (restatement of the reference path, all host threads): LinkCell
+    arithmetic ball query + NeighborList in reference order + RDF histogram.
+    sample=None runs the whole workload once (every query point) and also returns
+    the oracle's list and counts for the parity check; sample=M times the first M
+    query points against all points (a bounded sample; M = 0 scales M from a short
+    probe so the run takes about target_s seconds).
+    Returns (bonds/s, sample description, threads, seconds, (ij, d, v, counts) or None)."""
     from oracle import oracle as O
 
     threads = threads or (os.cpu_count() or 1)
     box = (L, L, L, 0.0, 0.0, 0.0, 0.0)
-    m = 20000
+    if sample is None:
+        t0 = time.perf_counter()
+        ij, d, v = O.query(box, pts, r_max=r_max, exclude_ii=True, arith=O.ARITH_WRAP, threads=threads)
+        counts = O.hist(d, bins, r_max)
+        dt = time.perf_counter() - t0
+        return (len(ij) / dt, "whole workload: LinkCell-arithmetic ball query r_max=%g over all %d query points + "
+                "NeighborList sort + RDF histogram, one run" % (r_max, len(pts)), threads, dt, (ij, d, v, counts))
+    m = sample if sample > 0 else 20000
+    if sample == 0:
+        t0 = time.perf_counter()
+        O.query(box, pts, query_points=pts[:m], r_max=r_max, exclude_ii=True, arith=O.ARITH_WRAP, threads=threads)
+        dt = time.perf_counter() - t0
+        m = int(min(len(pts), max(m, m * target_s / max(dt, 1e-3))))
     t0 = time.perf_counter()
     ij, d, v = O.query(box, pts, query_points=pts[:m], r_max=r_max, exclude_ii=True, arith=O.ARITH_WRAP,
                        threads=threads)
     O.hist(d, bins, r_max)
     dt = time.perf_counter() - t0
-    m2 = int(min(len(pts), max(m, m * target_s / max(dt, 1e-3))))
-    t0 = time.perf_counter()
-    ij, d, v = O.query(box, pts, query_points=pts[:m2], r_max=r_max, exclude_ii=True, arith=O.ARITH_WRAP,
-                       threads=threads)
-    O.hist(d, bins, r_max)
-    dt = time.perf_counter() - t0
-    return len(ij) / dt, ("LinkCell-arithmetic ball query r_max=3 + NeighborList sort + RDF histogram for the "
-                          "first %d of %d query points against all points" % (m2, len(pts))), threads, dt
+    return len(ij) / dt, ("LinkCell-arithmetic ball query r_max=%g + NeighborList sort + RDF histogram for the "
+                          "first %d of %d query points against all points" % (r_max, m, len(pts))), threads, dt, None
 
 
 def _median_wall(fn, steps, warmup):
@@ -326,10 +343,13 @@ def measure_pmft(freud, _lib, steps, warmup, cpu=True):
 
 def measure_c3(freud, _lib, steps, warmup, cpu=True):
     """Steinhardt([4, 6, 8, 10, 12], average, wl, wl_normalize) with 12 nearest
-    neighbours on a 256,000-point noisy FCC crystal."""
+    neighbours on a 256,000-point noisy FCC crystal. Parity: every particle's
+    averaged Ql and normalised Wl and the system order against the FP64 oracle
+    (whose run over the whole workload is also the CPU baseline)."""
     L, pts = c3_system()
     box = freud.box.Box.cube(float(L))
-    st = freud.order.Steinhardt([4, 6, 8, 10, 12], average=True, wl=True, wl_normalize=True)
+    ls = [4, 6, 8, 10, 12]
+    st = freud.order.Steinhardt(ls, average=True, wl=True, wl_normalize=True)
 
     def step():
         st.compute((box, pts), neighbors={"num_neighbors": 12})
@@ -342,24 +362,60 @@ def measure_c3(freud, _lib, steps, warmup, cpu=True):
     out = {"workload": "steinhardt_fcc_256000_k12_l4-12_ave_wl", "particles": n, "e2e_ms": t * 1e3, "e2e": n / t,
            "device_ms": dev_ms, "device": n / (dev_ms / 1e3), "unit": "particles/s", "launches_per_step": launches,
            "kernels_ms_per_step": top}
+    # roofline of the step: 12 N + 8 B + 8 N sum(2l+1) (1 + average) + 4 N n_l (1 + average + wl)
+    peak, peak_kind = read_peaks()
+    stride = sum(2 * l + 1 for l in ls)
+    alg = 12.0 * n + 8.0 * 12 * n + 8.0 * n * stride * 2 + 4.0 * n * len(ls) * 3
+    out["roofline"] = {"bound": "hbm", "algorithmic_bytes": alg, "achieved": alg / (dev_ms / 1e3) / 1e9,
+                       "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+                       "frac": alg / (dev_ms / 1e3) / 1e9 / peak,
+                       "formula": "12 N + 8 B + 8 N sum(2l+1) (1 + average) + 4 N n_l (1 + average + wl), B = 12 N"}
     if cpu:
         from oracle import oracle as O
 
         bx = (float(L),) * 3 + (0.0, 0.0, 0.0, 0.0)
-        m = 32000
+        threads = os.cpu_count() or 1
         t0 = time.perf_counter()
-        ij, d, v = O.query(bx, pts, query_points=pts[:m], num_neighbors=12, exclude_ii=True)
-        tq = time.perf_counter() - t0
-        ij_all, d_all, _ = O.query(bx, pts, num_neighbors=12, exclude_ii=True)
-        t0 = time.perf_counter()
-        O.steinhardt([4, 6, 8, 10, 12], bx, pts, ij_all, d_all, average=True, wl=True, wl_normalize=True)
-        ts = time.perf_counter() - t0
-        per_particle = tq / m + ts / n
-        out["cpu_baseline"] = {"value": 1.0 / per_particle, "unit": "particles/s", "cores": os.cpu_count() or 1,
-                               "kind": "port",
-                               "sample": "kNN query of %d query points (all threads) + FP64 Steinhardt of all %d "
-                                         "particles (1 thread)" % (m, n)}
+        ij, d, _v = O.query(bx, pts, num_neighbors=12, exclude_ii=True, threads=threads)
+        o = O.steinhardt(ls, bx, pts, ij, d, average=True, wl=True, wl_normalize=True, threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "particles/s", "cores": threads, "kind": "port",
+                               "sample": "whole workload: kNN query (k = 12) + FP64 Steinhardt l = 4..12, "
+                                         "average, wl, wl_normalize, one run", "seconds": round(dt, 2)}
+        out["parity"] = steinhardt_parity(st, o, ls)
     return out
+
+
+def steinhardt_parity(st, o, ls, wl=True):
+    """Errors of a computed Steinhardt against the FP64 oracle: Ql (averaged) 1e-5
+    relative; Wl |dw| <= 1e-5 |w| + WL_FLOOR (normalised Wl, absolute floor for
+    values near zero); system order 1e-5 relative (Wl order: + WL_FLOOR)."""
+    ql = np.asarray(st.ql, np.float64).reshape(o["ql_ave"].shape)
+    ref_ql = o["ql_ave"]
+    ok = np.isfinite(ref_ql)
+    ql_rel = float(np.max(np.abs(ql[ok] - ref_ql[ok]) / np.abs(ref_ql[ok])))
+    res = {"particles": int(ql.shape[0]), "ql_max_rel": ql_rel, "ql_tol_rel": 1e-5}
+    good = ql_rel <= 1e-5
+    if wl:
+        w = np.asarray(st.particle_order, np.float64).reshape(o["wl"].shape)
+        ref_w = o["wl"]
+        okw = np.isfinite(ref_w)
+        err = np.abs(w[okw] - ref_w[okw])
+        bound = 1e-5 * np.abs(ref_w[okw]) + WL_FLOOR
+        res.update(wl_max_rel=float(np.max(err / np.abs(ref_w[okw]))),
+                   wl_max_abs=float(np.max(err)), wl_tol="1e-5 |w| + %g" % WL_FLOOR,
+                   wl_within=bool(np.all(err <= bound)),
+                   wl_max_over_bound=float(np.max(err / bound)))
+        per_l = np.max(np.abs(w - ref_w) / (1e-5 * np.abs(ref_w) + WL_FLOOR), axis=0)
+        res["wl_max_over_bound_per_l"] = {str(l): float(x) for l, x in zip(ls, np.atleast_1d(per_l))}
+        good = good and res["wl_within"]
+    order = np.atleast_1d(np.asarray(st.order, np.float64))
+    ref_o = np.atleast_1d(o["order"])
+    oerr = np.abs(order - ref_o)
+    res["order_max_rel"] = float(np.max(oerr / np.abs(ref_o)))
+    good = good and bool(np.all(oerr <= 1e-5 * np.abs(ref_o) + (WL_FLOOR if wl else 0.0)))
+    res["status"] = "within tolerance" if good else "MISMATCH"
+    return res
 
 
 def measure_c4(freud, _lib, steps, warmup, nframes=64):
@@ -389,6 +445,7 @@ def measure_c4(freud, _lib, steps, warmup, nframes=64):
     ref = plain()
     got = batched()
     assert np.array_equal(ref, got), "batched RDF counts differ from the per-frame path"
+    parity, cpu = c4_oracle_check(freud, frames)
     small = measure_small_frames(freud, _lib, max(1, min(steps, 5)), max(1, warmup))
     pairs = int(got.sum())
     k = max(1, min(steps, 5))
@@ -406,7 +463,53 @@ def measure_c4(freud, _lib, steps, warmup, nframes=64):
                         "kernels_ms_per_step": top_batch},
             "speedup_e2e": t_plain / t_batch, "speedup_device": dev_plain / dev_batch if dev_batch else None,
             "small_frames": small,
-            "autotune": _lib.autotune_report().strip().splitlines()[-1:] }
+            "autotune": _lib.autotune_report().strip().splitlines()[-1:],
+            "parity": parity, "cpu_baseline": cpu}
+
+
+def c4_oracle_check(freud, frames, max_frames=8):
+    """Oracle parity on a sample of the trajectory's frames (every triclinic frame,
+    then the smallest and largest cubic ones, up to max_frames): per frame the RDF
+    counts (RDF(200, 4.0) on (box, points), bit-exact) and Steinhardt(6, average)
+    on r_max = 1.5 ball neighbours (1e-5 relative to the FP64 oracle), through the
+    public API on the GPU. The same oracle runs, timed, are the CPU baseline."""
+    from oracle import oracle as O
+
+    tric = [f for f, (b, _) in enumerate(frames) if b.xy != 0.0 or b.xz != 0.0]
+    cubic = sorted((f for f in range(len(frames)) if f not in tric), key=lambda f: len(frames[f][1]))
+    pick = (tric + cubic[:1] + cubic[-1:] + cubic[1:])[:max_frames]
+    threads = os.cpu_count() or 1
+    rdf = freud.density.RDF(200, 4.0)
+    st = freud.order.Steinhardt(6, average=True)
+    rows, cpu_s, pairs, parts = [], 0.0, 0, 0
+    ok = True
+    for f in pick:
+        box, p = frames[f]
+        c_gpu = np.asarray(rdf.compute((box, p)).bin_counts_u64)
+        q_gpu = np.asarray(st.compute((box, p), neighbors={"r_max": 1.5}).ql, np.float64)
+        bx = O.box7(box)
+        t0 = time.perf_counter()
+        c_ref = O.rdf_counts_query(bx, p, 200, 4.0, threads=threads)
+        ij, d, _ = O.query(bx, p, r_max=1.5, exclude_ii=True, threads=threads)
+        o = O.steinhardt([6], bx, p, ij, d, average=True, threads=threads)
+        cpu_s += time.perf_counter() - t0
+        q_ref = o["ql_ave"][:, 0]
+        fin = np.isfinite(q_ref)
+        same_nan = bool(np.array_equal(np.isfinite(q_gpu), fin))
+        q_rel = float(np.max(np.abs(q_gpu[fin] - q_ref[fin]) / np.abs(q_ref[fin]))) if fin.any() else 0.0
+        counts_ok = bool(np.array_equal(c_gpu, c_ref))
+        ok = ok and counts_ok and same_nan and q_rel <= 1e-5
+        pairs += int(c_ref.sum())
+        parts += len(p)
+        rows.append({"frame": int(f), "n": int(len(p)), "triclinic": f in tric, "rdf_counts_equal": counts_ok,
+                     "q6_max_rel": q_rel})
+    parity = {"frames": rows, "status": "within tolerance" if ok else "MISMATCH",
+              "what": "RDF counts bit-exact, averaged q6 within 1e-5 relative of the FP64 oracle, per frame"}
+    cpu = {"value": pairs / cpu_s, "unit": "pair evals/s", "particles_per_s": parts / cpu_s, "cores": threads,
+           "kind": "port", "seconds": round(cpu_s, 2),
+           "sample": "%d of the %d frames (%d points): RDF counts + ball query r_max 1.5 + FP64 Steinhardt "
+                     "l = 6 average" % (len(pick), len(frames), parts)}
+    return parity, cpu
 
 
 def measure_small_frames(freud, _lib, steps, warmup, nframes=1024, seed=44):
@@ -475,6 +578,26 @@ def measure_c5(freud, _lib, steps, warmup, small=False):
     got = np.asarray(st.ql, np.float64)[:m]
     ok = np.isfinite(ref)
     ql_err = float(np.max(np.abs(got[ok] - ref[ok]) / np.abs(ref[ok])))
+    # RDF counts of a spread sample of query points (every 64th point, exclude_ii off
+    # so query i need not be point i) against the oracle; its timed run is the CPU baseline
+    qs = np.ascontiguousarray(pts[::64])
+    r2 = freud.density.RDF(500, 5.0).compute((box, pts), query_points=qs,
+                                               neighbors={"r_max": 5.0, "exclude_ii": False})
+    c_gpu = np.asarray(r2.bin_counts_u64)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    c_ref = O.rdf_counts_query(bx, pts, 500, 5.0, query_points=qs, exclude_ii=False, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    counts_ok = bool(np.array_equal(c_gpu, c_ref))
+    parity = {"rdf_counts_equal": counts_ok, "query_points": int(len(qs)), "pairs": int(c_ref.sum()),
+              "q6_max_rel": ql_err, "q6_particles": int(m),
+              "status": "within tolerance" if counts_ok and ql_err <= 1e-5 else "MISMATCH",
+              "what": "RDF counts of every 64th point as a query point, bit-exact; q6 of the first 16,384 "
+                      "particles within 1e-5 relative of the FP64 oracle"}
+    cpu = {"value": float(c_ref.sum()) / cpu_s, "unit": "pair evals/s", "cores": threads, "kind": "port",
+           "seconds": round(cpu_s, 2),
+           "sample": "RDF(500, 5.0) counts of %d query points (every 64th) against all %d points"
+                     % (len(qs), len(pts))}
     # occupancy skew of the r_max = 5 cell grid (51^3 cells)
     nc = int(L // 5.0)
     idx = np.floor((pts.astype(np.float64) + L / 2) / L * nc).astype(np.int64) % nc
@@ -487,7 +610,8 @@ def measure_c5(freud, _lib, steps, warmup, small=False):
             "rdf_f32_vs_fp64_max_rel": float(np.max(np.abs(g32[nz] - g64[nz]) / g64[nz])),
             "q6_vs_fp64_oracle_max_rel": ql_err, "q6_checked_particles": int(m),
             "cell_occupancy": {"mean": float(occ.mean()), "max": int(occ.max()),
-                               "skew_max_over_mean": float(occ.max() / occ.mean())}}
+                               "skew_max_over_mean": float(occ.max() / occ.mean())},
+            "parity": parity, "cpu_baseline": cpu}
 
 
 def dist_env():
@@ -505,9 +629,9 @@ def run_reference(args):
     vals = []
     desc = cores = None
     for _ in range(args.warmup):
-        cpu_baseline(L, pts, target_s=2.0)
+        cpu_baseline(L, pts, target_s=2.0, sample=0)
     for _ in range(args.steps):
-        v, desc, cores, _dt = cpu_baseline(L, pts, target_s=8.0)
+        v, desc, cores, _dt, _ = cpu_baseline(L, pts, target_s=8.0, sample=0)
         vals.append(v)
     value = statistics.median(vals)
     # the whole step (every query point) at the sampled rate: 108 bonds per point on
@@ -587,6 +711,7 @@ def main():
 
     import freud_gb300 as freud
 
+    bad = []
     lib = _lib.lib
     # one dedicated stream for the library, the L2 flush and the timing events
     stream = torch.cuda.Stream()
@@ -651,36 +776,25 @@ def main():
     ms_per_step = total_ms / args.steps
     value = bonds * world * args.steps / (total_ms / 1e3)
 
-    # roofline of the dominant kernel
+    # roofline: the NeighborList build (every kernel of the step but the RDF over the
+    # finished list) against its algorithmic bytes, 12 N (positions read) + 24 B
+    # ((i, j) 8 B, distance 4 B, vector 12 B written per bond; weights are lazy)
     peak, peak_kind = read_peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else (None, (0, 0.0))
-    dom_name, (dom_n, dom_ms) = dom
-    per_launch_ms = dom_ms / max(dom_n, 1)
-    if dom_name is not None and ("EMIT" in dom_name or "emit" in dom_name):
-        alg_bytes = 12.0 * n + 24.0 * bonds  # positions read + (i,j) 8 B + distance 4 B + vector 12 B per bond
-        alg_desc = "12*N + 24*B (positions read; (i,j), distance, vector written; weights are lazy)"
-    elif dom_name is not None and "COUNT" in dom_name:
-        alg_bytes = 12.0 * n + 4.0 * n
-        alg_desc = "12*N + 4*N (positions read, counts written)"
-    elif dom_name is not None and "hist" in dom_name:
-        alg_bytes = 4.0 * bonds
-        alg_desc = "4*B (distances read)"
-    else:
-        alg_bytes = 12.0 * n
-        alg_desc = "12*N"
-    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
-    # the whole NeighborList build (grid + scan + write passes) against its output bytes
-    build_names = ("k_assign", "k_scatter", "k_sort_cells", "k_tile_scan", "k_tile_sums", "k_cell_scan<COUNT>",
-                   "k_cell_emit", "k_seg_from_offsets")
-    build_ms = sum(v[1] for k, v in prof.items() if k.startswith(build_names)) / max(args.steps, 1)
+    rdf_names = ("k_hist_distances",)
+    build = {k: v for k, v in prof.items() if not k.startswith(rdf_names)}
+    build_ms = sum(v[1] for v in build.values()) / max(args.steps, 1)
     build_bytes = 12.0 * n + 24.0 * bonds
     build_gbs = build_bytes / (build_ms / 1e3) / 1e9 if build_ms > 0 else 0.0
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(dom_name)
+            tj = json.load(f)
+        per_kernel = [tj.get(k) for k in build]
+        if per_kernel and all(x is not None for x in per_kernel):
+            traffic = float(sum(per_kernel))
     except (OSError, ValueError):
         pass
+    dom_name, (dom_n, dom_ms) = max(prof.items(), key=lambda kv: kv[1][1]) if prof else (None, (0, 0.0))
 
     # ---- e2e: public Python API with host (pinned) buffers --------------------------
     pinned = torch.from_numpy(pts_host).pin_memory().numpy()
@@ -699,12 +813,49 @@ def main():
         del lc, nlist, r, g
     e2e_value = bonds * world / statistics.median(e2e_times)
 
-    # ---- CPU baseline (rank 0, N=1 only) ---------------------------------------------
+    # ---- e2e with the NeighborList read back: nlist[:], distances, vectors as a freud
+    # user reads them (24 B per bond device -> host, weights filled on the host)
+    rb_times = []
+    gpu_list = None
+    for it in range(1 + max(1, min(args.steps, 3))):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lc = freud.locality.LinkCell(box, pinned, 3.0)
+        nlist = lc.query(pinned, {"r_max": 3.0, "exclude_ii": True}).toNeighborList()
+        r = freud.density.RDF(300, 3.0).compute(lc, neighbors=nlist)
+        counts = r.bin_counts
+        ij, d, v = nlist[:], nlist.distances, nlist.vectors
+        t1 = time.perf_counter()
+        if it >= 1:
+            rb_times.append(t1 - t0)
+        gpu_list = (ij, d, v, counts)
+        del lc, nlist, r
+    rb_value = bonds * world / statistics.median(rb_times)
+
+    # ---- CPU baseline (rank 0, N=1 only): the oracle over the whole workload, whose
+    # list is also the parity reference (identical neighbour sets, distances, vectors
+    # and RDF counts, in the reference's order) ------------------------------------------
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, desc, cores, dt = cpu_baseline(L, pts_host)
+        v, desc, cores, dt, ref = cpu_baseline(L, pts_host)
         cpu = {"value": v, "unit": "pair evals/s", "cores": cores, "kind": "port", "sample": desc,
                "seconds": round(dt, 2)}
+        ij, d, vv, counts = gpu_list
+        rij, rd, rv, rcounts = ref
+        same_n = len(ij) == len(rij)
+        checks = {"bonds_gpu": int(len(ij)), "bonds_oracle": int(len(rij)),
+                  "ij": bool(same_n and np.array_equal(ij, rij)),
+                  "distances": bool(same_n and np.array_equal(d.view(np.uint32), rd.view(np.uint32))),
+                  "vectors": bool(same_n and np.array_equal(vv.view(np.uint32), rv.view(np.uint32))),
+                  "rdf_counts": bool(np.array_equal(np.asarray(counts, np.uint64), rcounts))}
+        ok = all(checks[k] for k in ("ij", "distances", "vectors", "rdf_counts"))
+        parity = dict(checks, status="bit-exact" if ok else "MISMATCH",
+                      what="full NeighborList (every query point) and RDF counts, GPU through the public API "
+                           "vs the CPU oracle, bitwise")
+        del ref, rij, rd, rv
+    del gpu_list
 
     # ---- the other workloads (rank 0, N=1): plain RDF, Steinhardt, batched frames, stress
     secondary = None
@@ -733,32 +884,37 @@ def main():
             "config": {"workload": WORKLOAD if args.n_side == 102 else "%s_n%d" % (WORKLOAD, args.n_side), "n_points": n, "box_L": L, "cell_width": 3.0, "r_max": 3.0,
                        "bins": 300, "bonds_per_step": bonds, "l2": "flushed between steps (258 MB write)",
                        "parallelism": "replicas" if world > 1 else "single"},
-            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
-                         "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
-                         "algorithmic_bytes": alg_desc, "launch_ms": per_launch_ms,
-                         "note": ("the scan pass reads positions and writes counts only (its masks and "
-                                  "sorted candidate lists stay in L2): HBM is not what bounds it; ncu shows "
-                                  "it instruction-bound (66% issue-active, "
-                                  "profiles/k_cell_scan_k_cell_emit_k_hist_distances_262k.md); "
-                                  "roofline_build gives the whole NeighborList build against its output bytes")
-                         if dom_name is not None and "COUNT" in dom_name else None},
-            "roofline_build": {"bound": "hbm", "what": "NeighborList build: grid + scan + write passes",
-                               "achieved": build_gbs, "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
-                               "algorithmic_bytes": "12*N + 24*B", "ms_per_step": build_ms},
+            "roofline": {"bound": "hbm", "kernel": "NeighborList build: " + ", ".join(sorted(build)),
+                         "achieved": build_gbs, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+                         "frac": build_gbs / peak, "traffic": traffic, "algorithmic_bytes_per_launch": build_bytes,
+                         "algorithmic_bytes": "12*N + 24*B (positions read; (i,j), distance, vector written per "
+                                              "bond; weights are lazy)",
+                         "launch_ms": build_ms, "dominant_kernel": dom_name,
+                         "dominant_kernel_ms": dom_ms / max(dom_n, 1)},
             "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in sorted(prof.items())},
             "secondary": secondary,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "pair evals/s", "h2d_bytes_per_step": int(12 * n),
                     "d2h_bytes_per_step": int(300 * 4)},
+            "e2e_nlist_readback": {"value": rb_value, "unit": "pair evals/s", "h2d_bytes_per_step": int(12 * n),
+                                   "d2h_bytes_per_step": int(24 * bonds + 300 * 4),
+                                   "what": "the e2e step plus nlist[:], distances and vectors read to host"},
+            "parity": {"large_n_nlist_rdf": parity},
             "gpu_launches": int(launches),
             "clocks": clk,
         }
+        if secondary:
+            for k, sec in secondary.items():
+                if isinstance(sec, dict) and "parity" in sec:
+                    line["parity"][k] = sec["parity"]
         print(json.dumps(line), flush=True)
+        bad = [k for k, v in line["parity"].items() if v is not None and v.get("status") not in PARITY_OK]
+        if bad:
+            print("parity check failed for: " + ", ".join(bad), file=sys.stderr)
     lib.fg_rdf_destroy(rdf)
     if world > 1:
         torch.distributed.destroy_process_group()
-    return 0
+    return 1 if rank == 0 and bad else 0
 
 
 if __name__ == "__main__":
