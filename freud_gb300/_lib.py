@@ -119,6 +119,7 @@ SIGNATURES = {
     "fg_batch_set_config": [i32, i32, i32],
     "fg_autotune_report": [ctypes.c_char_p, ctypes.c_size_t],
     "fg_set_graphs": [i32],
+    "fg_set_count_kernel": [i32],
     "fg_check_division": [u64, u64, pu64, P],
 }
 _RESTYPES = {"fg_last_error": ctypes.c_char_p, "fg_version": ctypes.c_int}
@@ -182,6 +183,12 @@ def set_batch_config(shell=0, warps=8, copies=1):
 
 def set_graphs(enable):
     check(lib.fg_set_graphs(int(bool(enable))))
+
+
+def set_count_kernel(which):
+    """0: automatic choice of the NeighborList count pass; 1: block per cell with
+    lanes over candidates everywhere (both give the same lists)."""
+    check(lib.fg_set_count_kernel(int(which)))
 
 
 def set_stream(stream_ptr):

@@ -755,6 +755,10 @@ void make_ghost_query_set(fg_nq* nq, const GridEntry& g, const float* dq, uint32
     qs.qg = view(qs.own);
 }
 
+// Count-pass kernel choice (fg_set_count_kernel): 0 automatic, 1 block-per-cell
+// lanes over candidates only.
+static int g_count_kernel = 0;
+
 // Ball query -> NeighborList in reference order (count, scan, emit).
 void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a, int by_distance, fg_nlist& out)
 {
@@ -815,7 +819,17 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     reset_dev_err();
     uint32_t n_over = nqp;
     const uint32_t* list = nullptr;
-    if (cellwise)
+    if (cellwise && g_count_kernel == 0 && arith == ARITH_WRAP && pf.out2 > 0.0f && pf.cull2 > 0.0f &&
+        cap == CELL_CAP)
+    {
+        launch_nl_count(nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, pf.cull2, counts.as<uint32_t>(),
+                        gmask.as<uint32_t>(), gsorted.as<uint32_t>(), gtotal.as<uint32_t>(), over.as<uint32_t>(),
+                        over_n.as<uint32_t>(), s, nq->n);
+        FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        sync();
+        list = over.as<uint32_t>();
+    }
+    else if (cellwise)
     {
         // ghost grids hold copies of point indices; any index fits the same bound
         launch_cell_scan(0, nq->dbox, view(g), qs.qg, p, pf.out2, pf.in2, pf.cull2, counts.as<uint32_t>(),
@@ -3550,6 +3564,15 @@ fg_status fg_check_division(uint64_t samples, uint64_t seed, uint64_t* mismatche
             example[0] = hex[0];
             example[1] = hex[1];
         }
+    });
+}
+
+fg_status fg_set_count_kernel(int which)
+{
+    return guard([&] {
+        if (which != 0 && which != 1)
+            value_error("count kernel must be 0 (automatic) or 1 (block per cell, lanes over candidates)");
+        g_count_kernel = which;
     });
 }
 

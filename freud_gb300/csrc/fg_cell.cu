@@ -832,6 +832,421 @@ __global__ void __launch_bounds__(STHREADS, MODE == SM_COUNT ? (CAP <= 1024 ? 5 
     }
 }
 
+// ---------------------------------------------------------------------------
+// NeighborList count pass with lanes over queries (wrap arithmetic under the
+// cell-shift prefilter). A block of NLW warps takes one home cell:
+//  1. bounds of the cell's queries in cell-shifted coordinates;
+//  2. the stencil's candidates, a warp per stencil item (cell), culled against
+//     those bounds: a first sweep counts the kept candidates of each item, a
+//     second gives each its compact position t (items keep their order, so the
+//     kept candidates still form one index-sorted run per item) with the key
+//     (point index, t) and slot << 5 | wrap;
+//  3. the runs merged into point-index order by merge path: a thread owns a
+//     fixed range of output positions, finds where it starts in the two runs
+//     being merged by a binary search on the cross diagonal and merges it
+//     sequentially (about T / threads + log T steps per thread and level); the
+//     sorted candidates' prefilter positions and indices are then gathered;
+//  4. the sweep: lane = query, candidates broadcast from shared memory in index
+//     order, one 32-bit word of acceptance bits per 32 candidates kept in
+//     registers, so no per-pair ballot. Pairs inside r_max - delta are accepted,
+//     pairs beyond r_max + delta rejected and the few in between collected in a
+//     second word and tested exactly (box.wrap) once per 32 candidates. The
+//     pair of a query with its own index (exclude_ii) is found once per query by
+//     a binary search in the sorted keys (each point appears once in a stencil
+//     of distinct cells) and its bit cleared.
+// The outputs are those of the count mode of k_cell_scan: counts[query index],
+// gmask rows (sorted query position x CELL_CHUNKS words), gsorted[cell][e] =
+// slot << 5 | wrap of sorted candidate e, gtotal[cell]; cells over the capacity
+// hand their queries to the warp-per-query kernels through overflow.
+constexpr int NLW = 4; // warps per block
+constexpr int NLT = NLW * 32;
+
+// Prefilter position of a candidate: p moved into the box by its integer image
+// and by the lattice shift w of its cell's wrap (an approximation within the
+// prefilter's margin; both staging sweeps use it identically).
+__device__ __forceinline__ float3 nl_shifted(const DevBox& b, float4 p, const float* w)
+{
+    const int pim = __float_as_int(p.w);
+    if (pim != 0)
+    {
+        const float3 n = shifted(b, make_float4(0.f, 0.f, 0.f, 0.f), -img_ax(pim, 0), -img_ax(pim, 1),
+                                 -img_ax(pim, 2));
+        p.x += n.x;
+        p.y += n.y;
+        p.z += n.z;
+    }
+    return make_float3(p.x + w[0], p.y + w[1], p.z + w[2]);
+}
+
+template<typename K> struct NlShared
+{
+    K ka[CELL_CAP];
+    K kb[CELL_CAP];
+    uint32_t sw[CELL_CAP];   // slot << 5 | wrap, by compact position
+    float4 rec[CELL_CAP];    // sorted candidates: prefilter position, point index (bits)
+    uint32_t cnt[CELL_CAP];  // bond count per query of the cell
+    uint32_t kc[32];         // kept candidates per item
+    uint32_t ro[33];         // kept-run offsets (runs past the items are empty)
+    float wsh[32][3];        // lattice shift of each cell wrap code (0 .. 26)
+    float qb[NLW][6];
+    Items it;
+    int over;
+};
+
+// One merge-path level: runs are groups of G consecutive items (offsets ro,
+// ro[32] = total); pairs of groups (2k, 2k + 1) are merged from src into dst.
+// This thread writes outputs [e0, e1). The output loop has no branches: the
+// taken side's next key is reloaded through a selected index (clamped into the
+// array; a key read past a run's end is never selected).
+template<typename K>
+__device__ __forceinline__ void nl_merge_level(const K* __restrict__ src, K* __restrict__ dst,
+                                               const uint32_t* __restrict__ ro, int G, uint32_t e0, uint32_t e1)
+{
+    if (e0 >= e1)
+        return;
+    const int npairs = 16 / G;
+    // last pair starting at or before e0 (it contains e0: the next one starts after it)
+    int k = 0;
+#pragma unroll
+    for (int step = 8; step >= 1; step >>= 1)
+    {
+        if (k + step < npairs && ro[2 * (k + step) * G] <= e0)
+            k += step;
+    }
+    uint32_t e = e0;
+    while (e < e1)
+    {
+        const uint32_t a0 = ro[2 * k * G];
+        const uint32_t a1 = ro[(2 * k + 1) * G];
+        const uint32_t b1 = ro[(2 * k + 2) * G];
+        const uint32_t na = a1 - a0, nb = b1 - a1;
+        const uint32_t d = e - a0;
+        // i = number of A keys among the first d merged keys (keys are distinct)
+        uint32_t lo = d > nb ? d - nb : 0u, hi = min(d, na);
+        while (lo < hi)
+        {
+            const uint32_t mid = (lo + hi) >> 1;
+            const bool before = src[a0 + mid] < src[a1 + d - 1 - mid];
+            lo = before ? mid + 1 : lo;
+            hi = before ? hi : mid;
+        }
+        uint32_t i = lo, j = d - lo;
+        K va = src[min(a0 + i, static_cast<uint32_t>(CELL_CAP - 1))];
+        K vb = src[min(a1 + j, static_cast<uint32_t>(CELL_CAP - 1))];
+        const uint32_t stop = min(e1, b1);
+        for (; e < stop; ++e)
+        {
+            const bool ta = i < na && (j >= nb || va < vb);
+            dst[e] = ta ? va : vb;
+            i += ta ? 1u : 0u;
+            j += ta ? 0u : 1u;
+            const K nv = src[min(ta ? a0 + i : a1 + j, static_cast<uint32_t>(CELL_CAP - 1))];
+            va = ta ? nv : va;
+            vb = ta ? vb : nv;
+        }
+        ++k;
+    }
+}
+
+template<typename K>
+__global__ void __launch_bounds__(NLT, 6)
+    k_nl_count(DevBox b, DevGrid g, DevGrid qg, BallParams p, float pre_out2, float pre_in2, float cull2,
+               uint32_t* __restrict__ counts, uint32_t* __restrict__ gmask, uint32_t* __restrict__ gsorted,
+               uint32_t* __restrict__ gtotal, uint32_t* __restrict__ overflow, uint32_t* __restrict__ overflow_n)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NlShared<K>& S = *reinterpret_cast<NlShared<K>*>(smem_raw);
+    using KT = KeyTraits<K, 10>;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nitems = b.is2d ? 9 : 27;
+
+    for (int c = blockIdx.x; c < qg.ncell; c += gridDim.x)
+    {
+        const uint32_t q0 = qg.start[c];
+        const uint32_t nqc = qg.start[c + 1] - q0;
+        if (nqc == 0)
+            continue;
+        // ---- 1. bounds of the cell's queries (cell-shifted) and the stencil items
+        {
+            float lo[3] = {3e30f, 3e30f, 3e30f}, hi[3] = {-3e30f, -3e30f, -3e30f};
+            for (uint32_t k = tid; k < nqc; k += NLT)
+            {
+                const float4 q = qg.cpos[q0 + k];
+                const int qim = __float_as_int(q.w);
+                const float3 qs = shifted(b, q, -img_ax(qim, 0), -img_ax(qim, 1), -img_ax(qim, 2));
+                lo[0] = fminf(lo[0], qs.x);
+                lo[1] = fminf(lo[1], qs.y);
+                lo[2] = fminf(lo[2], qs.z);
+                hi[0] = fmaxf(hi[0], qs.x);
+                hi[1] = fmaxf(hi[1], qs.y);
+                hi[2] = fmaxf(hi[2], qs.z);
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    lo[a] = fminf(lo[a], __shfl_xor_sync(FULL, lo[a], o));
+                    hi[a] = fmaxf(hi[a], __shfl_xor_sync(FULL, hi[a], o));
+                }
+            }
+            if (lane == 0)
+            {
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                {
+                    S.qb[warp][a] = lo[a];
+                    S.qb[warp][3 + a] = hi[a];
+                }
+            }
+            if (warp == 0)
+            {
+                cell_items(b, g, ARITH_WRAP, c, S.it, lane);
+                const float3 w = shifted(b, make_float4(0.f, 0.f, 0.f, 0.f), lane % 3 - 1, (lane / 3) % 3 - 1,
+                                         lane / 9 - 1);
+                S.wsh[lane][0] = w.x;
+                S.wsh[lane][1] = w.y;
+                S.wsh[lane][2] = w.z;
+            }
+        }
+        __syncthreads();
+        float qf[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+        {
+            float v = S.qb[0][a];
+            for (int w = 1; w < NLW; ++w)
+                v = a < 3 ? fminf(v, S.qb[w][a]) : fmaxf(v, S.qb[w][a]);
+            qf[a] = v;
+        }
+        const bool too_big = S.it.maxrun > static_cast<uint32_t>(SORT_CELL_MAX);
+        // ---- 2. staging: a warp per item; kept = within the cull radius of the bounds
+        auto cand = [&](int s, uint32_t k, uint32_t& slot, int& wr, float4& pp) {
+            slot = S.it.start[s] + k;
+            wr = S.it.wrap[s];
+            pp = g.cpos[slot];
+            const float3 sp = nl_shifted(b, pp, S.wsh[wr]);
+            const float gx = fmaxf(fmaxf(qf[0] - sp.x, sp.x - qf[3]), 0.f);
+            const float gy = fmaxf(fmaxf(qf[1] - sp.y, sp.y - qf[4]), 0.f);
+            const float gz = fmaxf(fmaxf(qf[2] - sp.z, sp.z - qf[5]), 0.f);
+            return gx * gx + gy * gy + gz * gz <= cull2;
+        };
+        if (!too_big)
+        {
+            for (int s = warp; s < nitems; s += NLW)
+            {
+                const uint32_t n_s = S.it.off[s + 1] - S.it.off[s];
+                uint32_t kept = 0;
+                for (uint32_t k0 = 0; k0 < n_s; k0 += 32)
+                {
+                    bool keep = false;
+                    if (k0 + lane < n_s)
+                    {
+                        uint32_t slot;
+                        int wr;
+                        float4 pp;
+                        keep = cand(s, k0 + lane, slot, wr, pp);
+                    }
+                    kept += __popc(__ballot_sync(FULL, keep));
+                }
+                if (lane == 0)
+                    S.kc[s] = kept;
+            }
+        }
+        for (uint32_t k = tid; k < nqc && k < static_cast<uint32_t>(CELL_CAP); k += NLT)
+            S.cnt[k] = 0;
+        __syncthreads();
+        if (warp == 0)
+        {
+            const uint32_t v = (!too_big && lane < nitems) ? S.kc[lane] : 0u;
+            uint32_t incl = v;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t u = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o)
+                    incl += u;
+            }
+            S.ro[lane] = incl - v;
+            if (lane == 31)
+            {
+                S.ro[32] = incl;
+                S.over = too_big || incl > static_cast<uint32_t>(CELL_CAP);
+            }
+        }
+        __syncthreads();
+        if (S.over)
+        {
+            for (uint32_t k = tid; k < nqc; k += NLT)
+                overflow[atomicAdd(overflow_n, 1u)] = q0 + k;
+            if (tid == 0)
+                gtotal[c] = 0xffffffffu;
+            __syncthreads();
+            continue;
+        }
+        const uint32_t T = S.ro[32];
+        for (int s = warp; s < nitems; s += NLW)
+        {
+            const uint32_t n_s = S.it.off[s + 1] - S.it.off[s];
+            uint32_t pos = S.ro[s];
+            for (uint32_t k0 = 0; k0 < n_s; k0 += 32)
+            {
+                bool keep = false;
+                uint32_t slot = 0;
+                int wr = 0;
+                float4 pp;
+                if (k0 + lane < n_s)
+                    keep = cand(s, k0 + lane, slot, wr, pp);
+                const unsigned kb = __ballot_sync(FULL, keep);
+                if (keep)
+                {
+                    const uint32_t t = pos + __popc(kb & lt);
+                    S.ka[t] = KT::make(g.cidx[slot], t);
+                    S.sw[t] = (slot << 5) | static_cast<uint32_t>(wr);
+                }
+                pos += __popc(kb);
+            }
+        }
+        __syncthreads();
+        // ---- 3. merge the runs into point-index order, gather the sorted candidates
+        K* src = S.ka;
+        K* dst = S.kb;
+        {
+            const uint32_t per = (T + NLT - 1) / NLT;
+            const uint32_t e0 = min(T, per * tid);
+            const uint32_t e1 = min(T, e0 + per);
+            for (int G = 1; G < nitems; G <<= 1)
+            {
+                nl_merge_level(src, dst, S.ro, G, e0, e1);
+                __syncthreads();
+                K* tmp = src;
+                src = dst;
+                dst = tmp;
+            }
+        }
+        const K* order = src;
+        for (uint32_t e = tid; e < T; e += NLT)
+        {
+            const K key = order[e];
+            const uint32_t sw = S.sw[KT::pos(key)];
+            gsorted[static_cast<size_t>(c) * CELL_CAP + e] = sw;
+            const float4 pp = g.cpos[sw >> 5];
+            const float3 sp = nl_shifted(b, pp, S.wsh[sw & 31u]);
+            S.rec[e] = make_float4(sp.x, sp.y, sp.z, __uint_as_float(KT::index(key)));
+        }
+        if (tid == 0)
+            gtotal[c] = T;
+        __syncthreads();
+        // ---- 4. sweep: lane = query, candidates in index order
+        const uint32_t nchunks = (T + 31) / 32;
+        const uint32_t ngroups = (nqc + 31) / 32;
+        uint32_t cur_group = 0xffffffffu;
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 qs = make_float3(3e30f, 3e30f, 3e30f);
+        uint32_t self_e = 0xffffffffu; // sorted position of the query's own index
+        for (uint32_t item = warp; item < ngroups * nchunks; item += NLW)
+        {
+            const uint32_t gq = item / nchunks;
+            const uint32_t ch = item - gq * nchunks;
+            const uint32_t qk = gq * 32 + lane;
+            const bool live = qk < nqc;
+            if (gq != cur_group)
+            {
+                cur_group = gq;
+                qs = make_float3(3e30f, 3e30f, 3e30f);
+                self_e = 0xffffffffu;
+                if (live)
+                {
+                    q = qg.cpos[q0 + qk];
+                    const uint32_t qi = qg.cidx[q0 + qk];
+                    const int qim = __float_as_int(q.w);
+                    qs = shifted(b, q, -img_ax(qim, 0), -img_ax(qim, 1), -img_ax(qim, 2));
+                    if (p.exclude_ii)
+                    {
+                        // first sorted key with index >= qi
+                        uint32_t lo = 0, hi = T;
+                        const K kq = KT::make(qi, 0u);
+                        while (lo < hi)
+                        {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (order[mid] < kq)
+                                lo = mid + 1;
+                            else
+                                hi = mid;
+                        }
+                        if (lo < T && KT::index(order[lo]) == qi)
+                            self_e = lo;
+                    }
+                }
+            }
+            const uint32_t e0 = ch * 32;
+            uint32_t word = 0, und = 0;
+            const float4* rc = S.rec + e0;
+            if (e0 + 32 <= T)
+            {
+#pragma unroll
+                for (int bb = 0; bb < 32; ++bb)
+                {
+                    const float4 r = rc[bb];
+                    const float dx = r.x - qs.x, dy = r.y - qs.y, dz = r.z - qs.z;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 < pre_in2)
+                        word |= 1u << bb;
+                    if (d2 <= pre_out2)
+                        und |= 1u << bb;
+                }
+            }
+            else
+            {
+                const int ne = static_cast<int>(T - e0);
+                for (int bb = 0; bb < ne; ++bb)
+                {
+                    const float4 r = rc[bb];
+                    const float dx = r.x - qs.x, dy = r.y - qs.y, dz = r.z - qs.z;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 < pre_in2)
+                        word |= 1u << bb;
+                    if (d2 <= pre_out2)
+                        und |= 1u << bb;
+                }
+            }
+            if (self_e - e0 < 32u)
+            {
+                word &= ~(1u << (self_e - e0));
+                und &= ~(1u << (self_e - e0));
+            }
+            und &= ~word;
+            // pairs between the two prefilter radii: the exact test
+            while (__any_sync(FULL, und != 0))
+            {
+                if (und != 0)
+                {
+                    const int bb = __ffs(und) - 1;
+                    und &= und - 1u;
+                    const uint32_t sw = gsorted[static_cast<size_t>(c) * CELL_CAP + e0 + bb];
+                    const float4 pp = g.cpos[sw >> 5];
+                    float rx, ry, rz;
+                    box_wrap(b, __fsub_rn(pp.x, q.x), __fsub_rn(pp.y, q.y), __fsub_rn(pp.z, q.z), rx, ry, rz);
+                    const float rsq = dot3(rx, ry, rz);
+                    if (rsq < p.r_max_sq && rsq >= p.r_min_sq)
+                        word |= 1u << bb;
+                }
+            }
+            if (live)
+            {
+                gmask[static_cast<size_t>(q0 + qk) * CELL_CHUNKS + ch] = word;
+                atomicAdd(&S.cnt[qk], static_cast<uint32_t>(__popc(word)));
+            }
+        }
+        __syncthreads();
+        for (uint32_t k = tid; k < nqc; k += NLT)
+            counts[qg.cidx[q0 + k]] = S.cnt[k];
+        __syncthreads();
+    }
+}
+
 // Position of the k-th (from 0) set bit of w; k < popc(w).
 __device__ __forceinline__ uint32_t kth_set_bit(uint32_t w, uint32_t k)
 {
@@ -859,7 +1274,7 @@ __device__ __forceinline__ uint32_t kth_set_bit(uint32_t w, uint32_t k)
 // each round from the prefix sums and the k-th set bit of the chunk's mask.
 // Candidates are read through the cell's sorted list (gsorted) from L1/L2, where
 // the cell's other queries keep them.
-template<int CAP>
+template<int CAP, int ARITH>
 __global__ void __launch_bounds__(ETHREADS, 4)
     k_cell_emit(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
                 const uint32_t* __restrict__ gsorted, const uint32_t* __restrict__ gtotal,
@@ -967,7 +1382,7 @@ __global__ void __launch_bounds__(ETHREADS, 4)
                 // store bond bb from its candidate (entry ent of the sorted list, position pp, index jj)
                 auto store_bond = [&](uint32_t bb, uint32_t ent, float4 pp, uint32_t jj) {
                     float rx, ry, rz;
-                    exact_vec(b, img_s, p.arith, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
+                    exact_vec(b, img_s, ARITH, q, qimg, pp, static_cast<int>(ent & 31u), rx, ry, rz);
                     const uint64_t o = out + bb;
                     ij[o] = make_uint2(qi, jj);
                     dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
@@ -1165,6 +1580,33 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
         box, g, qg, p, pre_out2, 0.0f, 0.0f, counts, gmask, gsorted, gtotal, overflow, overflow_n, h, hist);
 }
 
+void launch_nl_count(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_out2,
+                     float pre_in2, float cull2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
+                     uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n, cudaStream_t s, uint32_t n_points)
+{
+    auto go = [&](auto kernel, size_t smem, bool& done) {
+        configure(kernel, smem, done);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, NLT, smem);
+        const int want = std::max(per_sm, 1) * sm_count_cell();
+        const int blocks = qg.ncell < want ? std::max(qg.ncell, 1) : want;
+        ProfScope prof_("k_nl_count", s);
+        kernel<<<blocks, NLT, smem, s>>>(box, g, qg, p, pre_out2, pre_in2, cull2, counts, gmask, gsorted, gtotal,
+                                         overflow, overflow_n);
+    };
+    // 32-bit keys (point index << 10 | compact position) below 2^22 points
+    if (n_points <= (1u << 22))
+    {
+        static bool done = false;
+        go(k_nl_count<unsigned int>, sizeof(NlShared<unsigned int>), done);
+    }
+    else
+    {
+        static bool done = false;
+        go(k_nl_count<unsigned long long>, sizeof(NlShared<unsigned long long>), done);
+    }
+}
+
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
                       uint2* ij, float* dist, float* vec, cudaStream_t s, int cap)
@@ -1189,10 +1631,26 @@ void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, co
         kernel<<<blocks, ETHREADS, 0, s>>>(box, g, qg, p, gmask, gsorted, gtotal, offsets, ij, dist, vec, p.nq,
                                            per_item);
     };
+    // the pair arithmetic is a template parameter, so the per-bond vector has no
+    // run-time branch on it
     if (cap > 1024)
-        go(k_cell_emit<4096>);
+    {
+        if (p.arith == ARITH_WRAP)
+            go(k_cell_emit<4096, ARITH_WRAP>);
+        else if (p.arith == ARITH_GHOST)
+            go(k_cell_emit<4096, ARITH_GHOST>);
+        else
+            go(k_cell_emit<4096, ARITH_AABB>);
+    }
     else
-        go(k_cell_emit<1024>);
+    {
+        if (p.arith == ARITH_WRAP)
+            go(k_cell_emit<1024, ARITH_WRAP>);
+        else if (p.arith == ARITH_GHOST)
+            go(k_cell_emit<1024, ARITH_GHOST>);
+        else
+            go(k_cell_emit<1024, ARITH_AABB>);
+    }
 }
 
 } // namespace fg

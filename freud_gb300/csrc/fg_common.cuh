@@ -77,21 +77,29 @@ __device__ __forceinline__ float fmod1(float a)
     return __fsub_rn(a, truncf(a));
 }
 
-// a / b rounded to nearest even, given y = RN(1 / b), for a / b normal or zero
-// (the box arithmetic divides coordinates by box lengths: no overflow or
-// underflow). q0 = RN(a y) is within 1.5 ulp of a / b; one correction
-// q1 = RN(q0 + (a - b q0) y) (fused, so the residual enters unrounded) brings it
-// within one ulp; from a q1 within one ulp and y = RN(1 / b), Markstein's theorem
-// (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of
-// Floating-Point Arithmetic, the theorem on correcting a quotient with the exact
-// FMA remainder) makes q1 + (a - b q1) y, rounded once, the correctly rounded
-// quotient. a = +-0 returns q0, which carries the sign of the exact quotient.
-__device__ __forceinline__ float div_rn_recip(float a, float b, float y)
+// a / b rounded to nearest even, given y = RN(1 / b), for a != -0 and a / b
+// normal or zero (the box arithmetic divides coordinates by box lengths: no
+// overflow or underflow). q0 = RN(a y) is within 1.5 ulp of a / b; one
+// correction q1 = RN(q0 + (a - b q0) y) (fused, so the residual enters
+// unrounded) brings it within one ulp; from a q1 within one ulp and
+// y = RN(1 / b), Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34(1),
+// 1990; Muller et al., Handbook of Floating-Point Arithmetic, the theorem on
+// correcting a quotient with the exact FMA remainder) makes q1 + (a - b q1) y,
+// rounded once, the correctly rounded quotient. a = +0 gives +0 at every step.
+// The box arithmetic divides v - lo with lo != 0, which is never -0 in
+// round-to-nearest (x - y is -0 only for x = -0, y = +0).
+__device__ __forceinline__ float div_rn_recip_nz(float a, float b, float y)
 {
     const float q0 = __fmul_rn(a, y);
     const float q1 = __fmaf_rn(__fmaf_rn(-q0, b, a), y, q0);
-    const float q2 = __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
-    return a == 0.0f ? q0 : q2;
+    return __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
+}
+
+// The same for any a: a = -0 returns a * y = -0 (the corrections would turn it
+// into +0).
+__device__ __forceinline__ float div_rn_recip(float a, float b, float y)
+{
+    return a == 0.0f ? __fmul_rn(a, y) : div_rn_recip_nz(a, b, y);
 }
 
 // util::modulusPositive(a, 1.0f) = fmod(fmod(a, 1) + 1, 1), utils.h:29-32
@@ -103,7 +111,8 @@ __device__ __forceinline__ float mod_pos1(float a)
 // Box::makeFractional, Box.h:243-255. In a box without tilt the tilt terms are
 // +-0 and subtracting them changes nothing (for finite v): dx = v - lo is never
 // -0 because lo != 0, so they are skipped there. Divisions by the box lengths are
-// correctly rounded (div_rn_recip), so the quotients equal IEEE division's.
+// correctly rounded (div_rn_recip_nz: v - lo is never -0), so the quotients equal
+// IEEE division's.
 __device__ __forceinline__ void make_fractional(const DevBox& b, float vx, float vy, float vz, float& fx,
                                                 float& fy, float& fz)
 {
@@ -116,9 +125,9 @@ __device__ __forceinline__ void make_fractional(const DevBox& b, float vx, float
         dx = __fsub_rn(dx, __fadd_rn(__fmul_rn(t2, vz), __fmul_rn(b.xy, vy)));
         dy = __fsub_rn(dy, __fmul_rn(b.yz, vz));
     }
-    fx = div_rn_recip(dx, b.L[0], b.rcp[0]);
-    fy = div_rn_recip(dy, b.L[1], b.rcp[1]);
-    fz = b.is2d ? 0.0f : div_rn_recip(dz, b.L[2], b.rcp[2]);
+    fx = div_rn_recip_nz(dx, b.L[0], b.rcp[0]);
+    fy = div_rn_recip_nz(dy, b.L[1], b.rcp[1]);
+    fz = b.is2d ? 0.0f : div_rn_recip_nz(dz, b.L[2], b.rcp[2]);
 }
 
 // Box::makeAbsolute, Box.h:212-222 (tilt terms skipped in a box without tilt:

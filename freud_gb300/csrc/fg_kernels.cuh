@@ -146,6 +146,12 @@ void launch_cell_scan(int hist_mode, const DevBox& box, const DevGrid& g, const 
                       uint32_t* gsorted, uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n,
                       const HistParams& h, unsigned long long* hist, cudaStream_t s,
                       uint32_t n_points = 0xffffffffu, int cap = CELL_CAP);
+// Count pass with lanes over queries (same outputs as the count mode of
+// launch_cell_scan, capacity CELL_CAP): wrap arithmetic with the prefilter on
+// (pre_out2 > 0) and the per-cell cull (cull2 > 0) only.
+void launch_nl_count(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p, float pre_out2,
+                     float pre_in2, float cull2, uint32_t* counts, uint32_t* gmask, uint32_t* gsorted,
+                     uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n, cudaStream_t s, uint32_t n_points);
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
                       uint2* ij, float* dist, float* vec, cudaStream_t s, int cap = CELL_CAP);

@@ -303,6 +303,12 @@ fg_status fg_steinhardt_num_frames(const fg_steinhardt* st, uint32_t* out);
  * privatised shared histograms per block. shell 0 (default) = autotuned: the
  * candidates are timed on the first batch of each kind and the fastest is kept. */
 fg_status fg_batch_set_config(int shell, int warps_per_block, int hist_copies);
+/* Count pass of ball-query NeighborLists: 0 (default) picks the lanes-over-queries
+ * kernel where it applies (LinkCell arithmetic with the cell-shift prefilter,
+ * stencils of at most 1024 candidates after the cull) and the block-per-cell
+ * lanes-over-candidates kernel elsewhere; 1 always takes the latter. Both give
+ * the same list; the switch exists to compare them. */
+fg_status fg_set_count_kernel(int which);
 /* Text log of the autotuner's measurements and choices. */
 fg_status fg_autotune_report(char* buf, size_t len);
 /* Batched calls record their device work as CUDA graphs and replay them (1,
