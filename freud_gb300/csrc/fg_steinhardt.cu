@@ -36,6 +36,31 @@ __constant__ float c_K[ST_MAX_L + 1];                    // Q_m^m prefactors
 __constant__ float c_a[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // a_lm at [l*(L+1)+m]
 __constant__ float c_b[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // b_lm
 
+// cos(theta) = clamp(dz / d) and sin(theta) of a bond (Steinhardt.cc:163-172: the
+// wrapped z over the bond distance, clamped; theta = 0 when d = 0). cos rounded
+// to float loses sin near the poles, where 1 - cos^2 cancels; the quotient's
+// residual lo = (dz - hi d) / d (the remainder is exact through an FMA) makes
+// 1 - cos^2 = (1 - hi^2) - 2 hi lo, each product fused, so sin(theta) is accurate
+// to about one ulp at every angle, as FP64 gives it.
+__device__ __forceinline__ void bond_angle(float dz, float d, float& ct, float& st)
+{
+    ct = 1.0f;
+    st = 0.0f;
+    if (d == 0.0f)
+        return;
+    const float hi = dz / d;
+    const float lo = __fmaf_rn(-hi, d, dz) / d;
+    if (hi > 1.0f || (hi == 1.0f && lo >= 0.0f))
+        return;
+    if (hi < -1.0f || (hi == -1.0f && lo <= 0.0f))
+    {
+        ct = -1.0f;
+        return;
+    }
+    ct = hi;
+    st = sqrtf(fmaxf(0.0f, __fmaf_rn(-2.0f * hi, lo, __fmaf_rn(-hi, hi, 1.0f))));
+}
+
 // LANES threads per particle; thread a owns the orders ma = a and mb = l_max - a
 // (when mb > ma), so the two normalised Legendre recurrences of a thread take
 // l_max steps together and no thread of the group waits on another.
@@ -126,8 +151,7 @@ __global__ void __launch_bounds__(128)
                     d = dist[e];
                 }
                 g_w = weighted ? weights[e] : 1.0f;
-                g_ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
-                g_st = sqrtf(fmaxf(0.0f, 1.0f - g_ct * g_ct));
+                bond_angle(dz, d, g_ct, g_st);
                 const float rho = sqrtf(dx * dx + dy * dy);
                 if (rho > 0.0f)
                 {
@@ -388,8 +412,8 @@ __global__ void __launch_bounds__(128)
                     d = dist[e];
                 }
                 const float w = weighted ? weights[e] : 1.0f;
-                const float ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
-                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                float ct, st;
+                bond_angle(dz, d, ct, st);
                 const float rho = sqrtf(dx * dx + dy * dy);
                 float cp = 1.0f, sp = 0.0f;
                 if (rho > 0.0f)
@@ -561,8 +585,7 @@ __global__ void __launch_bounds__(128)
                     d = dist[e];
                 }
                 g_w = weighted ? weights[e] : 1.0f;
-                g_ct = d == 0.0f ? 1.0f : fminf(1.0f, fmaxf(-1.0f, dz / d));
-                g_st = sqrtf(fmaxf(0.0f, 1.0f - g_ct * g_ct));
+                bond_angle(dz, d, g_ct, g_st);
                 const float rho = sqrtf(dx * dx + dy * dy);
                 if (rho > 0.0f)
                 {
