@@ -866,7 +866,7 @@ void ball_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a
     {
         launch_cell_emit(nq->dbox, view(g), qs.qg, p, gmask.as<uint32_t>(), gsorted.as<uint32_t>(),
                          gtotal.as<uint32_t>(), offsets.as<uint64_t>(), out.ij.as<uint2>(), out.dist.as<float>(),
-                         out.vec.as<float>(), s, cap);
+                         out.vec.as<float>(), s, cap, counts.as<uint32_t>());
     }
     if (n_over > 0)
     {

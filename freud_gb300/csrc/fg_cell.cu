@@ -886,6 +886,7 @@ template<typename K> struct NlShared
     float4 rec[CELL_CAP];    // sorted candidates: prefilter position, point index (bits)
     uint32_t cnt[CELL_CAP];  // bond count per query of the cell
     uint32_t kc[32];         // kept candidates per item
+    uint32_t kw[27][SORT_CELL_MAX / 32]; // kept flags of each item's candidates (first sweep)
     uint32_t ro[33];         // kept-run offsets (runs past the items are empty)
     float wsh[32][3];        // lattice shift of each cell wrap code (0 .. 26)
     float qb[NLW][6];
@@ -1050,7 +1051,10 @@ __global__ void __launch_bounds__(NLT, 6)
                         float4 pp;
                         keep = cand(s, k0 + lane, slot, wr, pp);
                     }
-                    kept += __popc(__ballot_sync(FULL, keep));
+                    const unsigned kb = __ballot_sync(FULL, keep);
+                    if (lane == 0)
+                        S.kw[s][k0 >> 5] = kb;
+                    kept += __popc(kb);
                 }
                 if (lane == 0)
                     S.kc[s] = kept;
@@ -1091,17 +1095,13 @@ __global__ void __launch_bounds__(NLT, 6)
         {
             const uint32_t n_s = S.it.off[s + 1] - S.it.off[s];
             uint32_t pos = S.ro[s];
+            const int wr = S.it.wrap[s];
             for (uint32_t k0 = 0; k0 < n_s; k0 += 32)
             {
-                bool keep = false;
-                uint32_t slot = 0;
-                int wr = 0;
-                float4 pp;
-                if (k0 + lane < n_s)
-                    keep = cand(s, k0 + lane, slot, wr, pp);
-                const unsigned kb = __ballot_sync(FULL, keep);
-                if (keep)
+                const unsigned kb = S.kw[s][k0 >> 5];
+                if ((kb >> lane) & 1u)
                 {
+                    const uint32_t slot = S.it.start[s] + k0 + static_cast<uint32_t>(lane);
                     const uint32_t t = pos + __popc(kb & lt);
                     S.ka[t] = KT::make(g.cidx[slot], t);
                     S.sw[t] = (slot << 5) | static_cast<uint32_t>(wr);
@@ -1114,9 +1114,12 @@ __global__ void __launch_bounds__(NLT, 6)
         K* src = S.ka;
         K* dst = S.kb;
         {
-            const uint32_t per = (T + NLT - 1) / NLT;
-            const uint32_t e0 = min(T, per * tid);
-            const uint32_t e1 = min(T, e0 + per);
+            // the first NLM threads merge (fewer threads: the per-thread searches are
+            // amortised over more outputs)
+            constexpr int NLM = 64;
+            const uint32_t per = (T + NLM - 1) / NLM;
+            const uint32_t e0 = tid < NLM ? min(T, per * tid) : T;
+            const uint32_t e1 = tid < NLM ? min(T, e0 + per) : T;
             for (int G = 1; G < nitems; G <<= 1)
             {
                 nl_merge_level(src, dst, S.ro, G, e0, e1);
@@ -1487,6 +1490,215 @@ __global__ void __launch_bounds__(ETHREADS, 4)
     }
 }
 
+// Write pass, block per cell, the bonds of all the cell's queries in full rounds
+// of 32 with no global load per bond. The block stages the cell's sorted
+// candidates (position, point index) in shared memory. For each group of 32 of
+// the cell's queries, warp 0 takes the exclusive prefix of the group's bond
+// counts (queries whose bonds would pass the list's capacity wait for the next
+// window); the warps then split each query's mask row by word ranges (lane =
+// query), count their bits, and list them, in order, as candidate positions (and
+// the bond's query) after the bits of the lower ranges; then every warp takes
+// rounds of 32 bonds: a bond's query and candidate come from the list, and it
+// writes the exact vector at the query's offset plus the bond's rank.
+constexpr int WW = 4;        // warps per block
+constexpr int WLIST = 4096;  // listed bonds per window
+
+struct NlWriteShared
+{
+    float4 cp[CELL_CAP];      // sorted candidates: position (w = packed box image)
+    uint32_t cj[CELL_CAP];    // point index
+    uint8_t cw[CELL_CAP];     // cell wrap code
+    uint16_t lst[WLIST];      // listed bond: candidate position | query (lane of the group) << 10
+    float4 qp[32];
+    uint32_t qi[32];
+    unsigned long long qo[32]; // output offset of the query's bonds minus its prefix in the list
+    uint32_t pre[33];
+    uint32_t wcnt[WW][32];    // bits of each warp's word range, per query
+    float img[27][3];
+};
+
+template<int ARITH>
+__global__ void __launch_bounds__(WW * 32, 7)
+    k_nl_write(DevBox b, DevGrid g, DevGrid qg, BallParams p, const uint32_t* __restrict__ gmask,
+               const uint32_t* __restrict__ gsorted, const uint32_t* __restrict__ gtotal,
+               const uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets, uint2* __restrict__ ij,
+               float* __restrict__ dist, float* __restrict__ vec)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NlWriteShared& S = *reinterpret_cast<NlWriteShared*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    for (int t = tid; t < 81; t += WW * 32)
+        S.img[t / 3][t % 3] = b.img[t / 3][t % 3];
+    for (int c = blockIdx.x; c < qg.ncell; c += gridDim.x)
+    {
+        const uint32_t q0 = qg.start[c];
+        const uint32_t nqc = qg.start[c + 1] - q0;
+        if (nqc == 0)
+            continue;
+        const uint32_t T = gtotal[c];
+        if (T > static_cast<uint32_t>(CELL_CAP))
+            continue; // the cell's queries are written by the warp-per-query kernels
+        const uint32_t nchunks = (T + 31) / 32;
+        __syncthreads(); // the previous cell's rounds are done with the shared arrays
+        {
+            // the cell's sorted candidates, four per thread at a time with every load
+            // issued before any use
+            constexpr int PER = 4;
+            for (uint32_t e0 = static_cast<uint32_t>(tid); e0 < T; e0 += PER * WW * 32)
+            {
+                uint32_t ent[PER];
+#pragma unroll
+                for (int k = 0; k < PER; ++k)
+                {
+                    const uint32_t e = e0 + static_cast<uint32_t>(k * WW * 32);
+                    ent[k] = e < T ? gsorted[static_cast<size_t>(c) * CELL_CAP + e] : 0u;
+                }
+                float4 cp[PER];
+                uint32_t cj[PER];
+#pragma unroll
+                for (int k = 0; k < PER; ++k)
+                {
+                    const uint32_t e = e0 + static_cast<uint32_t>(k * WW * 32);
+                    if (e < T)
+                    {
+                        cp[k] = g.cpos[ent[k] >> 5];
+                        cj[k] = g.cidx[ent[k] >> 5];
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < PER; ++k)
+                {
+                    const uint32_t e = e0 + static_cast<uint32_t>(k * WW * 32);
+                    if (e < T)
+                    {
+                        S.cp[e] = cp[k];
+                        S.cj[e] = cj[k];
+                        S.cw[e] = static_cast<uint8_t>(ent[k] & 31u);
+                    }
+                }
+            }
+        }
+        for (uint32_t g0 = 0; g0 < nqc; g0 += 32)
+        {
+            const uint32_t qk = g0 + static_cast<uint32_t>(lane);
+            const bool live = qk < nqc;
+            uint32_t cnt = 0, qi = 0;
+            const uint32_t* row = gmask + static_cast<size_t>(q0 + qk) * CELL_CHUNKS;
+            if (warp == 0 && live)
+            {
+                qi = qg.cidx[q0 + qk];
+                cnt = counts[qi];
+            }
+            int la = 0;
+            while (la < 32)
+            {
+                __syncthreads(); // the previous window's rounds are done with the shared arrays
+                if (warp == 0)
+                {
+                    if (la == 0 && live)
+                    {
+                        S.qp[lane] = qg.cpos[q0 + qk];
+                        S.qi[lane] = qi;
+                    }
+                    // exclusive prefix of the counts of lanes la .. 31
+                    const uint32_t cl = lane >= la ? cnt : 0u;
+                    uint32_t incl = cl;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1)
+                    {
+                        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                        if (lane >= o)
+                            incl += v;
+                    }
+                    const uint32_t pre = incl - cl;
+                    const bool in_win = lane >= la && incl <= static_cast<uint32_t>(WLIST);
+                    const unsigned wm = __ballot_sync(FULL, in_win);
+                    const int lb = 32 - __clz(wm); // a query never exceeds the list
+                    const uint32_t total = __shfl_sync(FULL, incl, lb - 1);
+                    S.pre[lane] = pre;
+                    if (in_win && live)
+                        S.qo[lane] = offsets[qi] - pre; // + the bond's list position (>= pre)
+                    if (lane == 0)
+                        S.pre[32] = (static_cast<uint32_t>(lb) << 16) | total;
+                }
+                __syncthreads();
+                const uint32_t win = S.pre[32];
+                const int lbw = static_cast<int>(win >> 16);
+                // list building split by mask words: warp w takes words [w0, w1) of every
+                // query of the window (lane = query), counts its bits, then lists them after
+                // the bits of the lower word ranges
+                const uint32_t per_w = (nchunks + WW - 1) / WW;
+                const uint32_t w0 = min(nchunks, per_w * warp);
+                const uint32_t w1 = min(nchunks, w0 + per_w);
+                const bool lane_in = lane >= la && lane < lbw && live;
+                uint32_t wv[8];
+                uint32_t mine = 0;
+                if (lane_in)
+                {
+#pragma unroll
+                    for (int t = 0; t < 8; ++t)
+                    {
+                        wv[t] = w0 + t < w1 ? row[w0 + t] : 0u;
+                        mine += __popc(wv[t]);
+                    }
+                    for (uint32_t k = w0 + 8; k < w1; ++k)
+                        mine += __popc(row[k]);
+                }
+                S.wcnt[warp][lane] = mine;
+                __syncthreads();
+                if (lane_in && mine > 0)
+                {
+                    uint32_t k = S.pre[lane];
+                    for (int w2 = 0; w2 < warp; ++w2)
+                        k += S.wcnt[w2][lane];
+#pragma unroll
+                    for (int t = 0; t < 8; ++t)
+                    {
+                        uint32_t w = wv[t];
+                        while (w != 0)
+                        {
+                            S.lst[k++] = static_cast<uint16_t>(((w0 + t) * 32u + static_cast<uint32_t>(__ffs(w) - 1)) |
+                                                               (static_cast<uint32_t>(lane) << 10));
+                            w &= w - 1u;
+                        }
+                    }
+                    for (uint32_t ch = w0 + 8; ch < w1; ++ch)
+                    {
+                        uint32_t w = row[ch];
+                        while (w != 0)
+                        {
+                            S.lst[k++] = static_cast<uint16_t>((ch * 32u + static_cast<uint32_t>(__ffs(w) - 1)) |
+                                                               (static_cast<uint32_t>(lane) << 10));
+                            w &= w - 1u;
+                        }
+                    }
+                }
+                __syncthreads();
+                const uint32_t total = win & 0xffffu;
+#pragma unroll 2
+                for (uint32_t bb = static_cast<uint32_t>(tid); bb < total; bb += WW * 32)
+                {
+                    const uint32_t le = S.lst[bb];
+                    const int own = static_cast<int>(le >> 10);
+                    const uint32_t e = le & 1023u;
+                    const float4 q = S.qp[own];
+                    float rx, ry, rz;
+                    exact_vec(b, S.img, ARITH, q, __float_as_int(q.w), S.cp[e], static_cast<int>(S.cw[e]), rx, ry, rz);
+                    const uint64_t o = S.qo[own] + bb;
+                    ij[o] = make_uint2(S.qi[own], S.cj[e]);
+                    dist[o] = __fsqrt_rn(dot3(rx, ry, rz));
+                    vec[3 * o] = rx;
+                    vec[3 * o + 1] = ry;
+                    vec[3 * o + 2] = rz;
+                }
+                la = lbw;
+            }
+        }
+    }
+}
+
 int sm_count_cell()
 {
     int dev = 0;
@@ -1609,8 +1821,34 @@ void launch_nl_count(const DevBox& box, const DevGrid& g, const DevGrid& qg, con
 
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
-                      uint2* ij, float* dist, float* vec, cudaStream_t s, int cap)
+                      uint2* ij, float* dist, float* vec, cudaStream_t s, int cap, const uint32_t* counts)
 {
+    if (cap <= CELL_CAP && counts != nullptr)
+    {
+        // block per cell when the cells keep every resident block busy (two or more each)
+        auto go_w = [&](auto kernel, bool& conf) {
+            const size_t smem = sizeof(NlWriteShared);
+            configure(kernel, smem, conf);
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, WW * 32, smem);
+            const int want = std::max(per_sm, 1) * sm_count_cell();
+            if (static_cast<uint64_t>(qg.ncell) < 2ull * want)
+                return false;
+            ProfScope prof_("k_nl_write", s);
+            kernel<<<want, WW * 32, smem, s>>>(box, g, qg, p, gmask, gsorted, gtotal, counts, offsets, ij, dist, vec);
+            return true;
+        };
+        bool done = false;
+        static bool conf_w = false, conf_g = false, conf_a = false;
+        if (p.arith == ARITH_WRAP)
+            done = go_w(k_nl_write<ARITH_WRAP>, conf_w);
+        else if (p.arith == ARITH_GHOST)
+            done = go_w(k_nl_write<ARITH_GHOST>, conf_g);
+        else
+            done = go_w(k_nl_write<ARITH_AABB>, conf_a);
+        if (done)
+            return;
+    }
     auto go = [&](auto kernel) {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ETHREADS, 0);

@@ -154,7 +154,8 @@ void launch_nl_count(const DevBox& box, const DevGrid& g, const DevGrid& qg, con
                      uint32_t* gtotal, uint32_t* overflow, uint32_t* overflow_n, cudaStream_t s, uint32_t n_points);
 void launch_cell_emit(const DevBox& box, const DevGrid& g, const DevGrid& qg, const BallParams& p,
                       const uint32_t* gmask, const uint32_t* gsorted, const uint32_t* gtotal, const uint64_t* offsets,
-                      uint2* ij, float* dist, float* vec, cudaStream_t s, int cap = CELL_CAP);
+                      uint2* ij, float* dist, float* vec, cudaStream_t s, int cap = CELL_CAP,
+                      const uint32_t* counts = nullptr);
 
 // Histogram of a distance array (RDF over a NeighborList).
 void launch_hist_distances(const float* dist, uint64_t nb, const HistParams& h, unsigned long long* hist,
