@@ -59,11 +59,12 @@ __device__ __forceinline__ uint32_t frame_of(const uint32_t* __restrict__ base, 
 __global__ void k_frames_assign(const FrameDesc* __restrict__ fd, const uint32_t* __restrict__ pt_base,
                                 uint32_t nframes, const float* __restrict__ pts, uint32_t n,
                                 uint32_t* __restrict__ cell_of, uint32_t* __restrict__ rank, float4* __restrict__ pos4,
-                                uint32_t* __restrict__ cell_count)
+                                uint32_t* __restrict__ cell_count, int* __restrict__ frame_out)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
-        const FrameDesc& F = fd[frame_of(pt_base, nframes, i)];
+        const uint32_t fi = frame_of(pt_base, nframes, i);
+        const FrameDesc& F = fd[fi];
         const float x = pts[3 * (size_t) i];
         const float y = pts[3 * (size_t) i + 1];
         const float z = pts[3 * (size_t) i + 2];
@@ -74,6 +75,8 @@ __global__ void k_frames_assign(const FrameDesc* __restrict__ fd, const uint32_t
         cell_of[i] = cell;
         rank[i] = atomicAdd(&cell_count[cell], 1u);
         pos4[i] = make_float4(x, y, F.b.is2d ? 0.0f : z, __int_as_float(img));
+        if (img != 0 && frame_out[fi] == 0)
+            atomicOr(&frame_out[fi], 1);
     }
 }
 
@@ -98,6 +101,7 @@ struct BItems
     uint32_t start[BT_ITEMS];
     uint32_t off[BT_ITEMS + 1];
     int wrap[BT_ITEMS];
+    unsigned char home[BT_ITEMS]; // 1: the home cell (half-stencil mode: pairs j > i only)
 };
 
 struct HistShared
@@ -106,6 +110,7 @@ struct HistShared
     float4 iv[BT_TILE];         // image vector for queries inside the box; w = 1 if |k| <= 1
     uint32_t j[BT_TILE];        // global point index
     unsigned char wr[BT_TILE];  // cell wrap code (wx + 1) + 3 (wy + 1) + 9 (wz + 1)
+    unsigned char home[BT_TILE]; // candidate of the home cell (half-stencil mode)
     float4 q[BT_QB];
     uint32_t qi[BT_QB];
     BItems it;
@@ -118,6 +123,7 @@ struct HistShared
     float qbox[8][6];           // per-warp bounds of the cell's queries (lo xyz, hi xyz)
     float qfin[6];              // their union
     int qout;                   // some query of the cell lies outside the box
+    int sym;                    // half-stencil mode for the current frame
     uint32_t hist[BT_HIST];
     uint32_t rb[BT_RB_WORDS];   // HistParams::rb, when given
 };
@@ -137,6 +143,7 @@ __device__ void frame_items(const HistShared& S, const uint32_t* __restrict__ st
     const int nrows = S.box.is2d ? w : w * w;
     uint32_t st[3] = {0u, 0u, 0u}, cnt[3] = {0u, 0u, 0u};
     int wc[3] = {13, 13, 13};
+    bool home0 = false;
     if (lane < nrows)
     {
         const int dy = lane % w - s;
@@ -146,8 +153,33 @@ __device__ void frame_items(const HistShared& S, const uint32_t* __restrict__ st
         const int wz = uz < 0 ? -1 : (uz >= d2 ? 1 : 0);
         const int row = d0 * ((uy - wy * d1) + d1 * (uz - wz * d2));
         const int x0 = cx - s, x1 = cx + s;
-        const int lo[3] = {x0 + d0, max(x0, 0), 0};
-        const int hi[3] = {x0 < 0 ? d0 - 1 : -1, min(x1, d0 - 1), x1 >= d0 ? x1 - d0 : -1};
+        int lo[3] = {x0 + d0, max(x0, 0), 0};
+        int hi[3] = {x0 < 0 ? d0 - 1 : -1, min(x1, d0 - 1), x1 >= d0 ? x1 - d0 : -1};
+        int xw[3] = {0, 1, 2}; // x-wrap code of each segment
+        if (S.sym)
+        {
+            // half stencil: rows after the home row whole, the home row from the home
+            // cell on (home cell alone, then the cells after it, then those wrapped)
+            const bool after = dz > 0 || (dz == 0 && dy > 0);
+            const bool before = dz < 0 || (dz == 0 && dy < 0);
+            if (before)
+            {
+                hi[0] = hi[1] = hi[2] = -1;
+            }
+            else if (!after)
+            {
+                lo[0] = cx;
+                hi[0] = cx;
+                xw[0] = 1;
+                lo[1] = cx + 1;
+                hi[1] = min(x1, d0 - 1);
+                xw[1] = 1;
+                lo[2] = 0;
+                hi[2] = x1 >= d0 ? x1 - d0 : -1;
+                xw[2] = 2;
+                home0 = true;
+            }
+        }
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
@@ -156,7 +188,7 @@ __device__ void frame_items(const HistShared& S, const uint32_t* __restrict__ st
                 const uint32_t base = S.cell_base + static_cast<uint32_t>(row);
                 st[k] = start[base + lo[k]];
                 cnt[k] = start[base + hi[k] + 1] - st[k];
-                wc[k] = k + 3 * (wy + 1) + 9 * (wz + 1);
+                wc[k] = xw[k] + 3 * (wy + 1) + 9 * (wz + 1);
             }
         }
     }
@@ -175,6 +207,7 @@ __device__ void frame_items(const HistShared& S, const uint32_t* __restrict__ st
         it.start[3 * lane + k] = st[k];
         it.off[3 * lane + k] = off;
         it.wrap[3 * lane + k] = wc[k];
+        it.home[3 * lane + k] = static_cast<unsigned char>(home0 && k == 0);
         off += cnt[k];
     }
     if (lane == 31)
@@ -193,10 +226,11 @@ __device__ __forceinline__ int bitem_of(const BItems& it, uint32_t t)
     return s;
 }
 
+// (shared memory holds four blocks per SM: registers up to that occupancy)
 template<int WARPS, int COPIES>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, 4)
     k_frames_hist(BatchGrid g, BallParams p, HistParams h, uint32_t cell_limit, uint32_t chunk,
-                  uint32_t* __restrict__ queue, unsigned long long* __restrict__ hist)
+                  uint32_t* __restrict__ queue, unsigned long long* __restrict__ hist, int sym_ok)
 {
     constexpr int THREADS = WARPS * 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -268,6 +302,8 @@ __global__ void __launch_bounds__(WARPS * 32)
                     S.dim[2] = F.dim[2];
                     S.shell = F.shell;
                     S.cell_base = F.cell_base;
+                    // half stencil: every point of the frame in the box (image 0)
+                    S.sym = sym_ok && g.frame_out[f] == 0;
                 }
                 // candidate cull radius of this frame: r_max plus a margin bounding the
                 // difference between the shifted float distance and the exact one
@@ -333,7 +369,8 @@ __global__ void __launch_bounds__(WARPS * 32)
                 __syncthreads();
             }
             // the cull needs every query in the box (image 0); otherwise all candidates stay
-            const bool cull = S.qout == 0 && !test_ii;
+            const bool sym = S.sym != 0;
+            const bool cull = S.qout == 0 && (!test_ii || sym);
             const uint32_t T = S.it.off[BT_ITEMS];
             for (uint32_t t0 = 0; t0 < T; t0 += BT_TILE)
             {
@@ -388,6 +425,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                         S.iv[idx] = iv;
                         S.j[idx] = g.cidx[slot];
                         S.wr[idx] = static_cast<unsigned char>(wr);
+                        S.home[idx] = S.it.home[bitem_of(S.it, t0 + tl)];
                     }
                 }
                 __syncthreads();
@@ -407,7 +445,9 @@ __global__ void __launch_bounds__(WARPS * 32)
                     }
                     // queries inside the box take a branch-free pair loop: invalid
                     // candidates (image beyond +-1) are moved out of range instead
-                    const bool general = __syncthreads_or(out_of_box) != 0 || test_ii;
+                    // (half-stencil frames hold no point outside the box and count no
+                    // pair of a point with itself)
+                    const bool general = (__syncthreads_or(out_of_box) != 0 || test_ii) && !sym;
                     if (!general && rbins)
                     {
                         for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
@@ -415,16 +455,41 @@ __global__ void __launch_bounds__(WARPS * 32)
                             const uint32_t e = ch * 32 + lane;
                             float4 pp = make_float4(3e30f, 3e30f, 3e30f, 0.f);
                             float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                            uint32_t jj = 0;
+                            bool hm = false;
                             if (e < TT)
                             {
                                 iv = S.iv[e];
                                 if (iv.w != 0.0f)
                                     pp = S.pos[e];
+                                jj = S.j[e];
+                                hm = S.home[e] != 0;
                             }
+                            const bool zero = iv.x == 0.0f && iv.y == 0.0f && iv.z == 0.0f;
+                            // exact r^2 -> bin (ok: r_min^2 <= r^2 < r_max^2 and inside the histogram)
+                            auto bin_of = [&](float rsq, bool& ok) {
+                                ok = rsq >= h.rb_a && rsq < h.rb_b;
+                                const uint32_t u = __float_as_uint(rsq);
+                                const uint32_t key = (ok && u >= h.rb_ut) ? ((u - h.rb_ut) >> h.rb_s) + 1u : 0u;
+                                const uint32_t b0 = rb_key[key];
+                                return b0 + (rsq >= rb_thr[b0 + 1] ? 1u : 0u) + (rsq >= rb_thr[b0 + 2] ? 1u : 0u);
+                            };
+                            auto add = [&](uint32_t bin, uint32_t w) {
+                                if (smem_hist)
+                                    atomicAdd(&my_hist[bin], w);
+                                else
+                                    atomicAdd(&hist[bin], static_cast<unsigned long long>(w));
+                            };
                             // image 0 for the whole chunk: q + 0 is q (up to the sign of a
-                            // zero, which r^2 does not see), so the three additions go
-                            auto sweep = [&](auto zero_image) {
+                            // zero, which r^2 does not see), so the three additions go.
+                            // Half stencil (SYM): a pair of image 0 is tested once and
+                            // counted twice - p_i - (p_j + 0) is exactly -(p_j - (p_i + 0)),
+                            // so both bonds fall in one bin; home-cell pairs only for j > i;
+                            // a pair of image k != 0 is tested from both ends: r_ij =
+                            // p_j - (p_i + v_k) and r_ji = p_i - (p_j + v_-k), v_-k = -v_k.
+                            auto sweep = [&](auto zero_image, auto half) {
                                 constexpr bool Z = decltype(zero_image)::value;
+                                constexpr bool SYM = decltype(half)::value;
 #pragma unroll 4
                                 for (uint32_t qq = 0; qq < nb; ++qq)
                                 {
@@ -432,26 +497,41 @@ __global__ void __launch_bounds__(WARPS * 32)
                                     const float rx = __fsub_rn(pp.x, Z ? q.x : __fadd_rn(q.x, iv.x));
                                     const float ry = __fsub_rn(pp.y, Z ? q.y : __fadd_rn(q.y, iv.y));
                                     const float rz = __fsub_rn(pp.z, Z ? q.z : __fadd_rn(q.z, iv.z));
-                                    const float rsq = dot3(rx, ry, rz);
-                                    const bool ok = rsq >= h.rb_a && rsq < h.rb_b;
-                                    const uint32_t u = __float_as_uint(rsq);
-                                    const uint32_t key = (ok && u >= h.rb_ut) ? ((u - h.rb_ut) >> h.rb_s) + 1u : 0u;
-                                    const uint32_t b0 = rb_key[key];
-                                    const uint32_t bin = b0 + (rsq >= rb_thr[b0 + 1] ? 1u : 0u) +
-                                        (rsq >= rb_thr[b0 + 2] ? 1u : 0u);
-                                    if (ok)
+                                    bool ok;
+                                    const uint32_t bin = bin_of(dot3(rx, ry, rz), ok);
+                                    uint32_t w = 1;
+                                    if (SYM)
+                                        w = hm ? (jj > S.qi[qq] ? 2u : 0u) : (zero ? 2u : 1u);
+                                    if (ok && w != 0)
+                                        add(bin, w);
+                                    if (SYM && !Z && !zero)
                                     {
-                                        if (smem_hist)
-                                            atomicAdd(&my_hist[bin], 1u);
-                                        else
-                                            atomicAdd(&hist[bin], 1ull);
+                                        const float sx = __fsub_rn(q.x, __fsub_rn(pp.x, iv.x));
+                                        const float sy = __fsub_rn(q.y, __fsub_rn(pp.y, iv.y));
+                                        const float sz = __fsub_rn(q.z, __fsub_rn(pp.z, iv.z));
+                                        bool ok2;
+                                        const uint32_t bin2 = bin_of(dot3(sx, sy, sz), ok2);
+                                        if (ok2)
+                                            add(bin2, 1u);
                                     }
                                 }
                             };
-                            if (__all_sync(FULL, iv.x == 0.0f && iv.y == 0.0f && iv.z == 0.0f))
-                                sweep(std::true_type {});
+                            const bool all_zero = __all_sync(FULL, zero);
+                            if (sym)
+                            {
+                                if (all_zero)
+                                    sweep(std::true_type {}, std::true_type {});
+                                else
+                                    sweep(std::false_type {}, std::true_type {});
+                            }
+                            else if (all_zero)
+                            {
+                                sweep(std::true_type {}, std::false_type {});
+                            }
                             else
-                                sweep(std::false_type {});
+                            {
+                                sweep(std::false_type {}, std::false_type {});
+                            }
                         }
                         continue;
                     }
@@ -462,20 +542,19 @@ __global__ void __launch_bounds__(WARPS * 32)
                             const uint32_t e = ch * 32 + lane;
                             float4 pp = make_float4(3e30f, 3e30f, 3e30f, 0.f);
                             float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                            uint32_t jj = 0;
+                            bool hm = false;
                             if (e < TT)
                             {
                                 iv = S.iv[e];
                                 if (iv.w != 0.0f)
                                     pp = S.pos[e];
+                                jj = S.j[e];
+                                hm = S.home[e] != 0;
                             }
-#pragma unroll 4
-                            for (uint32_t qq = 0; qq < nb; ++qq)
-                            {
-                                const float4 q = S.q[qq];
-                                const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, iv.x));
-                                const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iv.y));
-                                const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iv.z));
-                                const float rsq = dot3(rx, ry, rz);
+                            const bool zero = iv.x == 0.0f && iv.y == 0.0f && iv.z == 0.0f;
+                            // Histogram.h:327-351 binning of the distance of a pair that passed
+                            auto count = [&](float rsq, uint32_t w) {
                                 if (rsq < p.r_max_sq && rsq >= p.r_min_sq)
                                 {
                                     const float d = __fsqrt_rn(rsq);
@@ -486,10 +565,30 @@ __global__ void __launch_bounds__(WARPS * 32)
                                         if (bin == h.bins)
                                             bin = h.bins - 1;
                                         if (smem_hist)
-                                            atomicAdd(&my_hist[bin], 1u);
+                                            atomicAdd(&my_hist[bin], w);
                                         else
-                                            atomicAdd(&hist[bin], 1ull);
+                                            atomicAdd(&hist[bin], static_cast<unsigned long long>(w));
                                     }
+                                }
+                            };
+                            // half stencil as in the table path above
+                            const bool rev = sym && __any_sync(FULL, !zero);
+#pragma unroll 4
+                            for (uint32_t qq = 0; qq < nb; ++qq)
+                            {
+                                const float4 q = S.q[qq];
+                                const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, iv.x));
+                                const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iv.y));
+                                const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iv.z));
+                                const uint32_t w = sym ? (hm ? (jj > S.qi[qq] ? 2u : 0u) : (zero ? 2u : 1u)) : 1u;
+                                if (w != 0)
+                                    count(dot3(rx, ry, rz), w);
+                                if (rev && !zero)
+                                {
+                                    const float sx = __fsub_rn(q.x, __fsub_rn(pp.x, iv.x));
+                                    const float sy = __fsub_rn(q.y, __fsub_rn(pp.y, iv.y));
+                                    const float sz = __fsub_rn(q.z, __fsub_rn(pp.z, iv.z));
+                                    count(dot3(sx, sy, sz), 1u);
                                 }
                             }
                         }
@@ -566,7 +665,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                 }
                 __syncthreads();
             }
-            if (self_in_bin0 && tid == 0)
+            if (self_in_bin0 && !sym && tid == 0)
             {
                 // one self pair per query of the cell, counted into bin 0 above
                 if (smem_hist)
@@ -1024,19 +1123,25 @@ void hist_launch(const BatchGrid& g, const BallParams& p, const HistParams& h, u
     const uint32_t chunk =
         std::max<uint32_t>(1u, std::min<uint32_t>(BT_CHUNK_MAX, cell_limit / std::max<uint32_t>(1u, resident * 16)));
     const uint32_t blocks = std::min<uint32_t>(resident, std::max<uint32_t>(1u, (cell_limit + chunk - 1) / chunk));
-    ProfScope prof_("k_frames_hist", s);
-    k_frames_hist<WARPS, COPIES><<<blocks, WARPS * 32, smem, s>>>(g, p, h, cell_limit, chunk, queue, hist);
+    // each unordered pair once where the queries are the points (exclude_ii;
+    // frames with a point outside the box keep the whole stencil)
+    const int sym_ok = p.exclude_ii ? 1 : 0;
+    ProfScope prof_(sym_ok ? (h.rb != nullptr ? "k_frames_hist<half, r2 table>" : "k_frames_hist<half>")
+                           : "k_frames_hist", s);
+    k_frames_hist<WARPS, COPIES><<<blocks, WARPS * 32, smem, s>>>(g, p, h, cell_limit, chunk, queue, hist, sym_ok);
 }
 
 } // namespace
 
 void launch_frames_assign(const FrameDesc* fd, const uint32_t* pt_base, uint32_t nframes, const float* pts, uint32_t n,
-                          uint32_t* cell_of, uint32_t* rank, float4* pos4, uint32_t* cell_count, cudaStream_t s)
+                          uint32_t* cell_of, uint32_t* rank, float4* pos4, uint32_t* cell_count, int* frame_out,
+                          cudaStream_t s)
 {
     if (n == 0)
         return;
     ProfScope prof_("k_frames_assign", s);
-    k_frames_assign<<<grid_blocks(n, 256), 256, 0, s>>>(fd, pt_base, nframes, pts, n, cell_of, rank, pos4, cell_count);
+    k_frames_assign<<<grid_blocks(n, 256), 256, 0, s>>>(fd, pt_base, nframes, pts, n, cell_of, rank, pos4, cell_count,
+                                                         frame_out);
 }
 
 void launch_frames_scatter(uint32_t n, const uint32_t* cell_of, const uint32_t* rank, const float4* pos4,

@@ -40,6 +40,7 @@ struct BatchGrid
     const float4* cpos;        // cell-sorted positions, w = packed integer box image
     const uint32_t* cidx;      // global point index of each slot
     const uint32_t* cell_of;   // global cell of each point (by point index)
+    const int* frame_out;      // [nframes]: nonzero when some point of the frame lies outside its box
 };
 
 // Tunable launch shape of the batched histogram kernel.
@@ -52,15 +53,18 @@ struct BatchHistConfig
 
 // Counting sort of every frame's points into the batch grid. cell_count must be
 // zeroed ([ncell + 1]); pos4 receives (x, y, z, image) per point.
+// frame_out ([nframes], zeroed) is set for each frame with a point outside its box.
 void launch_frames_assign(const FrameDesc* fd, const uint32_t* pt_base, uint32_t nframes, const float* pts,
                           uint32_t n, uint32_t* cell_of, uint32_t* rank, float4* pos4, uint32_t* cell_count,
-                          cudaStream_t s);
+                          int* frame_out, cudaStream_t s);
 void launch_frames_scatter(uint32_t n, const uint32_t* cell_of, const uint32_t* rank, const float4* pos4,
                            const uint32_t* start, float4* cpos, uint32_t* cidx, cudaStream_t s);
 
 // Fused ball query + RDF histogram over every cell of the batch: persistent
 // blocks pull runs of cells from a device work counter (*queue, zeroed before
-// the launch) until cell_limit. hist is uint64[h.bins].
+// the launch) until cell_limit. hist is uint64[h.bins]. With exclude_ii, frames
+// whose points all lie in the box count each unordered pair once (half stencil;
+// see k_frames_hist).
 size_t frames_hist_smem_bytes();
 
 // h with its exact r^2 -> bin table filled in (the pair test r_min_sq <= r^2 <

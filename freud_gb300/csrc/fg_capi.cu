@@ -2919,6 +2919,7 @@ struct BatchGridBufs
     std::vector<FrameDesc> fd_host;
     std::vector<uint32_t> cell_base_host;
     DevBuf fd, cell_base, counts, start, cell_of, rank, pos4, cpos0, cidx0, cpos, cidx, scan;
+    DevBuf frame_out; // int per frame: some point outside the frame's box
 };
 
 } // namespace
@@ -2996,6 +2997,7 @@ BatchGridBufs& batch_grid(fg_frames* fr, float r_max, int shell)
     cudaStream_t s = stream();
     const uint32_t n = fr->total;
     g->fd.alloc(sizeof(FrameDesc) * F);
+    g->frame_out.alloc(sizeof(int) * F);
     g->cell_base.alloc(sizeof(uint32_t) * (F + 1));
     g->counts.alloc(sizeof(uint32_t) * (g->ncell + 1));
     g->start.alloc(sizeof(uint32_t) * (g->ncell + 1));
@@ -3022,9 +3024,10 @@ void enqueue_grid_build(fg_frames* fr, BatchGridBufs& g, cudaStream_t s, bool so
 {
     const uint32_t F = static_cast<uint32_t>(fr->n.size());
     FG_CUDA(cudaMemsetAsync(g.counts.p, 0, sizeof(uint32_t) * (g.ncell + 1), s));
+    FG_CUDA(cudaMemsetAsync(g.frame_out.p, 0, sizeof(int) * F, s));
     launch_frames_assign(g.fd.as<FrameDesc>(), fr->d_pt_base.as<uint32_t>(), F, fr->dpts, fr->total,
                          g.cell_of.as<uint32_t>(), g.rank.as<uint32_t>(), g.pos4.as<float4>(), g.counts.as<uint32_t>(),
-                         s);
+                         g.frame_out.as<int>(), s);
     scan_u32_to_u32(g.counts.as<uint32_t>(), g.start.as<uint32_t>(), static_cast<size_t>(g.ncell) + 1, g.scan.p, s);
     if (!sorted)
     {
@@ -3049,6 +3052,7 @@ BatchGrid batch_view(const fg_frames* fr, const BatchGridBufs& g)
     v.cpos = g.cpos.as<float4>();
     v.cidx = g.cidx.as<uint32_t>();
     v.cell_of = g.cell_of.as<uint32_t>();
+    v.frame_out = g.frame_out.as<int>();
     return v;
 }
 
