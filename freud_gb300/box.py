@@ -60,7 +60,9 @@ class Box:
 
     @classmethod
     def from_matrix(cls, box_matrix, dimensions=None):
-        m = np.asarray(box_matrix, dtype=np.float64)
+        # float32 first, as freud does (freud/box.py:862): the derived lengths and
+        # tilts then round exactly as the reference's
+        m = np.asarray(box_matrix, dtype=np.float32)
         v0, v1, v2 = m[:, 0], m[:, 1], m[:, 2]
         Lx = np.sqrt(np.dot(v0, v0))
         a2x = np.dot(v0, v1) / Lx

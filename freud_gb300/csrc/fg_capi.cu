@@ -652,6 +652,17 @@ void check_periodic(const HostBox& b)
         throw Error(FG_ERR_VALUE, "Pair queries in a non-periodic box are not implemented.");
 }
 
+// A (box, points) system queries without the check above in the reference
+// (RawPoints.h:50-62) and takes periodic images only along periodic axes
+// (NeighborQuery.h:496-564). The cell grids here fold every axis, so a box that is
+// not periodic on every axis is refused instead of answered with folded bonds.
+void check_periodic_raw(const HostBox& b)
+{
+    if (!(b.periodic[0] && b.periodic[1] && b.periodic[2]))
+        throw Error(FG_ERR_VALUE, "Pair queries of a (box, points) system in a box that is not periodic on every "
+                                  "axis are not implemented.");
+}
+
 // The sorted query set: the object's own cell-sorted points, or the query points
 // sorted into a grid with the same dims.
 struct QuerySet
@@ -1011,6 +1022,8 @@ void run_query(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args* ar
     fg_query_args a = *args;
     if (nq->kind != FG_NQ_RAWPOINTS)
         check_periodic(nq->box);
+    else
+        check_periodic_raw(nq->box);
     if (nq->kind == FG_NQ_CELLQUERY)
         validate_cellquery_args(nq->box, a);
     else
@@ -1743,6 +1756,8 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
         fg_query_args a = *args;
         if (nq->kind != FG_NQ_RAWPOINTS)
             check_periodic(nq->box);
+        else
+            check_periodic_raw(nq->box);
         if (nq->kind == FG_NQ_CELLQUERY)
             validate_cellquery_args(nq->box, a);
         else
@@ -1782,23 +1797,11 @@ static void rdf_accumulate(fg_rdf* rdf, fg_nq* nq, const float* dq, uint32_t nqp
             p.exclude_ii = a.exclude_ii;
             p.arith = arith;
             p.nq = nqp;
-            DevBuf over, over_n;
-            over.alloc(sizeof(uint32_t) * (nqp + 1));
-            over_n.alloc(sizeof(uint32_t));
-            FG_CUDA(cudaMemsetAsync(over_n.p, 0, sizeof(uint32_t), s));
             const Prefilter pf = prefilter(nq, p.arith, dim, a.r_max, a.r_min);
+            // the histogram pass takes every cell (large stencils in tiles): no
+            // queries are handed on, so it gets no overflow list
             launch_cell_scan(1, nq->dbox, view(g), qs.qg, p, pf.out2, 0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr,
-                             over.as<uint32_t>(), over_n.as<uint32_t>(), h, rdf->hist.as<unsigned long long>(), s);
-            uint32_t n_over = 0;
-            FG_CUDA(cudaMemcpyAsync(&n_over, over_n.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-            sync();
-            if (n_over > 0)
-            {
-                BallParams po = p;
-                po.nq = n_over;
-                launch_ball_hist(nq->dbox, view(g), qs.qpos, qs.qidx, po, h, rdf->hist.as<unsigned long long>(), s,
-                                 over.as<uint32_t>());
-            }
+                             nullptr, nullptr, h, rdf->hist.as<unsigned long long>(), s);
             FG_CUDA(cudaGetLastError());
             sync();
         }
@@ -2556,6 +2559,8 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
     return guard([&] {
         require(st, "steinhardt");
         require(nq, "nq");
+        // the bond vectors are box.wrap(p_j - p_i), which here wraps every axis
+        check_periodic_raw(nq->box);
         cudaStream_t s = stream();
         if (nlist == nullptr)
         {
@@ -2690,8 +2695,8 @@ constexpr size_t NA_CPOS = align256(NA_CIDX0 + 4ull * NOALLOC_MAX_POINTS);
 constexpr size_t NA_CIDX = align256(NA_CPOS + 16ull * NOALLOC_MAX_POINTS);
 constexpr size_t NA_SCAN = align256(NA_CIDX + 4ull * NOALLOC_MAX_POINTS);
 constexpr size_t NA_SCAN_BYTES = 8192; // scan_scratch_bytes(NOALLOC_MAX_CELLS + 1) is ~1.3 KB
-constexpr size_t NA_OVER = align256(NA_SCAN + NA_SCAN_BYTES);
-constexpr size_t NOALLOC_SCRATCH_BYTES = align256(NA_OVER + 64);
+constexpr size_t NOALLOC_SCRATCH_BYTES = align256(NA_SCAN + NA_SCAN_BYTES); // 4,203,520 bytes
+static_assert(NOALLOC_SCRATCH_BYTES == 4203520, "the documented size of the allocation-free scratch");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
@@ -2748,6 +2753,8 @@ fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points
         const HostBox hb = to_host_box(box);
         if (kind != FG_NQ_RAWPOINTS)
             check_periodic(hb);
+        else
+            check_periodic_raw(hb);
         const int arith = kind == FG_NQ_LINKCELL ? ARITH_WRAP : ARITH_AABB;
         float pd[3];
         nearest_plane(hb, pd);
@@ -2772,13 +2779,11 @@ fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points
         float4* cpos = reinterpret_cast<float4*>(base + NA_CPOS);
         uint32_t* cidx = reinterpret_cast<uint32_t*>(base + NA_CIDX);
         void* scan_scratch = base + NA_SCAN;
-        uint32_t* over = reinterpret_cast<uint32_t*>(base + NA_OVER);
         if (scan_scratch_bytes(static_cast<size_t>(ncell) + 1) > NA_SCAN_BYTES)
             runtime_error("scan scratch larger than reserved");
 
         // the cell counts start at zero; the output is this frame's counts
         FG_CUDA(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (ncell + 1), s));
-        FG_CUDA(cudaMemsetAsync(over, 0, 64, s));
         FG_CUDA(cudaMemsetAsync(device_counts, 0, sizeof(unsigned long long) * bins, s));
         launch_assign(db, device_points, n, dim, cell_of, rank, counts, s);
         scan_u32_to_u32(counts, start, static_cast<size_t>(ncell) + 1, scan_scratch, s);
@@ -2807,7 +2812,7 @@ fg_status fg_rdf_histogram_noalloc(const fg_box* box, const float* device_points
         fg_nq probe;
         probe.box = hb;
         const Prefilter pf = prefilter(&probe, arith, dim, r_max, 0.0f);
-        launch_cell_scan(1, db, g, g, p, pf.out2, 0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, over, over + 1, h,
+        launch_cell_scan(1, db, g, g, p, pf.out2, 0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, h,
                          device_counts, s);
         FG_CUDA(cudaGetLastError());
     });

@@ -122,7 +122,7 @@ void launch_ball_hist(const DevBox& box, const DevGrid& g, const float4* qpos, c
 // Block-per-cell ball kernels. qg is the cell-sorted query grid (same dims as g).
 // In the count pass, queries of cells whose candidate set exceeds CELL_CAP are
 // appended to overflow for the warp-per-query kernels; the histogram pass tiles
-// large candidate sets instead. pre_out2 > 0 enables the wrap-arithmetic
+// large candidate sets instead and never writes overflow (may be NULL there). pre_out2 > 0 enables the wrap-arithmetic
 // prefilter (pairs beyond sqrt(pre_out2) are rejected without the exact test);
 // pre_in2 > 0 lets the count pass accept pairs inside sqrt(pre_in2) unchecked.
 // Scan pass (hist_mode 0): counts per query, acceptance masks gmask[nq][CELL_CHUNKS]

@@ -79,5 +79,5 @@ def load_rdf_state(rdf, state):
     b = _lib.fg_box(Lx, Ly, Lz, xy, xz, yz, int(is2d), 1, 1, 1)
     _lib.check(_lib.lib.fg_rdf_set_state(rdf._h, _lib.ptr(counts), int(state.n_frames), ctypes.byref(b),
                                          int(state.n_points), int(state.n_query)))
-    rdf._called_compute = True
+    rdf._has_computed = True
     return rdf

@@ -1,44 +1,53 @@
 """Compute-class plumbing and argument conversion, API-compatible with freud.util
 (freud/util.py:4-168)."""
 
-from functools import wraps
+import functools
 
 import numpy as np
 
 
+class _ComputedProperty(property):
+    """A property that exists only once its object has run compute(): before
+    that, reading it raises AttributeError("Property not computed. Call compute
+    first."), the reference's message."""
+
+    def __get__(self, obj, objtype=None):
+        if obj is not None and not obj.__dict__.get("_has_computed", False):
+            raise AttributeError("Property not computed. Call compute first.")
+        return super().__get__(obj, objtype)
+
+
 class _Compute:
-    """Parent of all compute classes: guards access to properties before compute()."""
+    """Base of the compute classes. When a subclass is defined, its own compute()
+    is wrapped once so that a finished call marks the object as computed; results
+    are declared with _Compute._computed_property and raise AttributeError until
+    then (plot(), where a subclass has one, likewise)."""
+
+    _computed_property = _ComputedProperty
 
     def __init__(self):
-        self._called_compute = False
+        self._has_computed = False
 
-    def __getattribute__(self, attr):
-        attribute = object.__getattribute__(self, attr)
-        if attr == "compute":
-            compute = attribute
+    def __init_subclass__(cls, **kwargs):
+        super().__init_subclass__(**kwargs)
+        fn = cls.__dict__.get("compute")
+        if fn is not None:
+            @functools.wraps(fn)
+            def compute(self, *args, **kw):
+                result = fn(self, *args, **kw)
+                self._has_computed = True
+                return result
 
-            @wraps(compute)
-            def compute_wrapper(*args, **kwargs):
-                return_value = compute(*args, **kwargs)
-                self._called_compute = True
-                return return_value
+            cls.compute = compute
+        plot = cls.__dict__.get("plot")
+        if plot is not None:
+            @functools.wraps(plot)
+            def guarded_plot(self, *args, **kw):
+                if not self.__dict__.get("_has_computed", False):
+                    raise AttributeError("The compute method must be called before calling plot.")
+                return plot(self, *args, **kw)
 
-            return compute_wrapper
-        if attr == "plot":
-            if not object.__getattribute__(self, "__dict__").get("_called_compute", False):
-                raise AttributeError("The compute method must be called before calling plot.")
-        return attribute
-
-    @staticmethod
-    def _computed_property(prop):
-        @property
-        @wraps(prop)
-        def wrapper(self, *args, **kwargs):
-            if not self.__dict__.get("_called_compute", False):
-                raise AttributeError("Property not computed. Call compute first.")
-            return prop(self, *args, **kwargs)
-
-        return wrapper
+            cls.plot = guarded_plot
 
     def __str__(self):
         return repr(self)

@@ -252,7 +252,7 @@ fg_status fg_steinhardt_get(const fg_steinhardt* st, float* ql, float* particle_
  * cudaMalloc - this computes the uint64 RDF bin counts of one frame (the ball
  * query of radius r_max with bins over [r_min, r_max), as
  * RDF(bins, r_max, r_min).compute((box, points)) does, fused) without allocating
- * anything: its scratch is a fixed file-scope device array of about 3.7 MB that
+ * anything: its scratch is a fixed file-scope device array of 4,203,520 bytes that
  * every GPU loading the library holds until exit, which limits n to 65,536 points
  * (larger n is rejected with FG_ERR_VALUE). device_points (n x 3 float32) and
  * device_counts (bins uint64, overwritten) are the caller's device buffers.

@@ -29,7 +29,8 @@ sys.path.insert(0, ROOT)
 from freud_gb300 import gsd  # noqa: E402
 from oracle import ref as R  # noqa: E402
 
-REF = "/root/reference/tests"
+# the reference tree (FREUD_REFERENCE_DIR); this script only runs where it exists
+REF = os.path.join(os.environ.get("FREUD_REFERENCE_DIR", "/root/reference"), "tests")
 LJ_GSD = os.path.join(REF, "integration", "files", "lj", "lj.gsd")
 LJ_RDF = os.path.join(REF, "integration", "files", "lj", "rdf.npz")
 GC_DIR = os.path.join(REF, "validation", "files", "steinhardt_average")

@@ -443,3 +443,22 @@ def test_steinhardt_compute_twice(freud):
     a = st.compute((box, pts), neighbors={"num_neighbors": 12}).ql.copy()
     b = st.compute((box, pts), neighbors={"num_neighbors": 12}).ql
     np.testing.assert_array_equal(a, b)
+
+
+def test_partly_periodic_box_refused(freud):
+    """A box that is not periodic on every axis: the reference takes images only
+    along periodic axes for a (box, points) system; the cell grids here fold every
+    axis, so the query is refused with ValueError instead of answered with folded
+    bonds (LinkCell / AABBQuery refuse it as the reference does)."""
+    rs = np.random.RandomState(3)
+    box = freud.box.Box.cube(10.0)
+    box.periodic = [True, True, False]
+    pts = box.make_absolute(rs.random_sample((500, 3))).astype(np.float32)
+    with pytest.raises(ValueError):
+        freud.locality.AABBQuery(box, pts).query(pts, {"r_max": 1.0}).toNeighborList()
+    with pytest.raises(ValueError):
+        freud.locality.LinkCell(box, pts, 1.0).query(pts, {"r_max": 1.0}).toNeighborList()
+    with pytest.raises(ValueError):
+        freud.density.RDF(10, 1.0).compute((box, pts))
+    with pytest.raises(ValueError):
+        freud.order.Steinhardt(6).compute((box, pts), neighbors={"r_max": 1.5})

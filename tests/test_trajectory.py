@@ -14,7 +14,9 @@ from conftest import load_golden
 from gsd_bytes import gsd_bytes, trajectory_bytes
 from oracle import oracle as O
 
-REF_TESTS = "/root/reference/tests"
+# the reference's test tree, when the environment names it (not on the GPU machine)
+REF_TESTS = os.path.join(os.environ.get("FREUD_REFERENCE_DIR", ""), "tests") if os.environ.get(
+    "FREUD_REFERENCE_DIR") else ""
 
 
 def _gsd():
@@ -98,7 +100,8 @@ def test_reader_rejects_malformed(tmp_path):
         gsd.open(str(tmp_path / "empty.gsd"), "wb")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_TESTS), reason="reference tree not present")
+@pytest.mark.skipif(not REF_TESTS or not os.path.isdir(REF_TESTS),
+                    reason="FREUD_REFERENCE_DIR does not name the reference tree")
 def test_reader_on_reference_files():
     gsd = _gsd()
     lj = load_golden("lj_traj")
