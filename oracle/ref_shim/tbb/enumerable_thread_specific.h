@@ -1,6 +1,8 @@
 // TBB-compatible shim (test infrastructure): enumerable_thread_specific and flatten2d.
 #ifndef FG_TBB_SHIM_ETS_H
 #define FG_TBB_SHIM_ETS_H
+#include <atomic>
+#include <cstdint>
 #include <deque>
 #include <functional>
 #include <iterator>
@@ -46,27 +48,50 @@ public:
     }
     enumerable_thread_specific(enumerable_thread_specific&& o) noexcept
         : m_init(std::move(o.m_init)), m_items(std::move(o.m_items)), m_index(std::move(o.m_index))
-    {}
+    {
+        o.m_gen = next_gen();
+    }
     enumerable_thread_specific& operator=(enumerable_thread_specific&& o) noexcept
     {
         m_init = std::move(o.m_init);
         m_items = std::move(o.m_items);
         m_index = std::move(o.m_index);
+        m_gen = next_gen();
+        o.m_gen = next_gen();
         return *this;
     }
 
+    // The calling thread's element. A per-thread cache (this object, its
+    // generation, the element's address - deque elements do not move) answers
+    // repeated calls without the lock, as TBB's thread-local lookup does; the
+    // generation changes whenever the element set is rebuilt.
     reference local()
     {
+        thread_local const enumerable_thread_specific* owner = nullptr;
+        thread_local std::uint64_t owner_gen = 0;
+        thread_local T* cached = nullptr;
+        if (owner == this && owner_gen == m_gen)
+        {
+            return *cached;
+        }
         std::lock_guard<std::mutex> lock(m_mutex);
         const auto id = std::this_thread::get_id();
         auto found = m_index.find(id);
+        T* item;
         if (found != m_index.end())
         {
-            return m_items[found->second];
+            item = &m_items[found->second];
         }
-        m_items.push_back(m_init());
-        m_index[id] = m_items.size() - 1;
-        return m_items.back();
+        else
+        {
+            m_items.push_back(m_init());
+            m_index[id] = m_items.size() - 1;
+            item = &m_items.back();
+        }
+        owner = this;
+        owner_gen = m_gen;
+        cached = item;
+        return *item;
     }
 
     iterator begin() { return m_items.begin(); }
@@ -79,10 +104,22 @@ public:
     {
         m_items.clear();
         m_index.clear();
+        m_gen = next_gen();
     }
 
 private:
-    void rebuild_index(const enumerable_thread_specific& o) { m_index = o.m_index; }
+    void rebuild_index(const enumerable_thread_specific& o)
+    {
+        m_index = o.m_index;
+        m_gen = next_gen();
+    }
+    static std::uint64_t next_gen()
+    {
+        static std::atomic<std::uint64_t> counter {1};
+        return counter.fetch_add(1);
+    }
+
+    std::uint64_t m_gen = next_gen();
 
     std::function<T()> m_init;
     container m_items;
