@@ -665,7 +665,7 @@ def run_only(args):
     if args.batch_config:
         _lib.set_batch_config(*[int(x) for x in args.batch_config.split(",")])
     fns = {"plain_rdf": lambda: measure_c1(freud, _lib, args.steps, args.warmup, cpu=False),
-           "steinhardt": lambda: measure_c3(freud, _lib, args.steps, args.warmup, cpu=False),
+           "steinhardt": lambda: measure_c3(freud, _lib, args.steps, args.warmup, cpu=not args.no_cpu_baseline),
            "correlation_function": lambda: measure_cf(freud, _lib, args.steps, args.warmup, cpu=False),
            "pmft": lambda: measure_pmft(freud, _lib, args.steps, args.warmup, cpu=False),
            "batched_frames": lambda: measure_c4(freud, _lib, args.steps, args.warmup, 8 if args.small else 64),

@@ -377,7 +377,8 @@ struct fg_steinhardt
     StLs st {};
     size_t stride = 0; // sum of (2l + 1)
     DevBuf qlm, qlm_ave, ql, ql_ave, wlv, sys;
-    std::vector<DevBuf> w3j;
+    DevBuf wl_terms; // Wigner-3j term classes of every l (launch_wl)
+    WlTerms wt {};
     std::vector<std::vector<double>> w3j_host; // per l, for the system Wl (computed once)
     std::vector<float> order; // frames x n_l
     uint32_t frames = 1;
@@ -2496,19 +2497,24 @@ fg_status fg_steinhardt_create(const uint32_t* ls, uint32_t n_l, int average, in
         std::stable_sort(st->st.sorted_k, st->st.sorted_k + n_l,
                          [&](int a, int b) { return st->st.l[a] < st->st.l[b]; });
         st_upload_tables(stream());
+        std::vector<int4> terms;
         for (uint32_t k = 0; k < n_l; ++k)
         {
-            DevBuf b;
             st->w3j_host.emplace_back();
             if (st->wl)
             {
-                const std::vector<double> w = wigner3j_table(static_cast<int>(ls[k]));
-                st->w3j_host.back() = w;
-                std::vector<float> f(w.begin(), w.end());
-                b.alloc(sizeof(float) * f.size());
-                FG_CUDA(cudaMemcpyAsync(b.p, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice, stream()));
+                st->w3j_host.back() = wigner3j_table(static_cast<int>(ls[k]));
+                const std::vector<int4> t = wl_term_classes(static_cast<int>(ls[k]), wigner3j);
+                st->wt.off[k] = static_cast<int>(terms.size());
+                st->wt.cnt[k] = static_cast<int>(t.size());
+                terms.insert(terms.end(), t.begin(), t.end());
             }
-            st->w3j.push_back(std::move(b));
+        }
+        if (!terms.empty())
+        {
+            st->wl_terms.alloc(sizeof(int4) * terms.size());
+            FG_CUDA(cudaMemcpyAsync(st->wl_terms.p, terms.data(), sizeof(int4) * terms.size(), cudaMemcpyHostToDevice,
+                                    stream()));
         }
         sync();
         *out = st.release();
@@ -2593,7 +2599,7 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
         launch_qlm(nq->dbox, nq->dpts, n, nl->ij.as<uint2>(), nl->dist.as<float>(),
                    use_w ? nl->weights.as<float>() : nullptr, nl->seg.as<uint32_t>(), nl->cnt.as<uint32_t>(), st->st,
                    use_w ? 1 : 0, st->qlm.as<float2>(), st->ql.as<float>(), s, nullptr,
-                   static_cast<double>(nl->nb) / std::max<uint32_t>(n, 1));
+                   static_cast<double>(nl->nb) / std::max<uint32_t>(n, 1), st->wl ? 1 : 0);
         const float2* src = st->qlm.as<float2>();
         const float* qn = st->ql.as<float>();
         if (st->average)
@@ -2617,8 +2623,8 @@ fg_status fg_steinhardt_compute(fg_steinhardt* st, fg_nq* nq, const fg_nlist* nl
         if (st->wl)
         {
             st->wlv.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(n) * st->st.nl, 1));
-            for (int k = 0; k < st->st.nl; ++k)
-                launch_wl(n, st->st, k, src, st->w3j[k].as<float>(), qn, st->wl_normalize ? 1 : 0, st->wlv.as<float>(), s);
+            launch_wl(n, st->st, st->wt, st->wl_terms.as<int4>(), src, qn, st->wl_normalize ? 1 : 0,
+                      st->wlv.as<float>(), s);
         }
         FG_CUDA(cudaGetLastError());
         std::vector<double> sys(2 * st->stride);
@@ -3430,7 +3436,7 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
         for (int k = 0; k < st->st.nl; ++k)
         {
             key_b.push_back(static_cast<uint64_t>(st->st.l[k]));
-            key_b.push_back(reinterpret_cast<uint64_t>(st->w3j[k].p));
+            key_b.push_back(reinterpret_cast<uint64_t>(st->wl_terms.p));
         }
         run_graph(fr->st_graph_b, fr->graphs, key_b, "graph:steinhardt_frames", [&] {
             launch_frames_ball_fill(v, p, P, fr->st_offsets.as<uint64_t>(), fr->st_j.as<uint32_t>(),
@@ -3439,7 +3445,7 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
                                          fr->st_seg.as<uint32_t>(), s);
             launch_qlm(g.fd_host[0].b, fr->dpts, P, nullptr, nullptr, nullptr, fr->st_seg.as<uint32_t>(),
                        fr->st_counts.as<uint32_t>(), st->st, 0, st->qlm.as<float2>(), st->ql.as<float>(), s,
-                       fr->st_vd.as<float4>(), static_cast<double>(nb) / std::max<uint32_t>(P, 1));
+                       fr->st_vd.as<float4>(), static_cast<double>(nb) / std::max<uint32_t>(P, 1), st->wl ? 1 : 0);
             const float2* src = st->qlm.as<float2>();
             const float* qn = st->ql.as<float>();
             if (st->average)
@@ -3454,9 +3460,8 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
                               fr->st_partial.as<double>(), fr->st_sys.as<double>(), s);
             if (st->wl)
             {
-                for (int k = 0; k < st->st.nl; ++k)
-                    launch_wl(P, st->st, k, src, st->w3j[k].as<float>(), qn, st->wl_normalize ? 1 : 0,
-                              st->wlv.as<float>(), s);
+                launch_wl(P, st->st, st->wt, st->wl_terms.as<int4>(), src, qn, st->wl_normalize ? 1 : 0,
+                          st->wlv.as<float>(), s);
             }
         });
         FG_CUDA(cudaGetLastError());

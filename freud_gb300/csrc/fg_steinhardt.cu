@@ -15,10 +15,14 @@
 // scipy.special.sph_harm_y. Accumulates w * Y, divides by the total weight, and
 // reduces ql over the particle's lanes with shuffles.
 // k_ave: the same mapping gathers the neighbours' qlm (Steinhardt.cc:224-289).
-// k_wl: thread per (particle, l), Wigner-3j triple sum with compensated float sum.
+// k_wl: thread per particle, the Wigner-3j triple sums over classes of equal terms in float-float.
 // The FP64 system sums (qlm or averaged qlm over the particles, divided by N)
 // are taken by the per-frame column-sum kernels of fg_batch.cu.
 #include <algorithm>
+#include <array>
+#include <cstring>
+#include <utility>
+#include <vector>
 #include <cmath>
 #include <cstdint>
 
@@ -35,6 +39,11 @@ constexpr unsigned FULL = 0xffffffffu;
 __constant__ float c_K[ST_MAX_L + 1];                    // Q_m^m prefactors
 __constant__ float c_a[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // a_lm at [l*(L+1)+m]
 __constant__ float c_b[(ST_MAX_L + 1) * (ST_MAX_L + 1)]; // b_lm
+// float-float copies (hi, lo) of K_m and of the recurrence coefficients, with
+// a_{m+1,m} = sqrt(2m + 3) and b_{m+1,m} = 0 so one formula covers every step
+__constant__ float2 c_Kff[ST_MAX_L + 1];
+__constant__ float2 c_aff[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
+__constant__ float2 c_bff[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
 
 // cos(theta) = clamp(dz / d) and sin(theta) of a bond (Steinhardt.cc:163-172: the
 // wrapped z over the bond distance, clamped; theta = 0 when d = 0). cos rounded
@@ -697,6 +706,328 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// Float-float arithmetic: a value is the unevaluated sum h + l of two floats.
+// Products by Dekker's method with the exact FMA remainder; sums by Knuth's
+// TwoSum followed by a Fast2Sum renormalisation (the "sloppy" double-float add
+// of Hida, Li and Bailey's QD library). Each operation keeps about 2^-44 of the
+// value, so a 31-step Legendre recurrence stays far below one float ulp. Every
+// operation is an explicit round-to-nearest intrinsic, which the compiler neither
+// contracts nor reorders.
+struct ffl
+{
+    float h, l;
+};
+
+__device__ __forceinline__ ffl ff_mul(ffl a, ffl b)
+{
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return {p, e};
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ ffl ff_add(ffl a, ffl b)
+{
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ ffl ff_sub(ffl a, ffl b)
+{
+    return ff_add(a, {-b.h, -b.l});
+}
+
+__device__ __forceinline__ ffl ff_sqrt(ffl v)
+{
+    if (!(v.h > 0.0f))
+        return {0.0f, 0.0f};
+    const float s = __fsqrt_rn(v.h);
+    const float r = __fadd_rn(__fmaf_rn(-s, s, v.h), v.l);
+    return {s, __fdiv_rn(r, __fmul_rn(2.0f, s))};
+}
+
+// acc += y, hi parts by TwoSum, the rounding errors and lo parts summed apart
+__device__ __forceinline__ void ff_acc(float& ah, float& al, ffl y)
+{
+    float s, e;
+    two_sum(ah, y.h, s, e);
+    ah = s;
+    al = __fadd_rn(al, __fadd_rn(e, y.l));
+}
+
+// (h + l) / w rounded to float: quotient, exact remainder, one correction
+__device__ __forceinline__ float ff_div_f(float h, float l, float w)
+{
+    const float q = __fdiv_rn(h, w);
+    const float r = __fadd_rn(__fmaf_rn(-q, w, h), l);
+    return __fadd_rn(q, __fdiv_rn(r, w));
+}
+
+// Geometry of one bond in float-float, as the FP64 oracle takes it:
+// cos(theta) = clamp(dz / d) (Steinhardt.cc:163-172), sin(theta) =
+// sqrt(1 - cos^2), and w = sin(theta) e^{i phi} with e^{i phi} = (dx + i dy) / rho,
+// phi = atan2(dy, dx) (Steinhardt.cc:160).
+struct BondFF
+{
+    ffl ct;     // cos(theta)
+    ffl wr, wi; // sin(theta) e^{i phi}
+    float w;    // bond weight (0 for an empty slot)
+};
+
+__device__ __forceinline__ BondFF bond_ff(float dx, float dy, float dz, float d, float w)
+{
+    BondFF g;
+    g.w = w;
+    g.ct = {1.0f, 0.0f};
+    g.wr = {0.0f, 0.0f};
+    g.wi = {0.0f, 0.0f};
+    if (d == 0.0f)
+        return g;
+    const float hi = __fdiv_rn(dz, d);
+    const float lo = __fdiv_rn(__fmaf_rn(-hi, d, dz), d);
+    if (hi > 1.0f || (hi == 1.0f && lo >= 0.0f))
+        return g;
+    if (hi < -1.0f || (hi == -1.0f && lo <= 0.0f))
+    {
+        g.ct = {-1.0f, 0.0f};
+        return g;
+    }
+    g.ct = {hi, lo};
+    const ffl c2 = ff_mul(g.ct, g.ct);
+    const ffl st = ff_sqrt(ff_sub({1.0f, 0.0f}, c2));
+    // rho^2 = dx^2 + dy^2 exactly as two float-float products summed
+    const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy);
+    const ffl r2 = ff_add({px, __fmaf_rn(dx, dx, -px)}, {py, __fmaf_rn(dy, dy, -py)});
+    if (!(r2.h > 0.0f))
+    {
+        // on the z axis: atan2(+-0, x) is 0 for x = +0 and pi for x = -0
+        g.wr = {signbit(dx) ? -st.h : st.h, signbit(dx) ? -st.l : st.l};
+        return g;
+    }
+    const ffl rho = ff_sqrt(r2);
+    const float q = __frcp_rn(rho.h);
+    float e = __fmaf_rn(-rho.h, q, 1.0f);
+    e = __fmaf_rn(-rho.l, q, e);
+    const ffl inv = {q, __fmul_rn(e, q)};
+    const ffl sinv = ff_mul(st, inv);
+    g.wr = ff_mul(sinv, {dx, 0.0f});
+    g.wi = ff_mul(sinv, {dy, 0.0f});
+    return g;
+}
+
+// Every Y_l^m of a bond in float-float (Wl path): thread per particle, two bonds
+// per pass (their recurrences share the coefficient loads and give each step two
+// independent chains). Per order m the power (w sin(theta) e^{i phi})^m is one
+// complex float-float product from the previous order's, the prefactor K_m times
+// it, then the normalised recurrence R_{l+1} = a (ct R_l - b R_{l-1}) from R_m = 1
+// up to l_max, and at each requested l the term R_l x prefactor is added to the
+// particle's float-float sum of (l, m) in shared memory (acc[slot][thread]:
+// re hi, re lo, im hi, im lo). The weights are real, so the negative orders are
+// (-1)^m conj of the sums. The final division by the total weight rounds once,
+// so each qlm is the FP64 value to within about one float ulp. Rows are written
+// through the warp's shared-memory sums, one particle's row per pass, coalesced.
+template<int T>
+__global__ void __launch_bounds__(T, 256 / T)
+    k_qlm_ff(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
+             const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
+             const uint32_t* __restrict__ cnt, const float4* __restrict__ bvd, StLs ls, int weighted,
+             float2* __restrict__ qlm_out, float* __restrict__ ql_out)
+{
+    extern __shared__ float4 acc[]; // [slots][T]
+    __shared__ int s_lt[ST_MAX_NL + 1];
+    __shared__ int s_base[ST_MAX_NL + 1];
+    __shared__ int s_k[ST_MAX_NL];
+    __shared__ size_t s_off[ST_MAX_NL];
+    __shared__ float s_norm[ST_MAX_NL];
+    if (threadIdx.x == 0)
+    {
+        int o = 0;
+        for (int kk = 0; kk < ls.nl; ++kk)
+        {
+            const int k = ls.sorted_k[kk];
+            s_k[kk] = k;
+            s_lt[kk] = ls.l[k];
+            s_base[kk] = o;
+            s_off[kk] = ls.qlm_offset[k];
+            s_norm[kk] = ls.norm[k];
+            o += ls.l[k] + 1;
+        }
+        s_lt[ls.nl] = -1;
+        s_base[ls.nl] = o;
+    }
+    __syncthreads();
+    const int nl = ls.nl;
+    const int lmax = ls.max_l;
+    const int nslot = s_base[nl];
+    const int lane = threadIdx.x & 31;
+    float4* my = acc + threadIdx.x;
+    for (uint32_t i0 = blockIdx.x * T; i0 < n; i0 += gridDim.x * T)
+    {
+        const uint32_t i = i0 + threadIdx.x;
+        for (int o = 0; o < nslot; ++o)
+            my[o * T] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float tw = 0.0f;
+        if (i < n)
+        {
+            const uint32_t b0 = seg[i];
+            const uint32_t nbond = cnt[i];
+            float pix = 0.f, piy = 0.f, piz = 0.f;
+            if (bvd == nullptr)
+            {
+                pix = pts[3 * (size_t) i];
+                piy = pts[3 * (size_t) i + 1];
+                piz = pts[3 * (size_t) i + 2];
+            }
+            for (uint32_t e0 = 0; e0 < nbond; e0 += 2)
+            {
+                BondFF g[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+                {
+                    float dx = 0.f, dy = 0.f, dz = 0.f, d = 0.f, w = 0.f;
+                    if (e0 + u < nbond)
+                    {
+                        const uint32_t e = b0 + e0 + u;
+                        if (bvd != nullptr)
+                        {
+                            const float4 v = bvd[e];
+                            dx = v.x;
+                            dy = v.y;
+                            dz = v.z;
+                            d = v.w;
+                        }
+                        else
+                        {
+                            const uint32_t j = ij[e].y;
+                            box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pix), __fsub_rn(pts[3 * (size_t) j + 1], piy),
+                                     __fsub_rn(pts[3 * (size_t) j + 2], piz), dx, dy, dz);
+                            d = dist[e];
+                        }
+                        w = weighted ? weights[e] : 1.0f;
+                    }
+                    g[u] = bond_ff(dx, dy, dz, d, w);
+                    tw = __fadd_rn(tw, w);
+                }
+                // weight x (sin(theta) e^{i phi})^m, starting at m = 0
+                ffl pr[2] = {{g[0].w, 0.0f}, {g[1].w, 0.0f}};
+                ffl pi[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+                int kk0 = 0;
+                for (int m = 0; m <= lmax; ++m)
+                {
+                    if (m > 0)
+                    {
+#pragma unroll
+                        for (int u = 0; u < 2; ++u)
+                        {
+                            const ffl nr = ff_sub(ff_mul(pr[u], g[u].wr), ff_mul(pi[u], g[u].wi));
+                            pi[u] = ff_add(ff_mul(pr[u], g[u].wi), ff_mul(pi[u], g[u].wr));
+                            pr[u] = nr;
+                        }
+                    }
+                    while (s_lt[kk0] >= 0 && s_lt[kk0] < m)
+                        ++kk0;
+                    if (s_lt[kk0] < 0)
+                        break;
+                    const float2 kf = c_Kff[m];
+                    const ffl K = {kf.x, kf.y};
+                    ffl fr[2], fi[2], r1[2], r0[2];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                    {
+                        fr[u] = ff_mul(K, pr[u]);
+                        fi[u] = ff_mul(K, pi[u]);
+                        r1[u] = {1.0f, 0.0f};
+                        r0[u] = {0.0f, 0.0f};
+                    }
+                    int kk = kk0;
+                    for (int l = m;; ++l)
+                    {
+                        if (l == s_lt[kk])
+                        {
+                            float4* slot = my + (s_base[kk] + m - 0) * T;
+                            float4 v = *slot;
+#pragma unroll
+                            for (int u = 0; u < 2; ++u)
+                            {
+                                ff_acc(v.x, v.y, ff_mul(r1[u], fr[u]));
+                                ff_acc(v.z, v.w, ff_mul(r1[u], fi[u]));
+                            }
+                            *slot = v;
+                            ++kk;
+                            if (s_lt[kk] < 0)
+                                break;
+                        }
+                        const float2 af = c_aff[(l + 1) * (ST_MAX_L + 1) + m];
+                        const float2 bf = c_bff[(l + 1) * (ST_MAX_L + 1) + m];
+#pragma unroll
+                        for (int u = 0; u < 2; ++u)
+                        {
+                            const ffl t = ff_sub(ff_mul(g[u].ct, r1[u]), ff_mul({bf.x, bf.y}, r0[u]));
+                            r0[u] = r1[u];
+                            r1[u] = ff_mul({af.x, af.y}, t);
+                        }
+                    }
+                }
+            }
+        }
+        // sums -> qlm (m >= 0) in place, and ql
+        if (i < n)
+        {
+            for (int kk = 0; kk < nl; ++kk)
+            {
+                const int l = s_lt[kk];
+                float part = 0.0f;
+                for (int m = 0; m <= l; ++m)
+                {
+                    float4* slot = my + (s_base[kk] + m) * T;
+                    const float4 v = *slot;
+                    const float qr = ff_div_f(v.x, v.y, tw);
+                    const float qi = ff_div_f(v.z, v.w, tw);
+                    slot->x = qr;
+                    slot->y = qi;
+                    const float sq = __fmaf_rn(qr, qr, __fmul_rn(qi, qi));
+                    part = __fadd_rn(part, m > 0 ? __fmul_rn(2.0f, sq) : sq);
+                }
+                ql_out[static_cast<size_t>(i) * nl + s_k[kk]] = sqrtf(part * s_norm[kk]);
+            }
+        }
+        __syncwarp();
+        // the warp's rows: (2l + 1) consecutive float2 per particle, particles consecutive
+        const uint32_t w0 = i0 + (threadIdx.x & ~31u);
+        const int wcol = threadIdx.x & ~31;
+        for (int kk = 0; kk < nl; ++kk)
+        {
+            const int l = s_lt[kk];
+            const int width = 2 * l + 1;
+            float2* out = qlm_out + s_off[kk] + static_cast<size_t>(w0) * width;
+            for (int p = 0; p < 32 && w0 + p < n; ++p)
+            {
+                for (int c = lane; c < width; c += 32)
+                {
+                    const int m = c <= l ? c : c - l;
+                    const float4 v = acc[(s_base[kk] + m) * T + wcol + p];
+                    float2 q = make_float2(v.x, v.y);
+                    if (c > l)
+                        q = (m & 1) ? make_float2(-v.x, v.y) : make_float2(v.x, -v.y);
+                    out[static_cast<size_t>(p) * width + c] = q;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Neighbour averaging: ave(i) = (sum_j qlm(j) + qlm(i)) / (1 + n_i). Per l, the
 // neighbour indices of LANES bonds are loaded at once (one per lane) and
 // broadcast, so the row gathers do not wait on the index loads one by one.
@@ -777,62 +1108,182 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-// Wl per (particle, l): sum over m1 + m2 + m3 = 0 of w3j * Re(q_m1 q_m2 q_m3)
-// (Wigner3j.cc:22-57), coefficients in the reference's iteration order.
+// Neighbour averaging with the row entries of every l flattened: P lanes per
+// particle, lane s owns entries s, s + P, ... of the E = sum (2l + 1) entries
+// (each a fixed (l, column) of the per-l arrays), so one neighbour's whole row
+// is R independent loads per lane, contiguous across the lanes. Sums run over
+// the bonds in order, then the particle's own row, over (1 + n_i)
+// (Steinhardt.cc:224-289), as k_ave; ql per l is a shuffle reduction of the
+// lanes' squared magnitudes.
+template<int P, int R>
 __global__ void __launch_bounds__(128)
-    k_wl(uint32_t n, int l, int k, int nl, size_t qlm_offset, const float2* __restrict__ src,
-         const float* __restrict__ w3j, const float* __restrict__ qnorm, int normalize, float norm_factor,
-         float* __restrict__ wl_out)
+    k_ave_flat(uint32_t n, const uint2* __restrict__ ij, const uint32_t* __restrict__ bj,
+               const uint32_t* __restrict__ seg, const uint32_t* __restrict__ cnt, StLs ls, int E,
+               const float2* __restrict__ qlm, float2* __restrict__ ave, float* __restrict__ ql_ave,
+               const uint32_t* __restrict__ order)
 {
-    extern __shared__ float2 rows[];
-    const int nm = 2 * l + 1;
-    const uint32_t i0 = blockIdx.x * blockDim.x;
-    // the block's rows (coalesced), then the l's Wigner-3j coefficients (every
-    // thread reads coefficient c at the same time: a shared-memory broadcast)
-    float* w3s = reinterpret_cast<float*>(rows + blockDim.x * static_cast<uint32_t>(nm));
-    for (uint32_t e = threadIdx.x; e < blockDim.x * static_cast<uint32_t>(nm); e += blockDim.x)
+    const int lane = threadIdx.x & 31;
+    const int sub = lane % P;
+    const int group = lane / P;
+    const unsigned gmask = P == 32 ? FULL : (((1u << P) - 1u) << (group * P));
+    const int gpb = blockDim.x / P;
+    size_t off[R];
+    uint32_t width[R];
+    int kof[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
     {
-        const uint32_t gi = i0 + e / nm;
-        rows[e] = gi < n ? src[qlm_offset + static_cast<size_t>(i0) * nm + e] : make_float2(0.f, 0.f);
-    }
-    const int nterms = 3 * l * l + 3 * l + 1;
-    for (int e = threadIdx.x; e < nterms; e += blockDim.x)
-        w3s[e] = w3j[e];
-    __syncthreads();
-    const uint32_t i = i0 + threadIdx.x;
-    if (i >= n)
-    {
-        return;
-    }
-    const float2* q = rows + threadIdx.x * nm;
-    float sum = 0.0f, comp = 0.0f;
-    int c = 0;
-    for (int m1 = -l; m1 <= l; ++m1)
-    {
-        const float2 a = q[m1 < 0 ? l - m1 : m1];
-        const int lo = max(-l - m1, -l);
-        const int hi = min(l - m1, l);
-        for (int m2 = lo; m2 <= hi; ++m2, ++c)
+        const int e = sub + r * P;
+        off[r] = 0;
+        width[r] = 0;
+        kof[r] = -1;
+        int start = 0;
+        for (int k = 0; k < ls.nl; ++k)
         {
-            const int m3 = -m1 - m2;
-            const float2 bq = q[m2 < 0 ? l - m2 : m2];
-            const float2 cq = q[m3 < 0 ? l - m3 : m3];
-            const float abr = a.x * bq.x - a.y * bq.y;
-            const float abi = a.x * bq.y + a.y * bq.x;
-            const float term = w3s[c] * (abr * cq.x - abi * cq.y);
-            // compensated (Kahan) summation
-            const float y = term - comp;
-            const float t = sum + y;
-            comp = (t - sum) - y;
-            sum = t;
+            const int w = 2 * ls.l[k] + 1;
+            if (e >= start && e < start + w)
+            {
+                off[r] = ls.qlm_offset[k] + static_cast<size_t>(e - start);
+                width[r] = static_cast<uint32_t>(w);
+                kof[r] = k;
+            }
+            start += w;
         }
     }
-    if (normalize)
+    for (uint32_t t = blockIdx.x * gpb + threadIdx.x / P; t < n; t += gridDim.x * gpb)
     {
-        const float nf = sqrtf(norm_factor) / qnorm[static_cast<size_t>(i) * nl + k];
-        sum *= nf * nf * nf;
+        const uint32_t i = order != nullptr ? order[t] : t;
+        const uint32_t b0 = seg[i];
+        const uint32_t nbond = cnt[i];
+        float sr[R], si[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            sr[r] = si[r] = 0.0f;
+        for (uint32_t base = 0; base < nbond; base += P)
+        {
+            const uint32_t jl =
+                base + sub < nbond ? (bj != nullptr ? bj[b0 + base + sub] : ij[b0 + base + sub].y) : 0u;
+            const uint32_t nh = min(static_cast<uint32_t>(P), nbond - base);
+#pragma unroll 4
+            for (uint32_t u = 0; u < nh; ++u)
+            {
+                const uint32_t j = __shfl_sync(gmask, jl, u, P);
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+                {
+                    if (kof[r] >= 0)
+                    {
+                        const float2 v = qlm[off[r] + static_cast<size_t>(j) * width[r]];
+                        sr[r] += v.x;
+                        si[r] += v.y;
+                    }
+                }
+            }
+        }
+        const float cntf = static_cast<float>(1u + nbond);
+        float sq[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+        {
+            sq[r] = 0.0f;
+            if (kof[r] >= 0)
+            {
+                const size_t a = off[r] + static_cast<size_t>(i) * width[r];
+                const float2 own = qlm[a];
+                const float qr = (sr[r] + own.x) / cntf;
+                const float qi = (si[r] + own.y) / cntf;
+                ave[a] = make_float2(qr, qi);
+                sq[r] = qr * qr + qi * qi;
+            }
+        }
+        for (int k = 0; k < ls.nl; ++k)
+        {
+            float part = 0.0f;
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                part += kof[r] == k ? sq[r] : 0.0f;
+            for (int o = P / 2; o > 0; o >>= 1)
+                part += __shfl_xor_sync(gmask, part, o, P);
+            if (sub == 0)
+                ql_ave[static_cast<size_t>(i) * ls.nl + k] = sqrtf(part * ls.norm[k]);
+        }
     }
-    wl_out[static_cast<size_t>(i) * nl + k] = sum;
+}
+
+// Wl per particle, every l of the set: thread per particle, the block's rows of
+// m >= 0 entries staged in shared memory (odd row stride: conflict-free), the
+// l's term classes broadcast from shared memory. Each class adds
+// C x Re(q_a q_b q_c) in float-float (exact float products, TwoSum sums), so the
+// sum is the FP64 triple sum of the float qlm to within about 2^-44 of its terms;
+// it is rounded once, then normalised by (sqrt(4 pi / (2l + 1)) / ql)^3
+// (Steinhardt.cc:338-352).
+__device__ __forceinline__ float2 wl_member(const float2* row, unsigned rec, int slot)
+{
+    const float2 q = row[(rec >> (8 * slot)) & 0xffu];
+    const unsigned f = rec >> (24 + 2 * slot);
+    return make_float2(__int_as_float(__float_as_int(q.x) ^ ((f & 1u) << 31)),
+                       __int_as_float(__float_as_int(q.y) ^ (((f >> 1) & 1u) << 31)));
+}
+
+__device__ __forceinline__ ffl two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+constexpr int WL_T = 128;
+
+__global__ void __launch_bounds__(WL_T)
+    k_wl(uint32_t n, StLs ls, WlTerms wt, const int4* __restrict__ terms, const float2* __restrict__ src,
+         const float* __restrict__ qnorm, int normalize, float* __restrict__ wl_out)
+{
+    extern __shared__ float4 wl_smem[];
+    const uint32_t i0 = blockIdx.x * WL_T;
+    const uint32_t i = i0 + threadIdx.x;
+    for (int k = 0; k < ls.nl; ++k)
+    {
+        const int l = ls.l[k];
+        const int lp1 = l + 1;
+        const int stride = lp1 | 1;
+        int4* s_terms = reinterpret_cast<int4*>(wl_smem);
+        float2* rows = reinterpret_cast<float2*>(wl_smem + wt.cnt[k]);
+        __syncthreads();
+        for (int t = threadIdx.x; t < wt.cnt[k]; t += WL_T)
+            s_terms[t] = terms[wt.off[k] + t];
+        const float2* base = src + ls.qlm_offset[k];
+        for (int e = threadIdx.x; e < WL_T * lp1; e += WL_T)
+        {
+            const int p = e / lp1;
+            const int m = e - p * lp1;
+            rows[p * stride + m] =
+                i0 + p < n ? base[static_cast<size_t>(i0 + p) * (2 * l + 1) + m] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        if (i < n)
+        {
+            const float2* row = rows + threadIdx.x * stride;
+            float ah = 0.0f, al = 0.0f;
+            for (int t = 0; t < wt.cnt[k]; ++t)
+            {
+                const int4 rec = s_terms[t];
+                const unsigned r = static_cast<unsigned>(rec.x);
+                const float2 qa = wl_member(row, r, 0);
+                const float2 qb = wl_member(row, r, 1);
+                const float2 qc = wl_member(row, r, 2);
+                const ffl ur = ff_sub(two_prod(qa.x, qb.x), two_prod(qa.y, qb.y));
+                const ffl ui = ff_add(two_prod(qa.x, qb.y), two_prod(qa.y, qb.x));
+                const ffl re = ff_sub(ff_mul(ur, {qc.x, 0.0f}), ff_mul(ui, {qc.y, 0.0f}));
+                ff_acc(ah, al, ff_mul({__int_as_float(rec.y), __int_as_float(rec.z)}, re));
+            }
+            float sum = __fadd_rn(ah, al);
+            if (normalize)
+            {
+                const float nf = sqrtf(ls.norm[k]) / qnorm[static_cast<size_t>(i) * ls.nl + k];
+                sum *= nf * nf * nf;
+            }
+            wl_out[static_cast<size_t>(i) * ls.nl + k] = sum;
+        }
+    }
 }
 
 // FP64 column sums: sys[c] += sum_i src[i, c] / n over a row range, compensated.
@@ -881,6 +1332,39 @@ void st_upload_tables(cudaStream_t s)
             B[l * (L + 1) + m] = static_cast<float>(bb);
         }
     }
+    // float-float tables: hi = RN(x), lo = RN(x - hi) of the FP64 value
+    static float2 Kff[ST_MAX_L + 1];
+    static float2 Aff[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
+    static float2 Bff[(ST_MAX_L + 1) * (ST_MAX_L + 1)];
+    auto split = [](double x) {
+        const float h = static_cast<float>(x);
+        return make_float2(h, static_cast<float>(x - static_cast<double>(h)));
+    };
+    for (int m = 0; m <= L; ++m)
+    {
+        double lg = 0.5 * (std::log(2.0 * m + 1.0) - std::log(4.0 * M_PI) - std::lgamma(2.0 * m + 1.0));
+        for (int t = 1; t <= m; ++t)
+            lg += std::log(2.0 * t - 1.0);
+        Kff[m] = split(((m & 1) ? -1.0 : 1.0) * std::exp(lg));
+        for (int l = 0; l <= L; ++l)
+        {
+            double a = 0.0, bb = 0.0;
+            if (l == m + 1)
+            {
+                a = std::sqrt(2.0 * m + 3.0);
+            }
+            else if (l >= m + 2)
+            {
+                a = std::sqrt((4.0 * l * l - 1.0) / (static_cast<double>(l) * l - static_cast<double>(m) * m));
+                bb = std::sqrt(((l - 1.0) * (l - 1.0) - static_cast<double>(m) * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+            }
+            Aff[l * (L + 1) + m] = split(a);
+            Bff[l * (L + 1) + m] = split(bb);
+        }
+    }
+    cudaMemcpyToSymbolAsync(c_Kff, Kff, sizeof(Kff), 0, cudaMemcpyHostToDevice, s);
+    cudaMemcpyToSymbolAsync(c_aff, Aff, sizeof(Aff), 0, cudaMemcpyHostToDevice, s);
+    cudaMemcpyToSymbolAsync(c_bff, Bff, sizeof(Bff), 0, cudaMemcpyHostToDevice, s);
     cudaMemcpyToSymbolAsync(c_K, K, sizeof(K), 0, cudaMemcpyHostToDevice, s);
     cudaMemcpyToSymbolAsync(c_a, A, sizeof(A), 0, cudaMemcpyHostToDevice, s);
     cudaMemcpyToSymbolAsync(c_b, B, sizeof(B), 0, cudaMemcpyHostToDevice, s);
@@ -919,12 +1403,51 @@ void qlm_flat(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, 
 }
 } // namespace
 
+int qlm_ff_threads(const StLs& ls)
+{
+    int slots = 0;
+    for (int k = 0; k < ls.nl; ++k)
+        slots += ls.l[k] + 1;
+    return slots <= 64 ? 64 : 32;
+}
+
+size_t qlm_ff_smem(const StLs& ls)
+{
+    int slots = 0;
+    for (int k = 0; k < ls.nl; ++k)
+        slots += ls.l[k] + 1;
+    return static_cast<size_t>(slots) * qlm_ff_threads(ls) * sizeof(float4);
+}
+
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
-                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd, double mean_bonds)
+                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd, double mean_bonds, int precise)
 {
     if (n == 0)
     {
+        return;
+    }
+    if (precise)
+    {
+        const int T = qlm_ff_threads(ls);
+        const size_t smem = qlm_ff_smem(ls);
+        static bool configured = false;
+        if (!configured)
+        {
+            // the largest set: ten l values up to 31
+            const int most = 200 * 1024;
+            cudaFuncSetAttribute(k_qlm_ff<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+            cudaFuncSetAttribute(k_qlm_ff<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+            configured = true;
+        }
+        const uint32_t blocks = (n + T - 1) / T;
+        ProfScope prof_("k_qlm_ff", s);
+        if (T == 64)
+            k_qlm_ff<64><<<blocks, 64, smem, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm,
+                                                  ql);
+        else
+            k_qlm_ff<32><<<blocks, 32, smem, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm,
+                                                  ql);
         return;
     }
     if (ls.nl == 1 && ls.max_l <= 12)
@@ -1002,10 +1525,36 @@ void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t
     {
         return;
     }
+    int E = 0;
+    for (int k = 0; k < ls.nl; ++k)
+        E += 2 * ls.l[k] + 1;
+    const uint32_t cap = static_cast<uint32_t>(sm_count()) * 16;
+    if (E <= 128)
+    {
+        const int P = E <= 8 ? 8 : (E <= 16 ? 16 : 32);
+        const uint32_t per_block = 128 / P;
+        const uint32_t blocks = std::min<uint32_t>((n + per_block - 1) / per_block, cap);
+        auto go = [&](auto kernel) {
+            kernel<<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, E, qlm, ave, ql_ave, order);
+        };
+        ProfScope prof_("k_ave_flat", s);
+        if (P == 8)
+            go(k_ave_flat<8, 1>);
+        else if (P == 16)
+            go(k_ave_flat<16, 1>);
+        else if (E <= 32)
+            go(k_ave_flat<32, 1>);
+        else if (E <= 64)
+            go(k_ave_flat<32, 2>);
+        else if (E <= 96)
+            go(k_ave_flat<32, 3>);
+        else
+            go(k_ave_flat<32, 4>);
+        return;
+    }
     const int lanes = lanes_for(ls.max_l);
     const uint32_t groups = 128 / lanes;
     uint32_t blocks = (n + groups - 1) / groups;
-    const uint32_t cap = static_cast<uint32_t>(sm_count()) * 16;
     blocks = blocks < cap ? blocks : cap;
     if (lanes == 8)
         {
@@ -1024,29 +1573,66 @@ void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t
         }
 }
 
-void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float* w3j_dev, const float* qnorm,
-               int normalize, float* wl, cudaStream_t s)
+std::vector<int4> wl_term_classes(int l, double (*w3j)(int, int, int, int))
+{
+    // class of (m1, m2, m3): its sorted members or those of its negation,
+    // whichever sorts first; summed over the reference's index set
+    std::vector<std::pair<std::array<int, 3>, double>> cls;
+    for (int m1 = -l; m1 <= l; ++m1)
+    {
+        for (int m2 = std::max(-l - m1, -l); m2 <= std::min(l - m1, l); ++m2)
+        {
+            std::array<int, 3> t = {m1, m2, -m1 - m2};
+            std::sort(t.begin(), t.end());
+            std::array<int, 3> ng = {-t[2], -t[1], -t[0]};
+            const std::array<int, 3> key = ng < t ? ng : t;
+            auto it = std::find_if(cls.begin(), cls.end(), [&](const auto& c) { return c.first == key; });
+            const double v = w3j(l, m1, m2, -m1 - m2);
+            if (it == cls.end())
+                cls.push_back({key, v});
+            else
+                it->second += v;
+        }
+    }
+    std::vector<int4> out;
+    for (const auto& c : cls)
+    {
+        unsigned rec = 0;
+        for (int slot = 0; slot < 3; ++slot)
+        {
+            const int m = c.first[slot];
+            const int a = m < 0 ? -m : m;
+            rec |= static_cast<unsigned>(a) << (8 * slot);
+            if (m < 0)
+            {
+                // q_{-a} = (-1)^a conj(q_a): flip im for a even, re for a odd
+                rec |= ((a & 1) ? 1u : 2u) << (24 + 2 * slot);
+            }
+        }
+        const float h = static_cast<float>(c.second);
+        const float lo = static_cast<float>(c.second - static_cast<double>(h));
+        int4 r;
+        r.x = static_cast<int>(rec);
+        std::memcpy(&r.y, &h, 4);
+        std::memcpy(&r.z, &lo, 4);
+        r.w = 0;
+        out.push_back(r);
+    }
+    return out;
+}
+
+void launch_wl(uint32_t n, const StLs& ls, const WlTerms& wt, const int4* terms, const float2* src,
+               const float* qnorm, int normalize, float* wl, cudaStream_t s)
 {
     if (n == 0)
     {
         return;
     }
-    const int l = ls.l[k];
-    const size_t smem = 128 * static_cast<size_t>(2 * l + 1) * sizeof(float2) +
-                        static_cast<size_t>(3 * l * l + 3 * l + 1) * sizeof(float);
-    static bool configured = false;
-    if (!configured)
-    {
-        cudaFuncSetAttribute(k_wl, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(128 * (2 * ST_MAX_L + 1) * sizeof(float2) +
-                                              (3 * ST_MAX_L * ST_MAX_L + 3 * ST_MAX_L + 1) * sizeof(float)));
-        configured = true;
-    }
-    {
-        ProfScope prof_("k_wl", s);
-        k_wl<<<(n + 127) / 128, 128, smem, s>>>(n, l, k, ls.nl, ls.qlm_offset[k], src, w3j_dev, qnorm, normalize,
-                                                ls.norm[k], wl);
-    }
+    int most = 0;
+    for (int k = 0; k < ls.nl; ++k)
+        most = std::max(most, wt.cnt[k] * 16 + WL_T * ((ls.l[k] + 1) | 1) * 8);
+    ProfScope prof_("k_wl", s);
+    k_wl<<<(n + WL_T - 1) / WL_T, WL_T, most, s>>>(n, ls, wt, terms, src, qnorm, normalize, wl);
 }
 
 

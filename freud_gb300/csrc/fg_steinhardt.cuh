@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 
 #include "fg_common.cuh"
 
@@ -29,9 +30,12 @@ void st_upload_tables(cudaStream_t s);
 // and the bond distance, precomputed per bond (batched frames, where the box
 // differs per particle); without it they come from pts, box and dist.
 // mean_bonds (optional): bonds per particle, sizes the single-l kernel's work per warp.
+// precise: every Y_l^m and the sums over bonds in float-float, each qlm rounded
+// once (the Wl path, where the Wigner-3j triple sums cancel); else float32.
 void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, const float* dist,
                 const float* weights, const uint32_t* seg, const uint32_t* cnt, const StLs& ls, int weighted,
-                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd = nullptr, double mean_bonds = 0.0);
+                float2* qlm, float* ql, cudaStream_t s, const float4* bond_vd = nullptr, double mean_bonds = 0.0,
+                int precise = 0);
 // bond_j (optional): the neighbour index of each bond, used instead of ij[e].y.
 // order (optional): a permutation of the n particles to process them in (e.g. a
 // cell grid's slot order, so neighbours' qlm rows are reused from L2); results do
@@ -39,7 +43,21 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
 void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t* cnt, const StLs& ls,
                 const float2* qlm, float2* ave, float* ql_ave, cudaStream_t s, const uint32_t* bond_j = nullptr,
                 const uint32_t* order = nullptr);
-void launch_wl(uint32_t n, const StLs& ls, int k, const float2* src, const float* w3j_dev, const float* qnorm,
-               int normalize, float* wl, cudaStream_t s);
+// Wl of every requested l in one launch. The triple sum over m1 + m2 + m3 = 0 is
+// taken over classes of terms with equal Re(q_m1 q_m2 q_m3): the permutations of
+// (m1, m2, m3) and of (-m1, -m2, -m3) (q_{-m} = (-1)^m conj(q_m), and
+// m1 + m2 + m3 = 0). A class is one record (int4): |m| of its three members in
+// bits 0-7, 8-15, 16-23, per member a (re, im) sign flip in bits 24-29 (the
+// member is -|m|), then hi and lo floats of the FP64 sum of the Wigner-3j symbols
+// of the class (Wigner3j.cc:22-57 over the same index set). Records of l_k at
+// terms + off[k], cnt[k] of them.
+struct WlTerms
+{
+    int off[ST_MAX_NL];
+    int cnt[ST_MAX_NL];
+};
+std::vector<int4> wl_term_classes(int l, double (*w3j)(int, int, int, int));
+void launch_wl(uint32_t n, const StLs& ls, const WlTerms& wt, const int4* terms, const float2* src,
+               const float* qnorm, int normalize, float* wl, cudaStream_t s);
 
 } // namespace fg

@@ -99,8 +99,9 @@ def test_steinhardt_golden(freud, name):
     np.testing.assert_allclose(ql, g["ql"], rtol=1e-5, atol=1e-6)
     po = np.asarray(st.particle_order).reshape(g["particle_order"].shape)
     scale = np.max(np.abs(g["particle_order"]), axis=0)
-    # Wl: the reference itself is float32 with cancellation; compare on the |w| scale
-    assert np.all(np.abs(po - g["particle_order"]) <= 5e-4 * scale + 1e-6)
+    # Wl: the reference's own float32 triple sums sit up to 5.6e-6 of the |w| scale
+    # from FP64 (W10); the values here are within 1e-5 |w| + 1e-7 of FP64
+    assert np.all(np.abs(po - g["particle_order"]) <= 2e-5 * scale + 1e-7)
     np.testing.assert_allclose(np.atleast_1d(st.order), g["order"], rtol=5e-5, atol=1e-6)
     qlm = st.particle_harmonics
     qlm = np.concatenate([q.reshape(-1) for q in qlm]) if isinstance(qlm, list) else qlm.reshape(-1)
@@ -357,27 +358,27 @@ def test_empty_result(freud):
     np.testing.assert_array_equal(nl.neighbor_counts, np.zeros(100, np.uint32))
 
 
-def test_steinhardt_vs_fp64_oracle(freud):
-    """Ql within 1e-5 relative of the FP64 oracle. Wl: |dw| <= 1e-5 (|w| + M), where M
-    is the sum of the magnitudes of the Wigner-3j terms: 1e-5 relative to the scale of
-    the summands. The float32 Ylm / qlm feeding the sum carry ~1e-7 to 1e-6 relative
-    error, which the cancellation in the sum amplifies by M / |w| (W10 of near-perfect
-    FCC nearly cancels); where M / |w| is small this is a 1e-5 relative bound."""
+@pytest.mark.parametrize("average", [True, False])
+def test_steinhardt_vs_fp64_oracle(freud, average):
+    """16,384-point noisy FCC crystal, 12 nearest neighbours, l = 4..12: Ql within
+    1e-5 relative of the FP64 oracle; normalised Wl within 1e-5 |w| + 1e-7 for every
+    particle and l, W10 included (its Wigner-3j triple sum cancels hardest on FCC,
+    so the Wl path computes the harmonics and the sums over bonds in float-float)."""
     from golden.make_golden import fcc
 
-    box, pts = fcc(6, 1.5874, 0.05, 77)
+    box, pts = fcc(16, 1.5874, 0.05, 77)
     fbox = box_of(freud, np.asarray(box, np.float32))
     ls = [4, 6, 8, 10, 12]
-    st = freud.order.Steinhardt(ls, average=True, wl=True, wl_normalize=True)
+    st = freud.order.Steinhardt(ls, average=average, wl=True, wl_normalize=True)
     st.compute((fbox, pts), neighbors={"num_neighbors": 12})
     ij, d, v = O.query(box, pts, num_neighbors=12, exclude_ii=True)
-    o = O.steinhardt(ls, box, pts, ij, d, average=True, wl=True, wl_normalize=True)
-    np.testing.assert_allclose(st.ql, o["ql_ave"], rtol=1e-5)
-    w, mag = o["wl"], o["wl_mag"]
+    o = O.steinhardt(ls, box, pts, ij, d, average=average, wl=True, wl_normalize=True)
+    np.testing.assert_allclose(st.ql, o["ql_ave"] if average else o["ql"], rtol=1e-5)
+    w = o["wl"]
     err = np.abs(st.particle_order - w)
-    print("max |dw| / |w| per l:", np.max(err / np.abs(w), axis=0))
-    print("max |dw| / M per l:", np.max(err / mag, axis=0))
-    assert np.all(err <= 1e-5 * (np.abs(w) + mag))
+    print("max |dw| / (1e-5 |w| + 1e-7) per l:", np.max(err / (1e-5 * np.abs(w) + 1e-7), axis=0))
+    assert np.all(err <= 1e-5 * np.abs(w) + 1e-7)
+    np.testing.assert_allclose(np.atleast_1d(st.order), o["order"], rtol=1e-5, atol=1e-7)
     st2 = freud.order.Steinhardt(ls)
     st2.compute((fbox, pts), neighbors={"num_neighbors": 12})
     o2 = O.steinhardt(ls, box, pts, ij, d)

@@ -51,3 +51,57 @@ def test_disordered_averaged_q6(freud, tilt):
     ij, d, _ = O.query(bx, pts, r_max=1.5, exclude_ii=True)
     o = O.steinhardt([6], bx, pts, ij, d, average=True)
     assert rel_err(np.asarray(st.ql, np.float64), o["ql_ave"][:, 0]) <= 1e-5
+
+
+WL_FLOOR = 1e-7
+
+
+def wl_check(got, ref):
+    ok = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(got), ok)
+    err = np.abs(got[ok] - ref[ok])
+    assert np.all(err <= 1e-5 * np.abs(ref[ok]) + WL_FLOOR), float(np.max(err / (1e-5 * np.abs(ref[ok]) + WL_FLOOR)))
+
+
+@pytest.mark.parametrize("tilt", [(0.0, 0.0, 0.0), (0.2, 0.1, 0.0)])
+def test_wl_ball_neighbours(freud, tilt):
+    """Normalised W4, W6, W10 (unaveraged) of a noisy FCC crystal in a cubic and a
+    tilted box on r_max = 1.4 ball neighbours (uneven bond counts, odd ones
+    included): within 1e-5 |w| + 1e-7 of the FP64 oracle."""
+    from golden.make_golden import fcc
+
+    box, pts = fcc(12, 1.5874, 0.08, 5)
+    L = box[0]
+    fbox = freud.box.Box(L, L, L, *tilt)
+    pts = np.asarray(fbox.wrap(pts), np.float32)
+    ls = [4, 6, 10]
+    st = freud.order.Steinhardt(ls, wl=True, wl_normalize=True)
+    st.compute((fbox, pts), neighbors={"r_max": 1.4})
+    bx = O.box7(fbox)
+    ij, d, _ = O.query(bx, pts, r_max=1.4, exclude_ii=True)
+    counts = np.bincount(ij[:, 0], minlength=len(pts))
+    assert np.any(counts % 2 == 1)
+    o = O.steinhardt(ls, bx, pts, ij, d, wl=True, wl_normalize=True)
+    np.testing.assert_allclose(np.asarray(st.ql, np.float64), o["ql"], rtol=1e-5)
+    wl_check(np.asarray(st.particle_order, np.float64), o["wl"])
+
+
+def test_wl_batched_frames(freud):
+    """Wl through a FrameBatch (bond vectors precomputed per frame): two noisy FCC
+    frames of different sizes, Steinhardt([6, 10], average, wl) on r_max 1.4."""
+    from golden.make_golden import fcc
+
+    frames = []
+    for nc, seed in ((8, 1), (11, 2)):
+        box, pts = fcc(nc, 1.5874, 0.06, seed)
+        frames.append((freud.box.Box.cube(float(box[0])), pts))
+    st = freud.order.Steinhardt([6, 10], average=True, wl=True, wl_normalize=True)
+    st.compute(freud.locality.FrameBatch(frames), neighbors={"r_max": 1.4})
+    got = np.asarray(st.particle_order, np.float64).reshape(-1, 2)
+    start = 0
+    for fbox, pts in frames:
+        bx = O.box7(fbox)
+        ij, d, _ = O.query(bx, pts, r_max=1.4, exclude_ii=True)
+        o = O.steinhardt([6, 10], bx, pts, ij, d, average=True, wl=True, wl_normalize=True)
+        wl_check(got[start:start + len(pts)], o["wl"])
+        start += len(pts)

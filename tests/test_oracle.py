@@ -124,7 +124,9 @@ def test_steinhardt_matches_reference(name):
     np.testing.assert_allclose(ql, g["ql"], rtol=2e-5, atol=2e-6)
     po = o["wl"] if wl else ql
     scale = np.max(np.abs(po), axis=0)
-    assert np.all(np.abs(po - g["particle_order"]) <= 5e-4 * scale + 1e-6)
+    # the reference's float32 Wl (fsph harmonics, plain float triple sums) is within
+    # 5.6e-6 of the |w| scale of FP64 on these inputs (W10 of the kNN case)
+    assert np.all(np.abs(po - g["particle_order"]) <= 2e-5 * scale + 1e-7)
     np.testing.assert_allclose(o["order"], g["order"], rtol=5e-5, atol=1e-6)
     qlm = np.concatenate([q.reshape(-1) for q in o["qlm"]])
     np.testing.assert_allclose(qlm, g["qlm"], atol=5e-6)
