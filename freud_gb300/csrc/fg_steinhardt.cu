@@ -748,6 +748,21 @@ __device__ __forceinline__ ffl ff_sub(ffl a, ffl b)
     return ff_add(a, {-b.h, -b.l});
 }
 
+// TwoSum without the renormalisation: the pair (s, e) may carry |e| above half an
+// ulp of s after a cancellation, which keeps its value to about 2^-47 of the
+// operands' magnitude, as later products and sums need
+__device__ __forceinline__ ffl ff_add_lazy(ffl a, ffl b)
+{
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    return {s, __fadd_rn(e, __fadd_rn(a.l, b.l))};
+}
+
+__device__ __forceinline__ ffl ff_sub_lazy(ffl a, ffl b)
+{
+    return ff_add_lazy(a, {-b.h, -b.l});
+}
+
 __device__ __forceinline__ ffl ff_sqrt(ffl v)
 {
     if (!(v.h > 0.0f))
@@ -826,8 +841,8 @@ __device__ __forceinline__ BondFF bond_ff(float dx, float dy, float dz, float d,
     return g;
 }
 
-// Every Y_l^m of a bond in float-float (Wl path): thread per particle, two bonds
-// per pass (their recurrences share the coefficient loads and give each step two
+// Every Y_l^m of a bond in float-float (Wl path): thread per particle, BP bonds
+// per pass (their recurrences share the coefficient loads and give each step BP
 // independent chains). Per order m the power (w sin(theta) e^{i phi})^m is one
 // complex float-float product from the previous order's, the prefactor K_m times
 // it, then the normalised recurrence R_{l+1} = a (ct R_l - b R_{l-1}) from R_m = 1
@@ -837,7 +852,7 @@ __device__ __forceinline__ BondFF bond_ff(float dx, float dy, float dz, float d,
 // (-1)^m conj of the sums. The final division by the total weight rounds once,
 // so each qlm is the FP64 value to within about one float ulp. Rows are written
 // through the warp's shared-memory sums, one particle's row per pass, coalesced.
-template<int T>
+template<int T, int BP>
 __global__ void __launch_bounds__(T, 256 / T)
     k_qlm_ff(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
              const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
@@ -850,6 +865,7 @@ __global__ void __launch_bounds__(T, 256 / T)
     __shared__ int s_k[ST_MAX_NL];
     __shared__ size_t s_off[ST_MAX_NL];
     __shared__ float s_norm[ST_MAX_NL];
+    __shared__ int s_slot0[ST_MAX_L + 2]; // slot of (l, 0) for a requested l
     if (threadIdx.x == 0)
     {
         int o = 0;
@@ -861,6 +877,7 @@ __global__ void __launch_bounds__(T, 256 / T)
             s_base[kk] = o;
             s_off[kk] = ls.qlm_offset[k];
             s_norm[kk] = ls.norm[k];
+            s_slot0[ls.l[k]] = o;
             o += ls.l[k] + 1;
         }
         s_lt[ls.nl] = -1;
@@ -870,6 +887,9 @@ __global__ void __launch_bounds__(T, 256 / T)
     const int nl = ls.nl;
     const int lmax = ls.max_l;
     const int nslot = s_base[nl];
+    unsigned req = 0; // bit l: l requested
+    for (int kk = 0; kk < nl; ++kk)
+        req |= 1u << s_lt[kk];
     const int lane = threadIdx.x & 31;
     float4* my = acc + threadIdx.x;
     for (uint32_t i0 = blockIdx.x * T; i0 < n; i0 += gridDim.x * T)
@@ -889,11 +909,11 @@ __global__ void __launch_bounds__(T, 256 / T)
                 piy = pts[3 * (size_t) i + 1];
                 piz = pts[3 * (size_t) i + 2];
             }
-            for (uint32_t e0 = 0; e0 < nbond; e0 += 2)
+            for (uint32_t e0 = 0; e0 < nbond; e0 += BP)
             {
-                BondFF g[2];
+                BondFF g[BP];
 #pragma unroll
-                for (int u = 0; u < 2; ++u)
+                for (int u = 0; u < BP; ++u)
                 {
                     float dx = 0.f, dy = 0.f, dz = 0.f, d = 0.f, w = 0.f;
                     if (e0 + u < nbond)
@@ -920,60 +940,58 @@ __global__ void __launch_bounds__(T, 256 / T)
                     tw = __fadd_rn(tw, w);
                 }
                 // weight x (sin(theta) e^{i phi})^m, starting at m = 0
-                ffl pr[2] = {{g[0].w, 0.0f}, {g[1].w, 0.0f}};
-                ffl pi[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
-                int kk0 = 0;
+                ffl pr[BP], pi[BP];
+#pragma unroll
+                for (int u = 0; u < BP; ++u)
+                {
+                    pr[u] = {g[u].w, 0.0f};
+                    pi[u] = {0.0f, 0.0f};
+                }
                 for (int m = 0; m <= lmax; ++m)
                 {
                     if (m > 0)
                     {
 #pragma unroll
-                        for (int u = 0; u < 2; ++u)
+                        for (int u = 0; u < BP; ++u)
                         {
-                            const ffl nr = ff_sub(ff_mul(pr[u], g[u].wr), ff_mul(pi[u], g[u].wi));
-                            pi[u] = ff_add(ff_mul(pr[u], g[u].wi), ff_mul(pi[u], g[u].wr));
+                            const ffl nr = ff_sub_lazy(ff_mul(pr[u], g[u].wr), ff_mul(pi[u], g[u].wi));
+                            pi[u] = ff_add_lazy(ff_mul(pr[u], g[u].wi), ff_mul(pi[u], g[u].wr));
                             pr[u] = nr;
                         }
                     }
-                    while (s_lt[kk0] >= 0 && s_lt[kk0] < m)
-                        ++kk0;
-                    if (s_lt[kk0] < 0)
-                        break;
                     const float2 kf = c_Kff[m];
                     const ffl K = {kf.x, kf.y};
-                    ffl fr[2], fi[2], r1[2], r0[2];
+                    ffl fr[BP], fi[BP], r1[BP], r0[BP];
 #pragma unroll
-                    for (int u = 0; u < 2; ++u)
+                    for (int u = 0; u < BP; ++u)
                     {
                         fr[u] = ff_mul(K, pr[u]);
                         fi[u] = ff_mul(K, pi[u]);
                         r1[u] = {1.0f, 0.0f};
                         r0[u] = {0.0f, 0.0f};
                     }
-                    int kk = kk0;
                     for (int l = m;; ++l)
                     {
-                        if (l == s_lt[kk])
+                        if ((req >> l) & 1u)
                         {
-                            float4* slot = my + (s_base[kk] + m - 0) * T;
+                            float4* slot = my + (s_slot0[l] + m) * T;
                             float4 v = *slot;
 #pragma unroll
-                            for (int u = 0; u < 2; ++u)
+                            for (int u = 0; u < BP; ++u)
                             {
                                 ff_acc(v.x, v.y, ff_mul(r1[u], fr[u]));
                                 ff_acc(v.z, v.w, ff_mul(r1[u], fi[u]));
                             }
                             *slot = v;
-                            ++kk;
-                            if (s_lt[kk] < 0)
-                                break;
                         }
+                        if (l == lmax)
+                            break;
                         const float2 af = c_aff[(l + 1) * (ST_MAX_L + 1) + m];
                         const float2 bf = c_bff[(l + 1) * (ST_MAX_L + 1) + m];
 #pragma unroll
-                        for (int u = 0; u < 2; ++u)
+                        for (int u = 0; u < BP; ++u)
                         {
-                            const ffl t = ff_sub(ff_mul(g[u].ct, r1[u]), ff_mul({bf.x, bf.y}, r0[u]));
+                            const ffl t = ff_sub_lazy(ff_mul(g[u].ct, r1[u]), ff_mul({bf.x, bf.y}, r0[u]));
                             r0[u] = r1[u];
                             r1[u] = ff_mul({af.x, af.y}, t);
                         }
@@ -1116,7 +1134,7 @@ __global__ void __launch_bounds__(128)
 // (Steinhardt.cc:224-289), as k_ave; ql per l is a shuffle reduction of the
 // lanes' squared magnitudes.
 template<int P, int R>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 8)
     k_ave_flat(uint32_t n, const uint2* __restrict__ ij, const uint32_t* __restrict__ bj,
                const uint32_t* __restrict__ seg, const uint32_t* __restrict__ cnt, StLs ls, int E,
                const float2* __restrict__ qlm, float2* __restrict__ ave, float* __restrict__ ql_ave,
@@ -1127,14 +1145,16 @@ __global__ void __launch_bounds__(128)
     const int group = lane / P;
     const unsigned gmask = P == 32 ? FULL : (((1u << P) - 1u) << (group * P));
     const int gpb = blockDim.x / P;
-    size_t off[R];
+    // entry r of this lane: column base pointer and row width (width 0 and the
+    // array start for a lane past the last entry, whose sums are never used)
+    const float2* col[R];
     uint32_t width[R];
     int kof[R];
 #pragma unroll
     for (int r = 0; r < R; ++r)
     {
         const int e = sub + r * P;
-        off[r] = 0;
+        col[r] = qlm;
         width[r] = 0;
         kof[r] = -1;
         int start = 0;
@@ -1143,7 +1163,7 @@ __global__ void __launch_bounds__(128)
             const int w = 2 * ls.l[k] + 1;
             if (e >= start && e < start + w)
             {
-                off[r] = ls.qlm_offset[k] + static_cast<size_t>(e - start);
+                col[r] = qlm + ls.qlm_offset[k] + (e - start);
                 width[r] = static_cast<uint32_t>(w);
                 kof[r] = k;
             }
@@ -1164,19 +1184,16 @@ __global__ void __launch_bounds__(128)
             const uint32_t jl =
                 base + sub < nbond ? (bj != nullptr ? bj[b0 + base + sub] : ij[b0 + base + sub].y) : 0u;
             const uint32_t nh = min(static_cast<uint32_t>(P), nbond - base);
-#pragma unroll 4
+#pragma unroll 8
             for (uint32_t u = 0; u < nh; ++u)
             {
                 const uint32_t j = __shfl_sync(gmask, jl, u, P);
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                 {
-                    if (kof[r] >= 0)
-                    {
-                        const float2 v = qlm[off[r] + static_cast<size_t>(j) * width[r]];
-                        sr[r] += v.x;
-                        si[r] += v.y;
-                    }
+                    const float2 v = col[r][static_cast<size_t>(j) * width[r]];
+                    sr[r] += v.x;
+                    si[r] += v.y;
                 }
             }
         }
@@ -1188,11 +1205,11 @@ __global__ void __launch_bounds__(128)
             sq[r] = 0.0f;
             if (kof[r] >= 0)
             {
-                const size_t a = off[r] + static_cast<size_t>(i) * width[r];
-                const float2 own = qlm[a];
+                const size_t a = static_cast<size_t>(i) * width[r];
+                const float2 own = col[r][a];
                 const float qr = (sr[r] + own.x) / cntf;
                 const float qi = (si[r] + own.y) / cntf;
-                ave[a] = make_float2(qr, qi);
+                ave[(col[r] - qlm) + a] = make_float2(qr, qi);
                 sq[r] = qr * qr + qi * qi;
             }
         }
@@ -1210,25 +1227,26 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-// Wl per particle, every l of the set: thread per particle, the block's rows of
-// m >= 0 entries staged in shared memory (odd row stride: conflict-free), the
-// l's term classes broadcast from shared memory. Each class adds
-// C x Re(q_a q_b q_c) in float-float (exact float products, TwoSum sums), so the
-// sum is the FP64 triple sum of the float qlm to within about 2^-44 of its terms;
-// it is rounded once, then normalised by (sqrt(4 pi / (2l + 1)) / ql)^3
+// Wl per particle, every l of the set: thread per particle, the block's rows
+// staged in shared memory (a straight copy: rows of consecutive particles are
+// contiguous; the row length 2l + 1 is odd, so the rows' 8-byte reads are free of
+// bank conflicts), the l's term classes broadcast from shared memory. Each class
+// adds C x Re(q_a q_b q_c) in float-float (exact float products, TwoSum sums), so
+// the sum is the FP64 triple sum of the float qlm to within about 2^-44 of its
+// terms; it is rounded once, then normalised by (sqrt(4 pi / (2l + 1)) / ql)^3
 // (Steinhardt.cc:338-352).
-__device__ __forceinline__ float2 wl_member(const float2* row, unsigned rec, int slot)
-{
-    const float2 q = row[(rec >> (8 * slot)) & 0xffu];
-    const unsigned f = rec >> (24 + 2 * slot);
-    return make_float2(__int_as_float(__float_as_int(q.x) ^ ((f & 1u) << 31)),
-                       __int_as_float(__float_as_int(q.y) ^ (((f >> 1) & 1u) << 31)));
-}
-
 __device__ __forceinline__ ffl two_prod(float a, float b)
 {
     const float p = __fmul_rn(a, b);
     return {p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ ffl ff_mulf(ffl a, float b)
+{
+    const float p = __fmul_rn(a.h, b);
+    float e = __fmaf_rn(a.h, b, -p);
+    e = __fmaf_rn(a.l, b, e);
+    return {p, e};
 }
 
 constexpr int WL_T = 128;
@@ -1240,40 +1258,35 @@ __global__ void __launch_bounds__(WL_T)
     extern __shared__ float4 wl_smem[];
     const uint32_t i0 = blockIdx.x * WL_T;
     const uint32_t i = i0 + threadIdx.x;
+    const uint32_t rows_here = min(static_cast<uint32_t>(WL_T), n - i0);
     for (int k = 0; k < ls.nl; ++k)
     {
         const int l = ls.l[k];
-        const int lp1 = l + 1;
-        const int stride = lp1 | 1;
+        const int width = 2 * l + 1;
         int4* s_terms = reinterpret_cast<int4*>(wl_smem);
         float2* rows = reinterpret_cast<float2*>(wl_smem + wt.cnt[k]);
         __syncthreads();
         for (int t = threadIdx.x; t < wt.cnt[k]; t += WL_T)
             s_terms[t] = terms[wt.off[k] + t];
-        const float2* base = src + ls.qlm_offset[k];
-        for (int e = threadIdx.x; e < WL_T * lp1; e += WL_T)
-        {
-            const int p = e / lp1;
-            const int m = e - p * lp1;
-            rows[p * stride + m] =
-                i0 + p < n ? base[static_cast<size_t>(i0 + p) * (2 * l + 1) + m] : make_float2(0.f, 0.f);
-        }
+        const float2* base = src + ls.qlm_offset[k] + static_cast<size_t>(i0) * width;
+        for (uint32_t e = threadIdx.x; e < rows_here * width; e += WL_T)
+            rows[e] = base[e];
         __syncthreads();
         if (i < n)
         {
-            const float2* row = rows + threadIdx.x * stride;
+            const char* row = reinterpret_cast<const char*>(rows + threadIdx.x * width);
             float ah = 0.0f, al = 0.0f;
+#pragma unroll 2
             for (int t = 0; t < wt.cnt[k]; ++t)
             {
                 const int4 rec = s_terms[t];
-                const unsigned r = static_cast<unsigned>(rec.x);
-                const float2 qa = wl_member(row, r, 0);
-                const float2 qb = wl_member(row, r, 1);
-                const float2 qc = wl_member(row, r, 2);
-                const ffl ur = ff_sub(two_prod(qa.x, qb.x), two_prod(qa.y, qb.y));
-                const ffl ui = ff_add(two_prod(qa.x, qb.y), two_prod(qa.y, qb.x));
-                const ffl re = ff_sub(ff_mul(ur, {qc.x, 0.0f}), ff_mul(ui, {qc.y, 0.0f}));
-                ff_acc(ah, al, ff_mul({__int_as_float(rec.y), __int_as_float(rec.z)}, re));
+                const float2 qa = *reinterpret_cast<const float2*>(row + (rec.x & 0xffff));
+                const float2 qb = *reinterpret_cast<const float2*>(row + (static_cast<unsigned>(rec.x) >> 16));
+                const float2 qc = *reinterpret_cast<const float2*>(row + rec.y);
+                const ffl ur = ff_sub_lazy(two_prod(qa.x, qb.x), two_prod(qa.y, qb.y));
+                const ffl ui = ff_add_lazy(two_prod(qa.x, qb.y), two_prod(qa.y, qb.x));
+                const ffl re = ff_sub_lazy(ff_mulf(ur, qc.x), ff_mulf(ui, qc.y));
+                ff_acc(ah, al, ff_mul({__int_as_float(rec.z), __int_as_float(rec.w)}, re));
             }
             float sum = __fadd_rn(ah, al);
             if (normalize)
@@ -1436,18 +1449,22 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
         {
             // the largest set: ten l values up to 31
             const int most = 200 * 1024;
-            cudaFuncSetAttribute(k_qlm_ff<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
-            cudaFuncSetAttribute(k_qlm_ff<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+            cudaFuncSetAttribute(k_qlm_ff<64, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+            cudaFuncSetAttribute(k_qlm_ff<32, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
             configured = true;
         }
         const uint32_t blocks = (n + T - 1) / T;
         ProfScope prof_("k_qlm_ff", s);
+        auto go = [&](auto kernel, int threads) {
+            kernel<<<blocks, threads, smem, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm,
+                                                 ql);
+        };
+        // four bonds per pass: four independent recurrence chains per step
+        // (0.85 ms against 0.99 ms with two on the 256,000-point FCC set, l = 4..12)
         if (T == 64)
-            k_qlm_ff<64><<<blocks, 64, smem, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm,
-                                                  ql);
+            go(k_qlm_ff<64, 4>, 64);
         else
-            k_qlm_ff<32><<<blocks, 32, smem, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm,
-                                                  ql);
+            go(k_qlm_ff<32, 4>, 32);
         return;
     }
     if (ls.nl == 1 && ls.max_l <= 12)
@@ -1597,25 +1614,20 @@ std::vector<int4> wl_term_classes(int l, double (*w3j)(int, int, int, int))
     std::vector<int4> out;
     for (const auto& c : cls)
     {
-        unsigned rec = 0;
+        // byte offset of each member's column in the row (m order 0..l, -1..-l)
+        int col[3];
         for (int slot = 0; slot < 3; ++slot)
         {
             const int m = c.first[slot];
-            const int a = m < 0 ? -m : m;
-            rec |= static_cast<unsigned>(a) << (8 * slot);
-            if (m < 0)
-            {
-                // q_{-a} = (-1)^a conj(q_a): flip im for a even, re for a odd
-                rec |= ((a & 1) ? 1u : 2u) << (24 + 2 * slot);
-            }
+            col[slot] = 8 * (m >= 0 ? m : l - m);
         }
         const float h = static_cast<float>(c.second);
         const float lo = static_cast<float>(c.second - static_cast<double>(h));
         int4 r;
-        r.x = static_cast<int>(rec);
-        std::memcpy(&r.y, &h, 4);
-        std::memcpy(&r.z, &lo, 4);
-        r.w = 0;
+        r.x = col[0] | (col[1] << 16);
+        r.y = col[2];
+        std::memcpy(&r.z, &h, 4);
+        std::memcpy(&r.w, &lo, 4);
         out.push_back(r);
     }
     return out;
@@ -1630,7 +1642,14 @@ void launch_wl(uint32_t n, const StLs& ls, const WlTerms& wt, const int4* terms,
     }
     int most = 0;
     for (int k = 0; k < ls.nl; ++k)
-        most = std::max(most, wt.cnt[k] * 16 + WL_T * ((ls.l[k] + 1) | 1) * 8);
+        most = std::max(most, wt.cnt[k] * 16 + WL_T * (2 * ls.l[k] + 1) * 8);
+    static bool configured = false;
+    if (!configured)
+    {
+        // l = 31: 272 classes and 128 rows of 63 entries
+        cudaFuncSetAttribute(k_wl, cudaFuncAttributeMaxDynamicSharedMemorySize, 80 * 1024);
+        configured = true;
+    }
     ProfScope prof_("k_wl", s);
     k_wl<<<(n + WL_T - 1) / WL_T, WL_T, most, s>>>(n, ls, wt, terms, src, qnorm, normalize, wl);
 }

@@ -46,10 +46,10 @@ void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t
 // Wl of every requested l in one launch. The triple sum over m1 + m2 + m3 = 0 is
 // taken over classes of terms with equal Re(q_m1 q_m2 q_m3): the permutations of
 // (m1, m2, m3) and of (-m1, -m2, -m3) (q_{-m} = (-1)^m conj(q_m), and
-// m1 + m2 + m3 = 0). A class is one record (int4): |m| of its three members in
-// bits 0-7, 8-15, 16-23, per member a (re, im) sign flip in bits 24-29 (the
-// member is -|m|), then hi and lo floats of the FP64 sum of the Wigner-3j symbols
-// of the class (Wigner3j.cc:22-57 over the same index set). Records of l_k at
+// m1 + m2 + m3 = 0). A class is one record (int4): the byte offsets in the row
+// (m order 0..l, -1..-l) of its three members (x: first | second << 16, y:
+// third), then hi and lo floats of the FP64 sum of the Wigner-3j symbols of the
+// class (Wigner3j.cc:22-57 over the same index set). Records of l_k at
 // terms + off[k], cnt[k] of them.
 struct WlTerms
 {
