@@ -35,10 +35,11 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int BT_TILE = 1024;   // staged candidates per tile
-constexpr int BT_QB = 64;       // queries per shared-memory batch
+constexpr int BT_QB = 128;      // queries per shared-memory batch
 constexpr int BT_ITEMS = 96;    // stencil items: up to 32 rows x 3 x-segments
 constexpr int BT_HIST = 2048;   // shared histogram words (all copies)
 constexpr int BT_RB_WORDS = 1792; // exact r^2 -> bin table (thresholds + keys)
+constexpr int IV_INVALID = 255;    // staged candidate whose image (queries inside the box) is beyond +-1
 constexpr int BT_CHUNK_MAX = 4; // cells per work-counter pop (fewer for small grids)
 
 // Largest f with base[f] <= x (base[0] = 0 <= x < base[nframes]).
@@ -107,14 +108,19 @@ struct BItems
 struct HistShared
 {
     float4 pos[BT_TILE];        // candidate position, w = packed integer image
-    float4 iv[BT_TILE];         // image vector for queries inside the box; w = 1 if |k| <= 1
+    unsigned short lst[8][BT_TILE]; // octant lists: positions of the candidates near each octant
     uint32_t j[BT_TILE];        // global point index
+    unsigned char ivc[BT_TILE]; // image for queries inside the box: (kx+1)*9 + (ky+1)*3 + (kz+1), IV_INVALID beyond +-1
     unsigned char wr[BT_TILE];  // cell wrap code (wx + 1) + 3 (wy + 1) + 9 (wz + 1)
     unsigned char home[BT_TILE]; // candidate of the home cell (half-stencil mode)
-    float4 q[BT_QB];
+    float4 q[BT_QB];            // the query block, grouped by octant; w = point index (bits)
     uint32_t qi[BT_QB];
+    int qimg[BT_QB];            // packed integer image of each query
+    uint32_t qo[9];             // octant o's queries: q[qo[o], qo[o + 1])
+    uint32_t lcnt[8];           // octant list lengths
     BItems it;
     DevBox box;
+    float4 img4[27];            // box.img as float4 (one shared load per candidate)
     int dim[3];
     int shell;
     uint32_t cell_base;
@@ -263,6 +269,11 @@ __global__ void __launch_bounds__(WARPS * 32, 4)
             S.rb[t] = h.rb[t];
     }
     const float* rb_thr = reinterpret_cast<const float*>(S.rb);
+    // counted pairs: ua <= r^2 bits < ua + uspan (r^2 >= +0, so the bit patterns
+    // order like the values): the table's folded range, else [r_min^2, r_max^2)
+    const uint32_t ua = __float_as_uint(h.rb != nullptr ? h.rb_a : p.r_min_sq);
+    const uint32_t ub = __float_as_uint(h.rb != nullptr ? h.rb_b : p.r_max_sq);
+    const uint32_t uspan = ub > ua ? ub - ua : 0u;
     const unsigned short* rb_key = reinterpret_cast<const unsigned short*>(S.rb + h.bins + 2);
     int cur_frame = -1;
     float cull2 = 0.0f;
@@ -295,6 +306,8 @@ __global__ void __launch_bounds__(WARPS * 32, 4)
                 int* dst = reinterpret_cast<int*>(&S.box);
                 for (int t = tid; t < static_cast<int>(sizeof(DevBox) / sizeof(int)); t += THREADS)
                     dst[t] = src[t];
+                if (tid < 27)
+                    S.img4[tid] = make_float4(F.b.img[tid][0], F.b.img[tid][1], F.b.img[tid][2], 0.0f);
                 if (tid == 0)
                 {
                     S.dim[0] = F.dim[0];
@@ -372,45 +385,80 @@ __global__ void __launch_bounds__(WARPS * 32, 4)
             const bool sym = S.sym != 0;
             const bool cull = S.qout == 0 && (!test_ii || sym);
             const uint32_t T = S.it.off[BT_ITEMS];
+            // octant lists (cull mode, cells of r_max): the queries' bounds split at
+            // their middle into eight boxes; a candidate joins the list of each box it
+            // lies within the cull radius of, and a query meets only its own box's
+            // list (the cell-wide cull bounds a query's candidates by the whole cell,
+            // the octant's by an eighth of it; with cells of r_max / 2 the lists cost
+            // more than the pairs they drop)
+            const bool oct = cull && S.shell == 1;
+            const int G = oct ? 8 : 1;
+            float mid[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                mid[a] = 0.5f * (S.qfin[a] + S.qfin[3 + a]);
+            const unsigned lt = (1u << lane) - 1u;
             for (uint32_t t0 = 0; t0 < T; t0 += BT_TILE)
             {
                 const uint32_t TT0 = min(static_cast<uint32_t>(BT_TILE), T - t0);
                 if (tid == 0)
                     S.nkeep = 0;
+                if (tid < 8)
+                    S.lcnt[tid] = 0;
                 __syncthreads();
                 for (uint32_t base = 0; base < TT0; base += THREADS)
                 {
                     const uint32_t tl = base + tid;
                     bool keep = false;
-                    float4 pp = make_float4(0.f, 0.f, 0.f, 0.f), iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float4 pp = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float3 iv = make_float3(0.f, 0.f, 0.f);
+                    int code = IV_INVALID;
                     uint32_t slot = 0;
                     int wr = 13;
+                    unsigned om = 0;
+                    int s_item = 0;
                     if (tl < TT0)
                     {
                         const uint32_t t = t0 + tl;
-                        const int s = bitem_of(S.it, t);
-                        slot = S.it.start[s] + (t - S.it.off[s]);
+                        s_item = bitem_of(S.it, t);
+                        slot = S.it.start[s_item] + (t - S.it.off[s_item]);
                         pp = g.cpos[slot];
-                        wr = S.it.wrap[s];
+                        wr = S.it.wrap[s_item];
                         const int pim = __float_as_int(pp.w);
                         const int kx = img_ax(pim, 0) - (wr % 3 - 1);
                         const int ky = img_ax(pim, 1) - ((wr / 3) % 3 - 1);
                         const int kz = img_ax(pim, 2) - (wr / 9 - 1);
                         if (kx >= -1 && kx <= 1 && ky >= -1 && ky <= 1 && kz >= -1 && kz <= 1)
                         {
-                            const float* v = S.box.img[(kx + 1) * 9 + (ky + 1) * 3 + (kz + 1)];
-                            iv = make_float4(v[0], v[1], v[2], 1.0f);
+                            code = (kx + 1) * 9 + (ky + 1) * 3 + (kz + 1);
+                            const float* v = S.box.img[code];
+                            iv = make_float3(v[0], v[1], v[2]);
                         }
                         keep = true;
                         if (cull)
                         {
-                            // farther than r_max (+ margin) from every query of the cell:
+                            // farther than r_max (+ margin) from every query of an octant:
                             // no pair with any of them (invalid images are dropped too)
-                            const float sx = pp.x - iv.x, sy = pp.y - iv.y, sz = pp.z - iv.z;
-                            const float gx = fmaxf(fmaxf(S.qfin[0] - sx, sx - S.qfin[3]), 0.f);
-                            const float gy = fmaxf(fmaxf(S.qfin[1] - sy, sy - S.qfin[4]), 0.f);
-                            const float gz = fmaxf(fmaxf(S.qfin[2] - sz, sz - S.qfin[5]), 0.f);
-                            keep = iv.w != 0.0f && gx * gx + gy * gy + gz * gz <= cull2;
+                            const float sc[3] = {pp.x - iv.x, pp.y - iv.y, pp.z - iv.z};
+                            float gl[3], gh[3];
+#pragma unroll
+                            for (int a = 0; a < 3; ++a)
+                            {
+                                const float l0 = fmaxf(fmaxf(S.qfin[a] - sc[a], sc[a] - mid[a]), 0.f);
+                                const float h0 = fmaxf(fmaxf(mid[a] - sc[a], sc[a] - S.qfin[3 + a]), 0.f);
+                                gl[a] = l0 * l0;
+                                gh[a] = h0 * h0;
+                            }
+#pragma unroll
+                            for (int o = 0; o < 8; ++o)
+                            {
+                                const float d2 = ((o & 1) ? gh[0] : gl[0]) + ((o & 2) ? gh[1] : gl[1]) +
+                                                 ((o & 4) ? gh[2] : gl[2]);
+                                om |= (d2 <= cull2 ? 1u : 0u) << o;
+                            }
+                            keep = code != IV_INVALID && om != 0;
+                            if (!keep)
+                                om = 0;
                         }
                     }
                     const unsigned km = __ballot_sync(FULL, keep);
@@ -418,141 +466,225 @@ __global__ void __launch_bounds__(WARPS * 32, 4)
                     if (lane == 0 && km != 0)
                         wbase = atomicAdd(&S.nkeep, static_cast<uint32_t>(__popc(km)));
                     wbase = __shfl_sync(FULL, wbase, 0);
+                    const uint32_t idx = wbase + __popc(km & lt);
                     if (keep)
                     {
-                        const uint32_t idx = wbase + __popc(km & ((1u << lane) - 1u));
                         S.pos[idx] = pp;
-                        S.iv[idx] = iv;
+                        S.ivc[idx] = static_cast<unsigned char>(code);
                         S.j[idx] = g.cidx[slot];
                         S.wr[idx] = static_cast<unsigned char>(wr);
-                        S.home[idx] = S.it.home[bitem_of(S.it, t0 + tl)];
+                        S.home[idx] = S.it.home[s_item];
+                    }
+                    if (oct)
+                    {
+#pragma unroll
+                        for (int o = 0; o < 8; ++o)
+                        {
+                            const bool in = (om >> o) & 1u;
+                            const unsigned gm = __ballot_sync(FULL, in);
+                            if (gm == 0)
+                                continue;
+                            uint32_t gb = 0;
+                            if (lane == 0)
+                                gb = atomicAdd(&S.lcnt[o], static_cast<uint32_t>(__popc(gm)));
+                            gb = __shfl_sync(FULL, gb, 0);
+                            if (in)
+                                S.lst[o][gb + __popc(gm & lt)] = static_cast<unsigned short>(idx);
+                        }
                     }
                 }
                 __syncthreads();
                 const uint32_t TT = S.nkeep;
-                const uint32_t nchunks = (TT + 31) / 32;
                 for (uint32_t qb0 = 0; qb0 < nqc; qb0 += BT_QB)
                 {
                     const uint32_t nb = min(static_cast<uint32_t>(BT_QB), nqc - qb0);
                     __syncthreads();
+                    // the block's queries (with octants: grouped by octant, a ballot
+                    // counting sort by warp 0)
                     bool out_of_box = false;
-                    for (uint32_t k = tid; k < nb; k += THREADS)
+                    if (!oct)
                     {
-                        const float4 qv = g.cpos[q0 + qb0 + k];
-                        S.q[k] = qv;
-                        S.qi[k] = g.cidx[q0 + qb0 + k];
-                        out_of_box |= __float_as_int(qv.w) != 0;
+                        for (uint32_t k = tid; k < nb; k += THREADS)
+                        {
+                            const float4 qv = g.cpos[q0 + qb0 + k];
+                            const uint32_t qi = g.cidx[q0 + qb0 + k];
+                            S.q[k] = make_float4(qv.x, qv.y, qv.z, __uint_as_float(qi));
+                            S.qi[k] = qi;
+                            S.qimg[k] = __float_as_int(qv.w);
+                            out_of_box |= __float_as_int(qv.w) != 0;
+                        }
+                        if (tid == 0)
+                        {
+                            S.qo[0] = 0;
+                            S.qo[1] = nb;
+                        }
+                    }
+                    else if (warp == 0)
+                    {
+                        constexpr int QR = BT_QB / 32;
+                        float4 qv[QR];
+                        uint32_t qiv[QR];
+                        int og[QR];
+                        bool qlive[QR];
+#pragma unroll
+                        for (int r = 0; r < QR; ++r)
+                        {
+                            const uint32_t k = static_cast<uint32_t>(lane + 32 * r);
+                            qlive[r] = k < nb;
+                            qv[r] = qlive[r] ? g.cpos[q0 + qb0 + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+                            qiv[r] = qlive[r] ? g.cidx[q0 + qb0 + k] : 0u;
+                            out_of_box |= qlive[r] && __float_as_int(qv[r].w) != 0;
+                            og[r] = oct ? (qv[r].x >= mid[0] ? 1 : 0) + (qv[r].y >= mid[1] ? 2 : 0) +
+                                              (qv[r].z >= mid[2] ? 4 : 0)
+                                        : 0;
+                        }
+                        uint32_t qoff = 0;
+                        for (int o = 0; o < G; ++o)
+                        {
+                            if (lane == 0)
+                                S.qo[o] = qoff;
+#pragma unroll
+                            for (int r = 0; r < QR; ++r)
+                            {
+                                const bool in = qlive[r] && og[r] == o;
+                                const unsigned m = __ballot_sync(FULL, in);
+                                if (in)
+                                {
+                                    const uint32_t at = qoff + __popc(m & lt);
+                                    S.q[at] = make_float4(qv[r].x, qv[r].y, qv[r].z, __uint_as_float(qiv[r]));
+                                    S.qi[at] = qiv[r];
+                                    S.qimg[at] = __float_as_int(qv[r].w);
+                                }
+                                qoff += __popc(m);
+                            }
+                        }
+                        if (lane == 0)
+                            S.qo[G] = qoff;
                     }
                     // queries inside the box take a branch-free pair loop: invalid
                     // candidates (image beyond +-1) are moved out of range instead
                     // (half-stencil frames hold no point outside the box and count no
                     // pair of a point with itself)
                     const bool general = (__syncthreads_or(out_of_box) != 0 || test_ii) && !sym;
-                    if (!general && rbins)
+                    if (!general)
                     {
-                        for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
+                        // work items: (octant, chunk of 32 of its candidates) over octants
+                        // holding queries
+                        uint32_t nchk[8];
+                        uint32_t items = 0;
+#pragma unroll
+                        for (int o = 0; o < 8; ++o)
                         {
-                            const uint32_t e = ch * 32 + lane;
+                            const uint32_t L = o < G ? (oct ? S.lcnt[o] : TT) : 0u;
+                            nchk[o] = (o < G && S.qo[o + 1] > S.qo[o]) ? (L + 31) / 32 : 0u;
+                            items += nchk[o];
+                        }
+                        for (uint32_t item = warp; item < items; item += WARPS)
+                        {
+                            int o = 0;
+                            uint32_t ch = item;
+#pragma unroll
+                            for (int t = 0; t < 8; ++t)
+                            {
+                                if (o == t && ch >= nchk[t])
+                                {
+                                    ch -= nchk[t];
+                                    o = t + 1;
+                                }
+                            }
+                            const uint32_t L = oct ? S.lcnt[o] : TT;
+                            const uint32_t k = ch * 32 + lane;
                             float4 pp = make_float4(3e30f, 3e30f, 3e30f, 0.f);
-                            float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                            float3 iv = make_float3(0.f, 0.f, 0.f);
                             uint32_t jj = 0;
                             bool hm = false;
-                            if (e < TT)
+                            if (k < L)
                             {
-                                iv = S.iv[e];
-                                if (iv.w != 0.0f)
+                                const uint32_t e = oct ? S.lst[o][k] : k;
+                                const int code = S.ivc[e];
+                                if (code != IV_INVALID)
+                                {
                                     pp = S.pos[e];
+                                    const float4 v4 = S.img4[code];
+                                    iv = make_float3(v4.x, v4.y, v4.z);
+                                }
                                 jj = S.j[e];
                                 hm = S.home[e] != 0;
                             }
                             const bool zero = iv.x == 0.0f && iv.y == 0.0f && iv.z == 0.0f;
-                            // exact r^2 -> bin (ok: r_min^2 <= r^2 < r_max^2 and inside the histogram)
-                            auto bin_of = [&](float rsq, bool& ok) {
-                                ok = rsq >= h.rb_a && rsq < h.rb_b;
-                                const uint32_t u = __float_as_uint(rsq);
-                                const uint32_t key = (ok && u >= h.rb_ut) ? ((u - h.rb_ut) >> h.rb_s) + 1u : 0u;
-                                const uint32_t b0 = rb_key[key];
-                                return b0 + (rsq >= rb_thr[b0 + 1] ? 1u : 0u) + (rsq >= rb_thr[b0 + 2] ? 1u : 0u);
-                            };
+                            const uint32_t wrest = zero ? 2u : 1u; // weight of a pair off the home cell
+                            const uint32_t qa = S.qo[o], qz = S.qo[o + 1];
                             auto add = [&](uint32_t bin, uint32_t w) {
                                 if (smem_hist)
                                     atomicAdd(&my_hist[bin], w);
                                 else
                                     atomicAdd(&hist[bin], static_cast<unsigned long long>(w));
                             };
-                            // image 0 for the whole chunk: q + 0 is q (up to the sign of a
-                            // zero, which r^2 does not see), so the three additions go.
-                            // Half stencil (SYM): a pair of image 0 is tested once and
-                            // counted twice - p_i - (p_j + 0) is exactly -(p_j - (p_i + 0)),
-                            // so both bonds fall in one bin; home-cell pairs only for j > i;
-                            // a pair of image k != 0 is tested from both ends: r_ij =
-                            // p_j - (p_i + v_k) and r_ji = p_i - (p_j + v_-k), v_-k = -v_k.
-                            auto sweep = [&](auto zero_image, auto half) {
-                                constexpr bool Z = decltype(zero_image)::value;
-                                constexpr bool SYM = decltype(half)::value;
+                            if (rbins)
+                            {
+                                // exact r^2 -> bin (ok: r_min^2 <= r^2 < r_max^2 and inside the histogram)
+                                auto bin_of = [&](float rsq, bool& ok) {
+                                    // rb_a <= r^2 < rb_b on the bit patterns (r^2 >= +0)
+                                    const uint32_t u = __float_as_uint(rsq);
+                                    ok = u - ua < uspan;
+                                    const uint32_t key = (ok && u >= h.rb_ut) ? ((u - h.rb_ut) >> h.rb_s) + 1u : 0u;
+                                    const uint32_t b0 = rb_key[key];
+                                    return b0 + (rsq >= rb_thr[b0 + 1] ? 1u : 0u) + (rsq >= rb_thr[b0 + 2] ? 1u : 0u);
+                                };
+                                // image 0 for the whole chunk: q + 0 is q (up to the sign of a
+                                // zero, which r^2 does not see), so the three additions go.
+                                // Half stencil (SYM): a pair of image 0 is tested once and
+                                // counted twice - p_i - (p_j + 0) is exactly -(p_j - (p_i + 0)),
+                                // so both bonds fall in one bin; home-cell pairs only for j > i;
+                                // a pair of image k != 0 is tested from both ends: r_ij =
+                                // p_j - (p_i + v_k) and r_ji = p_i - (p_j + v_-k), v_-k = -v_k.
+                                auto sweep = [&](auto zero_image, auto half) {
+                                    constexpr bool Z = decltype(zero_image)::value;
+                                    constexpr bool SYM = decltype(half)::value;
 #pragma unroll 4
-                                for (uint32_t qq = 0; qq < nb; ++qq)
-                                {
-                                    const float4 q = S.q[qq];
-                                    const float rx = __fsub_rn(pp.x, Z ? q.x : __fadd_rn(q.x, iv.x));
-                                    const float ry = __fsub_rn(pp.y, Z ? q.y : __fadd_rn(q.y, iv.y));
-                                    const float rz = __fsub_rn(pp.z, Z ? q.z : __fadd_rn(q.z, iv.z));
-                                    bool ok;
-                                    const uint32_t bin = bin_of(dot3(rx, ry, rz), ok);
-                                    uint32_t w = 1;
-                                    if (SYM)
-                                        w = hm ? (jj > S.qi[qq] ? 2u : 0u) : (zero ? 2u : 1u);
-                                    if (ok && w != 0)
-                                        add(bin, w);
-                                    if (SYM && !Z && !zero)
+                                    for (uint32_t qq = qa; qq < qz; ++qq)
                                     {
-                                        const float sx = __fsub_rn(q.x, __fsub_rn(pp.x, iv.x));
-                                        const float sy = __fsub_rn(q.y, __fsub_rn(pp.y, iv.y));
-                                        const float sz = __fsub_rn(q.z, __fsub_rn(pp.z, iv.z));
-                                        bool ok2;
-                                        const uint32_t bin2 = bin_of(dot3(sx, sy, sz), ok2);
-                                        if (ok2)
-                                            add(bin2, 1u);
+                                        const float4 q = S.q[qq];
+                                        const float rx = __fsub_rn(pp.x, Z ? q.x : __fadd_rn(q.x, iv.x));
+                                        const float ry = __fsub_rn(pp.y, Z ? q.y : __fadd_rn(q.y, iv.y));
+                                        const float rz = __fsub_rn(pp.z, Z ? q.z : __fadd_rn(q.z, iv.z));
+                                        bool ok;
+                                        const uint32_t bin = bin_of(dot3(rx, ry, rz), ok);
+                                        uint32_t w = 1;
+                                        if (SYM)
+                                            w = hm ? (jj > __float_as_uint(q.w) ? 2u : 0u) : wrest;
+                                        if (ok && w != 0)
+                                            add(bin, w);
+                                        if (SYM && !Z && !zero)
+                                        {
+                                            const float sx = __fsub_rn(q.x, __fsub_rn(pp.x, iv.x));
+                                            const float sy = __fsub_rn(q.y, __fsub_rn(pp.y, iv.y));
+                                            const float sz = __fsub_rn(q.z, __fsub_rn(pp.z, iv.z));
+                                            bool ok2;
+                                            const uint32_t bin2 = bin_of(dot3(sx, sy, sz), ok2);
+                                            if (ok2)
+                                                add(bin2, 1u);
+                                        }
                                     }
+                                };
+                                const bool all_zero = __all_sync(FULL, zero);
+                                if (sym)
+                                {
+                                    if (all_zero)
+                                        sweep(std::true_type {}, std::true_type {});
+                                    else
+                                        sweep(std::false_type {}, std::true_type {});
                                 }
-                            };
-                            const bool all_zero = __all_sync(FULL, zero);
-                            if (sym)
-                            {
-                                if (all_zero)
-                                    sweep(std::true_type {}, std::true_type {});
+                                else if (all_zero)
+                                {
+                                    sweep(std::true_type {}, std::false_type {});
+                                }
                                 else
-                                    sweep(std::false_type {}, std::true_type {});
+                                {
+                                    sweep(std::false_type {}, std::false_type {});
+                                }
+                                continue;
                             }
-                            else if (all_zero)
-                            {
-                                sweep(std::true_type {}, std::false_type {});
-                            }
-                            else
-                            {
-                                sweep(std::false_type {}, std::false_type {});
-                            }
-                        }
-                        continue;
-                    }
-                    if (!general)
-                    {
-                        for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
-                        {
-                            const uint32_t e = ch * 32 + lane;
-                            float4 pp = make_float4(3e30f, 3e30f, 3e30f, 0.f);
-                            float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
-                            uint32_t jj = 0;
-                            bool hm = false;
-                            if (e < TT)
-                            {
-                                iv = S.iv[e];
-                                if (iv.w != 0.0f)
-                                    pp = S.pos[e];
-                                jj = S.j[e];
-                                hm = S.home[e] != 0;
-                            }
-                            const bool zero = iv.x == 0.0f && iv.y == 0.0f && iv.z == 0.0f;
                             // Histogram.h:327-351 binning of the distance of a pair that passed
                             auto count = [&](float rsq, uint32_t w) {
                                 if (rsq < p.r_max_sq && rsq >= p.r_min_sq)
@@ -564,23 +696,20 @@ __global__ void __launch_bounds__(WARPS * 32, 4)
                                             static_cast<uint32_t>(__fmul_rn(__fsub_rn(d, h.h_min), h.h_inv));
                                         if (bin == h.bins)
                                             bin = h.bins - 1;
-                                        if (smem_hist)
-                                            atomicAdd(&my_hist[bin], w);
-                                        else
-                                            atomicAdd(&hist[bin], static_cast<unsigned long long>(w));
+                                        add(bin, w);
                                     }
                                 }
                             };
                             // half stencil as in the table path above
                             const bool rev = sym && __any_sync(FULL, !zero);
 #pragma unroll 4
-                            for (uint32_t qq = 0; qq < nb; ++qq)
+                            for (uint32_t qq = qa; qq < qz; ++qq)
                             {
                                 const float4 q = S.q[qq];
                                 const float rx = __fsub_rn(pp.x, __fadd_rn(q.x, iv.x));
                                 const float ry = __fsub_rn(pp.y, __fadd_rn(q.y, iv.y));
                                 const float rz = __fsub_rn(pp.z, __fadd_rn(q.z, iv.z));
-                                const uint32_t w = sym ? (hm ? (jj > S.qi[qq] ? 2u : 0u) : (zero ? 2u : 1u)) : 1u;
+                                const uint32_t w = sym ? (hm ? (jj > __float_as_uint(q.w) ? 2u : 0u) : wrest) : 1u;
                                 if (w != 0)
                                     count(dot3(rx, ry, rz), w);
                                 if (rev && !zero)
@@ -594,27 +723,36 @@ __global__ void __launch_bounds__(WARPS * 32, 4)
                         }
                         continue;
                     }
+                    // general: queries outside the box or the per-pair index test (one
+                    // group: the cull, and so the octant lists, are off here)
+                    const uint32_t nchunks = (TT + 31) / 32;
                     for (uint32_t ch = warp; ch < nchunks; ch += WARPS)
                     {
                         const uint32_t e = ch * 32 + lane;
                         const bool live = e < TT;
                         float4 pp = make_float4(0.f, 0.f, 0.f, 0.f);
-                        float4 iv = make_float4(0.f, 0.f, 0.f, 0.f);
+                        float3 iv = make_float3(0.f, 0.f, 0.f);
+                        bool valid = false;
                         uint32_t jj = 0xffffffffu;
                         int wr = 13;
                         if (live)
                         {
                             pp = S.pos[e];
-                            iv = S.iv[e];
+                            const int code = S.ivc[e];
+                            valid = code != IV_INVALID;
+                            if (valid)
+                            {
+                                const float4 v4 = S.img4[code];
+                                iv = make_float3(v4.x, v4.y, v4.z);
+                            }
                             jj = S.j[e];
                             wr = S.wr[e];
                         }
-                        const bool valid = iv.w != 0.0f;
 #pragma unroll 4
                         for (uint32_t qq = 0; qq < nb; ++qq)
                         {
                             const float4 q = S.q[qq];
-                            const int qimg = __float_as_int(q.w);
+                            const int qimg = S.qimg[qq];
                             const bool ok = !(test_ii && jj == S.qi[qq]);
                             bool acc = false;
                             float rsq = 0.f;

@@ -1114,9 +1114,10 @@ __global__ void __launch_bounds__(NLT, 6)
         K* src = S.ka;
         K* dst = S.kb;
         {
-            // the first NLM threads merge (fewer threads: the per-thread searches are
-            // amortised over more outputs)
-            constexpr int NLM = 64;
+            // every thread merges (a merge level is a barrier-bound step: the block's
+            // other warps would only wait; 0.99 ms against 1.02 ms with 64 threads on
+            // the 102^3 lattice, 1.09 ms with 32)
+            constexpr int NLM = NLT;
             const uint32_t per = (T + NLM - 1) / NLM;
             const uint32_t e0 = tid < NLM ? min(T, per * tid) : T;
             const uint32_t e1 = tid < NLM ? min(T, e0 + per) : T;

@@ -274,6 +274,141 @@ __global__ void __launch_bounds__(KWARPS * 32)
     }
 }
 
+// Thread per query: the query's k nearest candidates of the 27-cell stencil kept
+// in registers, unordered, with the position of the current k-th (largest) key;
+// a candidate below it replaces it and the largest is found again. Slots k ..
+// KMAX - 1 hold key 0, so they are never the largest and never replaced, and the
+// first free slot is always the one replaced next (found entries stay in slots
+// 0 .. found - 1). Cell-sorted queries put neighbouring queries in one warp: they
+// walk nearly the same stencil, reading the same candidates from L1. Validity and
+// outputs as k_knn_warp; the rows are ordered afterwards by k_knn_compact.
+template<int KMAX>
+__global__ void __launch_bounds__(128)
+    k_knn_thread(DevBox b, DevGrid g, const float4* __restrict__ qpos, const uint32_t* __restrict__ qidx, KnnParams p,
+                 float half_min_plane, uint32_t* __restrict__ tj, float* __restrict__ td, float* __restrict__ tv,
+                 uint32_t* __restrict__ counts, uint32_t* fail_list, uint32_t* fail_count)
+{
+    __shared__ float s_img[27][3];
+    for (int t = threadIdx.x; t < 81; t += blockDim.x)
+        s_img[t / 3][t % 3] = b.img[t / 3][t % 3];
+    __syncthreads();
+    const unsigned long long NONE = ~0ull;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < p.nq; t += gridDim.x * blockDim.x)
+    {
+        const float4 q = qpos[t];
+        const uint32_t qi = qidx[t];
+        int cx, cy, cz, qimg;
+        query_cell_k(b, g, q, cx, cy, cz, qimg);
+        unsigned long long key[KMAX];
+        uint32_t pay[KMAX];
+#pragma unroll
+        for (int s = 0; s < KMAX; ++s)
+        {
+            key[s] = s < static_cast<int>(p.k) ? NONE : 0ull;
+            pay[s] = 0;
+        }
+        unsigned long long worst = NONE;
+        int widx = 0;
+        const int nst = b.is2d ? 9 : 27;
+        for (int c = 0; c < nst; ++c)
+        {
+            const int code = b.is2d ? c_order2d[c] : c_order3d[c];
+            const int dx = code % 3 - 1;
+            const int dy = (code / 3) % 3 - 1;
+            const int dz = b.is2d ? 0 : code / 9 - 1;
+            auto ok_axis = [&](int d, int dim) {
+                if (p.arith == ARITH_AABB || dim >= 3)
+                    return true;
+                return dim == 1 ? d == 0 : d >= 0;
+            };
+            if (!(ok_axis(dx, g.dim[0]) && ok_axis(dy, g.dim[1]) && (b.is2d || ok_axis(dz, g.dim[2]))))
+                continue;
+            const int ux = cx + dx, uy = cy + dy, uz = cz + dz;
+            const int wx = ux < 0 ? -1 : (ux >= g.dim[0] ? 1 : 0);
+            const int wy = uy < 0 ? -1 : (uy >= g.dim[1] ? 1 : 0);
+            const int wz = uz < 0 ? -1 : (uz >= g.dim[2] ? 1 : 0);
+            const int cell = (ux - wx * g.dim[0]) + g.dim[0] * ((uy - wy * g.dim[1]) + g.dim[1] * (uz - wz * g.dim[2]));
+            const int wrap = (wx + 1) + 3 * (wy + 1) + 9 * (wz + 1);
+            const uint32_t s0 = g.start[cell], s1 = g.start[cell + 1];
+#pragma unroll 4
+            for (uint32_t slot = s0; slot < s1; ++slot)
+            {
+                const float4 pj = g.cpos[slot];
+                const uint32_t j = g.cidx[slot];
+                float rx, ry, rz;
+                if ((p.exclude_ii && j == qi) || !pair_vec_k(b, s_img, p.arith, q, qimg, pj, wrap, rx, ry, rz))
+                    continue;
+                const float rsq = dot3(rx, ry, rz);
+                if (!knn_accept(p, rsq))
+                    continue;
+                const unsigned long long kk = (static_cast<unsigned long long>(__float_as_uint(rsq)) << 32) | j;
+                if (kk >= worst)
+                    continue;
+                const uint32_t pp = (slot << 5) | static_cast<uint32_t>(wrap);
+                worst = 0ull;
+#pragma unroll
+                for (int s = 0; s < KMAX; ++s)
+                {
+                    if (s == widx)
+                    {
+                        key[s] = kk;
+                        pay[s] = pp;
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < KMAX; ++s)
+                {
+                    if (key[s] > worst)
+                    {
+                        worst = key[s];
+                        widx = s;
+                    }
+                }
+            }
+        }
+        // validity: k-th neighbour provably inside the stencil
+        bool valid = true;
+        if (worst != NONE)
+        {
+            const float dk = __fsqrt_rn(__uint_as_float(static_cast<uint32_t>(worst >> 32)));
+            if (!(dk < p.covered))
+                valid = false;
+            if (p.arith == ARITH_AABB && !(dk < half_min_plane))
+                valid = false;
+        }
+        else if (!(sqrtf(p.r_max_sq) <= p.covered))
+        {
+            // fewer than k found: fine only if everything within r_max was inside the stencil
+            valid = false;
+        }
+        if (!valid)
+        {
+            fail_list[atomicAdd(fail_count, 1u)] = t;
+            continue;
+        }
+        uint32_t found = 0;
+#pragma unroll
+        for (int s = 0; s < KMAX; ++s)
+        {
+            if (s < static_cast<int>(p.k) && key[s] != NONE)
+            {
+                const uint32_t slot = pay[s] >> 5;
+                const int wrap = static_cast<int>(pay[s] & 31u);
+                float rx = 0.f, ry = 0.f, rz = 0.f;
+                pair_vec_k(b, s_img, p.arith, q, qimg, g.cpos[slot], wrap, rx, ry, rz);
+                const size_t row = static_cast<size_t>(qi) * p.k + found;
+                tj[row] = static_cast<uint32_t>(key[s] & 0xffffffffull);
+                td[row] = __fsqrt_rn(dot3(rx, ry, rz));
+                tv[3 * row] = rx;
+                tv[3 * row + 1] = ry;
+                tv[3 * row + 2] = rz;
+                ++found;
+            }
+        }
+        counts[qi] = found;
+    }
+}
+
 // Block-wide bitonic sort of key[0, m) with its payload (padded to a power of two
 // with the largest key).
 __device__ void block_sort_keys(unsigned long long* key, uint32_t* pay, uint32_t m)
@@ -444,6 +579,55 @@ __global__ void __launch_bounds__(256)
         counts[qi] = found;
 }
 
+// Thread per query, rows of at most KMAX entries held in registers: each entry's
+// rank in the row's order (by j, or by distance then j; keys are distinct) is
+// the number of smaller keys, and the entry is written at that rank.
+template<int KMAX>
+__global__ void __launch_bounds__(128)
+    k_knn_compact_reg(const uint32_t* __restrict__ tj, const float* __restrict__ td, const float* __restrict__ tv,
+                      uint32_t k, uint32_t nq, const uint32_t* __restrict__ counts,
+                      const uint64_t* __restrict__ offsets, int by_distance, uint2* __restrict__ ij,
+                      float* __restrict__ dist, float* __restrict__ vec)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t c = counts[i];
+        const size_t row = static_cast<size_t>(i) * k;
+        const uint64_t off = offsets[i];
+        uint64_t key[KMAX];
+#pragma unroll
+        for (int x = 0; x < KMAX; ++x)
+        {
+            key[x] = ~0ull;
+            if (static_cast<uint32_t>(x) < c)
+            {
+                const uint32_t j = tj[row + x];
+                const uint32_t db = __float_as_uint(td[row + x]);
+                key[x] = by_distance ? ((static_cast<uint64_t>(db) << 32) | j) : ((static_cast<uint64_t>(j) << 32) | db);
+            }
+        }
+#pragma unroll
+        for (int x = 0; x < KMAX; ++x)
+        {
+            if (static_cast<uint32_t>(x) < c)
+            {
+                uint32_t r = 0;
+#pragma unroll
+                for (int y = 0; y < KMAX; ++y)
+                    r += key[y] < key[x] ? 1u : 0u;
+                const uint64_t o = off + r;
+                const uint32_t j = by_distance ? static_cast<uint32_t>(key[x]) : static_cast<uint32_t>(key[x] >> 32);
+                const uint32_t db = by_distance ? static_cast<uint32_t>(key[x] >> 32) : static_cast<uint32_t>(key[x]);
+                ij[o] = make_uint2(i, j);
+                dist[o] = __uint_as_float(db);
+                vec[3 * o] = tv[3 * (row + x)];
+                vec[3 * o + 1] = tv[3 * (row + x) + 1];
+                vec[3 * o + 2] = tv[3 * (row + x) + 2];
+            }
+        }
+    }
+}
+
 // Thread per query: order its row (by j, or by distance then j) and copy it out.
 __global__ void k_knn_compact(const uint32_t* __restrict__ tj, const float* __restrict__ td,
                               const float* __restrict__ tv, uint32_t k, uint32_t nq, const uint32_t* __restrict__ counts,
@@ -505,6 +689,22 @@ void launch_knn_warp(const DevBox& box, const DevGrid& g, const float4* qpos, co
     float mp = fminf(pd0, pd1);
     if (!box.is2d)
         mp = fminf(mp, box.L[2]);
+    if (p.k <= 16)
+    {
+        // thread per query (cell-sorted queries: a warp walks nearly one stencil)
+        const uint32_t blocks = (p.nq + 127) / 128;
+        ProfScope prof_("k_knn_thread", s);
+        if (p.k <= 8)
+            k_knn_thread<8><<<blocks, 128, 0, s>>>(box, g, qpos, qidx, p, mp / 2.0f, tj, td, tv, counts, fail_list,
+                                                   fail_count);
+        else if (p.k <= 12)
+            k_knn_thread<12><<<blocks, 128, 0, s>>>(box, g, qpos, qidx, p, mp / 2.0f, tj, td, tv, counts, fail_list,
+                                                    fail_count);
+        else
+            k_knn_thread<16><<<blocks, 128, 0, s>>>(box, g, qpos, qidx, p, mp / 2.0f, tj, td, tv, counts, fail_list,
+                                                    fail_count);
+    }
+    else
     {
         ProfScope prof_("k_knn_warp", s);
         k_knn_warp<<<want < cap ? want : cap, KWARPS * 32, 0, s>>>(box, g, qpos, qidx, p, mp / 2.0f, tj, td, tv, counts,
@@ -543,6 +743,16 @@ void launch_knn_compact(const uint32_t* tj, const float* td, const float* tv, ui
     if (nq == 0)
         return;
     const uint32_t blocks = (nq + 127) / 128;
+    if (k <= 16)
+    {
+        ProfScope prof_("k_knn_compact", s);
+        const uint32_t b = blocks < 152 * 64 ? blocks : 152 * 64;
+        if (k <= 12)
+            k_knn_compact_reg<12><<<b, 128, 0, s>>>(tj, td, tv, k, nq, counts, offsets, by_distance, ij, dist, vec);
+        else
+            k_knn_compact_reg<16><<<b, 128, 0, s>>>(tj, td, tv, k, nq, counts, offsets, by_distance, ij, dist, vec);
+        return;
+    }
     {
         ProfScope prof_("k_knn_compact", s);
         k_knn_compact<<<blocks < 152 * 64 ? blocks : 152 * 64, 128, 0, s>>>(tj, td, tv, k, nq, counts, offsets,
