@@ -865,10 +865,23 @@ template<bool FILL> struct FBWarp
     int it_wrap[27];          // (wx + 1) + 3 (wy + 1) + 9 (wz + 1)
 };
 
-template<bool FILL>
+// ONE (one pass, FILL): no counts and offsets beforehand. Each warp takes chunks of
+// the bond arrays from a device counter (*alloc) and places each query's bonds at
+// its chunk's cursor; before a query the chunk must hold the cell's candidate
+// count, an upper bound on the query's bonds (else the rest of the chunk is left
+// and a new one taken). seg[i] / counts[i] receive the query's first bond and its
+// bond count. Bonds past cap are not written and a query whose bonds end past cap
+// gets count 0 (the caller compares *alloc with cap and reruns the two passes when
+// the arrays were too small; the kernels after this one never read past cap). A
+// query's bonds keep candidate order, so the per-particle sums downstream are the
+// same as with the two passes.
+constexpr uint32_t FB_CHUNK = 4096; // bond slots a warp takes at a time (one pass)
+
+template<bool FILL, bool ONE = false>
 __global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
     k_frames_ball(BatchGrid g, BallParams p, uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets,
-                  uint32_t* __restrict__ bj, float4* __restrict__ bvd)
+                  uint32_t* __restrict__ bj, float4* __restrict__ bvd, uint32_t* __restrict__ seg = nullptr,
+                  unsigned long long* __restrict__ alloc = nullptr, unsigned long long cap = 0)
 {
     __shared__ FBWarp<FILL> sw[FB_WARPS];
     const int lane = threadIdx.x & 31;
@@ -881,6 +894,7 @@ __global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
         return;
     uint32_t f = frame_of(g.cell_base, g.nframes, c);
     uint32_t qn = 0; // queued bonds (fill)
+    unsigned long long cur = 0, cend = 0; // one pass: the warp's chunk [cur, cend)
 
     // drain the first n queued bonds: exact box.wrap of p_j - q in frame f
     auto drain = [&](uint32_t n) {
@@ -891,8 +905,11 @@ __global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
             const float4 v = W.qv[lane];
             float wx, wy, wz;
             box_wrap(B, v.x, v.y, v.z, wx, wy, wz);
-            bj[e] = W.qj[lane];
-            bvd[e] = make_float4(wx, wy, wz, __fsqrt_rn(v.w));
+            if (!ONE || e < cap)
+            {
+                bj[e] = W.qj[lane];
+                bvd[e] = make_float4(wx, wy, wz, __fsqrt_rn(v.w));
+            }
         }
         __syncwarp();
     };
@@ -969,9 +986,12 @@ __global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
                 const uint32_t i = g.cidx[q0 + g0 + lane];
                 W.q[lane] = g.cpos[q0 + g0 + lane];
                 W.qi[lane] = i;
-                if (FILL)
+                if (FILL && !ONE)
                     my_off = offsets[i];
             }
+            // one pass over the cell's tiles for the group: counts only (fill_now
+            // false) or counts and bonds
+            auto run_tiles = [&](bool fill_now, bool alloc_per_query) {
             for (uint32_t tile = 0; tile < ntile; ++tile)
             {
                 const uint32_t t0 = tile * FB_TILE;
@@ -1020,7 +1040,24 @@ __global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
                     const uint32_t qi = W.qi[k];
                     const int qimg = __float_as_int(q.w);
                     uint32_t base = __shfl_sync(FULL, my_cnt, k);
-                    const uint64_t off = FILL ? __shfl_sync(FULL, my_off, k) : 0;
+                    uint64_t off = FILL && !ONE ? __shfl_sync(FULL, my_off, k) : 0;
+                    if (ONE && alloc_per_query)
+                    {
+                        // room for every candidate of the cell (bound on the bonds)
+                        if (cend - cur < T)
+                        {
+                            const unsigned long long want = T > FB_CHUNK ? T : FB_CHUNK;
+                            unsigned long long b0 = 0;
+                            if (lane == 0)
+                                b0 = atomicAdd(alloc, want);
+                            cur = __shfl_sync(FULL, b0, 0);
+                            cend = cur + want;
+                        }
+                        if (lane == static_cast<int>(k))
+                            my_off = cur;
+                    }
+                    if (ONE)
+                        off = __shfl_sync(FULL, my_off, k);
                     for (uint32_t r0 = 0; r0 < TT; r0 += 32)
                     {
                         const uint32_t tl = r0 + lane;
@@ -1059,7 +1096,7 @@ __global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
                             }
                         }
                         const unsigned bal = __ballot_sync(FULL, acc);
-                        if (FILL && bal != 0)
+                        if (FILL && fill_now && bal != 0)
                         {
                             if (acc)
                             {
@@ -1099,10 +1136,59 @@ __global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
                     }
                     if (lane == static_cast<int>(k))
                         my_cnt = base;
+                    if (ONE && alloc_per_query)
+                        cur += base; // the query's bonds are placed: advance the cursor
                 }
             }
-            if (!FILL && lane < static_cast<int>(ng))
-                counts[W.qi[lane]] = my_cnt;
+            };
+            if (!ONE)
+            {
+                run_tiles(FILL, false);
+            }
+            else if (ntile == 1)
+            {
+                // every candidate in one tile: each query's bonds are found in one
+                // sweep, placed at the cursor with room for all candidates
+                run_tiles(true, true);
+            }
+            else
+            {
+                // several tiles: count the group's bonds, place the group, then fill
+                run_tiles(false, false);
+                uint32_t incl = lane < static_cast<int>(ng) ? my_cnt : 0u;
+                const uint32_t mine = incl;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1)
+                {
+                    const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o)
+                        incl += v;
+                }
+                const unsigned long long tot = __shfl_sync(FULL, incl, 31);
+                if (cend - cur < tot)
+                {
+                    const unsigned long long want = tot > FB_CHUNK ? tot : FB_CHUNK;
+                    unsigned long long b0 = 0;
+                    if (lane == 0)
+                        b0 = atomicAdd(alloc, want);
+                    cur = __shfl_sync(FULL, b0, 0);
+                    cend = cur + want;
+                }
+                my_off = cur + (incl - mine);
+                cur += tot;
+                my_cnt = 0;
+                run_tiles(true, false);
+            }
+            if ((!FILL || ONE) && lane < static_cast<int>(ng))
+            {
+                // one pass: a query whose bonds do not fit below cap gets no bonds,
+                // so the kernels after this one read nothing past the arrays (the
+                // caller reruns the two passes)
+                const bool fits = !ONE || my_off + my_cnt <= cap;
+                counts[W.qi[lane]] = fits ? my_cnt : 0u;
+                if (ONE)
+                    seg[W.qi[lane]] = fits ? static_cast<uint32_t>(my_off) : 0u;
+            }
             __syncwarp();
         }
     }
@@ -1345,6 +1431,23 @@ void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n
     const uint32_t blocks = frames_ball_blocks(k_frames_ball<true>, g.ncell);
     ProfScope prof_("k_frames_ball<FILL>", s);
     k_frames_ball<true><<<blocks, FB_THREADS, 0, s>>>(g, p, nullptr, offsets, bond_j, bond_vd);
+}
+
+uint64_t frames_ball_onepass_slack(uint32_t ncell)
+{
+    // every warp may leave the rest of its last chunk unused
+    return static_cast<uint64_t>(frames_ball_blocks(k_frames_ball<true, true>, ncell)) * FB_WARPS * FB_CHUNK;
+}
+
+void launch_frames_ball_onepass(const BatchGrid& g, const BallParams& p, uint32_t n, uint32_t* counts, uint32_t* seg,
+                                uint32_t* bond_j, float4* bond_vd, unsigned long long* alloc, uint64_t cap,
+                                cudaStream_t s)
+{
+    if (n == 0 || g.ncell == 0)
+        return;
+    const uint32_t blocks = frames_ball_blocks(k_frames_ball<true, true>, g.ncell);
+    ProfScope prof_("k_frames_ball<ONE>", s);
+    k_frames_ball<true, true><<<blocks, FB_THREADS, 0, s>>>(g, p, counts, nullptr, bond_j, bond_vd, seg, alloc, cap);
 }
 
 int frames_sys_splits(uint32_t max_rows)

@@ -82,6 +82,14 @@ void launch_frames_hist(const BatchHistConfig& cfg, const BatchGrid& g, const Ba
 void launch_frames_ball_count(const BatchGrid& g, const BallParams& p, uint32_t n, uint32_t* counts, cudaStream_t s);
 void launch_frames_ball_fill(const BatchGrid& g, const BallParams& p, uint32_t n, const uint64_t* offsets,
                              uint32_t* bond_j, float4* bond_vd, cudaStream_t s);
+// One pass without the counts: warps take chunks of the bond arrays (capacity
+// cap) from *alloc (zeroed before the launch); seg[i] / counts[i] = the first bond
+// of point i and its bond count, its bonds in candidate order. *alloc > cap after
+// the launch: the arrays were too small and nothing past cap was written.
+uint64_t frames_ball_onepass_slack(uint32_t ncell); // bond slots the chunk tails may leave unused
+void launch_frames_ball_onepass(const BatchGrid& g, const BallParams& p, uint32_t n, uint32_t* counts, uint32_t* seg,
+                                uint32_t* bond_j, float4* bond_vd, unsigned long long* alloc, uint64_t cap,
+                                cudaStream_t s);
 
 // Per-frame FP64 system sums of the per-l (n, 2l + 1) qlm layout: sys[f][col]
 // (complex, col running over every l's m) = (FP64 sum over the frame's rows) /

@@ -381,6 +381,7 @@ struct fg_steinhardt
     WlTerms wt {};
     std::vector<std::vector<double>> w3j_host; // per l, for the system Wl (computed once)
     std::vector<float> order; // frames x n_l
+    uint64_t bond_hint = 0;   // batched frames: bond slots the last one pass took (or the bonds counted)
     uint32_t frames = 1;
     bool computed = false;
 };
@@ -2951,7 +2952,8 @@ struct fg_frames
     GraphCache rdf_graph;
     // Steinhardt workspace
     DevBuf st_counts, st_offsets, st_scan, st_j, st_vd, st_seg, st_partial, st_sys;
-    GraphCache st_graph_a, st_graph_b;
+    GraphCache st_graph_a, st_graph_b, st_graph_one;
+    DevBuf st_alloc; // one pass: bond slots taken
 };
 
 namespace {
@@ -3367,22 +3369,120 @@ fg_status fg_rdf_accumulate_frames(fg_rdf* rdf, fg_frames* fr, const fg_query_ar
 
 static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_args& a)
 {
+    cudaStream_t s = stream();
+    const uint32_t P = fr->total;
+    const uint32_t F = static_cast<uint32_t>(fr->n.size());
+    BallParams p;
+    p.r_max_sq = fmul(a.r_max, a.r_max);
+    p.r_min_sq = fmul(a.r_min, a.r_min);
+    p.exclude_ii = a.exclude_ii;
+    p.arith = ARITH_AABB;
+    p.nq = P;
+    BatchGridBufs& g = batch_grid(fr, a.r_max, 1);
+    const BatchGrid v = batch_view(fr, g);
+    fr->st_counts.alloc(sizeof(uint32_t) * (P + 1));
+    fr->st_seg.alloc(sizeof(uint32_t) * (P + 1));
+    // outputs and per-frame sums
+    st->n = P;
+    st->frames = F;
+    size_t off = 0;
+    for (int k = 0; k < st->st.nl; ++k)
     {
-        cudaStream_t s = stream();
-        const uint32_t P = fr->total;
-        const uint32_t F = static_cast<uint32_t>(fr->n.size());
-        BallParams p;
-        p.r_max_sq = fmul(a.r_max, a.r_max);
-        p.r_min_sq = fmul(a.r_min, a.r_min);
-        p.exclude_ii = a.exclude_ii;
-        p.arith = ARITH_AABB;
-        p.nq = P;
-        BatchGridBufs& g = batch_grid(fr, a.r_max, 1);
-        const BatchGrid v = batch_view(fr, g);
-        fr->st_counts.alloc(sizeof(uint32_t) * (P + 1));
+        st->st.qlm_offset[k] = off;
+        off += static_cast<size_t>(P) * (2 * st->st.l[k] + 1);
+    }
+    const int stride = static_cast<int>(st->stride);
+    const uint32_t max_rows = *std::max_element(fr->n.begin(), fr->n.end());
+    fr->st_partial.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * frames_sys_splits(max_rows) * stride);
+    fr->st_sys.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * stride);
+    st->qlm.alloc(sizeof(float2) * std::max<size_t>(off, 1));
+    st->ql.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
+    if (st->average)
+    {
+        st->qlm_ave.alloc(sizeof(float2) * std::max<size_t>(off, 1));
+        st->ql_ave.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
+    }
+    if (st->wl)
+        st->wlv.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
+    // expected bonds: N^2 / V times the ball volume per frame (uniform points)
+    double expect = 0.0;
+    for (uint32_t f = 0; f < F; ++f)
+    {
+        const HostBox& b = fr->boxes[f];
+        const double r = a.r_max;
+        const double vol = b.is2d ? static_cast<double>(b.L[0]) * b.L[1] : static_cast<double>(b.L[0]) * b.L[1] * b.L[2];
+        const double ball = b.is2d ? M_PI * r * r : 4.0 / 3.0 * M_PI * r * r * r;
+        expect += vol > 0.0 ? static_cast<double>(fr->n[f]) * fr->n[f] / vol * ball : 0.0;
+    }
+    // qlm, average, per-frame system sums, wl over the bonds (seg / counts / bond arrays)
+    auto enqueue_rest = [&](double mean_bonds) {
+        launch_qlm(g.fd_host[0].b, fr->dpts, P, nullptr, nullptr, nullptr, fr->st_seg.as<uint32_t>(),
+                   fr->st_counts.as<uint32_t>(), st->st, 0, st->qlm.as<float2>(), st->ql.as<float>(), s,
+                   fr->st_vd.as<float4>(), mean_bonds, st->wl ? 1 : 0);
+        const float2* src = st->qlm.as<float2>();
+        const float* qn = st->ql.as<float>();
+        if (st->average)
+        {
+            launch_ave(P, nullptr, fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st, st->qlm.as<float2>(),
+                       st->qlm_ave.as<float2>(), st->ql_ave.as<float>(), s, fr->st_j.as<uint32_t>(), v.cidx);
+            src = st->qlm_ave.as<float2>();
+            qn = st->ql_ave.as<float>();
+        }
+        launch_frames_sys(fr->d_pt_base.as<uint32_t>(), F, max_rows, st->st, stride, src, fr->st_partial.as<double>(),
+                          fr->st_sys.as<double>(), s);
+        if (st->wl)
+        {
+            launch_wl(P, st->st, st->wt, st->wl_terms.as<int4>(), src, qn, st->wl_normalize ? 1 : 0, st->wlv.as<float>(),
+                      s);
+        }
+    };
+    auto outputs_key = [&](std::vector<uint64_t> key) {
+        for (const void* ptr : {fr->st_j.p, fr->st_vd.p, fr->st_seg.p, fr->st_counts.p, fr->st_partial.p, fr->st_sys.p,
+                                st->qlm.p, st->ql.p, st->qlm_ave.p, st->ql_ave.p, st->wlv.p, st->wl_terms.p,
+                                static_cast<void*>(st)})
+            key.push_back(reinterpret_cast<uint64_t>(ptr));
+        for (uint64_t x : {fbits(a.r_max), fbits(a.r_min), static_cast<uint64_t>(a.exclude_ii),
+                           static_cast<uint64_t>(st->average), static_cast<uint64_t>(st->wl),
+                           static_cast<uint64_t>(st->wl_normalize)})
+            key.push_back(x);
+        for (int k = 0; k < st->st.nl; ++k)
+            key.push_back(static_cast<uint64_t>(st->st.l[k]));
+        return key;
+    };
+    std::vector<double> sys(2 * static_cast<size_t>(F) * stride);
+    bool done = false;
+    // one pass: bonds placed by per-warp chunks, no counts beforehand; arrays sized by
+    // the expected bonds or the last run's (whichever is larger) plus the chunk tails
+    const uint64_t cap = static_cast<uint64_t>(std::max(1.25 * expect, 1.1 * static_cast<double>(st->bond_hint))) +
+                         frames_ball_onepass_slack(g.ncell) + P;
+    if (cap < (1ull << 32))
+    {
+        fr->st_j.alloc(sizeof(uint32_t) * cap);
+        fr->st_vd.alloc(sizeof(float4) * cap);
+        fr->st_alloc.alloc(sizeof(unsigned long long));
+        std::vector<uint64_t> key = outputs_key({g.id, cap, reinterpret_cast<uint64_t>(fr->dpts),
+                                                 reinterpret_cast<uint64_t>(fr->st_alloc.p)});
+        run_graph(fr->st_graph_one, fr->graphs, key, "graph:steinhardt_frames", [&] {
+            enqueue_grid_build(fr, g, s, true);
+            FG_CUDA(cudaMemsetAsync(fr->st_alloc.p, 0, sizeof(unsigned long long), s));
+            launch_frames_ball_onepass(v, p, P, fr->st_counts.as<uint32_t>(), fr->st_seg.as<uint32_t>(),
+                                       fr->st_j.as<uint32_t>(), fr->st_vd.as<float4>(),
+                                       fr->st_alloc.as<unsigned long long>(), cap, s);
+            enqueue_rest(expect / std::max<uint32_t>(P, 1));
+        });
+        FG_CUDA(cudaGetLastError());
+        unsigned long long taken = 0;
+        FG_CUDA(cudaMemcpyAsync(&taken, fr->st_alloc.p, sizeof(taken), cudaMemcpyDeviceToHost, s));
+        FG_CUDA(cudaMemcpyAsync(sys.data(), fr->st_sys.p, sizeof(double) * sys.size(), cudaMemcpyDeviceToHost, s));
+        sync();
+        st->bond_hint = taken;
+        done = taken <= cap;
+    }
+    if (!done)
+    {
+        // two passes: bond counts and offsets, then the bonds at their offsets
         fr->st_offsets.alloc(sizeof(uint64_t) * (P + 1));
         fr->st_scan.alloc(scan_scratch_bytes(static_cast<size_t>(P) + 1));
-        // phase 1: grid, bond counts, offsets
         const std::vector<uint64_t> key_a = {g.id, reinterpret_cast<uint64_t>(fr->dpts),
                                              reinterpret_cast<uint64_t>(fr->st_counts.p),
                                              reinterpret_cast<uint64_t>(fr->st_offsets.p),
@@ -3400,79 +3500,25 @@ static void steinhardt_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_a
         sync();
         if (nb >= (1ull << 32))
             runtime_error("a batched Steinhardt neighbour list holds fewer than 2^32 bonds");
-        // phase 2: bonds, qlm, average, per-frame system sums, wl
-        st->n = P;
-        st->frames = F;
-        size_t off = 0;
-        for (int k = 0; k < st->st.nl; ++k)
-        {
-            st->st.qlm_offset[k] = off;
-            off += static_cast<size_t>(P) * (2 * st->st.l[k] + 1);
-        }
-        const int stride = static_cast<int>(st->stride);
+        st->bond_hint = std::max<uint64_t>(st->bond_hint, nb);
         fr->st_j.alloc(sizeof(uint32_t) * std::max<uint64_t>(nb, 1));
         fr->st_vd.alloc(sizeof(float4) * std::max<uint64_t>(nb, 1));
-        fr->st_seg.alloc(sizeof(uint32_t) * (P + 1));
-        const uint32_t max_rows = *std::max_element(fr->n.begin(), fr->n.end());
-        fr->st_partial.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * frames_sys_splits(max_rows) * stride);
-        fr->st_sys.alloc(sizeof(double) * 2 * static_cast<size_t>(F) * stride);
-        st->qlm.alloc(sizeof(float2) * std::max<size_t>(off, 1));
-        st->ql.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
-        if (st->average)
-        {
-            st->qlm_ave.alloc(sizeof(float2) * std::max<size_t>(off, 1));
-            st->ql_ave.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
-        }
-        if (st->wl)
-            st->wlv.alloc(sizeof(float) * std::max<size_t>(static_cast<size_t>(P) * st->st.nl, 1));
-        std::vector<uint64_t> key_b = {
-            g.id, nb, reinterpret_cast<uint64_t>(fr->st_j.p), reinterpret_cast<uint64_t>(fr->st_vd.p),
-            reinterpret_cast<uint64_t>(fr->st_seg.p), reinterpret_cast<uint64_t>(fr->st_partial.p),
-            reinterpret_cast<uint64_t>(fr->st_sys.p), reinterpret_cast<uint64_t>(st->qlm.p),
-            reinterpret_cast<uint64_t>(st->ql.p), reinterpret_cast<uint64_t>(st->qlm_ave.p),
-            reinterpret_cast<uint64_t>(st->ql_ave.p), reinterpret_cast<uint64_t>(st->wlv.p),
-            reinterpret_cast<uint64_t>(st), fbits(a.r_max), fbits(a.r_min), static_cast<uint64_t>(a.exclude_ii),
-            static_cast<uint64_t>(st->average), static_cast<uint64_t>(st->wl), static_cast<uint64_t>(st->wl_normalize)};
-        for (int k = 0; k < st->st.nl; ++k)
-        {
-            key_b.push_back(static_cast<uint64_t>(st->st.l[k]));
-            key_b.push_back(reinterpret_cast<uint64_t>(st->wl_terms.p));
-        }
+        std::vector<uint64_t> key_b = outputs_key({g.id, nb, reinterpret_cast<uint64_t>(fr->st_offsets.p)});
         run_graph(fr->st_graph_b, fr->graphs, key_b, "graph:steinhardt_frames", [&] {
             launch_frames_ball_fill(v, p, P, fr->st_offsets.as<uint64_t>(), fr->st_j.as<uint32_t>(),
                                     fr->st_vd.as<float4>(), s);
             launch_segments_from_offsets(fr->st_counts.as<uint32_t>(), fr->st_offsets.as<uint64_t>(), P,
                                          fr->st_seg.as<uint32_t>(), s);
-            launch_qlm(g.fd_host[0].b, fr->dpts, P, nullptr, nullptr, nullptr, fr->st_seg.as<uint32_t>(),
-                       fr->st_counts.as<uint32_t>(), st->st, 0, st->qlm.as<float2>(), st->ql.as<float>(), s,
-                       fr->st_vd.as<float4>(), static_cast<double>(nb) / std::max<uint32_t>(P, 1), st->wl ? 1 : 0);
-            const float2* src = st->qlm.as<float2>();
-            const float* qn = st->ql.as<float>();
-            if (st->average)
-            {
-                launch_ave(P, nullptr, fr->st_seg.as<uint32_t>(), fr->st_counts.as<uint32_t>(), st->st,
-                           st->qlm.as<float2>(), st->qlm_ave.as<float2>(), st->ql_ave.as<float>(), s,
-                           fr->st_j.as<uint32_t>(), v.cidx);
-                src = st->qlm_ave.as<float2>();
-                qn = st->ql_ave.as<float>();
-            }
-            launch_frames_sys(fr->d_pt_base.as<uint32_t>(), F, max_rows, st->st, stride, src,
-                              fr->st_partial.as<double>(), fr->st_sys.as<double>(), s);
-            if (st->wl)
-            {
-                launch_wl(P, st->st, st->wt, st->wl_terms.as<int4>(), src, qn, st->wl_normalize ? 1 : 0,
-                          st->wlv.as<float>(), s);
-            }
+            enqueue_rest(static_cast<double>(nb) / std::max<uint32_t>(P, 1));
         });
         FG_CUDA(cudaGetLastError());
-        std::vector<double> sys(2 * static_cast<size_t>(F) * stride);
         FG_CUDA(cudaMemcpyAsync(sys.data(), fr->st_sys.p, sizeof(double) * sys.size(), cudaMemcpyDeviceToHost, s));
         sync();
-        st->order.assign(static_cast<size_t>(F) * st->st.nl, 0.0f);
-        for (uint32_t f = 0; f < F; ++f)
-            normalize_system(st, &sys[2 * static_cast<size_t>(f) * stride], &st->order[static_cast<size_t>(f) * st->st.nl]);
-        st->computed = true;
     }
+    st->order.assign(static_cast<size_t>(F) * st->st.nl, 0.0f);
+    for (uint32_t f = 0; f < F; ++f)
+        normalize_system(st, &sys[2 * static_cast<size_t>(f) * stride], &st->order[static_cast<size_t>(f) * st->st.nl]);
+    st->computed = true;
 }
 
 fg_status fg_steinhardt_compute_frames(fg_steinhardt* st, fg_frames* fr, const fg_query_args* args)

@@ -375,9 +375,6 @@ __global__ void __launch_bounds__(128)
         }
         const uint32_t excl = incl - c;
         const uint32_t total = __shfl_sync(FULL, incl, 31);
-        // the warp's bonds are contiguous from the first particle that has any
-        const unsigned nz = __ballot_sync(FULL, c > 0);
-        const uint32_t base = nz ? __shfl_sync(FULL, sg, __ffs(nz) - 1) : 0u;
 #pragma unroll
         for (int v = 0; v < NV; ++v)
             acc[lane][v] = 0.0f;
@@ -395,13 +392,15 @@ __global__ void __launch_bounds__(128)
                 if (v <= bb)
                     k += step;
             }
+            // bond bb is bond bb - excl of its particle's segment (segments need not be
+            // contiguous from one particle to the next)
+            const uint32_t e = __shfl_sync(FULL, sg, k) + (bb - __shfl_sync(FULL, excl, k));
             float vals[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v)
                 vals[v] = 0.0f;
             if (live)
             {
-                const uint32_t e = base + bb;
                 float dx, dy, dz, d;
                 if (bvd != nullptr)
                 {
@@ -1546,20 +1545,19 @@ void launch_ave(uint32_t n, const uint2* ij, const uint32_t* seg, const uint32_t
     for (int k = 0; k < ls.nl; ++k)
         E += 2 * ls.l[k] + 1;
     const uint32_t cap = static_cast<uint32_t>(sm_count()) * 16;
-    if (E <= 128)
+    // rows of several l: flattened over the lanes (one l of up to 7 orders: the
+    // order-per-lane kernel below is faster, 4.5 ms against 6.7 ms for l = 6 on the
+    // 64 uneven frames)
+    if (E > 16 && E <= 128)
     {
-        const int P = E <= 8 ? 8 : (E <= 16 ? 16 : 32);
+        const int P = 32;
         const uint32_t per_block = 128 / P;
         const uint32_t blocks = std::min<uint32_t>((n + per_block - 1) / per_block, cap);
         auto go = [&](auto kernel) {
             kernel<<<blocks, 128, 0, s>>>(n, ij, bond_j, seg, cnt, ls, E, qlm, ave, ql_ave, order);
         };
         ProfScope prof_("k_ave_flat", s);
-        if (P == 8)
-            go(k_ave_flat<8, 1>);
-        else if (P == 16)
-            go(k_ave_flat<16, 1>);
-        else if (E <= 32)
+        if (E <= 32)
             go(k_ave_flat<32, 1>);
         else if (E <= 64)
             go(k_ave_flat<32, 2>);

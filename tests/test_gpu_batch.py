@@ -246,3 +246,29 @@ def test_steinhardt_ball_dense_cells_points_outside(freud, average):
         ok = np.isfinite(qref)
         assert np.array_equal(ok, np.isfinite(ql))
         np.testing.assert_allclose(ql[ok], qref[ok], rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize("average", [False, True])
+def test_steinhardt_frames_one_pass_after_two(freud, average):
+    """Dense clusters: the bonds far exceed the uniform-density estimate, so the first
+    batched call overflows the one-pass arrays and takes the two passes; the second
+    call is sized by the first and runs in one pass, with cells of several candidate
+    tiles counted then filled. Both give the same per-particle bonds in the same
+    order, so the same Ql bit for bit, within 1e-5 of the FP64 oracle."""
+    dense = _clustered_frame(freud, 81, blobs=4, per_blob=400)
+    uni = make_frames(freud, [2000], 82)[0]
+    st = freud.order.Steinhardt([4, 6], average=average)
+    batch = freud.locality.FrameBatch([dense, uni])
+    st.compute(batch, neighbors={"r_max": 1.2})
+    first = np.asarray(st.ql).copy()
+    st.compute(freud.locality.FrameBatch([dense, uni]), neighbors={"r_max": 1.2})
+    second = np.asarray(st.ql)
+    np.testing.assert_array_equal(first, second)
+    box, pts = dense
+    ij, d, v = O.query(box, pts, r_max=1.2, exclude_ii=True, arith=O.ARITH_AABB)
+    o = O.steinhardt([4, 6], box, pts, ij, d, average=average)
+    qref = o["ql_ave"] if average else o["ql"]
+    ql = second.reshape(-1, 2)[:len(pts)]
+    ok = np.isfinite(qref)
+    assert np.array_equal(ok, np.isfinite(ql))
+    np.testing.assert_allclose(ql[ok], qref[ok], rtol=1e-5, atol=1e-7)
