@@ -54,6 +54,8 @@ SIGNATURES = {
     "fg_launch_count": [pu64],
     "fg_profile_enable": [i32],
     "fg_profile_report": [ctypes.c_char_p, ctypes.c_size_t],
+    "fg_host_alloc": [ctypes.c_size_t, PP],
+    "fg_host_free": [P],
     "fg_nq_create": [pbox, P, u32, i32, f32, PP],
     "fg_nq_create_device": [pbox, P, u32, i32, f32, PP],
     "fg_nq_destroy": [P],
@@ -224,3 +226,56 @@ class Handle:
                 self._destroy(v)
             except Exception:  # interpreter shutdown
                 pass
+
+
+# ---- page-locked host arrays -----------------------------------------------------
+# Blocks of page-locked memory, pooled by size: a NeighborList read back to the host
+# lands in one (DMA at the link's rate), and returns to the pool when the last array
+# viewing it is dropped. The pool keeps at most _PINNED_KEEP bytes.
+
+_PINNED_KEEP = 16 << 30
+_pinned_free = {}
+_pinned_pooled = 0
+
+
+class _PinnedBlock:
+    __slots__ = ("addr", "nbytes")
+
+    def __init__(self, addr, nbytes):
+        self.addr = addr
+        self.nbytes = nbytes
+
+    def __del__(self):
+        global _pinned_pooled
+        try:
+            if _pinned_pooled + self.nbytes <= _PINNED_KEEP:
+                _pinned_free.setdefault(self.nbytes, []).append(self.addr)
+                _pinned_pooled += self.nbytes
+            else:
+                lib.fg_host_free(ctypes.c_void_p(self.addr))
+        except Exception:  # interpreter shutdown
+            pass
+
+
+def pinned_empty(shape, dtype):
+    """An uninitialised numpy array in page-locked host memory (pooled)."""
+    import numpy as np
+
+    global _pinned_pooled
+    dtype = np.dtype(dtype)
+    count = 1
+    for s in (shape if isinstance(shape, tuple) else (shape,)):
+        count *= int(s)
+    need = max(count * dtype.itemsize, 1)
+    nbytes = (need + (2 << 20) - 1) // (2 << 20) * (2 << 20)
+    free = _pinned_free.get(nbytes)
+    if free:
+        addr = free.pop()
+        _pinned_pooled -= nbytes
+    else:
+        out = ctypes.c_void_p()
+        check(lib.fg_host_alloc(nbytes, ctypes.byref(out)))
+        addr = out.value
+    raw = (ctypes.c_char * need).from_address(addr)
+    raw._owner = _PinnedBlock(addr, nbytes)
+    return np.frombuffer(raw, dtype=dtype, count=count).reshape(shape)

@@ -1460,6 +1460,25 @@ fg_status fg_nlist_num_points(const fg_nlist* nl, uint32_t* out)
     });
 }
 
+fg_status fg_host_alloc(size_t bytes, void** out)
+{
+    return guard([&] {
+        require(out, "out");
+        *out = nullptr;
+        if (bytes == 0)
+            return;
+        FG_CUDA(cudaMallocHost(out, bytes));
+    });
+}
+
+fg_status fg_host_free(void* p)
+{
+    return guard([&] {
+        if (p != nullptr)
+            FG_CUDA(cudaFreeHost(p));
+    });
+}
+
 fg_status fg_nlist_get(const fg_nlist* nl, uint32_t* neighbors, float* distances, float* weights, float* vectors)
 {
     return guard([&] {
@@ -1477,8 +1496,7 @@ fg_status fg_nlist_get(const fg_nlist* nl, uint32_t* neighbors, float* distances
         {
             if (nl->unit_weights)
             {
-                for (uint64_t b = 0; b < nl->nb; ++b)
-                    weights[b] = 1.0f;
+                std::fill(weights, weights + nl->nb, 1.0f);
             }
             else
             {

@@ -457,17 +457,20 @@ class NeighborList:
         new_copy.copy(self)
         return new_copy
 
+    # lists of at least this many bonds come back in page-locked host memory
+    _PINNED_BONDS = 1 << 20
+
     def _arrays(self):
         if "ij" not in self._cache:
             n = len(self)
-            ij = np.zeros((n, 2), np.uint32)
-            d = np.zeros(n, np.float32)
-            w = np.zeros(n, np.float32)
-            v = np.zeros((n, 3), np.float32)
-            _lib.check(_lib.lib.fg_nlist_get(self._h, _lib.ptr(ij), _lib.ptr(d), _lib.ptr(w), _lib.ptr(v)))
-            for a in (ij, d, w, v):
+            empty = _lib.pinned_empty if n >= self._PINNED_BONDS else np.empty
+            ij = empty((n, 2), np.uint32)
+            d = empty((n,), np.float32)
+            v = empty((n, 3), np.float32)
+            _lib.check(_lib.lib.fg_nlist_get(self._h, _lib.ptr(ij), _lib.ptr(d), None, _lib.ptr(v)))
+            for a in (ij, d, v):
                 a.flags.writeable = False
-            self._cache.update(ij=ij, d=d, w=w, v=v)
+            self._cache.update(ij=ij, d=d, v=v)
         return self._cache
 
     def __getitem__(self, key):
@@ -483,7 +486,12 @@ class NeighborList:
 
     @property
     def weights(self):
-        return self._arrays()["w"]
+        if "w" not in self._cache:
+            w = np.empty(len(self), np.float32)
+            _lib.check(_lib.lib.fg_nlist_get(self._h, None, None, _lib.ptr(w), None))
+            w.flags.writeable = False
+            self._cache["w"] = w
+        return self._cache["w"]
 
     @property
     def distances(self):

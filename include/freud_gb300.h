@@ -138,6 +138,13 @@ fg_status fg_nlist_num_points(const fg_nlist* nl, uint32_t* out);
  * any output may be NULL. */
 fg_status fg_nlist_get(const fg_nlist* nl, uint32_t* neighbors, float* distances, float* weights, float* vectors);
 /* Device pointers of the bond arrays (valid until the list is destroyed or modified). */
+/* Page-locked host memory (cudaMallocHost / cudaFreeHost), no reference counterpart:
+ * the Python layer returns large NeighborList arrays in such buffers (pooled), so
+ * fg_nlist_get copies them from the device by DMA at the link's rate instead of
+ * through the driver's staging of pageable memory. */
+fg_status fg_host_alloc(size_t bytes, void** out);
+fg_status fg_host_free(void* p);
+
 fg_status fg_nlist_device_arrays(const fg_nlist* nl, const uint32_t** neighbors, const float** distances,
                                  const float** vectors);
 /* getSegments / getCounts (NeighborList.cc:199-232). */
