@@ -583,13 +583,16 @@ __global__ void __launch_bounds__(WARPS * 32, 4)
                         {
                             int o = 0;
                             uint32_t ch = item;
-#pragma unroll
-                            for (int t = 0; t < 8; ++t)
+                            if (oct)
                             {
-                                if (o == t && ch >= nchk[t])
+#pragma unroll
+                                for (int t = 0; t < 8; ++t)
                                 {
-                                    ch -= nchk[t];
-                                    o = t + 1;
+                                    if (o == t && ch >= nchk[t])
+                                    {
+                                        ch -= nchk[t];
+                                        o = t + 1;
+                                    }
                                 }
                             }
                             const uint32_t L = oct ? S.lcnt[o] : TT;
