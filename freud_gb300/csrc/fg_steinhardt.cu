@@ -1045,6 +1045,228 @@ __global__ void __launch_bounds__(T, 256 / T)
     }
 }
 
+// The float-float harmonics with two threads per particle: thread parity p takes
+// the orders m = p, p + 2, ... (powers stepped by (sin(theta) e^{i phi})^2), so a
+// particle's float-float sums (one slot per requested (l, m) with m of the
+// thread's parity) take half the shared memory per thread and twice the particles
+// fit an SM. Both threads of a pair run the l loop of the pair's even order 2u:
+// the odd thread (m = 2u + 1) takes the step l = 2u with R = 0 and starts at
+// R_m = 1, so the two see every requested l in the same iteration. Sums, their
+// order and the rounding are those of k_qlm_ff.
+template<int T, int BP>
+__global__ void __launch_bounds__(T, 512 / T)
+    k_qlm_ff2(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
+              const float* __restrict__ dist, const float* __restrict__ weights, const uint32_t* __restrict__ seg,
+              const uint32_t* __restrict__ cnt, const float4* __restrict__ bvd, StLs ls, int weighted,
+              float2* __restrict__ qlm_out, float* __restrict__ ql_out)
+{
+    extern __shared__ float4 acc[]; // [slots of one parity][T]
+    __shared__ int s_lt[ST_MAX_NL + 1];
+    __shared__ int s_k[ST_MAX_NL];
+    __shared__ size_t s_off[ST_MAX_NL];
+    __shared__ float s_norm[ST_MAX_NL];
+    __shared__ int s_pb[2][ST_MAX_L + 2]; // slot of (l, m = parity) for a requested l, per parity
+    __shared__ int s_np;                  // slots of the larger parity
+    if (threadIdx.x == 0)
+    {
+        int o0 = 0, o1 = 0;
+        for (int kk = 0; kk < ls.nl; ++kk)
+        {
+            const int k = ls.sorted_k[kk];
+            const int l = ls.l[k];
+            s_k[kk] = k;
+            s_lt[kk] = l;
+            s_off[kk] = ls.qlm_offset[k];
+            s_norm[kk] = ls.norm[k];
+            s_pb[0][l] = o0;
+            s_pb[1][l] = o1;
+            o0 += l / 2 + 1;
+            o1 += (l + 1) / 2;
+        }
+        s_lt[ls.nl] = -1;
+        s_np = o0 > o1 ? o0 : o1;
+    }
+    __syncthreads();
+    const int nl = ls.nl;
+    const int lmax = ls.max_l;
+    const int par = threadIdx.x & 1;
+    const int lane = threadIdx.x & 31;
+    unsigned req = 0;
+    for (int kk = 0; kk < nl; ++kk)
+        req |= 1u << s_lt[kk];
+    const int* pb = s_pb[par];
+    float4* my = acc + threadIdx.x;
+    const int np = s_np;
+    constexpr int PPB = T / 2; // particles per block
+    for (uint32_t i0 = blockIdx.x * PPB; i0 < n; i0 += gridDim.x * PPB)
+    {
+        const uint32_t i = i0 + (threadIdx.x >> 1);
+        for (int o = 0; o < np; ++o)
+            my[o * T] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float tw = 0.0f;
+        if (i < n)
+        {
+            const uint32_t b0 = seg[i];
+            const uint32_t nbond = cnt[i];
+            float pix = 0.f, piy = 0.f, piz = 0.f;
+            if (bvd == nullptr)
+            {
+                pix = pts[3 * (size_t) i];
+                piy = pts[3 * (size_t) i + 1];
+                piz = pts[3 * (size_t) i + 2];
+            }
+            for (uint32_t e0 = 0; e0 < nbond; e0 += BP)
+            {
+                BondFF g[BP];
+                ffl w2r[BP], w2i[BP];
+                ffl pr[BP], pi[BP];
+#pragma unroll
+                for (int u = 0; u < BP; ++u)
+                {
+                    float dx = 0.f, dy = 0.f, dz = 0.f, d = 0.f, w = 0.f;
+                    if (e0 + u < nbond)
+                    {
+                        const uint32_t e = b0 + e0 + u;
+                        if (bvd != nullptr)
+                        {
+                            const float4 v = bvd[e];
+                            dx = v.x;
+                            dy = v.y;
+                            dz = v.z;
+                            d = v.w;
+                        }
+                        else
+                        {
+                            const uint32_t j = ij[e].y;
+                            box_wrap(b, __fsub_rn(pts[3 * (size_t) j], pix), __fsub_rn(pts[3 * (size_t) j + 1], piy),
+                                     __fsub_rn(pts[3 * (size_t) j + 2], piz), dx, dy, dz);
+                            d = dist[e];
+                        }
+                        w = weighted ? weights[e] : 1.0f;
+                    }
+                    g[u] = bond_ff(dx, dy, dz, d, w);
+                    tw = __fadd_rn(tw, w);
+                    // (s e^{i phi})^2, and the power of order par times the weight
+                    w2r[u] = ff_sub_lazy(ff_mul(g[u].wr, g[u].wr), ff_mul(g[u].wi, g[u].wi));
+                    w2i[u] = ff_add_lazy(ff_mul(g[u].wr, g[u].wi), ff_mul(g[u].wi, g[u].wr));
+                    if (par)
+                    {
+                        pr[u] = ff_mul(g[u].wr, {g[u].w, 0.0f});
+                        pi[u] = ff_mul(g[u].wi, {g[u].w, 0.0f});
+                    }
+                    else
+                    {
+                        pr[u] = {g[u].w, 0.0f};
+                        pi[u] = {0.0f, 0.0f};
+                    }
+                }
+                for (int m0 = 0; m0 <= lmax; m0 += 2)
+                {
+                    const int m = m0 + par; // may exceed lmax for the odd thread
+                    if (m0 > 0)
+                    {
+#pragma unroll
+                        for (int u = 0; u < BP; ++u)
+                        {
+                            const ffl nr = ff_sub_lazy(ff_mul(pr[u], w2r[u]), ff_mul(pi[u], w2i[u]));
+                            pi[u] = ff_add_lazy(ff_mul(pr[u], w2i[u]), ff_mul(pi[u], w2r[u]));
+                            pr[u] = nr;
+                        }
+                    }
+                    const float2 kf = c_Kff[m <= ST_MAX_L ? m : ST_MAX_L];
+                    const ffl K = {kf.x, kf.y};
+                    ffl fr[BP], fi[BP], r1[BP], r0[BP];
+#pragma unroll
+                    for (int u = 0; u < BP; ++u)
+                    {
+                        fr[u] = ff_mul(K, pr[u]);
+                        fi[u] = ff_mul(K, pi[u]);
+                        r1[u] = {par ? 0.0f : 1.0f, 0.0f};
+                        r0[u] = {0.0f, 0.0f};
+                    }
+                    for (int l = m0;; ++l)
+                    {
+                        if (((req >> l) & 1u) && l >= m)
+                        {
+                            float4* slot = my + (pb[l] + (m >> 1)) * T;
+                            float4 v = *slot;
+#pragma unroll
+                            for (int u = 0; u < BP; ++u)
+                            {
+                                ff_acc(v.x, v.y, ff_mul(r1[u], fr[u]));
+                                ff_acc(v.z, v.w, ff_mul(r1[u], fi[u]));
+                            }
+                            *slot = v;
+                        }
+                        if (l == lmax)
+                            break;
+                        const int mm = m <= ST_MAX_L ? m : ST_MAX_L;
+                        const float2 af = c_aff[(l + 1) * (ST_MAX_L + 1) + mm];
+                        const float2 bf = c_bff[(l + 1) * (ST_MAX_L + 1) + mm];
+                        const bool start = l + 1 == m; // odd thread: R_m = 1
+#pragma unroll
+                        for (int u = 0; u < BP; ++u)
+                        {
+                            const ffl t = ff_sub_lazy(ff_mul(g[u].ct, r1[u]), ff_mul({bf.x, bf.y}, r0[u]));
+                            const ffl nr = ff_mul({af.x, af.y}, t);
+                            r0[u] = r1[u];
+                            r1[u] = start ? ffl{1.0f, 0.0f} : nr;
+                        }
+                    }
+                }
+            }
+        }
+        // sums -> qlm (m of this parity) in place; ql from both threads' parts
+        for (int kk = 0; kk < nl; ++kk)
+        {
+            const int l = s_lt[kk];
+            float part = 0.0f;
+            if (i < n)
+            {
+                for (int m = par; m <= l; m += 2)
+                {
+                    float4* slot = my + (pb[l] + (m >> 1)) * T;
+                    const float4 v = *slot;
+                    const float qr = ff_div_f(v.x, v.y, tw);
+                    const float qi = ff_div_f(v.z, v.w, tw);
+                    slot->x = qr;
+                    slot->y = qi;
+                    const float sq = __fmaf_rn(qr, qr, __fmul_rn(qi, qi));
+                    part = __fadd_rn(part, m > 0 ? __fmul_rn(2.0f, sq) : sq);
+                }
+            }
+            // even orders' part + odd orders' part (the same order on both threads)
+            const float other = __shfl_xor_sync(FULL, part, 1);
+            const float tot = par ? __fadd_rn(other, part) : __fadd_rn(part, other);
+            if (i < n && par == 0)
+                ql_out[static_cast<size_t>(i) * nl + s_k[kk]] = sqrtf(tot * s_norm[kk]);
+        }
+        __syncwarp();
+        // the warp's 16 particles' rows, coalesced
+        const uint32_t w0 = i0 + ((threadIdx.x & ~31u) >> 1);
+        const int wcol = threadIdx.x & ~31;
+        for (int kk = 0; kk < nl; ++kk)
+        {
+            const int l = s_lt[kk];
+            const int width = 2 * l + 1;
+            float2* out = qlm_out + s_off[kk] + static_cast<size_t>(w0) * width;
+            for (int p = 0; p < 16 && w0 + p < n; ++p)
+            {
+                for (int c = lane; c < width; c += 32)
+                {
+                    const int m = c <= l ? c : c - l;
+                    const float4 v = acc[(s_pb[m & 1][l] + (m >> 1)) * T + wcol + 2 * p + (m & 1)];
+                    float2 q = make_float2(v.x, v.y);
+                    if (c > l)
+                        q = (m & 1) ? make_float2(-v.x, v.y) : make_float2(v.x, -v.y);
+                    out[static_cast<size_t>(p) * width + c] = q;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Neighbour averaging: ave(i) = (sum_j qlm(j) + qlm(i)) / (1 + n_i). Per l, the
 // neighbour indices of LANES bonds are loaded at once (one per lane) and
 // broadcast, so the row gathers do not wait on the index loads one by one.
@@ -1415,6 +1637,18 @@ void qlm_flat(const DevBox& box, const float* pts, uint32_t n, const uint2* ij, 
 }
 } // namespace
 
+// slots per thread of k_qlm_ff2: requested (l, m) with m of the larger parity count
+static size_t ff2_np(const StLs& ls)
+{
+    int o0 = 0, o1 = 0;
+    for (int k = 0; k < ls.nl; ++k)
+    {
+        o0 += ls.l[k] / 2 + 1;
+        o1 += (ls.l[k] + 1) / 2;
+    }
+    return static_cast<size_t>(o0 > o1 ? o0 : o1);
+}
+
 int qlm_ff_threads(const StLs& ls)
 {
     int slots = 0;
@@ -1452,14 +1686,23 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
             cudaFuncSetAttribute(k_qlm_ff<32, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
             configured = true;
         }
+        // four bonds per pass: four independent recurrence chains per step
+        // (0.85 ms against 0.99 ms with two on the 256,000-point FCC set, l = 4..12)
+        if (ff2_np(ls) * 64 * sizeof(float4) <= 48 * 1024)
+        {
+            // two threads per particle (orders by parity): twice the particles per SM
+            const uint32_t blocks2 = (n + 31) / 32;
+            ProfScope prof2_("k_qlm_ff2", s);
+            k_qlm_ff2<64, 4><<<blocks2, 64, ff2_np(ls) * 64 * sizeof(float4), s>>>(
+                box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm, ql);
+            return;
+        }
         const uint32_t blocks = (n + T - 1) / T;
         ProfScope prof_("k_qlm_ff", s);
         auto go = [&](auto kernel, int threads) {
             kernel<<<blocks, threads, smem, s>>>(box, pts, n, ij, dist, weights, seg, cnt, bond_vd, ls, weighted, qlm,
                                                  ql);
         };
-        // four bonds per pass: four independent recurrence chains per step
-        // (0.85 ms against 0.99 ms with two on the 256,000-point FCC set, l = 4..12)
         if (T == 64)
             go(k_qlm_ff<64, 4>, 64);
         else
