@@ -330,16 +330,45 @@ __global__ void __launch_bounds__(128)
             const int cell = (ux - wx * g.dim[0]) + g.dim[0] * ((uy - wy * g.dim[1]) + g.dim[1] * (uz - wz * g.dim[2]));
             const int wrap = (wx + 1) + 3 * (wy + 1) + 9 * (wz + 1);
             const uint32_t s0 = g.start[cell], s1 = g.start[cell + 1];
+            // AABB arithmetic, candidate inside the box (image 0): k = -n_q - wrap is the
+            // cell's, so its validity and image vector are taken once per cell
+            const int kx0 = -img_axis_k(qimg, 0) - wx, ky0 = -img_axis_k(qimg, 1) - wy,
+                      kz0 = -img_axis_k(qimg, 2) - wz;
+            const bool ok0 = kx0 >= -1 && kx0 <= 1 && ky0 >= -1 && ky0 <= 1 && kz0 >= -1 && kz0 <= 1;
+            float ivx = 0.f, ivy = 0.f, ivz = 0.f;
+            if (ok0)
+            {
+                const float* iv = s_img[(kx0 + 1) * 9 + (ky0 + 1) * 3 + (kz0 + 1)];
+                ivx = iv[0];
+                ivy = iv[1];
+                ivz = iv[2];
+            }
+            const float qx = __fadd_rn(q.x, ivx), qy = __fadd_rn(q.y, ivy), qz = __fadd_rn(q.z, ivz);
 #pragma unroll 4
             for (uint32_t slot = s0; slot < s1; ++slot)
             {
                 const float4 pj = g.cpos[slot];
                 const uint32_t j = g.cidx[slot];
-                float rx, ry, rz;
-                if ((p.exclude_ii && j == qi) || !pair_vec_k(b, s_img, p.arith, q, qimg, pj, wrap, rx, ry, rz))
+                if (p.exclude_ii && j == qi)
                     continue;
+                float rx, ry, rz;
+                if (p.arith == ARITH_AABB && __float_as_int(pj.w) == 0)
+                {
+                    if (!ok0)
+                        continue;
+                    rx = __fsub_rn(pj.x, qx);
+                    ry = __fsub_rn(pj.y, qy);
+                    rz = __fsub_rn(pj.z, qz);
+                }
+                else if (!pair_vec_k(b, s_img, p.arith, q, qimg, pj, wrap, rx, ry, rz))
+                {
+                    continue;
+                }
                 const float rsq = dot3(rx, ry, rz);
-                if (!knn_accept(p, rsq))
+                if (!(rsq < p.r_max_sq))
+                    continue;
+                // r_min: the square root only when r_min > 0 (sqrt(r^2) >= 0 always holds)
+                if (p.arith == ARITH_WRAP ? !(rsq >= p.r_min_sq) : (p.r_min > 0.0f && !(__fsqrt_rn(rsq) >= p.r_min)))
                     continue;
                 const unsigned long long kk = (static_cast<unsigned long long>(__float_as_uint(rsq)) << 32) | j;
                 if (kk >= worst)
