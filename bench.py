@@ -789,7 +789,8 @@ def main():
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             tj = json.load(f)
-        per_kernel = [tj.get(k) for k in build]
+        # DRAM bytes per launch x launches per step, over the build's kernels
+        per_kernel = [None if tj.get(k) is None else tj[k] * v[0] / max(args.steps, 1) for k, v in build.items()]
         if per_kernel and all(x is not None for x in per_kernel):
             traffic = float(sum(per_kernel))
     except (OSError, ValueError):
