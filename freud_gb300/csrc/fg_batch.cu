@@ -1391,16 +1391,23 @@ void launch_frames_hist(const BatchHistConfig& cfg, const BatchGrid& g, const Ba
 {
     if (cell_limit == 0)
         return;
+    // copies == warps: a histogram per warp (no two warps add into one bin), when
+    // every copy fits the shared histogram
+    const bool per_warp = cfg.copies == cfg.warps && h.bins * static_cast<uint32_t>(cfg.warps) <= BT_HIST;
     if (cfg.warps == 4)
     {
-        if (cfg.copies == 2)
+        if (per_warp)
+            hist_launch<4, 4>(g, p, h, cell_limit, queue, hist, s);
+        else if (cfg.copies == 2)
             hist_launch<4, 2>(g, p, h, cell_limit, queue, hist, s);
         else
             hist_launch<4, 1>(g, p, h, cell_limit, queue, hist, s);
     }
     else
     {
-        if (cfg.copies == 2)
+        if (per_warp)
+            hist_launch<8, 8>(g, p, h, cell_limit, queue, hist, s);
+        else if (cfg.copies == 2)
             hist_launch<8, 2>(g, p, h, cell_limit, queue, hist, s);
         else
             hist_launch<8, 1>(g, p, h, cell_limit, queue, hist, s);

@@ -3173,7 +3173,7 @@ BatchHistConfig tuned_config(fg_frames* fr, const BallParams& p, const HistParam
         const BatchGrid v = batch_view(fr, g);
         for (int warps : {4, 8})
         {
-            for (int copies : {1, 2})
+            for (int copies : {1, 2, warps})
             {
                 const BatchHistConfig cfg {shell, warps, copies};
                 float ms = std::numeric_limits<float>::infinity();
@@ -3568,8 +3568,8 @@ fg_status fg_batch_set_config(int shell, int warps_per_block, int hist_copies)
             return;
         }
         if (shell < 1 || shell > 2 || (warps_per_block != 4 && warps_per_block != 8) ||
-            (hist_copies != 1 && hist_copies != 2))
-            value_error("batch config: shell 1 or 2, 4 or 8 warps per block, 1 or 2 histogram copies");
+            (hist_copies != 1 && hist_copies != 2 && hist_copies != warps_per_block))
+            value_error("batch config: shell 1 or 2, 4 or 8 warps per block, 1, 2 or one per warp histogram copies");
         g_forced = BatchHistConfig {shell, warps_per_block, hist_copies};
     });
 }
