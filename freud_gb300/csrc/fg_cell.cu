@@ -878,15 +878,20 @@ __device__ __forceinline__ float3 nl_shifted(const DevBox& b, float4 p, const fl
     return make_float3(p.x + w[0], p.y + w[1], p.z + w[2]);
 }
 
+// The kept flags of the staging sweeps live where the sorted candidates go later
+// (rec is written after the merge), and the per-query bond counts in the merge
+// buffer the merge leaves free: 29 KB per block, seven blocks per SM.
 template<typename K> struct NlShared
 {
     K ka[CELL_CAP];
     K kb[CELL_CAP];
     uint32_t sw[CELL_CAP];   // slot << 5 | wrap, by compact position
-    float4 rec[CELL_CAP];    // sorted candidates: prefilter position, point index (bits)
-    uint32_t cnt[CELL_CAP];  // bond count per query of the cell
+    union
+    {
+        float4 rec[CELL_CAP];                // sorted candidates: prefilter position, point index (bits)
+        uint32_t kw[27][SORT_CELL_MAX / 32]; // staging: kept flags of each item's candidates
+    };
     uint32_t kc[32];         // kept candidates per item
-    uint32_t kw[27][SORT_CELL_MAX / 32]; // kept flags of each item's candidates (first sweep)
     uint32_t ro[33];         // kept-run offsets (runs past the items are empty)
     float wsh[32][3];        // lattice shift of each cell wrap code (0 .. 26)
     float qb[NLW][6];
@@ -1060,8 +1065,6 @@ __global__ void __launch_bounds__(NLT, 6)
                     S.kc[s] = kept;
             }
         }
-        for (uint32_t k = tid; k < nqc && k < static_cast<uint32_t>(CELL_CAP); k += NLT)
-            S.cnt[k] = 0;
         __syncthreads();
         if (warp == 0)
         {
@@ -1131,6 +1134,10 @@ __global__ void __launch_bounds__(NLT, 6)
             }
         }
         const K* order = src;
+        // bond counts of the cell's queries, in the merge buffer the merge left free
+        uint32_t* cnt = reinterpret_cast<uint32_t*>(dst);
+        for (uint32_t k = tid; k < nqc && k < static_cast<uint32_t>(CELL_CAP); k += NLT)
+            cnt[k] = 0;
         for (uint32_t e = tid; e < T; e += NLT)
         {
             const K key = order[e];
@@ -1241,12 +1248,12 @@ __global__ void __launch_bounds__(NLT, 6)
             if (live)
             {
                 gmask[static_cast<size_t>(q0 + qk) * CELL_CHUNKS + ch] = word;
-                atomicAdd(&S.cnt[qk], static_cast<uint32_t>(__popc(word)));
+                atomicAdd(&cnt[qk], static_cast<uint32_t>(__popc(word)));
             }
         }
         __syncthreads();
         for (uint32_t k = tid; k < nqc; k += NLT)
-            counts[qg.cidx[q0 + k]] = S.cnt[k];
+            counts[qg.cidx[q0 + k]] = cnt[k];
         __syncthreads();
     }
 }
