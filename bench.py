@@ -815,7 +815,7 @@ def main():
     e2e_value = bonds * world / statistics.median(e2e_times)
 
     # ---- e2e with the NeighborList read back: nlist[:], distances, vectors as a freud
-    # user reads them (24 B per bond device -> host, weights filled on the host)
+    # user reads them (24 B per bond device -> host; weights are read only when asked for)
     rb_times = []
     gpu_list = None
     for it in range(1 + max(1, min(args.steps, 3))):

@@ -132,3 +132,28 @@ def test_count_kernel_dense_cluster(freud, both_kernels):
     assert lists_equal(new, old)
     ij, d, v = O.query(box, pts, r_max=2.5, exclude_ii=True, arith=O.ARITH_WRAP)
     assert_oracle(new, ij, d, v)
+
+
+def test_large_list_readback_in_page_locked_arrays(freud):
+    """A list of at least 2^20 bonds comes back in pooled page-locked arrays: read-only,
+    bit-equal to the oracle's list, and a dropped list's blocks return to the pool."""
+    import gc
+
+    from freud_gb300 import _lib
+
+    rs = np.random.RandomState(47)
+    box = freud.box.Box.cube(40.0)
+    pts = box.make_absolute(rs.random_sample((60000, 3))).astype(np.float32)
+    nl = freud.locality.LinkCell(box, pts, 2.5).query(pts, {"r_max": 2.5, "exclude_ii": True}).toNeighborList()
+    assert len(nl) >= 1 << 20
+    ij, d, v = nl[:], nl.distances, nl.vectors
+    for a in (ij, d, v):
+        assert not a.flags.writeable
+    oij, od, ov = O.query(O.box7(box), pts, r_max=2.5, exclude_ii=True, arith=O.ARITH_WRAP)
+    np.testing.assert_array_equal(ij, oij)
+    np.testing.assert_array_equal(d, od)
+    np.testing.assert_array_equal(v, ov)
+    pooled = sum(len(x) for x in _lib._pinned_free.values())
+    del ij, d, v, nl
+    gc.collect()
+    assert sum(len(x) for x in _lib._pinned_free.values()) >= pooled + 3
