@@ -154,6 +154,6 @@ def test_large_list_readback_in_page_locked_arrays(freud):
     np.testing.assert_array_equal(d, od)
     np.testing.assert_array_equal(v, ov)
     pooled = sum(len(x) for x in _lib._pinned_free.values())
-    del ij, d, v, nl
+    del ij, d, v, nl, a
     gc.collect()
     assert sum(len(x) for x in _lib._pinned_free.values()) >= pooled + 3
