@@ -1019,7 +1019,9 @@ void knn_nlist(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args& a,
     sync();
 }
 
-void run_query(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args* args, int by_distance, fg_nlist& out)
+// The query arguments as a query of nq runs them (mode inferred), after the
+// reference's checks of the box and the arguments.
+fg_query_args checked_args(const fg_nq* nq, const fg_query_args* args)
 {
     fg_query_args a = *args;
     if (nq->kind != FG_NQ_RAWPOINTS)
@@ -1030,6 +1032,12 @@ void run_query(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args* ar
         validate_cellquery_args(nq->box, a);
     else
         validate_args(a);
+    return a;
+}
+
+void run_query(fg_nq* nq, const float* dq, uint32_t nqp, const fg_query_args* args, int by_distance, fg_nlist& out)
+{
+    const fg_query_args a = checked_args(nq, args);
     if (a.mode == FG_MODE_BALL)
         ball_nlist(nq, dq, nqp, a, by_distance, out);
     else
@@ -1055,6 +1063,69 @@ void upload_points(const float* host, uint32_t n, DevBuf& buf)
     if (n > 0)
         FG_CUDA(cudaMemcpyAsync(buf.p, host, sizeof(float) * 3 * static_cast<size_t>(n), cudaMemcpyHostToDevice,
                                 stream()));
+}
+
+// Second stream of the calling thread and device, for host-to-device copies that
+// overlap kernels on the library stream, with the two events that order them.
+struct CopyLane
+{
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    int dev = -1;
+};
+
+CopyLane& copy_lane()
+{
+    static thread_local CopyLane c;
+    int dev = 0;
+    FG_CUDA(cudaGetDevice(&dev));
+    if (c.s == nullptr || c.dev != dev)
+    {
+        FG_CUDA(cudaStreamCreateWithFlags(&c.s, cudaStreamNonBlocking));
+        FG_CUDA(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
+        FG_CUDA(cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming));
+        c.dev = dev;
+    }
+    return c;
+}
+
+// The object's own cell grid for a ball query with arguments a (the grid that
+// ball_nlist looks up), built ahead of the query.
+void prebuild_ball_grid(fg_nq* nq, const fg_query_args& a)
+{
+    if (a.mode != FG_MODE_BALL || nq->kind == FG_NQ_CELLQUERY)
+        return;
+    int dim[3];
+    grid_dims(nq->box, a.r_max * (1.0f + 1e-5f), nq->n, dim);
+    nq_grid(nq, dim);
+}
+
+// Copies n host query points to buf on the copy lane while the object's cell
+// grid for the query is built on the library stream; the library stream waits
+// for the copy before anything that follows. If the build fails, the copy is
+// waited for before the error leaves (the caller may release its points then).
+void upload_query_points(fg_nq* nq, const fg_query_args& a, const float* host, uint32_t n, DevBuf& buf)
+{
+    buf.alloc(sizeof(float) * 3 * static_cast<size_t>(n));
+    if (n == 0)
+        return;
+    const cudaStream_t s = stream();
+    CopyLane& c = copy_lane();
+    FG_CUDA(cudaEventRecord(c.fork, s)); // the buffer's allocation is ordered on s
+    FG_CUDA(cudaStreamWaitEvent(c.s, c.fork, 0));
+    FG_CUDA(cudaMemcpyAsync(buf.p, host, sizeof(float) * 3 * static_cast<size_t>(n), cudaMemcpyHostToDevice, c.s));
+    FG_CUDA(cudaEventRecord(c.join, c.s));
+    try
+    {
+        prebuild_ball_grid(nq, a);
+    }
+    catch (...)
+    {
+        cudaStreamWaitEvent(s, c.join, 0);
+        cudaStreamSynchronize(c.s);
+        throw;
+    }
+    FG_CUDA(cudaStreamWaitEvent(s, c.join, 0));
 }
 
 // Whether n query points already on the device (dq) equal the object's points
@@ -1272,7 +1343,7 @@ fg_status fg_nq_query(fg_nq* nq, const float* query_points, uint32_t n_query, co
         uint32_t nqp = nq->n;
         if (query_points != nullptr)
         {
-            upload_points(query_points, n_query, dq);
+            upload_query_points(nq, checked_args(nq, args), query_points, n_query, dq);
             if (!same_as_points(nq, dq.as<float>(), n_query))
             {
                 qp = dq.as<float>();
