@@ -463,7 +463,7 @@ def measure_c4(freud, _lib, steps, warmup, nframes=64):
                         "kernels_ms_per_step": top_batch},
             "speedup_e2e": t_plain / t_batch, "speedup_device": dev_plain / dev_batch if dev_batch else None,
             "small_frames": small,
-            "autotune": _lib.autotune_report().strip().splitlines()[-1:],
+            "autotune": _lib.autotune_report().strip().splitlines(),
             "parity": parity, "cpu_baseline": cpu}
 
 
