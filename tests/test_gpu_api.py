@@ -146,6 +146,25 @@ def test_no_bonds(freud, kind):
 
 
 @pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("qargs", [dict(r_max=2.0, exclude_ii=False), dict(num_neighbors=4, exclude_ii=False)])
+def test_zero_query_points(freud, kind, qargs):
+    """A query with an empty (0, 3) array of query points gives an empty list over
+    no query points, and the object answers the next query as before."""
+    if kind == "cellquery" and "num_neighbors" in qargs:
+        pytest.skip("CellQuery answers ball queries only")
+    rs = np.random.RandomState(5)
+    box = freud.box.Box.cube(10)
+    pts = (rs.rand(300, 3) * 10 - 5).astype(np.float32)
+    nq = make(freud, kind, box, pts, 2.0)
+    nl = nq.query(np.zeros((0, 3), np.float32), qargs).toNeighborList()
+    assert len(nl) == 0 and nl[:].shape == (0, 2)
+    assert nl.num_query_points == 0 and nl.num_points == 300
+    assert nl.neighbor_counts.shape == (0,)
+    full = nq.query(pts[:50].copy(), qargs).toNeighborList()
+    assert full.num_query_points == 50 and len(full) > 0
+
+
+@pytest.mark.parametrize("kind", KINDS)
 def test_corner_2d(freud, kind):
     # four points near the four corners of a square box are mutual neighbours through the images
     box = freud.box.Box.square(10)
