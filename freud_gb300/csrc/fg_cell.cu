@@ -1685,7 +1685,7 @@ __global__ void __launch_bounds__(WW * 32, 7)
                 }
                 __syncthreads();
                 const uint32_t total = win & 0xffffu;
-#pragma unroll 2
+#pragma unroll 1
                 for (uint32_t bb = static_cast<uint32_t>(tid); bb < total; bb += WW * 32)
                 {
                     const uint32_t le = S.lst[bb];
