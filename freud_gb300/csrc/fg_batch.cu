@@ -881,7 +881,7 @@ template<bool FILL> struct FBWarp
 constexpr uint32_t FB_CHUNK = 4096; // bond slots a warp takes at a time (one pass)
 
 template<bool FILL, bool ONE = false>
-__global__ void __launch_bounds__(FB_THREADS, FILL ? 6 : 10)
+__global__ void __launch_bounds__(FB_THREADS, FILL ? 8 : 10)
     k_frames_ball(BatchGrid g, BallParams p, uint32_t* __restrict__ counts, const uint64_t* __restrict__ offsets,
                   uint32_t* __restrict__ bj, float4* __restrict__ bvd, uint32_t* __restrict__ seg = nullptr,
                   unsigned long long* __restrict__ alloc = nullptr, unsigned long long cap = 0)
