@@ -34,7 +34,7 @@ namespace fg {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int BT_TILE = 1024;   // staged candidates per tile
+constexpr int BT_TILE = 896;    // staged candidates per tile (four blocks of HistShared fit an SM)
 constexpr int BT_QB = 128;      // queries per shared-memory batch
 constexpr int BT_ITEMS = 96;    // stencil items: up to 32 rows x 3 x-segments
 constexpr int BT_HIST = 2048;   // shared histogram words (all copies)
