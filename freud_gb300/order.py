@@ -85,18 +85,28 @@ class Steinhardt(_PairCompute):
         _lib.check(_lib.lib.fg_steinhardt_num_frames(self._h, ctypes.byref(nf)))
         return n.value, nf.value, len(self._ls)
 
+    # outputs of at least this many bytes are read into page-locked arrays from the
+    # library's pool (the device-to-host copy then runs by DMA)
+    _PINNED_BYTES = 1 << 20
+
     def _fetch(self, key):
-        """One output array, copied from the device on first access after a compute."""
+        """One output array, copied from the device on first access after a compute
+        (every element is written by the copy)."""
         if self._cache is None:
             self._cache = {}
         if key in self._cache:
             return self._cache[key]
         n, nf, nl = self._dims()
+
+        def empty(shape):
+            count = int(np.prod(shape))
+            return (_lib.pinned_empty if 4 * count >= self._PINNED_BYTES else np.empty)(shape, np.float32)
+
         if key == "ql":
-            out = np.zeros((n, nl), np.float32)
+            out = empty((n, nl))
             _lib.check(_lib.lib.fg_steinhardt_get(self._h, _lib.ptr(out), None, None, None))
         elif key == "po":
-            out = np.zeros((n, nl), np.float32)
+            out = empty((n, nl))
             _lib.check(_lib.lib.fg_steinhardt_get(self._h, None, _lib.ptr(out), None, None))
         elif key == "order":
             out = np.zeros(nf * nl, np.float32)
@@ -105,7 +115,7 @@ class Steinhardt(_PairCompute):
                 out = out.reshape(nf, nl)
         else:
             stride = sum(2 * l + 1 for l in self._ls)
-            qlm = np.zeros(n * stride * 2, np.float32)
+            qlm = empty((n * stride * 2,))
             _lib.check(_lib.lib.fg_steinhardt_get(self._h, None, None, _lib.ptr(qlm), None))
             qc = qlm.view(np.complex64)
             out, off = [], 0
