@@ -340,9 +340,11 @@ __global__ void __launch_bounds__(128)
 // One l value, bonds spread flat over the lanes: a warp takes per_warp consecutive
 // particles (a few bonds each), lane t of a round computes every order m of
 // Y_l^m for bond round*32 + t of the warp's particles (one geometry and l(l+1)/2
-// recurrence steps per bond, all lanes busy), and a segmented shuffle scan keyed
-// by particle adds each particle's part of the round into its shared-memory row.
-// Summation order is fixed (tree within a round, rounds in sequence).
+// recurrence steps per bond, all lanes busy) and stores them in a shared-memory
+// row; then lanes take (particle, value) pairs, each adding its particle's bonds
+// of the round for one value in bond order, into the particle's accumulator
+// (values of up to two particles at a time when a row has at most 16 values).
+// Summation order is fixed (bond order within a round, rounds in sequence).
 template<int L>
 __global__ void __launch_bounds__(128)
     k_qlm_flat(DevBox b, const float* __restrict__ pts, uint32_t n, const uint2* __restrict__ ij,
@@ -351,10 +353,15 @@ __global__ void __launch_bounds__(128)
                uint32_t per_warp, float2* __restrict__ qlm_out, float* __restrict__ ql_out)
 {
     constexpr int NV = 2 * (L + 1) + 1; // re, im for m = 0..L, then the weight (odd: no bank conflicts)
+    constexpr int SEGS = NV <= 16 ? 2 : 1; // particles summed at a time
+    constexpr int SPAN = 32 / SEGS;        // lanes per particle (value v = lane % SPAN)
+    static_assert(NV <= 32, "a row's values must fit the lanes of a warp");
     __shared__ float acc_s[4][32][NV];
+    __shared__ float val_s[4][32][NV];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     float (*acc)[NV] = acc_s[warp];
+    float (*val)[NV] = val_s[warp];
     const uint32_t nwarps = gridDim.x * 4;
     for (uint32_t p0 = (blockIdx.x * 4 + warp) * per_warp; p0 < n; p0 += nwarps * per_warp)
     {
@@ -460,27 +467,37 @@ __global__ void __launch_bounds__(128)
                 }
                 vals[NV - 1] = w;
             }
-            // segmented inclusive scan keyed by particle slot (dead lanes get unique keys)
-            const int key = live ? k : 32 + lane;
-#pragma unroll
-            for (int dlt = 1; dlt < 32; dlt <<= 1)
+            if (live)
             {
-                const int kup = __shfl_up_sync(FULL, key, dlt);
-                const bool take = lane >= dlt && kup == key;
 #pragma unroll
                 for (int v = 0; v < NV; ++v)
-                {
-                    const float up = __shfl_up_sync(FULL, vals[v], dlt);
-                    if (take)
-                        vals[v] += up;
-                }
+                    val[lane][v] = vals[v];
             }
-            const int knext = __shfl_down_sync(FULL, key, 1);
-            if (live && (lane == 31 || knext != key))
+            __syncwarp();
+            // the round's bonds are lanes [0, nlive), particle slots kf .. kl (bonds of
+            // one slot are consecutive lanes; slots between with no bonds add nothing)
+            const int nlive = static_cast<int>(min(32u, total - r0));
+            const int kf = __shfl_sync(FULL, k, 0);
+            const int kl = __shfl_sync(FULL, k, nlive - 1);
+            const int v = lane % SPAN;
+            for (int s0 = kf; s0 <= kl; s0 += SEGS)
             {
-#pragma unroll
-                for (int v = 0; v < NV; ++v)
-                    acc[k][v] += vals[v];
+                const int sl = s0 + lane / SPAN;
+                const int src = sl < 32 ? sl : 31;
+                const int xs = static_cast<int>(__shfl_sync(FULL, excl, src)) - static_cast<int>(r0);
+                const int xe = xs + static_cast<int>(__shfl_sync(FULL, c, src));
+                if (sl <= kl && v < NV)
+                {
+                    const int lo = xs > 0 ? xs : 0;
+                    const int hi = xe < nlive ? xe : nlive;
+                    if (hi > lo)
+                    {
+                        float sum = val[lo][v];
+                        for (int t = lo + 1; t < hi; ++t)
+                            sum += val[t][v];
+                        acc[sl][v] += sum;
+                    }
+                }
             }
             __syncwarp();
         }
