@@ -109,7 +109,10 @@ fg_status fg_nq_get_points(const fg_nq* nq, float* out);
 /* NeighborQuery::query(...) -> NeighborQueryIterator::toNeighborList(sort_by_distance)
  * (freud/locality/NeighborQuery.h:130-142, 434-481; export-NeighborQuery.cc:26-33,130-135).
  * query_points == NULL queries the object's own points. Bonds come out in the
- * reference order: (i, j, weight, distance), or (i, distance, j, weight). */
+ * reference order: (i, j, weight, distance), or (i, distance, j, weight). Host
+ * query points are copied on a second stream the library owns while the object's
+ * cell grid is built; the call returns after the copy and the query are done, so
+ * the caller may release query_points then. */
 fg_status fg_nq_query(fg_nq* nq, const float* query_points, uint32_t n_query, const fg_query_args* args,
                       int sort_by_distance, fg_nlist** out);
 /* Same with query points already on the device. */
