@@ -1728,9 +1728,11 @@ void launch_qlm(const DevBox& box, const float* pts, uint32_t n, const uint2* ij
     }
     if (ls.nl == 1 && ls.max_l <= 12)
     {
-        // one l: bonds flat over the lanes, about three rounds of 32 per warp
+        // one l: bonds flat over the lanes, about six rounds of 32 per warp group (64
+        // uneven frames at density 0.85, r_max 1.5: 4.58 ms against 5.21 ms with three;
+        // 4,096 Gaussian blobs, r_max 1.2: 1.57 against 1.53 ms)
         const double mb = mean_bonds > 0.0 ? mean_bonds : 24.0;
-        const uint32_t per_warp = static_cast<uint32_t>(std::min(32.0, std::max(1.0, std::floor(96.0 / mb))));
+        const uint32_t per_warp = static_cast<uint32_t>(std::min(32.0, std::max(1.0, std::floor(192.0 / mb))));
         switch (ls.max_l)
         {
         case 0: qlm_flat<0>(box, pts, n, ij, dist, weights, seg, cnt, ls, weighted, qlm, ql, s, bond_vd, per_warp); return;
